@@ -1,0 +1,231 @@
+"""circlecover_gb300 -- GB300 (sm_103a) prover for the rectangle-covering-by-
+disks proofs of phillip-keldenich/circlecover.
+
+Python host mirror of the C ABI in ``include/circlecover_gb300.h`` (ctypes
+over ``_build/libcirclecover_gb300.so``).  The names follow the reference:
+``Prover.tight_find_critical_intervals`` is the reference's
+``circlecover::tight_rectangle::find_critical_intervals()``
+(tight_rectangle/tight_rectangle.cu:458), ``Prover.tight_eval`` evaluates the
+criteria declared in tight_rectangle/strategies.cuh:54-87.
+
+There is no CPU fallback: if the CUDA library is missing or no device is
+usable, every entry point raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .workloads import TIGHT_BOX, SB_BOX  # noqa: F401
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libcirclecover_gb300.so")
+
+MAX_GEN = 32
+
+# verdict bits (CC_TV_*)
+TV_R1, TV_R1R2, TV_R1R2R3, TV_TWO_BY_TWO, TV_R1R2R3_LEAF, TV_GAPS, TV_R_EMPTY = (1 << k for k in range(7))
+TV_TRAPPED = 1 << 31
+
+# reference split counts (tight_rectangle.cu:44-58)
+REFERENCE_GRID = dict(la_init=256, r_init=(128, 128, 128, 128), gens=(1, 2, 2, 2, 2, 1, 2, 1, 2, 1, 2),
+                      r_gen=(128, 128, 128, 64))
+
+
+class CudaError(RuntimeError):
+    pass
+
+
+class CcIv(ctypes.Structure):
+    _fields_ = [("lb", ctypes.c_double), ("ub", ctypes.c_double)]
+
+
+class CcTightBox(ctypes.Structure):
+    _fields_ = [("la", CcIv), ("r", CcIv * 4)]
+
+
+class CcTightGrid(ctypes.Structure):
+    _fields_ = [
+        ("la_splits_init", ctypes.c_int),
+        ("r_splits_init", ctypes.c_int * 4),
+        ("num_generations", ctypes.c_int),
+        ("la_splits_gen", ctypes.c_int * MAX_GEN),
+        ("r_splits_gen", ctypes.c_int * 4),
+    ]
+
+
+class CcProveStats(ctypes.Structure):
+    _fields_ = [
+        ("counts", (ctypes.c_uint64 * 8) * 4),
+        ("digest", ctypes.c_uint64),
+        ("leaf_evals", ctypes.c_uint64),
+        ("trapped_leaves", ctypes.c_uint64),
+        ("gen_sizes", ctypes.c_uint64 * (MAX_GEN + 1)),
+        ("generations_run", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("seconds", ctypes.c_double),
+        ("kernel_launches", ctypes.c_uint64),
+    ]
+
+
+def make_grid(la_init, r_init, gens=(), r_gen=(128, 128, 128, 64)):
+    g = CcTightGrid()
+    g.la_splits_init = int(la_init)
+    for k in range(4):
+        g.r_splits_init[k] = int(r_init[k])
+        g.r_splits_gen[k] = int(r_gen[k])
+    if len(gens) > MAX_GEN:
+        raise ValueError("at most %d generations" % MAX_GEN)
+    g.num_generations = len(gens)
+    for i, s in enumerate(gens):
+        g.la_splits_gen[i] = int(s)
+    return g
+
+
+def stats_to_dict(s):
+    return {
+        "counts": [[int(s.counts[l][k]) for k in range(8)] for l in range(4)],
+        "digest": int(s.digest),
+        "leaf_evals": int(s.leaf_evals),
+        "trapped_leaves": int(s.trapped_leaves),
+        "gen_sizes": [int(s.gen_sizes[g]) for g in range(int(s.generations_run) + 1)],
+        "generations_run": int(s.generations_run),
+        "seconds": float(s.seconds),
+        "kernel_launches": int(s.kernel_launches),
+    }
+
+
+_lib = None
+
+EXPORTS = [
+    "cc_create", "cc_destroy", "cc_status_str", "cc_last_error", "cc_tight_eval", "cc_tight_eval_device",
+    "cc_last_launch_count", "cc_tight_prove", "cc_tight_summary", "cc_interrupt", "cc_free",
+]
+
+
+def load_library(path=LIB_PATH):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise CudaError("CUDA library not built: %s (run __graft_entry__.build())" % path)
+    lib = ctypes.CDLL(path)
+    vp, sz = ctypes.c_void_p, ctypes.c_size_t
+    lib.cc_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int]
+    lib.cc_destroy.argtypes = [vp]
+    lib.cc_status_str.argtypes = [ctypes.c_int]
+    lib.cc_status_str.restype = ctypes.c_char_p
+    lib.cc_last_error.argtypes = [vp]
+    lib.cc_last_error.restype = ctypes.c_char_p
+    lib.cc_tight_eval.argtypes = [vp, vp, sz, vp]
+    lib.cc_tight_eval_device.argtypes = [vp, vp, sz, vp, vp]
+    lib.cc_last_launch_count.argtypes = [vp]
+    lib.cc_last_launch_count.restype = ctypes.c_uint64
+    missing = [name for name in EXPORTS if not hasattr(lib, name)]
+    if missing:
+        raise CudaError("library %s lacks %s" % (path, ", ".join(missing)))
+    lib.cc_tight_prove.argtypes = [vp, ctypes.POINTER(CcTightBox), ctypes.POINTER(CcTightGrid), ctypes.POINTER(vp),
+                                   ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
+    lib.cc_tight_summary.argtypes = [vp, vp, sz, vp]
+    lib.cc_interrupt.argtypes = [vp]
+    lib.cc_free.argtypes = [vp]
+    if hasattr(lib, "cc_selftest_round"):
+        lib.cc_selftest_round.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, sz]
+        lib.cc_selftest_subinterval.argtypes = [vp, vp, vp, vp, vp, sz, vp, vp]
+    _lib = lib
+    return lib
+
+
+def box_struct(b):
+    s = CcTightBox()
+    s.la.lb, s.la.ub = float(b["la"][0]), float(b["la"][1])
+    for k in range(4):
+        s.r[k].lb, s.r[k].ub = float(b["r"][k][0]), float(b["r"][k][1])
+    return s
+
+
+class Prover:
+    """One CUDA device and stream; mirrors the reference's entry points."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.cc_create(ctypes.byref(h), int(device))
+        if rc != 0:
+            raise CudaError("cc_create(device=%d): %s" % (device, self.lib.cc_status_str(rc).decode()))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.cc_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise CudaError("%s: %s (%s)" % (what, self.lib.cc_status_str(rc).decode(),
+                                             self.lib.cc_last_error(self.h).decode()))
+
+    @property
+    def last_launch_count(self):
+        return int(self.lib.cc_last_launch_count(self.h))
+
+    def tight_eval(self, boxes):
+        """Verdict masks (TV_* bits) of host boxes (TIGHT_BOX records)."""
+        boxes = np.ascontiguousarray(boxes, dtype=TIGHT_BOX)
+        masks = np.zeros(len(boxes), dtype=np.uint32)
+        self._check(self.lib.cc_tight_eval(self.h, boxes.ctypes.data, len(boxes), masks.ctypes.data), "cc_tight_eval")
+        return masks
+
+    def tight_eval_device(self, soa_ptr, n, masks_ptr, stream_ptr=None):
+        """Device-resident variant: SoA (10 x n float64) in, uint32 masks out;
+        asynchronous on `stream_ptr` (raw cudaStream_t) or the handle's stream."""
+        self._check(self.lib.cc_tight_eval_device(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
+                                                  ctypes.c_void_p(stream_ptr) if stream_ptr else None),
+                    "cc_tight_eval_device")
+
+    def tight_find_critical_intervals(self, root, grid):
+        """The tight proof from `root` (a TIGHT_BOX record) with split counts
+        `grid` (make_grid); returns (criticals, stats)."""
+        rs = box_struct(root)
+        out = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcProveStats()
+        self._check(self.lib.cc_tight_prove(self.h, ctypes.byref(rs), ctypes.byref(grid), ctypes.byref(out),
+                                            ctypes.byref(n), ctypes.byref(st)), "cc_tight_prove")
+        arr = np.zeros(n.value, dtype=TIGHT_BOX)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)
+        self.lib.cc_free(out)
+        return arr, stats_to_dict(st)
+
+    def interrupt(self):
+        self.lib.cc_interrupt(self.h)
+
+    # diagnostics
+    def selftest_round(self, op, up, a, b=None):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64) if b is not None else None
+        out = np.empty_like(a)
+        self._check(self.lib.cc_selftest_round(self.h, op, 1 if up else 0, a.ctypes.data,
+                                               bb.ctypes.data if bb is not None else None, out.ctypes.data, len(a)),
+                    "cc_selftest_round")
+        return out
+
+    def selftest_subinterval(self, lo, hi, idx, cnt):
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        hi = np.ascontiguousarray(hi, dtype=np.float64)
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        cnt = np.ascontiguousarray(cnt, dtype=np.int32)
+        a = np.empty(2 * len(lo))
+        b = np.empty(2 * len(lo))
+        self._check(self.lib.cc_selftest_subinterval(self.h, lo.ctypes.data, hi.ctypes.data, idx.ctypes.data,
+                                                     cnt.ctypes.data, len(lo), a.ctypes.data, b.ctypes.data),
+                    "cc_selftest_subinterval")
+        return a.reshape(-1, 2), b.reshape(-1, 2)

@@ -1,0 +1,81 @@
+"""In-tree build of the prover's CUDA library for sm_103a.
+
+``libcirclecover_gb300.so`` (under ``circlecover_gb300/_build/``) exports the C
+ABI of ``include/circlecover_gb300.h``.  Two translation units are compiled in
+parallel with nvcc and linked as a shared library; the main one with
+``-fmad=false`` (no implicit FMA contraction), the diagnostic one with nvcc's
+default contraction on purpose.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OUT = os.path.join(PKG, "_build")
+LIB = os.path.join(OUT, "libcirclecover_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+                 "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
+UNITS = [
+    ("cc_prover.cu", ["-fmad=false", "-Xptxas", "-v"]),
+    ("cc_selftest_fmad.cu", []),
+]
+
+
+def nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.isabs(c) and os.path.exists(c) or not os.path.isabs(c)):
+            return c
+    return "nvcc"
+
+
+def _deps():
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "circlecover_gb300.h")]
+
+
+def _stale():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    return any(os.path.getmtime(d) > t for d in _deps()) or os.path.getmtime(__file__) > t
+
+
+def _compile(unit):
+    name, extra = unit
+    src = os.path.join(CSRC, name)
+    obj = os.path.join(OUT, name.replace(".cu", ".o"))
+    cmd = [nvcc()] + COMMON + extra + ["-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (name, r.stdout, r.stderr))
+    with open(obj + ".log", "w") as f:
+        f.write(r.stdout + r.stderr)
+    return obj
+
+
+def build(force=False, verbose=False):
+    """Compile (if stale) and return the path of the shared library."""
+    os.makedirs(OUT, exist_ok=True)
+    if not force and not _stale():
+        return LIB
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(_compile, UNITS))
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, LIB)
+    if verbose:
+        for name, _ in UNITS:
+            log = os.path.join(OUT, name.replace(".cu", ".o.log"))
+            sys.stdout.write(open(log).read())
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

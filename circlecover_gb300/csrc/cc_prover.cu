@@ -1,0 +1,574 @@
+// The prover's single CUDA translation unit for sm_103a: kernels and the
+// extern "C" entry points of include/circlecover_gb300.h.
+//
+// One translation unit (no -rdc) so that every criterion inlines into the
+// kernels; the reference compiles with separable compilation
+// (algcuda/UseCUDA.cmake:30-31, 42), which keeps each criterion an opaque call.
+// Built with -fmad=false: the only contraction the reference relies on,
+// get_subinterval's FMA, is written out explicitly (cc_iv.cuh).
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "cc_runtime.cuh"
+#include "cc_tight.cuh"
+#include "cc_tight_prove.cuh"
+#include "cc_tight_summary.cuh"
+
+#include <algorithm>
+
+using cc::Iv;
+namespace ct = cc::tight;
+
+// ===================================================================== eval
+// Layout of a box batch in device memory.
+enum class Layout { AoS, SoA };
+
+template <Layout L>
+__device__ __forceinline__ ct::Box load_box(const double* __restrict__ in, size_t n, size_t i) {
+    ct::Box b;
+    double v[10];
+    if (L == Layout::SoA) {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) v[k] = __ldg(in + (size_t)k * n + i);
+    } else {
+        const double2* p = reinterpret_cast<const double2*>(in + i * 10);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            double2 t = __ldg(p + k);
+            v[2 * k] = t.x;
+            v[2 * k + 1] = t.y;
+        }
+    }
+    b.la = Iv{v[0], v[1]};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) b.r[k] = Iv{v[2 + 2 * k], v[3 + 2 * k]};
+    return b;
+}
+
+// One box per thread, grid-stride over the batch.  FP64-pipe bound: each box
+// costs hundreds to thousands of directed-rounding operations against 80 bytes
+// loaded, so memory is irrelevant and the grid is sized to keep every SM's
+// FP64 units fed (a multiple of the SM count).
+template <Layout L>
+__global__ void __launch_bounds__(128) k_tight_eval(const double* __restrict__ in, size_t n, uint32_t* __restrict__ masks) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        ct::Box b = load_box<L>(in, n, i);
+        masks[i] = ct::eval_all(b);
+    }
+}
+
+static int eval_grid(cc_handle* h, size_t n) {
+    size_t blocks = (n + 127) / 128;
+    size_t cap = (size_t)h->sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (int)blocks;
+}
+
+// ================================================================ self-test
+// Directed-rounding primitives exactly as the criteria call them, for the
+// bit-equality test against the host rounding layer.
+__global__ void k_selftest_round(int op, int up, const double* a, const double* b, double* out, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x = a[i], y = b ? b[i] : 0.0, r = 0.0;
+    switch (op) {
+        case 0: r = up ? cc::add_up(x, y) : cc::add_dn(x, y); break;
+        case 1: r = up ? cc::mul_up(x, y) : cc::mul_dn(x, y); break;
+        case 2: r = up ? cc::div_up(x, y) : cc::div_dn(x, y); break;
+        case 3: r = up ? cc::sqrt_up(x) : cc::sqrt_dn(x); break;
+        case 4: r = up ? cc::rcp_up(x) : cc::rcp_dn(x); break;
+    }
+    out[i] = r;
+}
+
+// FP64 pipe throughput probe: independent chains of directed-rounding adds
+// and multiplies (the instructions the criteria issue), or of FMAs.  8
+// independent chains per thread hide the pipe latency.
+__global__ void __launch_bounds__(256) k_fp64_peak(double* out, int iters, int use_fma) {
+    double a[8], b = 1.0000000001, c = 1e-9;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = threadIdx.x * 1e-7 + k;
+    if (use_fma) {
+        for (int i = 0; i < iters; ++i) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+        }
+    } else {
+        for (int i = 0; i < iters; ++i) {
+#pragma unroll
+            for (int k = 0; k < 8; k += 2) {
+                a[k] = __dadd_rd(a[k], c);
+                a[k + 1] = __dmul_ru(a[k + 1], b);
+            }
+        }
+    }
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    if (s == 12345.678) out[0] = s;  // keeps the chains alive
+}
+
+extern "C" int cc_selftest_subinterval_contracted(const double* lo, const double* hi, const int* idx, const int* cnt,
+                                                  double* out, size_t n, void* stream);
+
+__global__ void k_selftest_subinterval(const double* lo, const double* hi, const int* idx, const int* cnt, double* out,
+                                       size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Iv r = cc::subinterval(Iv{lo[i], hi[i]}, idx[i], cnt[i]);
+    out[2 * i] = r.lo;
+    out[2 * i + 1] = r.hi;
+}
+
+// ============================================================== C ABI
+extern "C" {
+
+const char* cc_status_str(int s) {
+    switch (s) {
+        case CC_OK: return "ok";
+        case CC_ERR_CUDA: return "CUDA error";
+        case CC_ERR_PARAM: return "invalid parameter";
+        case CC_ERR_QUEUE_OVERFLOW: return "device queue overflow";
+        case CC_ERR_TIMEOUT: return "device wait timed out";
+        case CC_ERR_INTERRUPTED: return "interrupted";
+        case CC_ERR_NO_DEVICE: return "no usable CUDA device";
+        case CC_ERR_OOM: return "out of memory";
+        default: return "unknown status";
+    }
+}
+
+int cc_create(cc_handle** out, int device) {
+    if (!out) return CC_ERR_PARAM;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        return CC_ERR_NO_DEVICE;
+    }
+    cc_handle* h = new cc_handle();
+    h->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        cudaGetLastError();
+        return CC_ERR_NO_DEVICE;
+    }
+    // the kernels must exist for this device (built for sm_103a only)
+    cudaFuncAttributes attr;
+    if (cudaFuncGetAttributes(&attr, k_tight_eval<Layout::SoA>) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return CC_ERR_NO_DEVICE;
+    }
+    *out = h;
+    return CC_OK;
+}
+
+int cc_destroy(cc_handle* h) {
+    if (!h) return CC_ERR_PARAM;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto& b : h->bufs)
+        if (b.ptr) cudaFree(b.ptr);
+    if (h->pinned) cudaFreeHost(h->pinned);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return CC_OK;
+}
+
+const char* cc_last_error(cc_handle* h) { return h ? h->last_error.c_str() : "no handle"; }
+uint64_t cc_last_launch_count(cc_handle* h) { return h ? h->launches : 0; }
+void cc_interrupt(cc_handle* h) {
+    if (h) h->interrupt.store(1);
+}
+void cc_free(void* p) { std::free(p); }
+
+int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* masks, void* stream) {
+    if (!h || (n && (!soa || !masks))) return CC_ERR_PARAM;
+    h->launches = 0;
+    if (n == 0) return CC_OK;
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    k_tight_eval<Layout::SoA><<<eval_grid(h, n), 128, 0, s>>>(soa, n, masks);
+    CC_LAUNCHED(h);
+    return CC_OK;
+}
+
+// Host-memory entry point: boxes are staged through pinned memory in chunks,
+// copied, evaluated in AoS form on the device, and the masks copied back; the
+// copy of chunk k+1 overlaps the evaluation of chunk k (two buffers, one
+// stream each direction is not needed: one stream, async copies).
+int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* masks) {
+    if (!h || (n && (!boxes || !masks))) return CC_ERR_PARAM;
+    h->launches = 0;
+    if (n == 0) return CC_OK;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    const size_t chunk = n < ((size_t)1 << 21) ? n : ((size_t)1 << 21);
+    const size_t in_bytes = chunk * sizeof(cc_tight_box);
+    const size_t out_bytes = chunk * sizeof(uint32_t);
+    void* d_in[2];
+    void* d_out[2];
+    for (int k = 0; k < 2; ++k) {
+        int st = ccrt::ensure(h, 0 + k, in_bytes, &d_in[k]);
+        if (st) return st;
+        st = ccrt::ensure(h, 2 + k, out_bytes, &d_out[k]);
+        if (st) return st;
+    }
+    int st = ccrt::ensure_pinned(h, 2 * (in_bytes + out_bytes));
+    if (st) return st;
+    char* pin = (char*)h->pinned;
+    char* pin_in[2] = {pin, pin + in_bytes};
+    char* pin_out[2] = {pin + 2 * in_bytes, pin + 2 * in_bytes + out_bytes};
+    cudaEvent_t done[2];
+    CC_CUDA(h, cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming));
+    CC_CUDA(h, cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming));
+    size_t prev_off[2] = {0, 0}, prev_cnt[2] = {0, 0};
+    int k = 0;
+    for (size_t off = 0; off < n; off += chunk, k ^= 1) {
+        size_t cnt = n - off < chunk ? n - off : chunk;
+        // wait until this buffer's previous chunk is done, then hand out its masks
+        if (prev_cnt[k]) {
+            CC_CUDA(h, cudaEventSynchronize(done[k]));
+            std::memcpy(masks + prev_off[k], pin_out[k], prev_cnt[k] * sizeof(uint32_t));
+        }
+        std::memcpy(pin_in[k], boxes + off, cnt * sizeof(cc_tight_box));
+        CC_CUDA(h, cudaMemcpyAsync(d_in[k], pin_in[k], cnt * sizeof(cc_tight_box), cudaMemcpyHostToDevice, h->stream));
+        k_tight_eval<Layout::AoS><<<eval_grid(h, cnt), 128, 0, h->stream>>>((const double*)d_in[k], cnt, (uint32_t*)d_out[k]);
+        CC_LAUNCHED(h);
+        CC_CUDA(h, cudaMemcpyAsync(pin_out[k], d_out[k], cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+        CC_CUDA(h, cudaEventRecord(done[k], h->stream));
+        prev_off[k] = off;
+        prev_cnt[k] = cnt;
+    }
+    for (int j = 0; j < 2; ++j) {
+        if (prev_cnt[j]) {
+            CC_CUDA(h, cudaEventSynchronize(done[j]));
+            std::memcpy(masks + prev_off[j], pin_out[j], prev_cnt[j] * sizeof(uint32_t));
+        }
+    }
+    cudaEventDestroy(done[0]);
+    cudaEventDestroy(done[1]);
+    return CC_OK;
+}
+
+// Diagnostic: measured FP64 instruction throughput of this device in
+// operations per second (one op = one FP64 instruction; an FMA counts 1).
+int cc_selftest_fp64_peak(cc_handle* h, int use_fma, double* ops_per_s) {
+    if (!h || !ops_per_s) return CC_ERR_PARAM;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    void* d;
+    int st = ccrt::ensure(h, 0, 64, &d);
+    if (st) return st;
+    const int blocks = h->sm_count * 8, threads = 256, iters = 4096;
+    cudaEvent_t e0, e1;
+    CC_CUDA(h, cudaEventCreate(&e0));
+    CC_CUDA(h, cudaEventCreate(&e1));
+    k_fp64_peak<<<blocks, threads, 0, h->stream>>>((double*)d, 64, use_fma);  // warm-up
+    CC_LAUNCHED(h);
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+        CC_CUDA(h, cudaEventRecord(e0, h->stream));
+        k_fp64_peak<<<blocks, threads, 0, h->stream>>>((double*)d, iters, use_fma);
+        CC_LAUNCHED(h);
+        CC_CUDA(h, cudaEventRecord(e1, h->stream));
+        CC_CUDA(h, cudaEventSynchronize(e1));
+        float ms = 0;
+        CC_CUDA(h, cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ops_per_s = (double)blocks * threads * iters * 8 / (best * 1e-3);
+    return CC_OK;
+}
+
+// Diagnostic: the device's directed-rounding primitives on host arrays
+// (op: 0 add, 1 mul, 2 div, 3 sqrt, 4 reciprocal; b may be NULL for 3, 4).
+int cc_selftest_round(cc_handle* h, int op, int up, const double* a, const double* b, double* out, size_t n) {
+    if (!h || !a || !out) return CC_ERR_PARAM;
+    h->launches = 0;
+    if (n == 0) return CC_OK;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    void *da, *db, *dout;
+    int st = ccrt::ensure(h, 0, n * 8, &da);
+    if (!st) st = ccrt::ensure(h, 1, n * 8, &db);
+    if (!st) st = ccrt::ensure(h, 2, n * 8, &dout);
+    if (st) return st;
+    CC_CUDA(h, cudaMemcpyAsync(da, a, n * 8, cudaMemcpyHostToDevice, h->stream));
+    if (b) CC_CUDA(h, cudaMemcpyAsync(db, b, n * 8, cudaMemcpyHostToDevice, h->stream));
+    k_selftest_round<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(op, up, (const double*)da, b ? (const double*)db : nullptr,
+                                                                        (double*)dout, n);
+    CC_LAUNCHED(h);
+    CC_CUDA(h, cudaMemcpyAsync(out, dout, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CC_OK;
+}
+
+// Diagnostic: subinterval splits computed (a) with the explicit FMA the
+// prover uses and (b) by the plain expression `lb + diff*i` compiled with
+// nvcc's default contraction (cc_selftest_fmad.cu); out_a/out_b get 2n doubles.
+int cc_selftest_subinterval(cc_handle* h, const double* lo, const double* hi, const int* idx, const int* cnt, size_t n,
+                            double* out_a, double* out_b) {
+    if (!h || !lo || !hi || !idx || !cnt || !out_a || !out_b) return CC_ERR_PARAM;
+    h->launches = 0;
+    if (n == 0) return CC_OK;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    void *dlo, *dhi, *didx, *dcnt, *da, *db;
+    int st = ccrt::ensure(h, 0, n * 8, &dlo);
+    if (!st) st = ccrt::ensure(h, 1, n * 8, &dhi);
+    if (!st) st = ccrt::ensure(h, 2, n * 4, &didx);
+    if (!st) st = ccrt::ensure(h, 3, n * 4, &dcnt);
+    if (!st) st = ccrt::ensure(h, 4, n * 16, &da);
+    if (!st) st = ccrt::ensure(h, 5, n * 16, &db);
+    if (st) return st;
+    CC_CUDA(h, cudaMemcpyAsync(dlo, lo, n * 8, cudaMemcpyHostToDevice, h->stream));
+    CC_CUDA(h, cudaMemcpyAsync(dhi, hi, n * 8, cudaMemcpyHostToDevice, h->stream));
+    CC_CUDA(h, cudaMemcpyAsync(didx, idx, n * 4, cudaMemcpyHostToDevice, h->stream));
+    CC_CUDA(h, cudaMemcpyAsync(dcnt, cnt, n * 4, cudaMemcpyHostToDevice, h->stream));
+    k_selftest_subinterval<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>((const double*)dlo, (const double*)dhi,
+                                                                              (const int*)didx, (const int*)dcnt, (double*)da, n);
+    CC_LAUNCHED(h);
+    st = cc_selftest_subinterval_contracted((const double*)dlo, (const double*)dhi, (const int*)didx, (const int*)dcnt,
+                                            (double*)db, n, h->stream);
+    if (st) return ccrt::fail(h, st, "contracted subinterval kernel");
+    h->launches += 1;
+    CC_CUDA(h, cudaMemcpyAsync(out_a, da, n * 16, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaMemcpyAsync(out_b, db, n * 16, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CC_OK;
+}
+
+}  // extern "C"
+
+// ========================================================= tight proof host
+namespace {
+
+using namespace cc::prove;
+
+// buffer slots in the handle
+enum Slot { S_PARENTS = 6, S_TASKS, S_CELL2, S_CELL3, S_CELL4, S_LEAF, S_CRIT, S_COUNTERS };
+
+struct GenTotals {
+    unsigned long long counts[4][8] = {};
+    unsigned long long digest = 0, leaf_evals = 0, trapped = 0;
+};
+
+int stage_grid(cc_handle* h) { return h->sm_count * 6; }
+
+bool valid_split(int s) { return s >= 1 && s < 2048; }
+
+// merge_adjacent_r1 of one task's critical leaves (tight_rectangle.cu:121-159)
+void merge_by_r1(std::vector<cc_tight_box>& v, std::vector<cc_tight_box>& out) {
+    if (v.empty()) return;
+    std::sort(v.begin(), v.end(), [](const cc_tight_box& a, const cc_tight_box& b) {
+        return a.r[0].lb < b.r[0].lb || (a.r[0].lb == b.r[0].lb && a.r[0].ub < b.r[0].ub);
+    });
+    size_t first = out.size();
+    out.push_back(v.front());
+    for (const cc_tight_box& b : v) {
+        cc_tight_box& p = out.back();
+        bool merge = (p.r[0].lb <= b.r[0].lb) ? (p.r[0].ub >= b.r[0].lb) : (b.r[0].ub >= p.r[0].lb);
+        if (merge) {
+            for (int k = 0; k < 4; ++k) {
+                if (b.r[k].lb < p.r[k].lb) p.r[k].lb = b.r[k].lb;
+                if (b.r[k].ub > p.r[k].ub) p.r[k].ub = b.r[k].ub;
+            }
+            continue;
+        }
+        out.push_back(b);
+    }
+    (void)first;
+}
+
+// One chunk of parents [a, b) of a generation; returns CC_QUEUE_OVERFLOW
+// (without side effects on `out`/`tot`) when a device queue ran full.
+int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, size_t b, int k, const int s[4], Caps caps,
+              std::vector<cc_tight_box>& out, GenTotals& tot, unsigned long long task_base) {
+    const size_t np = b - a;
+    const size_t ntasks = np * (size_t)k;
+    void *d_par, *d_tasks, *d_c2, *d_c3, *d_c4, *d_leaf, *d_crit, *d_cnt;
+    int st;
+    if ((st = ccrt::ensure(h, S_PARENTS, np * sizeof(cc_tight_box), &d_par))) return st;
+    if ((st = ccrt::ensure(h, S_TASKS, ntasks * sizeof(Task), &d_tasks))) return st;
+    if ((st = ccrt::ensure(h, S_CELL2, caps.cell2 * sizeof(Cell2), &d_c2))) return st;
+    if ((st = ccrt::ensure(h, S_CELL3, caps.cell3 * sizeof(Cell3), &d_c3))) return st;
+    if ((st = ccrt::ensure(h, S_CELL4, caps.cell4 * sizeof(Cell4), &d_c4))) return st;
+    if ((st = ccrt::ensure(h, S_LEAF, caps.leaf * sizeof(Leaf), &d_leaf))) return st;
+    if ((st = ccrt::ensure(h, S_CRIT, caps.crit * sizeof(Critical), &d_crit))) return st;
+    if ((st = ccrt::ensure(h, S_COUNTERS, sizeof(Counters), &d_cnt))) return st;
+    Counters* cnt = (Counters*)d_cnt;
+    cudaStream_t sm = h->stream;
+    CC_CUDA(h, cudaMemcpyAsync(d_par, parents.data() + a, np * sizeof(cc_tight_box), cudaMemcpyHostToDevice, sm));
+    CC_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(Counters), sm));
+    const int g = stage_grid(h);
+    k_tasks<<<(unsigned)((ntasks + 127) / 128), 128, 0, sm>>>((const Box*)d_par, (int)np, k, (Task*)d_tasks);
+    CC_LAUNCHED(h);
+    k_stage1<<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (int)ntasks, s[0], (Cell2*)d_c2, caps, cnt, task_base);
+    CC_LAUNCHED(h);
+    k_stage2<<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell2*)d_c2, s[1], (Cell3*)d_c3, caps, cnt,
+                                task_base);
+    CC_LAUNCHED(h);
+    k_stage3<<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell3*)d_c3, s[2], (Cell4*)d_c4, caps, cnt,
+                                task_base);
+    CC_LAUNCHED(h);
+    k_stage4a<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf, caps, cnt, task_base);
+    CC_LAUNCHED(h);
+    k_stage4b<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3], (Critical*)d_crit, caps,
+                                 cnt, task_base);
+    CC_LAUNCHED(h);
+    Counters hc;
+    CC_CUDA(h, cudaMemcpyAsync(&hc, cnt, sizeof(Counters), cudaMemcpyDeviceToHost, sm));
+    CC_CUDA(h, cudaStreamSynchronize(sm));
+    if (hc.overflow) return CC_ERR_QUEUE_OVERFLOW;
+    std::vector<Critical> crit(hc.n_crit);
+    if (hc.n_crit) {
+        CC_CUDA(h, cudaMemcpyAsync(crit.data(), d_crit, hc.n_crit * sizeof(Critical), cudaMemcpyDeviceToHost, sm));
+        CC_CUDA(h, cudaStreamSynchronize(sm));
+    }
+    // group by task (counting sort keeps the per-task lists contiguous)
+    std::vector<size_t> start(ntasks + 1, 0);
+    for (const Critical& c : crit) start[(size_t)c.task + 1] += 1;
+    for (size_t t = 0; t < ntasks; ++t) start[t + 1] += start[t];
+    std::vector<cc_tight_box> sorted(crit.size());
+    std::vector<size_t> fill(start.begin(), start.end() - 1);
+    unsigned long long trapped = 0;
+    for (const Critical& c : crit) {
+        cc_tight_box bx;
+        static_assert(sizeof(bx) == sizeof(c.box), "box layout");
+        std::memcpy(&bx, &c.box, sizeof(bx));
+        sorted[fill[c.task]++] = bx;
+        trapped += c.flags ? 1 : 0;
+    }
+    std::vector<cc_tight_box> one;
+    for (size_t t = 0; t < ntasks; ++t) {
+        if (start[t] == start[t + 1]) continue;
+        one.assign(sorted.begin() + start[t], sorted.begin() + start[t + 1]);
+        merge_by_r1(one, out);
+    }
+    for (int l = 0; l < 4; ++l)
+        for (int o = 0; o < 8; ++o) tot.counts[l][o] += hc.counts[l][o];
+    tot.digest += hc.digest;
+    tot.leaf_evals += hc.leaf_evals;
+    tot.trapped += trapped;
+    return CC_OK;
+}
+
+// all tasks of one generation, in parent chunks that fit the device queues
+int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k, const int s[4],
+                   std::vector<cc_tight_box>& out, GenTotals& tot, Caps& caps) {
+    const size_t max_tasks_chunk = 1 << 16;
+    size_t a = 0;
+    size_t chunk = std::max<size_t>(1, max_tasks_chunk / (size_t)k);
+    while (a < parents.size()) {
+        size_t b = std::min(parents.size(), a + chunk);
+        Caps cp = caps;
+        cp.cell2 = (unsigned long long)(b - a) * k * s[0];
+        std::vector<cc_tight_box> part;
+        GenTotals t;
+        int st = run_chunk(h, parents, a, b, k, s, cp, part, t, (unsigned long long)a * k);
+        if (st == CC_ERR_QUEUE_OVERFLOW) {
+            if (b - a > 1) {
+                chunk = std::max<size_t>(1, (b - a) / 2);
+            } else {
+                caps.cell3 *= 2;
+                caps.cell4 *= 2;
+                caps.leaf *= 2;
+                caps.crit *= 2;
+                if (caps.cell4 > (1ULL << 31)) return ccrt::fail(h, CC_ERR_QUEUE_OVERFLOW, "tight proof: one box exceeds the queue limit");
+            }
+            continue;
+        }
+        if (st) return st;
+        out.insert(out.end(), part.begin(), part.end());
+        for (int l = 0; l < 4; ++l)
+            for (int o = 0; o < 8; ++o) tot.counts[l][o] += t.counts[l][o];
+        tot.digest += t.digest;
+        tot.leaf_evals += t.leaf_evals;
+        tot.trapped += t.trapped;
+        a = b;
+    }
+    return CC_OK;
+}
+
+}  // namespace
+
+extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, cc_tight_box** criticals,
+                              size_t* n_crit, cc_prove_stats* stats) {
+    if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
+    if (grid->la_splits_init < 1 || grid->num_generations < 0 || grid->num_generations > CC_MAX_GENERATIONS)
+        return ccrt::fail(h, CC_ERR_PARAM, "grid: bad lambda splits or generation count");
+    for (int k = 0; k < 4; ++k)
+        if (!valid_split(grid->r_splits_init[k]) || (grid->num_generations && !valid_split(grid->r_splits_gen[k])))
+            return ccrt::fail(h, CC_ERR_PARAM, "grid: radius splits must be in [1, 2047]");
+    for (int g = 0; g < grid->num_generations; ++g)
+        if (grid->la_splits_gen[g] < 1) return ccrt::fail(h, CC_ERR_PARAM, "grid: bad lambda splits");
+    *criticals = nullptr;
+    *n_crit = 0;
+    h->launches = 0;
+    h->interrupt.store(0);
+    CC_CUDA(h, cudaSetDevice(h->device));
+    auto t0 = std::chrono::steady_clock::now();
+
+    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 20};
+    GenTotals tot;
+    std::vector<cc_tight_box> cur{*root}, next;
+    uint64_t gen_sizes[CC_MAX_GENERATIONS + 1] = {};
+    int gens_run = 0;
+    int status = CC_OK;
+    for (int g = 0; g <= grid->num_generations; ++g) {
+        if (g > 0 && cur.empty()) break;
+        const int k = g == 0 ? grid->la_splits_init : grid->la_splits_gen[g - 1];
+        const int* s = g == 0 ? grid->r_splits_init : grid->r_splits_gen;
+        next.clear();
+        int st = run_generation(h, cur, k, s, next, tot, caps);
+        if (st) return st;
+        cur.swap(next);
+        gen_sizes[g] = cur.size();
+        gens_run = g;
+        if (h->interrupt.load()) {
+            status = CC_ERR_INTERRUPTED;
+            break;
+        }
+    }
+    *n_crit = cur.size();
+    *criticals = (cc_tight_box*)std::malloc(sizeof(cc_tight_box) * (cur.size() + 1));
+    if (!*criticals) return ccrt::fail(h, CC_ERR_OOM, "malloc criticals");
+    if (!cur.empty()) std::memcpy(*criticals, cur.data(), sizeof(cc_tight_box) * cur.size());
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        std::memcpy(stats->counts, tot.counts, sizeof(stats->counts));
+        stats->digest = tot.digest;
+        stats->leaf_evals = tot.leaf_evals;
+        stats->trapped_leaves = tot.trapped;
+        std::memcpy(stats->gen_sizes, gen_sizes, sizeof(gen_sizes));
+        stats->generations_run = gens_run;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        stats->kernel_launches = h->launches;
+    }
+    return status;
+}
+
+extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_tight_summary_t* out) {
+    if (!h || !out || (n && !criticals)) return CC_ERR_PARAM;
+    h->launches = 0;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    void *d_in = nullptr, *d_out = nullptr;
+    int st;
+    if ((st = ccrt::ensure(h, 0, (n + 1) * sizeof(cc_tight_box), &d_in))) return st;
+    if ((st = ccrt::ensure(h, 1, sizeof(cc_tight_summary_t), &d_out))) return st;
+    if (n) CC_CUDA(h, cudaMemcpyAsync(d_in, criticals, n * sizeof(cc_tight_box), cudaMemcpyHostToDevice, h->stream));
+    cc::summary::k_summary<<<1, 1, 0, h->stream>>>((const cc::tight::Box*)d_in, n, (cc_tight_summary_t*)d_out);
+    CC_LAUNCHED(h);
+    CC_CUDA(h, cudaMemcpyAsync(out, d_out, sizeof(cc_tight_summary_t), cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CC_OK;
+}

@@ -1,0 +1,98 @@
+// Host-side runtime of the C ABI: the handle (one device, one stream, owned
+// device buffers), CUDA error capture and launch accounting.  The reference's
+// counterpart is its RAII wrapper algcuda::device::Memory<T> plus
+// throw_if_cuda_error (algcuda/cuda-cpp-wrapper/include/algcuda/memory.hpp:
+// 39-110, error.hpp:84-98); here errors become status codes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <string>
+
+#include "../../include/circlecover_gb300.h"
+
+struct cc_handle {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    uint64_t launches = 0;
+    std::atomic<int> interrupt{0};
+
+    // growable device scratch buffers, keyed by purpose
+    struct Buf {
+        void* ptr = nullptr;
+        size_t bytes = 0;
+    };
+    Buf bufs[24];
+    // pinned host staging for the host-memory entry points
+    void* pinned = nullptr;
+    size_t pinned_bytes = 0;
+};
+
+namespace ccrt {
+
+inline int fail(cc_handle* h, int status, const char* what, cudaError_t e = cudaSuccess) {
+    if (h) {
+        h->last_error = what;
+        if (e != cudaSuccess) {
+            h->last_error += ": ";
+            h->last_error += cudaGetErrorString(e);
+        }
+    }
+    return status;
+}
+
+#define CC_CUDA(h, call)                                                              \
+    do {                                                                              \
+        cudaError_t cc_e_ = (call);                                                   \
+        if (cc_e_ != cudaSuccess) return ccrt::fail((h), CC_ERR_CUDA, #call, cc_e_); \
+    } while (0)
+
+#define CC_LAUNCHED(h)                                                                  \
+    do {                                                                                \
+        cudaError_t cc_e_ = cudaGetLastError();                                         \
+        if (cc_e_ != cudaSuccess) return ccrt::fail((h), CC_ERR_CUDA, "launch", cc_e_); \
+        (h)->launches += 1;                                                             \
+    } while (0)
+
+// grow-only device buffer; contents are not preserved
+inline int ensure(cc_handle* h, int slot, size_t bytes, void** out) {
+    cc_handle::Buf& b = h->bufs[slot];
+    if (b.bytes < bytes) {
+        if (b.ptr) {
+            cudaFree(b.ptr);
+            b.ptr = nullptr;
+            b.bytes = 0;
+        }
+        size_t want = bytes + bytes / 4 + 4096;
+        cudaError_t e = cudaMalloc(&b.ptr, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, CC_ERR_OOM, "cudaMalloc", e);
+        }
+        b.bytes = want;
+    }
+    *out = b.ptr;
+    return CC_OK;
+}
+
+inline int ensure_pinned(cc_handle* h, size_t bytes) {
+    if (h->pinned_bytes < bytes) {
+        if (h->pinned) cudaFreeHost(h->pinned);
+        h->pinned = nullptr;
+        h->pinned_bytes = 0;
+        cudaError_t e = cudaMallocHost(&h->pinned, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, CC_ERR_OOM, "cudaMallocHost", e);
+        }
+        h->pinned_bytes = bytes;
+    }
+    return CC_OK;
+}
+
+}  // namespace ccrt

@@ -1,0 +1,660 @@
+// Covering-strategy criteria of the tight-rectangle proof: a lambda x 1
+// rectangle, lambda in [1, 2.0898841580413818342], is to be covered by disks
+// whose total weight (sum of squared radii) is the critical amount
+// required_weight_for(lambda).  Every predicate returns true only if its
+// covering strategy is certified by outward-rounded FP64 interval arithmetic.
+//
+// Each function restates the reference function cited next to it with the
+// same sequence of directed-rounding operations, so verdicts are
+// bit-identical; the structure (names, early exits that cannot change a
+// result, hoisted constants) is this project's own.
+#pragma once
+
+#include "cc_sb_common.cuh"
+
+namespace cc {
+namespace tight {
+
+// A box of the tight proof: aspect ratio and the four largest squared radii
+// (reference: tight_rectangle/strategies.cuh:33-50, same 80-byte layout).
+struct Box {
+    Iv la;
+    Iv r[4];
+};
+
+// Break-even aspect ratio lambda_2 = sqrt(sqrt(7)/2 - 1/4) between the
+// three-disk and the two-disk worst case, as outward-rounded bounds
+// (critical_ratio.cu:60-61 recomputes these on every call).
+CC_FN double break_even_lo() { return sqrt_dn(add_dn(mul_dn(0.5, sqrt_dn(7.0)), -0.25)); }
+CC_FN double break_even_hi() { return sqrt_up(add_up(mul_up(0.5, sqrt_up(7.0)), -0.25)); }
+
+// Worst-case covering ratio (weight per area) of a lambda x 1 rectangle,
+// lambda >= 1 (critical_ratio.cu:58-78):
+//   lambda <= lambda_2:  (3/256)/lambda * (16 lambda^2 + 40 + 9/lambda^2)
+//   lambda >= lambda_2:  lambda/4 + 1/(2 lambda)
+CC_FN Iv ratio_three_disk(Iv la) {
+    Iv la2 = square(la);
+    return ((3.0 / 256.0) / la) * (16.0 * la2 + 40.0 + 9.0 / la2);
+}
+CC_FN Iv ratio_two_disk(Iv la) { return 0.25 * la + 0.5 * reciprocal(la); }
+
+CC_FN Iv critical_ratio(Iv la) {
+    const double be_lo = break_even_lo();
+    const double be_hi = break_even_hi();
+    if (definitely(la <= be_lo)) {
+        return ratio_three_disk(la);
+    }
+    if (definitely(la >= be_hi)) {
+        return ratio_two_disk(la);
+    }
+    Iv a = ratio_three_disk(la);
+    Iv b = ratio_two_disk(la);
+    return Iv{a.lo < b.lo ? a.lo : b.lo, a.hi < b.hi ? b.hi : a.hi};
+}
+
+// ratio for a w x h rectangle in either orientation (critical_ratio.cu:32-52)
+CC_FN Iv critical_ratio(Iv w, Iv h) {
+    if (w.hi <= h.lo) {
+        return critical_ratio(h / w);
+    }
+    if (h.hi <= w.lo) {
+        return critical_ratio(w / h);
+    }
+    Iv tall = h / w;
+    tighten_lb(tall, 1.0);
+    Iv wide = w / h;
+    tighten_lb(wide, 1.0);
+    Iv a = critical_ratio(tall);
+    Iv b = critical_ratio(wide);
+    return Iv{a.lo < b.lo ? a.lo : b.lo, a.hi < b.hi ? b.hi : a.hi};
+}
+
+CC_FN Iv required_weight_for(Iv w, Iv h) { return critical_ratio(w, h) * w * h; }  // critical_ratio.cu:80-82
+CC_FN Iv required_weight_for(Iv la) { return critical_ratio(la) * la; }            // critical_ratio.cu:84-86
+
+// can_apply_size_bounded_covering.cu:49-52
+CC_FN double required_weight_for_bounded_size(double ub_w, double ub_h) {
+    return mul_up(sb::kCriticalRatio, mul_up(ub_w, ub_h));
+}
+
+// Can a rectangle of at most ub_w x ub_h be covered recursively by disks of
+// weight <= ub_largest and total weight >= lb_weight?  Best of the worst-case
+// ratio, the size-bounded corollary and the 9/64 size-bound ratio
+// (can_recurse.cu:32-62).
+CC_FN bool can_recurse(double ub_w, double ub_h, double ub_largest, double lb_weight) {
+    double ub_area = mul_up(ub_w, ub_h);
+    double side_min = ub_w < ub_h ? ub_w : ub_h;
+    double s = rcp_up(side_min);
+    double s_sq = mul_up(s, s);
+    double largest_norm = mul_up(s_sq, ub_largest);
+
+    double ratio;
+    if (largest_norm <= sb::kUbDiskWeight) {
+        // the size-bound ratio replaces whatever was computed before
+        ratio = sb::kCriticalRatio;
+    } else {
+        ratio = critical_ratio(ivp(ub_w), ivp(ub_h)).hi;
+        double ratio_cor = mul_up(0.5, sqrt_up(add_up(sqrt_up(add_up(mul_up(largest_norm, largest_norm), 1.0)), 1.0)));
+        if (ratio_cor < 195.0 / 256) {
+            ratio_cor = 195.0 / 256;
+        }
+        if (ratio > ratio_cor) {
+            ratio = ratio_cor;
+        }
+    }
+    double ub_needed = mul_up(ratio, ub_area);
+    return lb_weight >= ub_needed;
+}
+
+// ------------------------------------------------------------ one disk
+// Place disk 1 as a full-height strip, in a corner, or as an uneven split;
+// recurse on the rest (r1_strategies.cu:27-87).
+CC_FN_INL bool r1_strategies(Iv la, Iv r1, double ub_r2) {
+    double square_w = sqrt_dn(mul_dn(2.0, r1.lo));
+    double strip_w = add_dn(mul_dn(4.0, r1.lo), -1.0);
+    const double lb_rem = (required_weight_for(la) - r1).lo;
+
+    if (strip_w > 0.0) {
+        strip_w = sqrt_dn(strip_w);
+        Iv w_rest = la - strip_w;
+        if (can_recurse(w_rest.hi, 1.0, ub_r2, lb_rem)) {
+            return true;
+        }
+    }
+
+    if (square_w < 1.0) {
+        double w_right = add_up(la.hi, -square_w);
+        double min_right = w_right < 1.0 ? w_right : 1.0;
+        double ub_weight_right;
+        if (sb::disk_satisfies_size_bound(ub_r2, min_right)) {
+            ub_weight_right = mul_up(w_right, sb::kCriticalRatio);
+        } else {
+            ub_weight_right = required_weight_for(ivp(w_right), ivp(1.0)).hi;
+        }
+        ub_weight_right = add_up(ub_weight_right, ub_r2);
+        double lb_rem_top = add_dn(lb_rem, -ub_weight_right);
+        if (lb_rem_top > 0) {
+            double h_top = add_up(1.0, -square_w);
+            if (can_recurse(square_w, h_top, ub_r2, lb_rem_top)) {
+                return true;
+            }
+        }
+    }
+
+    double lb_S1 = add_dn(mul_dn(4.0, r1.lo), -1.0);
+    if (lb_S1 > 0.0) {
+        lb_S1 = sqrt_dn(lb_S1);
+        double t = add_up(la.hi, -mul_dn(0.5, lb_S1));
+        t = mul_up(t, t);
+        double lb_h1 = add_dn(r1.lo, -t);
+        if (lb_h1 > 0.0) {
+            lb_h1 = mul_dn(2.0, sqrt_dn(lb_h1));
+            double ub_pocket_h = mul_up(0.5, add_up(1.0, -lb_h1));
+            double ub_pocket_w = add_up(la.hi, -lb_S1);
+            double lb_rem_half = mul_dn(0.5, add_dn(lb_rem, -ub_r2));
+            if (lb_rem_half > 0 && can_recurse(ub_pocket_w, ub_pocket_h, ub_r2, lb_rem_half)) {
+                return true;
+            }
+        }
+    }
+    return false;
+}
+
+// ----------------------------------------------------------- two disks
+// Region around the two-disk worst case settled by hand in the paper
+// (r1_r2_strategies.cu:29-46).
+CC_FN bool two_pocket_by_hand(Iv la, Iv r1, Iv r2) {
+    if (r2.lo < 0.2400000000000000188 || r1.lo < 0.4900000000000000466) {
+        return false;
+    }
+    Iv la2 = square(la);
+    double r1_need = (0.25 * (la2 + 1.0) - 0.00999999999999999847).hi;
+    if (r1.lo < r1_need) {
+        return false;
+    }
+    Iv S1 = 2.0 * sqrt(r1 - 0.25);
+    Iv pocket = la - S1;
+    tighten_lb(pocket, 0.0);
+    double r2_need = (0.25 + square(pocket) - 0.00999999999999999847).hi;
+    return r2.lo >= r2_need;
+}
+
+// disks 1 and 2 side by side as a strip (r1_r2_strategies.cu:48-72)
+CC_FN bool r1_r2_side_by_side(Iv la, Iv r1, Iv r2, double ub_r3) {
+    if (two_pocket_by_hand(la, r1, r2)) {
+        return true;
+    }
+    double lb_width = sb::two_disks_maximize_height(r1, r2, 1.0);
+    if (lb_width <= 0.0) {
+        return false;
+    }
+    double lb_w2 = add_dn(mul_dn(4.0, r2.lo), -1.0);
+    if (lb_w2 > 0.0) {
+        lb_w2 = sqrt_dn(lb_w2);
+        double lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
+        double lb_w = add_dn(lb_w1, lb_w2);
+        if (lb_w > lb_width) {
+            lb_width = lb_w;
+            if (lb_w > la.hi) {
+                return true;
+            }
+        }
+    }
+    double w_rem = add_dn(la.hi, lb_width);  // sic: '+' (parity)
+    double lb_R3 = (required_weight_for(la) - r1 - r2).lo;
+    return can_recurse(w_rem, 1.0, ub_r3, lb_R3);
+}
+
+// disk 1 in a corner square, disk 2 across the top (r1_r2_strategies.cu:74-129)
+CC_FN bool r1_r2_stacked(Iv la, Iv r1, Iv r2, double ub_r3) {
+    double sq_side = sqrt_dn(mul_dn(2.0, r1.lo));
+    if (sq_side > 1.0) {
+        return false;
+    }
+    double h_top = add_up(1.0, -sq_side);
+    double lb_w2 = add_dn(mul_dn(4.0, r2.lo), -mul_up(h_top, h_top));
+    if (lb_w2 < 0.0) {
+        return false;
+    }
+    lb_w2 = sqrt_dn(lb_w2);
+
+    double w_top = add_up(la.hi, -lb_w2);
+    double w_bot = add_up(la.hi, -sq_side);
+    double top_min = w_top < h_top ? w_top : h_top;
+    double bot_min = w_bot < sq_side ? w_bot : sq_side;
+    double lb_R3 = (required_weight_for(la) - r1 - r2).lo;
+
+    if (sb::disk_satisfies_size_bound(ub_r3, top_min)) {
+        double need_top = add_up(required_weight_for_bounded_size(w_top, h_top), ub_r3);
+        double left = add_dn(lb_R3, -need_top);
+        if (left > 0.0 && can_recurse(w_bot, sq_side, ub_r3, left)) {
+            return true;
+        }
+    } else if (sb::disk_satisfies_size_bound(ub_r3, bot_min)) {
+        double need_bot = add_up(required_weight_for_bounded_size(w_bot, sq_side), ub_r3);
+        double left = add_dn(lb_R3, -need_bot);
+        if (left > 0.0 && can_recurse(w_top, h_top, ub_r3, left)) {
+            return true;
+        }
+    } else {
+        double need_top = required_weight_for(ivp(w_top), ivp(h_top)).hi;
+        need_top = add_up(need_top, ub_r3);
+        double left = add_dn(lb_R3, -need_top);
+        if (left > 0.0) {
+            return can_recurse(w_bot, sq_side, ub_r3, left);
+        }
+    }
+    return false;
+}
+
+// r1_r2_strategies.cu:131-133
+CC_FN_INL bool r1_r2_strategies(Iv la, Iv r1, Iv r2, double ub_r3) {
+    return r1_r2_side_by_side(la, r1, r2, ub_r3) || r1_r2_stacked(la, r1, r2, ub_r3);
+}
+
+// --------------------------------------------------------- three disks
+// three full-height strips (r1_r2_r3_strategies.cu:28-47)
+CC_FN bool r1_r2_r3_three_strips(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
+    double lb_w3 = add_dn(mul_dn(4.0, r3.lo), -1.0);
+    if (lb_w3 <= 0.0) {
+        return false;
+    }
+    lb_w3 = sqrt_dn(lb_w3);
+    double lb_w2 = sqrt_dn(add_dn(mul_dn(4.0, r2.lo), -1.0));
+    double lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
+    double lb_cov = add_dn(lb_w1, add_dn(lb_w2, lb_w3));
+    double lb_R4 = (required_weight_for(la) - r1 - r2 - r3).lo;
+    double ub_rem = add_up(la.hi, -lb_cov);
+    if (ub_rem <= 0.0) {
+        return true;
+    }
+    return can_recurse(ub_rem, 1.0, ub_r4, lb_R4);
+}
+
+// Disk 1 on top of a strip of width w, disks 2 and 3 below it side by side
+// (r1_r2_r3_strategies.cu:49-67).
+CC_FN bool strip_width_realizable(double r1, double r2, double r3, double w) {
+    double h1 = add_dn(mul_dn(4.0, r1), -mul_up(w, w));
+    if (h1 <= 0.0) {
+        return false;
+    }
+    h1 = sqrt_dn(h1);
+    double h_rem = add_up(1.0, -h1);
+    double h_sq = mul_up(h_rem, h_rem);
+    double w2 = add_dn(mul_dn(4.0, r2), -h_sq);
+    double w3 = add_dn(mul_dn(4.0, r3), -h_sq);
+    if (w3 <= 0.0 || w2 <= 0.0) {
+        return false;
+    }
+    w2 = sqrt_dn(w2);
+    w3 = sqrt_dn(w3);
+    return add_dn(w2, w3) >= w;
+}
+
+// widest such strip, by bisection to the FP64 fixpoint (r1_r2_r3_strategies.cu:69-94)
+CC_FN_INL bool r1_r2_r3_cover_strip(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
+    double lo = 0.3;
+    double hi = la.hi;
+    if (!strip_width_realizable(r1.lo, r2.lo, r3.lo, lo)) {
+        return false;
+    }
+    for (int it = 0;; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) {
+            break;
+        }
+        if (it >= CC_BISECTION_CAP) {
+            trap(TRAP_BISECTION_CAP);
+            break;
+        }
+        if (strip_width_realizable(r1.lo, r2.lo, r3.lo, mid)) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    double ub_rem = add_up(la.hi, -lo);
+    double lb_R4 = (required_weight_for(la) - r1 - r2 - r3).lo;
+    return can_recurse(ub_rem, 1.0, ub_r4, lb_R4);
+}
+
+// r1_r2_r3_strategies.cu:96-99
+CC_FN_INL bool r1_r2_r3_strategies(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
+    return r1_r2_r3_three_strips(la, r1, r2, r3, ub_r4) || r1_r2_r3_cover_strip(la, r1, r2, r3, ub_r4);
+}
+
+// Disks 2 and 3 form a strip, disk 1 covers the rest of a column
+// (r1_r2_r3_strategies.cu:101-121).
+CC_FN bool three_disk_big_strip(double ub_la, double r1, double r2, double r3, double ub_r4, double lb_R4) {
+    double S_sq = add_dn(add_dn(mul_dn(2.0, r2), add_dn(mul_dn(2.0, r3), -0.25)),
+                         add_dn(add_dn(-mul_up(4.0, mul_up(r2, r2)), mul_dn(8.0, mul_dn(r2, r3))),
+                                -mul_up(4.0, mul_up(r3, r3))));
+    if (S_sq <= 0.0) {
+        return false;
+    }
+    double S = sqrt_dn(S_sq);
+    double la_rem = add_up(ub_la, -S);
+    double h1_sq = add_dn(mul_dn(4.0, r1), -mul_up(la_rem, la_rem));
+    if (h1_sq <= 0.0) {
+        return false;
+    }
+    if (h1_sq >= 1.0) {
+        return true;
+    }
+    double h_rem = add_up(1.0, -sqrt_dn(h1_sq));
+    return can_recurse(la_rem, h_rem, ub_r4, lb_R4);
+}
+
+// disk 3 in a corner, disks 1 and 2 along its sides (r1_r2_r3_strategies.cu:123-165)
+CC_FN bool three_disk_small_corner(double ub_la, double r1, double r2, double r3, double ub_r4, double lb_R4) {
+    double c3 = sqrt_dn(mul_dn(2.0, r3));
+    if (c3 >= 1.0) {
+        return false;
+    }
+    double la_left = add_up(ub_la, -c3);
+    double la_half = mul_up(la_left, 0.5);
+    double one_left = add_up(1.0, -c3);
+
+    if (la_half <= sqrt_dn(r2)) {
+        double c1 = sqrt_dn(add_dn(mul_dn(4.0, r1), -mul_up(one_left, one_left)));
+        double la_after_1 = add_up(ub_la, -c1);
+        double c2 = sqrt_dn(add_dn(mul_dn(4.0, r2), -mul_up(la_left, la_left)));
+        double one_after_2 = add_up(1.0, -c2);
+        return can_recurse(la_after_1, one_after_2, ub_r4, lb_R4);
+    }
+    if (la_half >= sqrt_dn(r1)) {
+        return false;
+    }
+    if (one_left >= mul_dn(2.0, sqrt_dn(r2))) {
+        return false;
+    }
+    double c2 = sqrt_dn(add_dn(mul_dn(4.0, r2), -mul_up(one_left, one_left)));
+    double la_after_2 = add_up(ub_la, -c2);
+    double c1 = sqrt_dn(add_dn(mul_dn(4.0, r1), -mul_up(la_left, la_left)));
+    double one_after_1 = add_up(1.0, -c1);
+    return can_recurse(la_after_2, one_after_1, ub_r4, lb_R4);
+}
+
+// disks 1 and 3 at the sides, 2 in between, a pocket remains
+// (r1_r2_r3_strategies.cu:167-204)
+CC_FN bool three_disk_r1_r3_pocket(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4, double lb_R4) {
+    if (r1.lo <= 0.25) {
+        return false;
+    }
+    Iv S1 = 2.0 * sqrt(r1 - 0.25);
+    Iv la_m_S1 = la - S1;
+    Iv h2_rest = 0.25 * la_m_S1 * la_m_S1;
+    if (r2.lo <= h2_rest.hi) {
+        return false;
+    }
+    Iv h2 = 2.0 * sqrt(r2 - h2_rest);
+    Iv one_m_h2 = 1.0 - h2;
+    Iv S3_rest = 0.25 * one_m_h2 * one_m_h2;
+    if (r3.lo <= S3_rest.hi) {
+        return false;
+    }
+    Iv S3 = 2.0 * sqrt(r3 - S3_rest);
+    Iv X = la - S1 - S3;
+    if (X.hi <= 0.0) {
+        return true;
+    }
+    Iv t = la - 0.5 * S1 - S3;
+    Iv Y_rest = t * t;
+    if (r1.lo <= Y_rest.hi) {
+        return false;
+    }
+    Iv Y = 0.5 - sqrt(r1 - Y_rest);
+    if (Y.hi <= 0.0) {
+        return true;
+    }
+    return can_recurse(X.hi, Y.hi, ub_r4, lb_R4);
+}
+
+// Region around the three-disk worst case settled by hand in the paper
+// (r1_r2_r3_strategies.cu:206-247).
+CC_FN bool three_disk_pocket_by_hand(Iv la, Iv r1, Iv r2, Iv r3) {
+    if (la.hi > 1.0499999999999998) {
+        return false;
+    }
+    Iv la2 = square(la);
+    Iv rstar = 0.0625 * la2 + 0.15625 + 0.03515625 / la2;
+    Iv d1 = rstar - r1;
+    if (d1.lo < -0.0009999999999999998 || d1.hi > 0.0009999999999999998) {
+        return false;
+    }
+    Iv d2 = rstar - r2;
+    if (d2.lo < -0.0019999999999999996 || d2.hi > 0.0019999999999999996) {
+        return false;
+    }
+    Iv d3 = rstar - r3;
+    if (d3.lo < -0.0029999999999999996 || d3.hi > 0.0029999999999999996) {
+        return false;
+    }
+    Iv S1 = 2.0 * sqrt(r1 - 0.25);
+    Iv la_m_S1 = la - S1;
+    Iv h2_rest = 0.25 * la_m_S1 * la_m_S1;
+    if (r2.lo <= h2_rest.hi) {
+        return false;
+    }
+    Iv h2 = 2.0 * sqrt(r2 - h2_rest);
+    Iv one_m_h2 = 1.0 - h2;
+    Iv S3_rest = 0.25 * one_m_h2 * one_m_h2;
+    if (r3.lo <= S3_rest.hi) {
+        return false;
+    }
+    Iv S3 = 2.0 * sqrt(r3 - S3_rest);
+    Iv X = la - S1 - S3;
+    return !(X.hi > 0.046999999999999993);
+}
+
+// r1_r2_r3_strategies.cu:249-260
+CC_FN_INL bool r1_r2_r3_strategies(const Box& b, Iv R4) {
+    const double ub_la = b.la.hi;
+    const double r1 = b.r[0].lo, r2 = b.r[1].lo, r3 = b.r[2].lo;
+    const double ub_r4 = b.r[3].hi;
+    const double lb_R4 = R4.lo;
+    return three_disk_big_strip(ub_la, r1, r2, r3, ub_r4, lb_R4) ||
+           three_disk_small_corner(ub_la, r1, r2, r3, ub_r4, lb_R4) ||
+           three_disk_r1_r3_pocket(b.la, b.r[0], b.r[1], b.r[2], ub_r4, lb_R4) ||
+           three_disk_pocket_by_hand(b.la, b.r[0], b.r[1], b.r[2]);
+}
+
+// ------------------------------------------------------------ 2 x 2
+// disk 1 as a full-height strip, disks 2..4 stacked beside it
+// (two_by_two_strategies.cu:29-53)
+CC_FN bool two_by_two_r1_large(const Box& b, Iv R) {
+    double w1 = sqrt_dn(add_dn(mul_dn(4.0, b.r[0].lo), -1.0));
+    double w_rem = add_up(b.la.hi, -w1);
+    double w_rem_sq = mul_up(w_rem, w_rem);
+    double h4 = add_dn(mul_dn(4.0, b.r[3].lo), -w_rem_sq);
+    if (h4 <= 0.0) {
+        return false;
+    }
+    h4 = sqrt_dn(h4);
+    double h3 = sqrt_dn(add_dn(mul_dn(4.0, b.r[2].lo), -w_rem_sq));
+    double h2 = sqrt_dn(add_dn(mul_dn(4.0, b.r[1].lo), -w_rem_sq));
+    double h_tot = add_dn(h2, add_dn(h3, h4));
+    if (h_tot >= 1.0) {
+        return true;
+    }
+    double h_rem = add_up(1.0, -h_tot);
+    double ub_r5 = b.r[3].hi < R.hi ? b.r[3].hi : R.hi;
+    return can_recurse(w_rem, h_rem, ub_r5, R.lo);
+}
+
+// disk 1 in a corner, 2 beside, 4 above, 3 in the opposite corner
+// (two_by_two_strategies.cu:55-86)
+CC_FN bool two_by_two_lambda_small(const Box& b, Iv R) {
+    double sq_side = sqrt_dn(mul_dn(2.0, b.r[0].lo));
+    if (sq_side >= 1.0) {
+        return two_by_two_r1_large(b, R);
+    }
+    double w_rem = add_up(b.la.hi, -sq_side);
+    double h_rem = add_up(1.0, -sq_side);
+    double h2 = add_dn(mul_dn(4.0, b.r[1].lo), -mul_up(w_rem, w_rem));
+    double w4 = add_dn(mul_dn(4.0, b.r[3].lo), -mul_up(h_rem, h_rem));
+    if (h2 <= 0.0 || w4 <= 0.0) {
+        return false;
+    }
+    h2 = sqrt_dn(h2);
+    w4 = sqrt_dn(w4);
+    if (w4 > sq_side) w4 = sq_side;
+    if (h2 > sq_side) h2 = sq_side;
+    double h = add_up(1.0, -h2);
+    double w = add_up(b.la.hi, -w4);
+    double diag = add_up(mul_up(h, h), mul_up(w, w));
+    return mul_dn(4.0, b.r[2].lo) >= diag;
+}
+
+// best pairing of the four disks into two full-height pairs
+// (two_by_two_strategies.cu:88-111)
+CC_FN bool two_by_two_lambda_big(const Box& b, Iv R) {
+    double lb_w = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[1], 1.0),
+                         sb::two_disks_maximize_height(b.r[2], b.r[3], 1.0));
+    double w_1423 = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[3], 1.0),
+                           sb::two_disks_maximize_height(b.r[1], b.r[2], 1.0));
+    if (w_1423 > lb_w) lb_w = w_1423;
+    double w_1324 = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[2], 1.0),
+                           sb::two_disks_maximize_height(b.r[1], b.r[3], 1.0));
+    if (w_1324 > lb_w) lb_w = w_1324;
+    if (lb_w <= 0.0) {
+        return false;
+    }
+    double ub_r5 = R.hi < b.r[3].hi ? R.hi : b.r[3].hi;
+    return can_recurse(add_up(b.la.hi, -lb_w), 1.0, ub_r5, R.lo);
+}
+
+// two_by_two_strategies.cu:113-115
+CC_FN_INL bool two_by_two_strategies(const Box& b, Iv R) {
+    return two_by_two_lambda_small(b, R) || two_by_two_lambda_big(b, R);
+}
+
+// ---------------------------------------------- gap closed by disk 4
+// Disks 1 and 2 as strips with a gap of width g between them; the gap is
+// closed at the bottom by disk 4 (and symmetrically at the top by disk 3)
+// (r1_r2_large_r3_r4_gaps_strategy.cu:29-59).
+CC_FN bool gap_width_realizable(double g, double r1, double w1, double r2, double w2, double r4) {
+    Iv y4 = r4 - 0.25 * ivp(g) * g;
+    if (possibly(y4 <= 0.0)) {
+        return false;
+    }
+    Iv x1 = ivp(0.5) * w1;
+    Iv x2 = ivp(0.5) * w2 + g + w1;
+    Circle c1{Point{x1, ivp(0.5)}, ivp(r1)};
+    Circle c2{Point{x2, ivp(0.5)}, ivp(r2)};
+    Isect x12 = intersection(c1, c2);
+    if (!x12.definitely_intersecting) {
+        return false;
+    }
+    Ub first_lower = x12.p[0].y <= x12.p[1].y;
+    if (!is_certain(first_lower)) {
+        return false;
+    }
+    Iv x4 = ivp(0.5) * g + w1;
+    y4 = sqrt(y4);
+    Point p4{x4, y4};
+    const Point& px = x12.p[first_lower.lo ? 0 : 1];
+    return definitely(squared_distance(p4, px) <= r4);
+}
+
+// widest gap by bisection, then recurse on the rest of the rectangle
+// (r1_r2_large_r3_r4_gaps_strategy.cu:61-98)
+CC_FN_INL bool r1_r2_large_r3_r4_gaps_strategy(const Box& b, Iv R) {
+    const double r1 = b.r[0].lo;
+    const double r2 = b.r[1].lo;
+    const double r4 = b.r[3].lo;
+    double w1 = add_dn(mul_dn(4.0, r1), -1.0);
+    double w2 = add_dn(mul_dn(4.0, r2), -1.0);
+    if (w1 <= 0.0 || w2 <= 0.0) {
+        return false;
+    }
+    w1 = sqrt_dn(w1);
+    w2 = sqrt_dn(w2);
+
+    double lo = 0.0, hi = add_dn(sqrt_dn(r1), sqrt_dn(r2));
+    for (int it = 0;; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) {
+            break;
+        }
+        if (it >= CC_BISECTION_CAP) {
+            trap(TRAP_BISECTION_CAP);
+            break;
+        }
+        if (gap_width_realizable(mid, r1, w1, r2, w2, r4)) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    double w_tot = add_dn(w1, add_dn(lo, w2));
+    double w_rem = add_up(b.la.hi, -w_tot);
+    if (w_rem <= 0.0) {
+        return true;
+    }
+    double ub_r5 = R.hi;
+    if (ub_r5 > b.r[3].hi) {
+        ub_r5 = b.r[3].hi;
+    }
+    return can_recurse(w_rem, 1.0, ub_r5, R.lo);
+}
+
+// --------------------------------------------------- range of each radius
+// feasible ranges for r1..r4 given lambda (reference: tight_rectangle.cu:72-102)
+CC_FN Iv r1_range(Iv la) {
+    double f = div_dn(critical_ratio(la).lo, sb::kCriticalRatio);
+    if (f <= 1.0) {
+        f = 1.0;
+    }
+    double lo = mul_dn(sb::kUbDiskWeight, f);
+    double hi = mul_up(0.25, add_up(1.0, mul_up(la.hi, la.hi)));
+    return Iv{lo, hi};
+}
+CC_FN Iv r2_range(Iv weight, Iv r1) {
+    double u1 = r1.hi;
+    double u2 = (weight - r1).hi;
+    return Iv{0.0, u1 < u2 ? u1 : u2};
+}
+CC_FN Iv r3_range(Iv weight, Iv r1, Iv r2) {
+    double u1 = r2.hi;
+    double u2 = (weight - r1 - r2).hi;
+    return Iv{0.0, u1 < u2 ? u1 : u2};
+}
+CC_FN Iv r4_range(Iv weight, Iv r1, Iv r2, Iv r3) {
+    double u1 = r3.hi;
+    double u2 = (weight - r1 - r2 - r3).hi;
+    return Iv{0.0, u1 < u2 ? u1 : u2};
+}
+
+// ------------------------------------------------ per-box verdict mask
+// All six exported criteria at the arguments the reference's leaf passes
+// them (tight_rectangle.cu:229-248): the first three on the box as given,
+// the last three on the box with lower bounds tightened (r3 >= r4 >= ...)
+// and with the remaining weights R (all four disks) and R4 (first three).
+// Bit layout: CC_TV_* in include/circlecover_gb300.h.
+CC_FN_INL uint32_t eval_all(const Box& in) {
+    trap_clear();
+    const Iv la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2], r4 = in.r[3];
+    Iv weight = required_weight_for(la);
+    uint32_t m = 0;
+    if (r1_strategies(la, r1, r2.hi)) m |= 1u << 0;
+    if (r1_r2_strategies(la, r1, r2, r3.hi)) m |= 1u << 1;
+    if (r1_r2_r3_strategies(la, r1, r2, r3, r4.hi)) m |= 1u << 2;
+    Iv R4 = weight - r1 - r2 - r3;
+    tighten_lb(R4, 0.0);
+    Box v{la, {r1, r2, r3, r4}};
+    tighten_lb(v.r[2], v.r[3].lo);
+    tighten_lb(v.r[1], v.r[2].lo);
+    tighten_lb(v.r[0], v.r[1].lo);
+    Iv R = weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+    tighten_lb(R, 0.0);
+    if (two_by_two_strategies(v, R)) m |= 1u << 3;
+    if (r1_r2_r3_strategies(v, R4)) m |= 1u << 4;
+    if (r1_r2_large_r3_r4_gaps_strategy(v, R)) m |= 1u << 5;
+    if (empty(R4) || empty(R)) m |= 1u << 6;
+    if (trap_status() != TRAP_NONE) m |= 1u << 31;
+    return m;
+}
+
+}  // namespace tight
+}  // namespace cc

@@ -1,0 +1,409 @@
+// Device engine of the tight-rectangle proof (reference:
+// tight_rectangle/tight_rectangle.cu:161-320 and 458-498).
+//
+// The reference launches one kernel per lambda box, each a fixed
+// (r1,r2)-blocks x (r3,r4)-threads grid in which every thread re-evaluates
+// the outer checks, with a host synchronisation after every launch.  Here all
+// lambda boxes ("tasks") of a generation go through the same five stages, one
+// persistent-grid kernel each, in stream order without host synchronisation:
+//
+//   stage 1  (task, i1)        r1 cells:  r2 range, r1_strategies
+//   stage 2  (r1 cell, i2)     r2 cells:  r1_strategies, r3 range, r1_r2_strategies
+//   stage 3  (r2 cell, i3)     r3 cells:  r1_r2_strategies, r4 range, r1_r2_r3_strategies, R4
+//   stage 4a (r3 cell, i4)     leaves:    r1_r2_r3_strategies, R, two_by_two
+//   stage 4b (leaf queue)      leaves:    r1_r2_r3_strategies(box, R4), gaps
+//
+// Each stage reads its item count from device memory and appends survivors
+// to the next stage's queue with one atomic per warp (warp-aggregated
+// atomics).  The expensive leaf strategies run in stage 4b on a compacted
+// queue, so a warp evaluates them on 32 leaves that all need them.
+// Critical leaves carry their task index; the host merges them per task by r1
+// (merge_adjacent_r1, tight_rectangle.cu:121-159), which restores the
+// reference's order exactly.
+//
+// Every grid cell visited contributes one (level, outcome) count and
+// mix64(key) to a digest; the oracle computes the same trace.
+#pragma once
+
+#include "cc_tight.cuh"
+
+namespace cc {
+namespace prove {
+
+using tight::Box;
+
+struct Task {
+    Iv la, weight, r1r;
+    int parent;
+    int live;  // r1r not empty
+};
+
+struct Cell2 {  // a surviving r1 cell
+    Iv r1, r2r;
+    int task, i1;
+};
+
+struct Cell3 {  // a surviving r2 cell
+    Iv r1, r2, r3r;
+    int task;
+    int16_t i1, i2;
+};
+
+struct Cell4 {  // a surviving r3 cell
+    Iv r1, r2, r3, r4r, R4;
+    int task;
+    int16_t i1, i2, i3, pad;
+};
+
+struct Leaf {  // a leaf that survived stage 4a
+    uint32_t cell4;
+    uint16_t i4;
+    uint16_t trapped;
+};
+
+struct Critical {
+    Box box;
+    int task;
+    uint32_t flags;
+};
+
+struct Counters {
+    unsigned long long n_cell2, n_cell3, n_cell4, n_leaf, n_crit;
+    unsigned long long overflow;
+    unsigned long long leaf_evals;
+    unsigned long long digest;
+    unsigned long long counts[4][8];
+};
+
+struct Caps {
+    unsigned long long cell2, cell3, cell4, leaf, crit;
+};
+
+CC_FN uint64_t mix64(uint64_t x) {
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ULL;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebULL;
+    x ^= x >> 31;
+    return x;
+}
+
+// same packing as the oracle's trace_key
+CC_FN uint64_t trace_key(uint64_t task, int level, int i1, int i2, int i3, int i4, int outcome) {
+    uint64_t packed = ((uint64_t)outcome) | ((uint64_t)i4 << 4) | ((uint64_t)i3 << 15) | ((uint64_t)i2 << 26) |
+                      ((uint64_t)i1 << 37) | ((uint64_t)level << 48);
+    return mix64(packed ^ mix64(task + 0x9e3779b97f4a7c15ULL));
+}
+
+#if CC_DEVICE_BUILD
+
+// per-block trace accumulation in shared memory, flushed once per block
+struct BlockTrace {
+    unsigned long long counts[8];
+    unsigned long long digest;
+};
+
+__device__ __forceinline__ void trace_init(BlockTrace& bt) {
+    if (threadIdx.x < 8) bt.counts[threadIdx.x] = 0;
+    if (threadIdx.x == 0) bt.digest = 0;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void trace_note(BlockTrace& bt, bool valid, uint64_t key, int outcome) {
+    // warp-reduce the digest, shared atomics for the counts
+    uint64_t d = valid ? key : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&bt.digest, (unsigned long long)d);
+    if (valid) atomicAdd(&bt.counts[outcome], 1ULL);
+}
+
+__device__ __forceinline__ void trace_flush(BlockTrace& bt, Counters* c, int level) {
+    __syncthreads();
+    if (threadIdx.x < 8 && bt.counts[threadIdx.x]) atomicAdd(&c->counts[level][threadIdx.x], bt.counts[threadIdx.x]);
+    if (threadIdx.x == 0 && bt.digest) atomicAdd(&c->digest, bt.digest);
+}
+
+// Warp-aggregated append: every lane of the warp calls this (full mask);
+// lanes with `want` get consecutive slots.  Returns the slot or ~0 if the
+// queue is full (then the overflow flag is raised and nothing is written).
+__device__ __forceinline__ unsigned long long warp_append(unsigned long long* counter, bool want, unsigned long long cap,
+                                                          unsigned long long* overflow) {
+    const unsigned lane = threadIdx.x & 31;
+    unsigned ballot = __ballot_sync(0xffffffffu, want);
+    if (ballot == 0) return ~0ULL;
+    unsigned long long base = 0;
+    if (lane == (unsigned)(__ffs(ballot) - 1)) base = atomicAdd(counter, (unsigned long long)__popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
+    unsigned long long slot = base + __popc(ballot & ((1u << lane) - 1));
+    if (!want) return ~0ULL;
+    if (slot >= cap) {
+        atomicExch(overflow, 1ULL);
+        return ~0ULL;
+    }
+    return slot;
+}
+
+// stage 0: one thread per task
+__global__ void k_tasks(const Box* __restrict__ parents, int n_parents, int la_splits, Task* __restrict__ tasks) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_parents * la_splits) return;
+    trap_clear();
+    int p = t / la_splits;
+    int k = t % la_splits;
+    Task tk;
+    tk.la = subinterval(parents[p].la, k, la_splits);
+    tk.weight = tight::required_weight_for(tk.la);
+    tk.r1r = intersect(tight::r1_range(tk.la), parents[p].r[0]);
+    tk.parent = p;
+    tk.live = !empty(tk.r1r);
+    tasks[t] = tk;
+}
+
+// stage 1: r1 cells (tight_rectangle.cu:182-191)
+__global__ void __launch_bounds__(128) k_stage1(const Box* __restrict__ parents, const Task* __restrict__ tasks, int n_tasks,
+                                                int s1, Cell2* __restrict__ out, Caps caps, Counters* c,
+                                                unsigned long long task_base) {
+    __shared__ BlockTrace bt;
+    trace_init(bt);
+    trap_clear();
+    const unsigned long long total = (unsigned long long)n_tasks * s1;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
+         base += stride) {
+        unsigned long long idx = base + (threadIdx.x & 31);
+        bool valid = idx < total;
+        int task = valid ? (int)(idx / s1) : 0;
+        int i1 = valid ? (int)(idx % s1) : 0;
+        int outcome = -1;
+        Cell2 cell;
+        if (valid) {
+            Task tk = tasks[task];
+            if (!tk.live) {
+                valid = false;  // the reference returns before its r1 loop
+            } else {
+                cell.r1 = subinterval(tk.r1r, i1, s1);
+                cell.r2r = intersect(tight::r2_range(tk.weight, cell.r1), parents[tk.parent].r[1]);
+                cell.task = task;
+                cell.i1 = i1;
+                if (empty(cell.r2r)) outcome = CC_T_L1_EMPTY;
+                else if (tight::r1_strategies(tk.la, cell.r1, cell.r2r.hi)) outcome = CC_T_L1_R1;
+                else outcome = CC_T_L1_SPLIT;
+            }
+        }
+        __syncwarp();
+        trace_note(bt, valid, valid ? trace_key(task_base + task, 0, i1, 0, 0, 0, outcome) : 0, outcome);
+        unsigned long long slot = warp_append(&c->n_cell2, valid && outcome == CC_T_L1_SPLIT, caps.cell2, &c->overflow);
+        if (slot != ~0ULL) out[slot] = cell;
+    }
+    trace_flush(bt, c, 0);
+}
+
+// stage 2: r2 cells (tight_rectangle.cu:193-206)
+__global__ void __launch_bounds__(128) k_stage2(const Box* __restrict__ parents, const Task* __restrict__ tasks,
+                                                const Cell2* __restrict__ in, int s2, Cell3* __restrict__ out, Caps caps,
+                                                Counters* c, unsigned long long task_base) {
+    __shared__ BlockTrace bt;
+    trace_init(bt);
+    trap_clear();
+    const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cell2;
+    const unsigned long long total = (n_in < caps.cell2 ? n_in : caps.cell2) * s2;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
+         base += stride) {
+        unsigned long long idx = base + (threadIdx.x & 31);
+        bool valid = idx < total;
+        int outcome = -1;
+        Cell3 cell;
+        int i2 = 0;
+        Cell2 p;
+        if (valid) {
+            p = in[idx / s2];
+            i2 = (int)(idx % s2);
+            const Task tk = tasks[p.task];
+            cell.r1 = p.r1;
+            cell.r2 = subinterval(p.r2r, i2, s2);
+            cell.task = p.task;
+            cell.i1 = (int16_t)p.i1;
+            cell.i2 = (int16_t)i2;
+            if (tight::r1_strategies(tk.la, p.r1, cell.r2.hi)) {
+                outcome = CC_T_L2_R1;
+            } else {
+                cell.r3r = intersect(tight::r3_range(tk.weight, p.r1, cell.r2), parents[tk.parent].r[2]);
+                if (empty(cell.r3r)) outcome = CC_T_L2_EMPTY;
+                else if (tight::r1_r2_strategies(tk.la, p.r1, cell.r2, cell.r3r.hi)) outcome = CC_T_L2_R12;
+                else outcome = CC_T_L2_SPLIT;
+            }
+        }
+        __syncwarp();
+        trace_note(bt, valid, valid ? trace_key(task_base + p.task, 1, p.i1, i2, 0, 0, outcome) : 0, outcome);
+        unsigned long long slot = warp_append(&c->n_cell3, valid && outcome == CC_T_L2_SPLIT, caps.cell3, &c->overflow);
+        if (slot != ~0ULL) out[slot] = cell;
+    }
+    trace_flush(bt, c, 1);
+}
+
+// stage 3: r3 cells (tight_rectangle.cu:208-227)
+__global__ void __launch_bounds__(128) k_stage3(const Box* __restrict__ parents, const Task* __restrict__ tasks,
+                                                const Cell3* __restrict__ in, int s3, Cell4* __restrict__ out, Caps caps,
+                                                Counters* c, unsigned long long task_base) {
+    __shared__ BlockTrace bt;
+    trace_init(bt);
+    trap_clear();
+    const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cell3;
+    const unsigned long long total = (n_in < caps.cell3 ? n_in : caps.cell3) * s3;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
+         base += stride) {
+        unsigned long long idx = base + (threadIdx.x & 31);
+        bool valid = idx < total;
+        int outcome = -1;
+        Cell4 cell;
+        int i3 = 0;
+        Cell3 p;
+        if (valid) {
+            p = in[idx / s3];
+            i3 = (int)(idx % s3);
+            const Task tk = tasks[p.task];
+            cell.r1 = p.r1;
+            cell.r2 = p.r2;
+            cell.r3 = subinterval(p.r3r, i3, s3);
+            cell.task = p.task;
+            cell.i1 = p.i1;
+            cell.i2 = p.i2;
+            cell.i3 = (int16_t)i3;
+            if (tight::r1_r2_strategies(tk.la, p.r1, p.r2, cell.r3.hi)) {
+                outcome = CC_T_L3_R12;
+            } else {
+                cell.r4r = intersect(tight::r4_range(tk.weight, p.r1, p.r2, cell.r3), parents[tk.parent].r[3]);
+                if (empty(cell.r4r)) {
+                    outcome = CC_T_L3_EMPTY;
+                } else if (tight::r1_r2_r3_strategies(tk.la, p.r1, p.r2, cell.r3, cell.r4r.hi)) {
+                    outcome = CC_T_L3_R123;
+                } else {
+                    cell.R4 = tk.weight - p.r1 - p.r2 - cell.r3;
+                    tighten_lb(cell.R4, 0.0);
+                    outcome = empty(cell.R4) ? CC_T_L3_R4EMPTY : CC_T_L3_SPLIT;
+                }
+            }
+        }
+        __syncwarp();
+        trace_note(bt, valid, valid ? trace_key(task_base + p.task, 2, p.i1, p.i2, i3, 0, outcome) : 0, outcome);
+        unsigned long long slot = warp_append(&c->n_cell4, valid && outcome == CC_T_L3_SPLIT, caps.cell4, &c->overflow);
+        if (slot != ~0ULL) out[slot] = cell;
+    }
+    trace_flush(bt, c, 2);
+}
+
+__device__ __forceinline__ Box leaf_box(const Cell4& p, Iv r4) {
+    Box v{Iv{0, 0}, {p.r1, p.r2, p.r3, r4}};
+    tighten_lb(v.r[2], v.r[3].lo);
+    tighten_lb(v.r[1], v.r[2].lo);
+    tighten_lb(v.r[0], v.r[1].lo);
+    return v;
+}
+
+// stage 4a: leaves, the cheap checks (tight_rectangle.cu:229-246)
+__global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks, const Cell4* __restrict__ in, int s4,
+                                                 Leaf* __restrict__ out, Caps caps, Counters* c,
+                                                 unsigned long long task_base) {
+    __shared__ BlockTrace bt;
+    trace_init(bt);
+    const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cell4;
+    const unsigned long long total = (n_in < caps.cell4 ? n_in : caps.cell4) * s4;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    unsigned long long evals = 0;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
+         base += stride) {
+        unsigned long long idx = base + (threadIdx.x & 31);
+        bool valid = idx < total;
+        int outcome = -1;
+        uint32_t pidx = 0;
+        int i4 = 0;
+        Cell4 p;
+        Box v;
+        bool trapped = false;
+        if (valid) {
+            evals += 1;
+            pidx = (uint32_t)(idx / s4);
+            i4 = (int)(idx % s4);
+            p = in[pidx];
+            const Task tk = tasks[p.task];
+            trap_clear();
+            Iv r4 = subinterval(p.r4r, i4, s4);
+            if (tight::r1_r2_r3_strategies(tk.la, p.r1, p.r2, p.r3, r4.hi)) {
+                outcome = CC_T_L4_R123;
+            } else {
+                v = leaf_box(p, r4);
+                v.la = tk.la;
+                Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+                tighten_lb(R, 0.0);
+                if (empty(R)) {
+                    outcome = CC_T_L4_REMPTY;
+                } else {
+                    bool ok = tight::two_by_two_strategies(v, R);
+                    trapped = trap_status() != TRAP_NONE;
+                    if (ok && !trapped) outcome = CC_T_L4_2X2;
+                    else outcome = -2;  // undecided: goes on to stage 4b
+                }
+            }
+        }
+        __syncwarp();
+        bool decided = valid && outcome >= 0;
+        trace_note(bt, decided, decided ? trace_key(task_base + p.task, 3, p.i1, p.i2, p.i3, i4, outcome) : 0, decided ? outcome : 0);
+        unsigned long long slot = warp_append(&c->n_leaf, valid && outcome == -2, caps.leaf, &c->overflow);
+        if (slot != ~0ULL) out[slot] = Leaf{pidx, (uint16_t)i4, (uint16_t)(trapped ? 1 : 0)};
+    }
+    for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
+    if ((threadIdx.x & 31) == 0 && evals) atomicAdd(&c->leaf_evals, evals);
+    trace_flush(bt, c, 3);
+}
+
+// stage 4b: leaves that need the expensive strategies (tight_rectangle.cu:246-255)
+__global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
+                                                 const Leaf* __restrict__ in, int s4, Critical* __restrict__ crit, Caps caps,
+                                                 Counters* c, unsigned long long task_base) {
+    __shared__ BlockTrace bt;
+    trace_init(bt);
+    const unsigned long long n_in = *(volatile unsigned long long*)&c->n_leaf;
+    const unsigned long long total = n_in < caps.leaf ? n_in : caps.leaf;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
+         base += stride) {
+        unsigned long long idx = base + (threadIdx.x & 31);
+        bool valid = idx < total;
+        int outcome = -1;
+        Cell4 p;
+        Leaf lf;
+        Box v;
+        bool trapped = false;
+        if (valid) {
+            lf = in[idx];
+            p = cells[lf.cell4];
+            const Task tk = tasks[p.task];
+            trap_clear();
+            if (lf.trapped) trap(TRAP_BISECTION_CAP);
+            Iv r4 = subinterval(p.r4r, lf.i4, s4);
+            v = leaf_box(p, r4);
+            v.la = tk.la;
+            Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+            tighten_lb(R, 0.0);
+            if (tight::r1_r2_r3_strategies(v, p.R4)) outcome = CC_T_L4_R123LEAF;
+            else if (tight::r1_r2_large_r3_r4_gaps_strategy(v, R)) outcome = CC_T_L4_GAPS;
+            else outcome = CC_T_L4_CRITICAL;
+            trapped = trap_status() != TRAP_NONE;
+            if (trapped) outcome = CC_T_L4_TRAPPED;
+        }
+        __syncwarp();
+        trace_note(bt, valid, valid ? trace_key(task_base + p.task, 3, p.i1, p.i2, p.i3, lf.i4, outcome) : 0, valid ? outcome : 0);
+        bool keep = valid && (outcome == CC_T_L4_CRITICAL || outcome == CC_T_L4_TRAPPED);
+        unsigned long long slot = warp_append(&c->n_crit, keep, caps.crit, &c->overflow);
+        if (slot != ~0ULL) crit[slot] = Critical{v, p.task, trapped ? 1u : 0u};
+    }
+    trace_flush(bt, c, 3);
+}
+
+#endif  // CC_DEVICE_BUILD
+
+}  // namespace prove
+}  // namespace cc

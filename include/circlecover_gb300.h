@@ -1,0 +1,200 @@
+/*
+ * circlecover_gb300 — C ABI of the GB300 (sm_103a) prover for the
+ * rectangle-covering-by-disks proofs of phillip-keldenich/circlecover.
+ *
+ * The reference has no plugin or FFI layer; its boundary is a set of C++
+ * declarations.  Each entry point below names the reference interface it
+ * replaces (paths relative to the reference's Prover/ directory):
+ *
+ *   cc_tight_eval / cc_tight_eval_device
+ *       the six exported tight-rectangle criteria, evaluated per box
+ *       (tight_rectangle/strategies.cuh:54-87: r1_strategies,
+ *       r1_r2_strategies, both r1_r2_r3_strategies overloads,
+ *       two_by_two_strategies, r1_r2_large_r3_r4_gaps_strategy) at the
+ *       arguments the reference's leaf passes them
+ *       (tight_rectangle/tight_rectangle.cu:229-248)
+ *   cc_tight_prove
+ *       circlecover::tight_rectangle::find_critical_intervals()
+ *       (tight_rectangle/tight_rectangle.cu:458-537; called by prover.cpp:33),
+ *       with the split counts as parameters instead of compile-time constants
+ *       (tight_rectangle.cu:44-68)
+ *   cc_tight_summary
+ *       kernel_compute_distance_from_theoretical_worst_cases
+ *       (tight_rectangle.cu:322-456)
+ *
+ * Conventions: plain C types, caller-owned buffers unless stated, status
+ * codes instead of exceptions (the reference throws std::system_error or
+ * std::logic_error, or kills the CUDA context with a device trap).  A handle
+ * owns one CUDA stream and its device buffers; calls on one handle must not
+ * overlap (not thread-safe per handle).
+ */
+#ifndef CIRCLECOVER_GB300_H
+#define CIRCLECOVER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* == algcuda::Interval<double> (interval.hpp:84-242): {lb, ub} */
+typedef struct cc_iv {
+    double lb, ub;
+} cc_iv;
+
+/* == circlecover::tight_rectangle::Variables (tight_rectangle/strategies.cuh:33-35) */
+typedef struct cc_tight_box {
+    cc_iv la;
+    cc_iv r[4]; /* squared radii r1^2 >= r2^2 >= r3^2 >= r4^2 */
+} cc_tight_box;
+
+/* == circlecover::rectangle_size_bound::Variables (rectangle_size_bound/variables.hpp:33-35) */
+typedef struct cc_sb_box {
+    cc_iv la;
+    cc_iv r[6];
+} cc_sb_box;
+
+enum cc_status {
+    CC_OK = 0,
+    CC_ERR_CUDA = 1,           /* a CUDA runtime call failed */
+    CC_ERR_PARAM = 2,          /* invalid argument */
+    CC_ERR_QUEUE_OVERFLOW = 3, /* a device work queue exceeded its capacity */
+    CC_ERR_TIMEOUT = 4,        /* a bounded device wait ran out */
+    CC_ERR_INTERRUPTED = 5,    /* cc_interrupt() was called during a proof */
+    CC_ERR_NO_DEVICE = 6,      /* no CUDA device / not built for this device */
+    CC_ERR_OOM = 7             /* device or host allocation failed */
+};
+
+/* ---- per-box verdict mask of cc_tight_eval ------------------------------- */
+#define CC_TV_R1 (1u << 0)          /* r1_strategies(la, r1, r2.ub) */
+#define CC_TV_R1R2 (1u << 1)        /* r1_r2_strategies(la, r1, r2, r3.ub) */
+#define CC_TV_R1R2R3 (1u << 2)      /* r1_r2_r3_strategies(la, r1, r2, r3, r4.ub) */
+#define CC_TV_TWO_BY_TWO (1u << 3)  /* two_by_two_strategies(tightened box, R) */
+#define CC_TV_R1R2R3_LEAF (1u << 4) /* r1_r2_r3_strategies(tightened box, R4) */
+#define CC_TV_GAPS (1u << 5)        /* r1_r2_large_r3_r4_gaps_strategy(tightened box, R) */
+#define CC_TV_R_EMPTY (1u << 6)     /* R or R4 is empty: the reference's leaf skips the box */
+#define CC_TV_TRAPPED (1u << 31)    /* a criterion hit a reference trap site */
+
+/* ---- outcome codes of the proof trace (one per grid cell visited) -------- */
+enum cc_trace_outcome {
+    /* level 0: r1 cells */
+    CC_T_L1_EMPTY = 0, CC_T_L1_R1 = 1, CC_T_L1_SPLIT = 2,
+    /* level 1: r2 cells */
+    CC_T_L2_R1 = 0, CC_T_L2_EMPTY = 1, CC_T_L2_R12 = 2, CC_T_L2_SPLIT = 3,
+    /* level 2: r3 cells */
+    CC_T_L3_R12 = 0, CC_T_L3_EMPTY = 1, CC_T_L3_R123 = 2, CC_T_L3_R4EMPTY = 3, CC_T_L3_SPLIT = 4,
+    /* level 3: r4 cells (leaves) */
+    CC_T_L4_R123 = 0, CC_T_L4_REMPTY = 1, CC_T_L4_2X2 = 2, CC_T_L4_R123LEAF = 3, CC_T_L4_GAPS = 4,
+    CC_T_L4_CRITICAL = 5, CC_T_L4_TRAPPED = 6
+};
+
+#define CC_MAX_GENERATIONS 32
+
+/* Split counts of the tight proof.  The reference's values
+ * (tight_rectangle.cu:44-58) are la_splits_init 256, r_splits_init
+ * {128,128,128,128}, num_generations 11, la_splits_gen
+ * {1,2,2,2,2,1,2,1,2,1,2}, r_splits_gen {128,128,128,64}. */
+typedef struct cc_tight_grid {
+    int la_splits_init;
+    int r_splits_init[4];
+    int num_generations;
+    int la_splits_gen[CC_MAX_GENERATIONS];
+    int r_splits_gen[4];
+} cc_tight_grid;
+
+typedef struct cc_prove_stats {
+    uint64_t counts[4][8];     /* grid cells visited, by level and outcome */
+    uint64_t digest;           /* sum of mix64(cell key) over all cells */
+    uint64_t leaf_evals;       /* r4 cells evaluated */
+    uint64_t trapped_leaves;   /* leaves kept as critical because of a trap */
+    uint64_t gen_sizes[CC_MAX_GENERATIONS + 1]; /* criticals after init, gen 1, ... */
+    int32_t generations_run;
+    int32_t reserved;
+    double seconds;            /* wall time of the call */
+    uint64_t kernel_launches;  /* kernels launched by the call */
+} cc_prove_stats;
+
+/* summary of the final criticals vs the theoretical worst cases;
+ * == Max_distances (tight_rectangle.cu:322-341) */
+typedef struct cc_tight_summary_t {
+    int32_t have_range_2d, have_range_3d;
+    cc_iv la_range_2d, la_range_3d;
+    cc_iv dist_r1_2d;
+    cc_tight_box dist_r1_2d_criticals[2];
+    cc_iv dist_r2_2d;
+    cc_tight_box dist_r2_2d_criticals[2];
+    double lb_h1_2d;
+    double ub_la_by_S1;
+    double ub_R3_2d;
+    cc_iv dist_r1_3d;
+    cc_tight_box dist_r1_3d_criticals[2];
+    cc_iv dist_r2_3d;
+    cc_tight_box dist_r2_3d_criticals[2];
+    cc_iv dist_r3_3d;
+    cc_tight_box dist_r3_3d_criticals[2];
+    double ub_R4_3d;
+    cc_iv S1, h2, S3;
+    double pocket_width_3d;
+} cc_tight_summary_t;
+
+typedef struct cc_handle cc_handle;
+
+/* Open a handle on CUDA device `device` (creates one stream). */
+int cc_create(cc_handle** out, int device);
+int cc_destroy(cc_handle* h);
+const char* cc_status_str(int status);
+/* text of the last error on this handle (CUDA error string etc.) */
+const char* cc_last_error(cc_handle* h);
+
+/* Evaluate the six tight criteria on n boxes given in HOST memory (AoS);
+ * verdict masks (CC_TV_*) are written to host memory.  Includes the
+ * host<->device copies. */
+int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* masks);
+
+/* Same on DEVICE memory: `soa` holds 10 arrays of n doubles each, in the order
+ * la.lb, la.ub, r1.lb, r1.ub, ..., r4.ub (structure of arrays, element i of
+ * array k at soa[k*n + i]); masks is a device array of n uint32.  Launches on
+ * `stream` (a cudaStream_t; NULL = the handle's stream) and does not
+ * synchronise. */
+int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* masks, void* stream);
+
+/* Number of kernels the last call on this handle launched. */
+uint64_t cc_last_launch_count(cc_handle* h);
+
+/* Run the tight proof from `root` with split counts `grid`.  On success
+ * *criticals points to *n_crit boxes (release with cc_free), in the order the
+ * reference's driver produces them; stats may be NULL. */
+int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, cc_tight_box** criticals,
+                   size_t* n_crit, cc_prove_stats* stats);
+
+/* Summary of a critical set vs the 2- and 3-disk worst cases
+ * (kernel_compute_distance_from_theoretical_worst_cases). */
+int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_tight_summary_t* out);
+
+/* Ask a running cc_tight_prove on this handle to stop after the current
+ * generation (the reference's Ctrl-C behaviour, interrupt.cpp:30-46). */
+void cc_interrupt(cc_handle* h);
+
+void cc_free(void* p);
+
+/* ---- diagnostics (no reference counterpart) ------------------------------ */
+/* The device's FP64 directed-rounding primitives on host arrays, for the
+ * bit-equality check against a host implementation (op: 0 add, 1 mul, 2 div,
+ * 3 sqrt, 4 reciprocal; up: round toward +inf, else toward -inf; b unused for
+ * ops 3 and 4). */
+int cc_selftest_round(cc_handle* h, int op, int up, const double* a, const double* b, double* out, size_t n);
+/* Equal splits computed with the prover's explicit FMA (out_a) and with the
+ * reference's plain expression under nvcc's default contraction (out_b),
+ * 2n doubles each (reference: subintervals.hpp:33-43). */
+int cc_selftest_subinterval(cc_handle* h, const double* lo, const double* hi, const int* idx, const int* cnt, size_t n,
+                            double* out_a, double* out_b);
+/* Measured FP64 instruction throughput of the device (ops/s; one FP64
+ * instruction = one op): chains of directed-rounding add/mul, or of FMA. */
+int cc_selftest_fp64_peak(cc_handle* h, int use_fma, double* ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

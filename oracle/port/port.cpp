@@ -1,0 +1,164 @@
+/*
+ * ORACLE / TEST INFRASTRUCTURE ONLY.
+ *
+ * The CPU port: the prover's own criteria headers (circlecover_gb300/csrc)
+ * compiled for the host with the exact directed-rounding layer of
+ * oracle/shim/cc_rounding.h.  It restates the reference algorithm
+ * (every function cites the reference file:line it follows) and is pinned
+ * bit for bit to the reference's own code (oracle/_ref, built from the
+ * reference sources) by the CPU test suite.  Where the reference sources are
+ * absent (the GPU machine) it is the CPU checker and the timed CPU baseline.
+ */
+#include "../shim/cc_rounding.h"
+
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+thread_local unsigned long long cc_port_op_count = 0;
+#ifdef CC_PORT_COUNT
+#define CC_PORT_TICK() (++cc_port_op_count)
+#else
+#define CC_PORT_TICK() ((void)0)
+#endif
+
+#define CC_HOST_PORT 1
+#include "../../circlecover_gb300/csrc/cc_tight.cuh"
+
+namespace cc {
+thread_local uint32_t cc_port_trap_word = 0;
+}
+
+#include "../tight_driver.hpp"
+
+using cc::Iv;
+namespace ct = cc::tight;
+
+struct PortCriteria {
+    using V = Iv;
+    static V make(double l, double u) { return Iv{l, u}; }
+    static double lo(const V& v) { return v.lo; }
+    static double hi(const V& v) { return v.hi; }
+    static V sub(const V& a, const V& b) { return a - b; }
+    static void tighten_lb(V& v, double x) { cc::tighten_lb(v, x); }
+    static void do_join(V& a, const V& b) { cc::do_join(a, b); }
+    static V intersect(const V& a, const V& b) { return cc::intersect(a, b); }
+    static bool empty(const V& v) { return cc::empty(v); }
+    static V subinterval(const V& v, int i, int n) { return cc::subinterval(v, i, n); }
+    static V required_weight(const V& la) { return ct::required_weight_for(la); }
+    static V r1_range(const V& la) { return ct::r1_range(la); }
+    static V r2_range(const V& w, const V& r1) { return ct::r2_range(w, r1); }
+    static V r3_range(const V& w, const V& r1, const V& r2) { return ct::r3_range(w, r1, r2); }
+    static V r4_range(const V& w, const V& r1, const V& r2, const V& r3) { return ct::r4_range(w, r1, r2, r3); }
+    static bool r1_strategies(const V& la, const V& r1, double ub) { return ct::r1_strategies(la, r1, ub); }
+    static bool r1_r2_strategies(const V& la, const V& r1, const V& r2, double ub) { return ct::r1_r2_strategies(la, r1, r2, ub); }
+    static bool r1_r2_r3_strategies(const V& la, const V& r1, const V& r2, const V& r3, double ub) {
+        return ct::r1_r2_r3_strategies(la, r1, r2, r3, ub);
+    }
+    template <class B>
+    static ct::Box box(const B& b) {
+        return ct::Box{b.la, {b.r[0], b.r[1], b.r[2], b.r[3]}};
+    }
+    template <class B>
+    static bool two_by_two(const B& b, const V& R) { return ct::two_by_two_strategies(box(b), R); }
+    template <class B>
+    static bool r1_r2_r3_leaf(const B& b, const V& R4) { return ct::r1_r2_r3_strategies(box(b), R4); }
+    template <class B>
+    static bool gaps(const B& b, const V& R) { return ct::r1_r2_large_r3_r4_gaps_strategy(box(b), R); }
+    static uint32_t trapped() { return cc::trap_status(); }
+    static void clear_trap() { cc::trap_clear(); }
+};
+
+using Driver = cc_oracle::TightDriver<PortCriteria>;
+
+static Iv to_iv(const cc_iv& x) { return Iv{x.lb, x.ub}; }
+
+static uint32_t eval_one(const cc_tight_box& in) {
+    ct::Box b{to_iv(in.la), {to_iv(in.r[0]), to_iv(in.r[1]), to_iv(in.r[2]), to_iv(in.r[3])}};
+    return ct::eval_all(b);
+}
+
+extern "C" {
+
+int ccport_tight_eval(const cc_tight_box* boxes, size_t n, uint32_t* masks, uint64_t* ops, int threads) {
+    auto body = [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+            unsigned long long before = cc_port_op_count;
+            masks[i] = eval_one(boxes[i]);
+            if (ops) ops[i] = cc_port_op_count - before;
+        }
+    };
+    if (threads <= 1 || n < 1024) {
+        body(0, n);
+        return 0;
+    }
+    std::vector<std::thread> pool;
+    size_t chunk = (n + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) {
+        size_t b = t * chunk, e = b + chunk < n ? b + chunk : n;
+        if (b >= e) break;
+        pool.emplace_back(body, b, e);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+int ccport_tight_prove(const cc_tight_box* root, const cc_tight_grid* grid, int threads, cc_tight_box** out, size_t* n_out,
+                       cc_prove_stats* stats) {
+    Driver::Box r{to_iv(root->la), {to_iv(root->r[0]), to_iv(root->r[1]), to_iv(root->r[2]), to_iv(root->r[3])}};
+    Driver::Result res = Driver::prove(r, *grid, threads);
+    *n_out = res.criticals.size();
+    *out = (cc_tight_box*)std::malloc(sizeof(cc_tight_box) * (res.criticals.size() + 1));
+    for (size_t i = 0; i < res.criticals.size(); ++i) {
+        (*out)[i].la = cc_iv{res.criticals[i].la.lo, res.criticals[i].la.hi};
+        for (int k = 0; k < 4; ++k) (*out)[i].r[k] = cc_iv{res.criticals[i].r[k].lo, res.criticals[i].r[k].hi};
+    }
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        std::memcpy(stats->counts, res.trace.counts, sizeof(stats->counts));
+        stats->digest = res.trace.digest;
+        stats->leaf_evals = res.trace.leaf_evals;
+        stats->trapped_leaves = res.trapped_leaves;
+        for (size_t g = 0; g < res.gen_sizes.size() && g <= CC_MAX_GENERATIONS; ++g) stats->gen_sizes[g] = res.gen_sizes[g];
+        stats->generations_run = res.generations_run;
+    }
+    return 0;
+}
+
+void ccport_free(void* p) { std::free(p); }
+
+/* the rounding layer itself, for the primitive tests (op: 0 add, 1 mul, 2 div, 3 sqrt, 4 rcp) */
+void ccport_round(int op, int up, int exact_fenv, const double* a, const double* b, double* out, size_t n) {
+    for (size_t i = 0; i < n; ++i) {
+        double x = a[i], y = b ? b[i] : 0.0, r = 0.0;
+        if (exact_fenv) {
+            switch (op) {
+                case 0: r = up ? cc_fe_add_ru(x, y) : cc_fe_add_rd(x, y); break;
+                case 1: r = up ? cc_fe_mul_ru(x, y) : cc_fe_mul_rd(x, y); break;
+                case 2: r = up ? cc_fe_div_ru(x, y) : cc_fe_div_rd(x, y); break;
+                case 3: r = up ? cc_fe_sqrt_ru(x) : cc_fe_sqrt_rd(x); break;
+                case 4: r = up ? cc_fe_div_ru(1.0, x) : cc_fe_div_rd(1.0, x); break;
+            }
+        } else {
+            switch (op) {
+                case 0: r = up ? cc_sw_add_ru(x, y) : cc_sw_add_rd(x, y); break;
+                case 1: r = up ? cc_sw_mul_ru(x, y) : cc_sw_mul_rd(x, y); break;
+                case 2: r = up ? cc_sw_div_ru(x, y) : cc_sw_div_rd(x, y); break;
+                case 3: r = up ? cc_sw_sqrt_ru(x) : cc_sw_sqrt_rd(x); break;
+                case 4: r = up ? cc_sw_rcp_ru(x) : cc_sw_rcp_rd(x); break;
+            }
+        }
+        out[i] = r;
+    }
+}
+
+/* subinterval (get_subinterval with its FMA), for the split tests */
+void ccport_subinterval(double lo, double hi, int i, int n, double* out) {
+    Iv r = cc::subinterval(Iv{lo, hi}, i, n);
+    out[0] = r.lo;
+    out[1] = r.hi;
+}
+
+}  // extern "C"
