@@ -159,7 +159,10 @@ def run_ours(args, ws, rank, local):
     soa = torch.from_numpy(W.to_soa(boxes)).to("cuda")
     masks = torch.empty(n, dtype=torch.int32, device="cuda")
     prover = cg.Prover(local)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the kernels launch on it and the CUDA
+    # events are recorded on it
+    stream = torch.cuda.Stream()
+    assert stream.cuda_stream != 0
 
     def step():
         prover.tight_eval_device(soa.data_ptr(), n, masks.data_ptr(), stream.cuda_stream)
@@ -170,6 +173,7 @@ def run_ours(args, ws, rank, local):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    barrier()  # inputs were copied on the default stream
     for _ in range(args.warmup):
         step()
     barrier()

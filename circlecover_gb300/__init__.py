@@ -99,7 +99,7 @@ _lib = None
 
 EXPORTS = [
     "cc_create", "cc_destroy", "cc_status_str", "cc_last_error", "cc_tight_eval", "cc_tight_eval_device",
-    "cc_last_launch_count", "cc_tight_prove", "cc_tight_summary", "cc_interrupt", "cc_free",
+    "cc_last_launch_count", "cc_tight_prove", "cc_tight_prove_ex", "cc_tight_summary", "cc_interrupt", "cc_free",
 ]
 
 
@@ -127,6 +127,8 @@ def load_library(path=LIB_PATH):
         raise CudaError("library %s lacks %s" % (path, ", ".join(missing)))
     lib.cc_tight_prove.argtypes = [vp, ctypes.POINTER(CcTightBox), ctypes.POINTER(CcTightGrid), ctypes.POINTER(vp),
                                    ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
+    lib.cc_tight_prove_ex.argtypes = [vp, ctypes.POINTER(CcTightBox), ctypes.POINTER(CcTightGrid), ctypes.c_int,
+                                      ctypes.POINTER(vp), ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
     lib.cc_tight_summary.argtypes = [vp, vp, sz, vp]
     lib.cc_interrupt.argtypes = [vp]
     lib.cc_free.argtypes = [vp]
@@ -190,15 +192,17 @@ class Prover:
                                                   ctypes.c_void_p(stream_ptr) if stream_ptr else None),
                     "cc_tight_eval_device")
 
-    def tight_find_critical_intervals(self, root, grid):
+    def tight_find_critical_intervals(self, root, grid, plain=False):
         """The tight proof from `root` (a TIGHT_BOX record) with split counts
-        `grid` (make_grid); returns (criticals, stats)."""
+        `grid` (make_grid); returns (criticals, stats).  plain=True runs the
+        plain form (every criterion re-evaluated in every cell)."""
         rs = box_struct(root)
         out = ctypes.c_void_p()
         n = ctypes.c_size_t()
         st = CcProveStats()
-        self._check(self.lib.cc_tight_prove(self.h, ctypes.byref(rs), ctypes.byref(grid), ctypes.byref(out),
-                                            ctypes.byref(n), ctypes.byref(st)), "cc_tight_prove")
+        self._check(self.lib.cc_tight_prove_ex(self.h, ctypes.byref(rs), ctypes.byref(grid), 1 if plain else 0,
+                                               ctypes.byref(out), ctypes.byref(n), ctypes.byref(st)),
+                    "cc_tight_prove_ex")
         arr = np.zeros(n.value, dtype=TIGHT_BOX)
         if n.value:
             ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)

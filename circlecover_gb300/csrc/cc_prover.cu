@@ -62,6 +62,99 @@ __global__ void __launch_bounds__(128) k_tight_eval(const double* __restrict__ i
     }
 }
 
+// ---- three-pass evaluation ------------------------------------------------
+// A warp pays for every path any of its lanes takes.  The two bisections
+// (cover strip: ~19% of boxes, ~700 operations; gaps: ~30% of boxes, ~6000
+// operations) would make almost every warp wait for one lane, so the main
+// pass only decides whether a box needs them and appends the box's inputs
+// to a queue (one atomic per warp); each bisection then runs as its own pass
+// over full warps of boxes that all need it.
+struct EvalQueues {
+    ct::CoverJob* cover;
+    uint32_t* cover_box;
+    ct::GapsJob* gaps;
+    uint32_t* gaps_box;
+    unsigned long long* counts;  // [0] cover, [1] gaps, [2] overflow
+    unsigned long long cap;
+};
+
+template <Layout L>
+__global__ void __launch_bounds__(128) k_eval_main(const double* __restrict__ in, size_t n, uint32_t* __restrict__ masks,
+                                                   EvalQueues q) {
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n;
+         base += stride) {
+        unsigned long long i = base + (threadIdx.x & 31);
+        bool valid = i < n;
+        bool need_cover = false, need_gaps = false;
+        ct::CoverJob cj;
+        ct::GapsJob gj;
+        if (valid) {
+            ct::Box b = load_box<L>(in, n, i);
+            masks[i] = ct::eval_main(b, need_cover, cj, need_gaps, gj);
+        }
+        __syncwarp();
+        unsigned long long s = cc::prove::warp_append(&q.counts[0], valid && need_cover, q.cap, &q.counts[2]);
+        if (s != ~0ULL) {
+            q.cover[s] = cj;
+            q.cover_box[s] = (uint32_t)i;
+        }
+        s = cc::prove::warp_append(&q.counts[1], valid && need_gaps, q.cap, &q.counts[2]);
+        if (s != ~0ULL) {
+            q.gaps[s] = gj;
+            q.gaps_box[s] = (uint32_t)i;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_eval_cover(EvalQueues q, uint32_t* __restrict__ masks) {
+    const unsigned long long n = q.counts[0] < q.cap ? q.counts[0] : q.cap;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t m = ct::cover_pass(q.cover[i]);
+        if (m) masks[q.cover_box[i]] |= m;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_eval_gaps(EvalQueues q, uint32_t* __restrict__ masks) {
+    const unsigned long long n = q.counts[1] < q.cap ? q.counts[1] : q.cap;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t m = ct::gaps_pass(q.gaps[i]);
+        if (m) masks[q.gaps_box[i]] |= m;
+    }
+}
+
+// queue buffers for up to `cap` boxes in handle slots 16..20
+static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
+    void *a, *b, *c, *d, *e;
+    int st;
+    if ((st = ccrt::ensure(h, 16, cap * sizeof(ct::CoverJob), &a))) return st;
+    if ((st = ccrt::ensure(h, 17, cap * sizeof(uint32_t), &b))) return st;
+    if ((st = ccrt::ensure(h, 18, cap * sizeof(ct::GapsJob), &c))) return st;
+    if ((st = ccrt::ensure(h, 19, cap * sizeof(uint32_t), &d))) return st;
+    if ((st = ccrt::ensure(h, 20, 4 * sizeof(unsigned long long), &e))) return st;
+    *q = EvalQueues{(ct::CoverJob*)a, (uint32_t*)b, (ct::GapsJob*)c, (uint32_t*)d, (unsigned long long*)e, cap};
+    return CC_OK;
+}
+
+// the three passes on one batch already on the device
+template <Layout L>
+static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks, cudaStream_t s) {
+    EvalQueues q;
+    int st = eval_queues(h, n, &q);
+    if (st) return st;
+    CC_CUDA(h, cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s));
+    const int g = h->sm_count * 8;
+    k_eval_main<L><<<g, 128, 0, s>>>(in, n, masks, q);
+    CC_LAUNCHED(h);
+    k_eval_cover<<<g, 128, 0, s>>>(q, masks);
+    CC_LAUNCHED(h);
+    k_eval_gaps<<<g, 128, 0, s>>>(q, masks);
+    CC_LAUNCHED(h);
+    return CC_OK;
+}
+
 static int eval_grid(cc_handle* h, size_t n) {
     size_t blocks = (n + 127) / 128;
     size_t cap = (size_t)h->sm_count * 8;
@@ -198,9 +291,7 @@ int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* ma
     if (n == 0) return CC_OK;
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     CC_CUDA(h, cudaSetDevice(h->device));
-    k_tight_eval<Layout::SoA><<<eval_grid(h, n), 128, 0, s>>>(soa, n, masks);
-    CC_LAUNCHED(h);
-    return CC_OK;
+    return eval_batch<Layout::SoA>(h, soa, n, masks, s);
 }
 
 // Host-memory entry point: boxes are staged through pinned memory in chunks,
@@ -242,8 +333,8 @@ int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* m
         }
         std::memcpy(pin_in[k], boxes + off, cnt * sizeof(cc_tight_box));
         CC_CUDA(h, cudaMemcpyAsync(d_in[k], pin_in[k], cnt * sizeof(cc_tight_box), cudaMemcpyHostToDevice, h->stream));
-        k_tight_eval<Layout::AoS><<<eval_grid(h, cnt), 128, 0, h->stream>>>((const double*)d_in[k], cnt, (uint32_t*)d_out[k]);
-        CC_LAUNCHED(h);
+        st = eval_batch<Layout::AoS>(h, (const double*)d_in[k], cnt, (uint32_t*)d_out[k], h->stream);
+        if (st) return st;
         CC_CUDA(h, cudaMemcpyAsync(pin_out[k], d_out[k], cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
         CC_CUDA(h, cudaEventRecord(done[k], h->stream));
         prev_off[k] = off;
@@ -355,7 +446,8 @@ namespace {
 using namespace cc::prove;
 
 // buffer slots in the handle
-enum Slot { S_PARENTS = 6, S_TASKS, S_CELL2, S_CELL3, S_CELL4, S_LEAF, S_CRIT, S_COUNTERS };
+enum Slot { S_PARENTS = 6, S_TASKS, S_CELL2, S_CELL3, S_CELL4, S_LEAF, S_CRIT, S_COUNTERS, S_GAPS };
+static_assert(S_GAPS < 16, "proof buffers overlap the evaluation queues");
 
 struct GenTotals {
     unsigned long long counts[4][8] = {};
@@ -392,11 +484,12 @@ void merge_by_r1(std::vector<cc_tight_box>& v, std::vector<cc_tight_box>& out) {
 // One chunk of parents [a, b) of a generation; returns CC_QUEUE_OVERFLOW
 // (without side effects on `out`/`tot`) when a device queue ran full.
 int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, size_t b, int k, const int s[4], Caps caps,
-              std::vector<cc_tight_box>& out, GenTotals& tot, unsigned long long task_base) {
+              std::vector<cc_tight_box>& out, GenTotals& tot, unsigned long long task_base, bool hoist) {
     const size_t np = b - a;
     const size_t ntasks = np * (size_t)k;
-    void *d_par, *d_tasks, *d_c2, *d_c3, *d_c4, *d_leaf, *d_crit, *d_cnt;
+    void *d_par, *d_tasks, *d_c2, *d_c3, *d_c4, *d_leaf, *d_gaps, *d_crit, *d_cnt;
     int st;
+    if ((st = ccrt::ensure(h, S_GAPS, caps.gaps * sizeof(GapsLeaf), &d_gaps))) return st;
     if ((st = ccrt::ensure(h, S_PARENTS, np * sizeof(cc_tight_box), &d_par))) return st;
     if ((st = ccrt::ensure(h, S_TASKS, ntasks * sizeof(Task), &d_tasks))) return st;
     if ((st = ccrt::ensure(h, S_CELL2, caps.cell2 * sizeof(Cell2), &d_c2))) return st;
@@ -412,18 +505,37 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
     const int g = stage_grid(h);
     k_tasks<<<(unsigned)((ntasks + 127) / 128), 128, 0, sm>>>((const Box*)d_par, (int)np, k, (Task*)d_tasks);
     CC_LAUNCHED(h);
-    k_stage1<<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (int)ntasks, s[0], (Cell2*)d_c2, caps, cnt, task_base);
+    if (hoist) {
+        k_stage1<true><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (int)ntasks, s[0], (Cell2*)d_c2, caps, cnt,
+                                          task_base);
+        CC_LAUNCHED(h);
+        k_stage2<true><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell2*)d_c2, s[1], (Cell3*)d_c3, caps,
+                                          cnt, task_base);
+        CC_LAUNCHED(h);
+        k_stage3<true><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell3*)d_c3, s[2], (Cell4*)d_c4, caps,
+                                          cnt, task_base);
+        CC_LAUNCHED(h);
+        k_stage4a<true><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf, caps, cnt, task_base);
+        CC_LAUNCHED(h);
+    } else {
+        k_stage1<false><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (int)ntasks, s[0], (Cell2*)d_c2, caps, cnt,
+                                           task_base);
+        CC_LAUNCHED(h);
+        k_stage2<false><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell2*)d_c2, s[1], (Cell3*)d_c3,
+                                           caps, cnt, task_base);
+        CC_LAUNCHED(h);
+        k_stage3<false><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell3*)d_c3, s[2], (Cell4*)d_c4,
+                                           caps, cnt, task_base);
+        CC_LAUNCHED(h);
+        k_stage4a<false><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf, caps, cnt,
+                                            task_base);
+        CC_LAUNCHED(h);
+    }
+    k_stage4b<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3], (GapsLeaf*)d_gaps,
+                                 (Critical*)d_crit, caps, cnt, task_base);
     CC_LAUNCHED(h);
-    k_stage2<<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell2*)d_c2, s[1], (Cell3*)d_c3, caps, cnt,
-                                task_base);
-    CC_LAUNCHED(h);
-    k_stage3<<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell3*)d_c3, s[2], (Cell4*)d_c4, caps, cnt,
-                                task_base);
-    CC_LAUNCHED(h);
-    k_stage4a<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf, caps, cnt, task_base);
-    CC_LAUNCHED(h);
-    k_stage4b<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3], (Critical*)d_crit, caps,
-                                 cnt, task_base);
+    k_stage4c<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const GapsLeaf*)d_gaps, s[3], (Critical*)d_crit,
+                                 caps, cnt, task_base);
     CC_LAUNCHED(h);
     Counters hc;
     CC_CUDA(h, cudaMemcpyAsync(&hc, cnt, sizeof(Counters), cudaMemcpyDeviceToHost, sm));
@@ -464,7 +576,7 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
 
 // all tasks of one generation, in parent chunks that fit the device queues
 int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k, const int s[4],
-                   std::vector<cc_tight_box>& out, GenTotals& tot, Caps& caps) {
+                   std::vector<cc_tight_box>& out, GenTotals& tot, Caps& caps, bool hoist) {
     const size_t max_tasks_chunk = 1 << 16;
     size_t a = 0;
     size_t chunk = std::max<size_t>(1, max_tasks_chunk / (size_t)k);
@@ -474,7 +586,7 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
         cp.cell2 = (unsigned long long)(b - a) * k * s[0];
         std::vector<cc_tight_box> part;
         GenTotals t;
-        int st = run_chunk(h, parents, a, b, k, s, cp, part, t, (unsigned long long)a * k);
+        int st = run_chunk(h, parents, a, b, k, s, cp, part, t, (unsigned long long)a * k, hoist);
         if (st == CC_ERR_QUEUE_OVERFLOW) {
             if (b - a > 1) {
                 chunk = std::max<size_t>(1, (b - a) / 2);
@@ -482,6 +594,7 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
                 caps.cell3 *= 2;
                 caps.cell4 *= 2;
                 caps.leaf *= 2;
+                caps.gaps *= 2;
                 caps.crit *= 2;
                 if (caps.cell4 > (1ULL << 31)) return ccrt::fail(h, CC_ERR_QUEUE_OVERFLOW, "tight proof: one box exceeds the queue limit");
             }
@@ -501,8 +614,9 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
 
 }  // namespace
 
-extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, cc_tight_box** criticals,
-                              size_t* n_crit, cc_prove_stats* stats) {
+extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, int flags,
+                                 cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats) {
+    const bool hoist = !(flags & CC_PROVE_PLAIN);
     if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
     if (grid->la_splits_init < 1 || grid->num_generations < 0 || grid->num_generations > CC_MAX_GENERATIONS)
         return ccrt::fail(h, CC_ERR_PARAM, "grid: bad lambda splits or generation count");
@@ -518,7 +632,7 @@ extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_t
     CC_CUDA(h, cudaSetDevice(h->device));
     auto t0 = std::chrono::steady_clock::now();
 
-    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 20};
+    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 22, 1ULL << 20};
     GenTotals tot;
     std::vector<cc_tight_box> cur{*root}, next;
     uint64_t gen_sizes[CC_MAX_GENERATIONS + 1] = {};
@@ -529,7 +643,7 @@ extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_t
         const int k = g == 0 ? grid->la_splits_init : grid->la_splits_gen[g - 1];
         const int* s = g == 0 ? grid->r_splits_init : grid->r_splits_gen;
         next.clear();
-        int st = run_generation(h, cur, k, s, next, tot, caps);
+        int st = run_generation(h, cur, k, s, next, tot, caps, hoist);
         if (st) return st;
         cur.swap(next);
         gen_sizes[g] = cur.size();
@@ -555,6 +669,11 @@ extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_t
         stats->kernel_launches = h->launches;
     }
     return status;
+}
+
+extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, cc_tight_box** criticals,
+                              size_t* n_crit, cc_prove_stats* stats) {
+    return cc_tight_prove_ex(h, root, grid, 0, criticals, n_crit, stats);
 }
 
 extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_tight_summary_t* out) {

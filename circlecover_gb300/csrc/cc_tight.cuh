@@ -23,10 +23,14 @@ struct Box {
 };
 
 // Break-even aspect ratio lambda_2 = sqrt(sqrt(7)/2 - 1/4) between the
-// three-disk and the two-disk worst case, as outward-rounded bounds
-// (critical_ratio.cu:60-61 recomputes these on every call).
-CC_FN double break_even_lo() { return sqrt_dn(add_dn(mul_dn(0.5, sqrt_dn(7.0)), -0.25)); }
-CC_FN double break_even_hi() { return sqrt_up(add_up(mul_up(0.5, sqrt_up(7.0)), -0.25)); }
+// three-disk and the two-disk worst case, as outward-rounded bounds.  The
+// reference recomputes them on every call (critical_ratio.cu:60-61: four
+// directed square roots); they are constants, evaluated once with exact
+// directed rounding and checked against the formula by the tests.
+static constexpr double kBreakEvenLo = 0x1.0929ffddd109ap+0;  // 1.0357971111816711
+static constexpr double kBreakEvenHi = 0x1.0929ffddd109bp+0;  // 1.0357971111816713
+CC_FN double break_even_lo_formula() { return sqrt_dn(add_dn(mul_dn(0.5, sqrt_dn(7.0)), -0.25)); }
+CC_FN double break_even_hi_formula() { return sqrt_up(add_up(mul_up(0.5, sqrt_up(7.0)), -0.25)); }
 
 // Worst-case covering ratio (weight per area) of a lambda x 1 rectangle,
 // lambda >= 1 (critical_ratio.cu:58-78):
@@ -39,12 +43,10 @@ CC_FN Iv ratio_three_disk(Iv la) {
 CC_FN Iv ratio_two_disk(Iv la) { return 0.25 * la + 0.5 * reciprocal(la); }
 
 CC_FN Iv critical_ratio(Iv la) {
-    const double be_lo = break_even_lo();
-    const double be_hi = break_even_hi();
-    if (definitely(la <= be_lo)) {
+    if (definitely(la <= kBreakEvenLo)) {
         return ratio_three_disk(la);
     }
-    if (definitely(la >= be_hi)) {
+    if (definitely(la >= kBreakEvenHi)) {
         return ratio_two_disk(la);
     }
     Iv a = ratio_three_disk(la);
@@ -108,11 +110,13 @@ CC_FN bool can_recurse(double ub_w, double ub_h, double ub_largest, double lb_we
 
 // ------------------------------------------------------------ one disk
 // Place disk 1 as a full-height strip, in a corner, or as an uneven split;
-// recurse on the rest (r1_strategies.cu:27-87).
-CC_FN_INL bool r1_strategies(Iv la, Iv r1, double ub_r2) {
+// recurse on the rest (r1_strategies.cu:27-87).  `weight` is
+// required_weight_for(la), which the reference recomputes inside every
+// criterion; callers compute it once per box (same bits).
+CC_FN_INL bool r1_strategies(Iv la, Iv weight, Iv r1, double ub_r2) {
     double square_w = sqrt_dn(mul_dn(2.0, r1.lo));
     double strip_w = add_dn(mul_dn(4.0, r1.lo), -1.0);
-    const double lb_rem = (required_weight_for(la) - r1).lo;
+    const double lb_rem = (weight - r1).lo;
 
     if (strip_w > 0.0) {
         strip_w = sqrt_dn(strip_w);
@@ -180,7 +184,7 @@ CC_FN bool two_pocket_by_hand(Iv la, Iv r1, Iv r2) {
 }
 
 // disks 1 and 2 side by side as a strip (r1_r2_strategies.cu:48-72)
-CC_FN bool r1_r2_side_by_side(Iv la, Iv r1, Iv r2, double ub_r3) {
+CC_FN bool r1_r2_side_by_side(Iv la, Iv weight, Iv r1, Iv r2, double ub_r3) {
     if (two_pocket_by_hand(la, r1, r2)) {
         return true;
     }
@@ -201,12 +205,12 @@ CC_FN bool r1_r2_side_by_side(Iv la, Iv r1, Iv r2, double ub_r3) {
         }
     }
     double w_rem = add_dn(la.hi, lb_width);  // sic: '+' (parity)
-    double lb_R3 = (required_weight_for(la) - r1 - r2).lo;
+    double lb_R3 = (weight - r1 - r2).lo;
     return can_recurse(w_rem, 1.0, ub_r3, lb_R3);
 }
 
 // disk 1 in a corner square, disk 2 across the top (r1_r2_strategies.cu:74-129)
-CC_FN bool r1_r2_stacked(Iv la, Iv r1, Iv r2, double ub_r3) {
+CC_FN bool r1_r2_stacked(Iv la, Iv weight, Iv r1, Iv r2, double ub_r3) {
     double sq_side = sqrt_dn(mul_dn(2.0, r1.lo));
     if (sq_side > 1.0) {
         return false;
@@ -222,7 +226,7 @@ CC_FN bool r1_r2_stacked(Iv la, Iv r1, Iv r2, double ub_r3) {
     double w_bot = add_up(la.hi, -sq_side);
     double top_min = w_top < h_top ? w_top : h_top;
     double bot_min = w_bot < sq_side ? w_bot : sq_side;
-    double lb_R3 = (required_weight_for(la) - r1 - r2).lo;
+    double lb_R3 = (weight - r1 - r2).lo;
 
     if (sb::disk_satisfies_size_bound(ub_r3, top_min)) {
         double need_top = add_up(required_weight_for_bounded_size(w_top, h_top), ub_r3);
@@ -248,13 +252,13 @@ CC_FN bool r1_r2_stacked(Iv la, Iv r1, Iv r2, double ub_r3) {
 }
 
 // r1_r2_strategies.cu:131-133
-CC_FN_INL bool r1_r2_strategies(Iv la, Iv r1, Iv r2, double ub_r3) {
-    return r1_r2_side_by_side(la, r1, r2, ub_r3) || r1_r2_stacked(la, r1, r2, ub_r3);
+CC_FN_INL bool r1_r2_strategies(Iv la, Iv weight, Iv r1, Iv r2, double ub_r3) {
+    return r1_r2_side_by_side(la, weight, r1, r2, ub_r3) || r1_r2_stacked(la, weight, r1, r2, ub_r3);
 }
 
 // --------------------------------------------------------- three disks
 // three full-height strips (r1_r2_r3_strategies.cu:28-47)
-CC_FN bool r1_r2_r3_three_strips(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
+CC_FN bool r1_r2_r3_three_strips(Iv la, Iv weight, Iv r1, Iv r2, Iv r3, double ub_r4) {
     double lb_w3 = add_dn(mul_dn(4.0, r3.lo), -1.0);
     if (lb_w3 <= 0.0) {
         return false;
@@ -263,7 +267,7 @@ CC_FN bool r1_r2_r3_three_strips(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
     double lb_w2 = sqrt_dn(add_dn(mul_dn(4.0, r2.lo), -1.0));
     double lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
     double lb_cov = add_dn(lb_w1, add_dn(lb_w2, lb_w3));
-    double lb_R4 = (required_weight_for(la) - r1 - r2 - r3).lo;
+    double lb_R4 = (weight - r1 - r2 - r3).lo;
     double ub_rem = add_up(la.hi, -lb_cov);
     if (ub_rem <= 0.0) {
         return true;
@@ -291,13 +295,16 @@ CC_FN bool strip_width_realizable(double r1, double r2, double r3, double w) {
     return add_dn(w2, w3) >= w;
 }
 
-// widest such strip, by bisection to the FP64 fixpoint (r1_r2_r3_strategies.cu:69-94)
-CC_FN_INL bool r1_r2_r3_cover_strip(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
+// The cover-strip strategy (r1_r2_r3_strategies.cu:69-94) in three pieces,
+// so that the bisection can run as its own pass over the boxes that need it:
+//   enters: the strip of width 0.3 is realizable (else the strategy fails);
+//   width:  the widest realizable strip, by bisection to the FP64 fixpoint;
+//   finish: recursion on the rest of the rectangle.
+CC_FN bool cover_strip_enters(double r1, double r2, double r3) { return strip_width_realizable(r1, r2, r3, 0.3); }
+
+CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
     double lo = 0.3;
-    double hi = la.hi;
-    if (!strip_width_realizable(r1.lo, r2.lo, r3.lo, lo)) {
-        return false;
-    }
+    double hi = la_hi;
     for (int it = 0;; ++it) {
         double mid = 0.5 * (lo + hi);
         if (mid <= lo || mid >= hi) {
@@ -307,20 +314,31 @@ CC_FN_INL bool r1_r2_r3_cover_strip(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
             trap(TRAP_BISECTION_CAP);
             break;
         }
-        if (strip_width_realizable(r1.lo, r2.lo, r3.lo, mid)) {
+        if (strip_width_realizable(r1, r2, r3, mid)) {
             lo = mid;
         } else {
             hi = mid;
         }
     }
-    double ub_rem = add_up(la.hi, -lo);
-    double lb_R4 = (required_weight_for(la) - r1 - r2 - r3).lo;
+    return lo;
+}
+
+CC_FN bool cover_strip_finish(double la_hi, double width, double ub_r4, double lb_R4) {
+    double ub_rem = add_up(la_hi, -width);
     return can_recurse(ub_rem, 1.0, ub_r4, lb_R4);
 }
 
+CC_FN_INL bool r1_r2_r3_cover_strip(Iv la, Iv weight, Iv r1, Iv r2, Iv r3, double ub_r4) {
+    if (!cover_strip_enters(r1.lo, r2.lo, r3.lo)) {
+        return false;
+    }
+    double width = cover_strip_width(la.hi, r1.lo, r2.lo, r3.lo);
+    return cover_strip_finish(la.hi, width, ub_r4, (weight - r1 - r2 - r3).lo);
+}
+
 // r1_r2_r3_strategies.cu:96-99
-CC_FN_INL bool r1_r2_r3_strategies(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
-    return r1_r2_r3_three_strips(la, r1, r2, r3, ub_r4) || r1_r2_r3_cover_strip(la, r1, r2, r3, ub_r4);
+CC_FN_INL bool r1_r2_r3_strategies(Iv la, Iv weight, Iv r1, Iv r2, Iv r3, double ub_r4) {
+    return r1_r2_r3_three_strips(la, weight, r1, r2, r3, ub_r4) || r1_r2_r3_cover_strip(la, weight, r1, r2, r3, ub_r4);
 }
 
 // Disks 2 and 3 form a strip, disk 1 covers the rest of a column
@@ -557,20 +575,29 @@ CC_FN bool gap_width_realizable(double g, double r1, double w1, double r2, doubl
     return definitely(squared_distance(p4, px) <= r4);
 }
 
-// widest gap by bisection, then recurse on the rest of the rectangle
-// (r1_r2_large_r3_r4_gaps_strategy.cu:61-98)
-CC_FN_INL bool r1_r2_large_r3_r4_gaps_strategy(const Box& b, Iv R) {
-    const double r1 = b.r[0].lo;
-    const double r2 = b.r[1].lo;
-    const double r4 = b.r[3].lo;
+// The gaps strategy (r1_r2_large_r3_r4_gaps_strategy.cu:61-98) in three
+// pieces, so that the bisection can run as its own pass over the boxes that
+// need it:
+//   enters: disks 1 and 2 both cover full-height strips (widths w1, w2);
+//   width:  the widest gap disk 4 can close, by bisection to the FP64 fixpoint;
+//   finish: recursion on the rest of the rectangle.
+struct GapsStart {
+    double w1, w2;
+};
+
+CC_FN bool gaps_enters(double r1, double r2, GapsStart& g) {
     double w1 = add_dn(mul_dn(4.0, r1), -1.0);
     double w2 = add_dn(mul_dn(4.0, r2), -1.0);
     if (w1 <= 0.0 || w2 <= 0.0) {
         return false;
     }
-    w1 = sqrt_dn(w1);
-    w2 = sqrt_dn(w2);
+    g.w1 = sqrt_dn(w1);
+    g.w2 = sqrt_dn(w2);
+    return true;
+}
 
+CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
+    const double w1 = g.w1, w2 = g.w2;
     double lo = 0.0, hi = add_dn(sqrt_dn(r1), sqrt_dn(r2));
     for (int it = 0;; ++it) {
         double mid = 0.5 * (lo + hi);
@@ -587,16 +614,29 @@ CC_FN_INL bool r1_r2_large_r3_r4_gaps_strategy(const Box& b, Iv R) {
             hi = mid;
         }
     }
-    double w_tot = add_dn(w1, add_dn(lo, w2));
-    double w_rem = add_up(b.la.hi, -w_tot);
+    return lo;
+}
+
+CC_FN bool gaps_finish(double la_hi, GapsStart g, double gap, double r4_hi, Iv R) {
+    double w_tot = add_dn(g.w1, add_dn(gap, g.w2));
+    double w_rem = add_up(la_hi, -w_tot);
     if (w_rem <= 0.0) {
         return true;
     }
     double ub_r5 = R.hi;
-    if (ub_r5 > b.r[3].hi) {
-        ub_r5 = b.r[3].hi;
+    if (ub_r5 > r4_hi) {
+        ub_r5 = r4_hi;
     }
     return can_recurse(w_rem, 1.0, ub_r5, R.lo);
+}
+
+CC_FN_INL bool r1_r2_large_r3_r4_gaps_strategy(const Box& b, Iv R) {
+    GapsStart g;
+    if (!gaps_enters(b.r[0].lo, b.r[1].lo, g)) {
+        return false;
+    }
+    double gap = gaps_width(b.r[0].lo, b.r[1].lo, b.r[3].lo, g);
+    return gaps_finish(b.la.hi, g, gap, b.r[3].hi, R);
 }
 
 // --------------------------------------------------- range of each radius
@@ -632,14 +672,35 @@ CC_FN Iv r4_range(Iv weight, Iv r1, Iv r2, Iv r3) {
 // the last three on the box with lower bounds tightened (r3 >= r4 >= ...)
 // and with the remaining weights R (all four disks) and R4 (first three).
 // Bit layout: CC_TV_* in include/circlecover_gb300.h.
-CC_FN_INL uint32_t eval_all(const Box& in) {
+//
+// eval_main decides everything except the two bisections and says which of
+// them the box still needs; cover_pass / gaps_pass finish them.  eval_all
+// chains the three for one box.  The result does not depend on the split:
+// every criterion is a pure function of the box, and the trap bit is an OR.
+
+// inputs of the deferred cover-strip bisection (bit 2)
+struct CoverJob {
+    double la_hi, r1, r2, r3, ub_r4, lb_R4;
+};
+// inputs of the deferred gaps bisection (bit 5)
+struct GapsJob {
+    double la_hi, r1, r2, r4, r4_hi, w1, w2, R_lo, R_hi;
+};
+
+CC_FN_INL uint32_t eval_main(const Box& in, bool& need_cover, CoverJob& cj, bool& need_gaps, GapsJob& gj) {
     trap_clear();
     const Iv la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2], r4 = in.r[3];
-    Iv weight = required_weight_for(la);
+    const Iv weight = required_weight_for(la);
     uint32_t m = 0;
-    if (r1_strategies(la, r1, r2.hi)) m |= 1u << 0;
-    if (r1_r2_strategies(la, r1, r2, r3.hi)) m |= 1u << 1;
-    if (r1_r2_r3_strategies(la, r1, r2, r3, r4.hi)) m |= 1u << 2;
+    if (r1_strategies(la, weight, r1, r2.hi)) m |= 1u << 0;
+    if (r1_r2_strategies(la, weight, r1, r2, r3.hi)) m |= 1u << 1;
+    need_cover = false;
+    if (r1_r2_r3_three_strips(la, weight, r1, r2, r3, r4.hi)) {
+        m |= 1u << 2;
+    } else if (cover_strip_enters(r1.lo, r2.lo, r3.lo)) {
+        need_cover = true;
+        cj = CoverJob{la.hi, r1.lo, r2.lo, r3.lo, r4.hi, (weight - r1 - r2 - r3).lo};
+    }
     Iv R4 = weight - r1 - r2 - r3;
     tighten_lb(R4, 0.0);
     Box v{la, {r1, r2, r3, r4}};
@@ -650,10 +711,275 @@ CC_FN_INL uint32_t eval_all(const Box& in) {
     tighten_lb(R, 0.0);
     if (two_by_two_strategies(v, R)) m |= 1u << 3;
     if (r1_r2_r3_strategies(v, R4)) m |= 1u << 4;
-    if (r1_r2_large_r3_r4_gaps_strategy(v, R)) m |= 1u << 5;
+    GapsStart g;
+    need_gaps = gaps_enters(v.r[0].lo, v.r[1].lo, g);
+    if (need_gaps) {
+        gj = GapsJob{la.hi, v.r[0].lo, v.r[1].lo, v.r[3].lo, v.r[3].hi, g.w1, g.w2, R.lo, R.hi};
+    }
     if (empty(R4) || empty(R)) m |= 1u << 6;
     if (trap_status() != TRAP_NONE) m |= 1u << 31;
     return m;
+}
+
+CC_FN_INL uint32_t cover_pass(const CoverJob& j) {
+    trap_clear();
+    double width = cover_strip_width(j.la_hi, j.r1, j.r2, j.r3);
+    uint32_t m = cover_strip_finish(j.la_hi, width, j.ub_r4, j.lb_R4) ? (1u << 2) : 0u;
+    if (trap_status() != TRAP_NONE) m |= 1u << 31;
+    return m;
+}
+
+CC_FN_INL uint32_t gaps_pass(const GapsJob& j) {
+    trap_clear();
+    GapsStart g{j.w1, j.w2};
+    double gap = gaps_width(j.r1, j.r2, j.r4, g);
+    uint32_t m = gaps_finish(j.la_hi, g, gap, j.r4_hi, Iv{j.R_lo, j.R_hi}) ? (1u << 5) : 0u;
+    if (trap_status() != TRAP_NONE) m |= 1u << 31;
+    return m;
+}
+
+CC_FN_INL uint32_t eval_all(const Box& in) {
+    bool need_cover, need_gaps;
+    CoverJob cj;
+    GapsJob gj;
+    uint32_t m = eval_main(in, need_cover, cj, need_gaps, gj);
+    if (need_cover) m |= cover_pass(cj);
+    if (need_gaps) m |= gaps_pass(gj);
+    return m;
+}
+
+// ------------------------------------------------ prepared (hoisted) forms
+// In the proof's nested grid a criterion is evaluated for every cell of the
+// next radius with only that radius' upper bound changing: r1_strategies(la,
+// r1, r2.hi) for every r2 cell, r1_r2_strategies(la, r1, r2, r3.hi) for every
+// r3 cell, r1_r2_r3_strategies(la, r1, r2, r3, r4.hi) for every r4 leaf
+// (tight_rectangle.cu:195, 210, 231).  Everything that does not depend on that
+// bound -- including the cover-strip bisection -- is computed once per parent
+// cell ("prepare"); the per-cell "check" redoes only the operations that
+// involve the bound.  check(prepare(x), ub) performs the same directed-rounding
+// operations on the same values as the criterion itself, so the verdicts are
+// identical for every ub.
+
+// can_recurse(w, h, ub_largest, lb_weight) for fixed w, h (can_recurse.cu:32-62)
+struct CrPrep {
+    double area, s_sq, ratio_wh;
+};
+CC_FN CrPrep cr_prepare(double ub_w, double ub_h) {
+    CrPrep p;
+    p.area = mul_up(ub_w, ub_h);
+    double side_min = ub_w < ub_h ? ub_w : ub_h;
+    double s = rcp_up(side_min);
+    p.s_sq = mul_up(s, s);
+    p.ratio_wh = critical_ratio(ivp(ub_w), ivp(ub_h)).hi;
+    return p;
+}
+CC_FN bool cr_check(const CrPrep& p, double ub_largest, double lb_weight) {
+    double largest_norm = mul_up(p.s_sq, ub_largest);
+    double ratio;
+    if (largest_norm <= sb::kUbDiskWeight) {
+        ratio = sb::kCriticalRatio;
+    } else {
+        ratio = p.ratio_wh;
+        double ratio_cor = mul_up(0.5, sqrt_up(add_up(sqrt_up(add_up(mul_up(largest_norm, largest_norm), 1.0)), 1.0)));
+        if (ratio_cor < 195.0 / 256) {
+            ratio_cor = 195.0 / 256;
+        }
+        if (ratio > ratio_cor) {
+            ratio = ratio_cor;
+        }
+    }
+    return lb_weight >= mul_up(ratio, p.area);
+}
+
+// r1_strategies(la, r1, ub_r2) for fixed la, r1 (r1_strategies.cu:27-87)
+struct R1Prep {
+    double lb_rem;
+    CrPrep strip;                    // block 1: strip of disk 1
+    double min_right, w_sb, w_rec;   // block 2: disk 1 in a corner
+    CrPrep corner;
+    CrPrep pocket;                   // block 3: uneven split
+    uint8_t has_strip, has_corner, has_pocket;
+};
+CC_FN R1Prep r1_prepare(Iv la, Iv weight, Iv r1) {
+    R1Prep p;
+    double square_w = sqrt_dn(mul_dn(2.0, r1.lo));
+    double strip_w = add_dn(mul_dn(4.0, r1.lo), -1.0);
+    p.lb_rem = (weight - r1).lo;
+    p.has_strip = strip_w > 0.0;
+    if (p.has_strip) {
+        strip_w = sqrt_dn(strip_w);
+        p.strip = cr_prepare((la - strip_w).hi, 1.0);
+    }
+    p.has_corner = square_w < 1.0;
+    if (p.has_corner) {
+        double w_right = add_up(la.hi, -square_w);
+        p.min_right = w_right < 1.0 ? w_right : 1.0;
+        p.w_sb = mul_up(w_right, sb::kCriticalRatio);
+        p.w_rec = required_weight_for(ivp(w_right), ivp(1.0)).hi;
+        p.corner = cr_prepare(square_w, add_up(1.0, -square_w));
+    }
+    p.has_pocket = 0;
+    double lb_S1 = add_dn(mul_dn(4.0, r1.lo), -1.0);
+    if (lb_S1 > 0.0) {
+        lb_S1 = sqrt_dn(lb_S1);
+        double t = add_up(la.hi, -mul_dn(0.5, lb_S1));
+        t = mul_up(t, t);
+        double lb_h1 = add_dn(r1.lo, -t);
+        if (lb_h1 > 0.0) {
+            lb_h1 = mul_dn(2.0, sqrt_dn(lb_h1));
+            p.pocket = cr_prepare(add_up(la.hi, -lb_S1), mul_up(0.5, add_up(1.0, -lb_h1)));
+            p.has_pocket = 1;
+        }
+    }
+    return p;
+}
+CC_FN bool r1_check(const R1Prep& p, double ub_r2) {
+    if (p.has_strip && cr_check(p.strip, ub_r2, p.lb_rem)) {
+        return true;
+    }
+    if (p.has_corner) {
+        double w = sb::disk_satisfies_size_bound(ub_r2, p.min_right) ? p.w_sb : p.w_rec;
+        w = add_up(w, ub_r2);
+        double left = add_dn(p.lb_rem, -w);
+        if (left > 0 && cr_check(p.corner, ub_r2, left)) {
+            return true;
+        }
+    }
+    if (p.has_pocket) {
+        double half = mul_dn(0.5, add_dn(p.lb_rem, -ub_r2));
+        if (half > 0 && cr_check(p.pocket, ub_r2, half)) {
+            return true;
+        }
+    }
+    return false;
+}
+
+// r1_r2_strategies(la, r1, r2, ub_r3) for fixed la, r1, r2 (r1_r2_strategies.cu:29-133)
+struct R12Prep {
+    double lb_R3;
+    CrPrep side;                      // side by side: 0 fails, 1 holds, 2 recursion check
+    double top_min, bot_min, need_top_sb, need_bot_sb, need_top_rec;
+    CrPrep bot, top;                  // stacked: (w_bot x sq_side), (w_top x h_top)
+    uint8_t side_state, stacked;
+};
+CC_FN R12Prep r12_prepare(Iv la, Iv weight, Iv r1, Iv r2) {
+    R12Prep p;
+    p.lb_R3 = (weight - r1 - r2).lo;
+    p.side_state = 2;
+    if (two_pocket_by_hand(la, r1, r2)) {
+        p.side_state = 1;
+    } else {
+        double lb_width = sb::two_disks_maximize_height(r1, r2, 1.0);
+        if (lb_width <= 0.0) {
+            p.side_state = 0;
+        } else {
+            double lb_w2 = add_dn(mul_dn(4.0, r2.lo), -1.0);
+            if (lb_w2 > 0.0) {
+                lb_w2 = sqrt_dn(lb_w2);
+                double lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
+                double lb_w = add_dn(lb_w1, lb_w2);
+                if (lb_w > lb_width) {
+                    lb_width = lb_w;
+                    if (lb_w > la.hi) p.side_state = 1;
+                }
+            }
+            if (p.side_state == 2) p.side = cr_prepare(add_dn(la.hi, lb_width), 1.0);  // sic: '+' (parity)
+        }
+    }
+    if (p.side_state == 1) {
+        p.stacked = 0;
+        return p;
+    }
+    p.stacked = 0;
+    double sq_side = sqrt_dn(mul_dn(2.0, r1.lo));
+    if (sq_side > 1.0) return p;
+    double h_top = add_up(1.0, -sq_side);
+    double lb_w2 = add_dn(mul_dn(4.0, r2.lo), -mul_up(h_top, h_top));
+    if (lb_w2 < 0.0) return p;
+    lb_w2 = sqrt_dn(lb_w2);
+    double w_top = add_up(la.hi, -lb_w2);
+    double w_bot = add_up(la.hi, -sq_side);
+    p.top_min = w_top < h_top ? w_top : h_top;
+    p.bot_min = w_bot < sq_side ? w_bot : sq_side;
+    p.need_top_sb = required_weight_for_bounded_size(w_top, h_top);
+    p.need_bot_sb = required_weight_for_bounded_size(w_bot, sq_side);
+    p.need_top_rec = required_weight_for(ivp(w_top), ivp(h_top)).hi;
+    p.bot = cr_prepare(w_bot, sq_side);
+    p.top = cr_prepare(w_top, h_top);
+    p.stacked = 1;
+    return p;
+}
+CC_FN bool r12_check(const R12Prep& p, double ub_r3) {
+    if (p.side_state == 1) return true;
+    if (p.side_state == 2 && cr_check(p.side, ub_r3, p.lb_R3)) return true;
+    if (!p.stacked) return false;
+    if (sb::disk_satisfies_size_bound(ub_r3, p.top_min)) {
+        double left = add_dn(p.lb_R3, -add_up(p.need_top_sb, ub_r3));
+        return left > 0.0 && cr_check(p.bot, ub_r3, left);
+    }
+    if (sb::disk_satisfies_size_bound(ub_r3, p.bot_min)) {
+        double left = add_dn(p.lb_R3, -add_up(p.need_bot_sb, ub_r3));
+        return left > 0.0 && cr_check(p.top, ub_r3, left);
+    }
+    double left = add_dn(p.lb_R3, -add_up(p.need_top_rec, ub_r3));
+    return left > 0.0 && cr_check(p.bot, ub_r3, left);
+}
+
+// r1_r2_r3_strategies(la, r1, r2, r3, ub_r4) for fixed la, r1..r3
+// (r1_r2_r3_strategies.cu:28-99); holds the cover-strip bisection result
+struct R123Prep {
+    double lb_R4;
+    CrPrep strips, cover;
+    uint8_t strips_state;  // 0 fails, 1 holds, 2 recursion check
+    uint8_t has_cover;
+    uint8_t trapped;       // the bisection hit its iteration cap
+};
+CC_FN R123Prep r123_prepare(Iv la, Iv weight, Iv r1, Iv r2, Iv r3) {
+    R123Prep p;
+    p.lb_R4 = (weight - r1 - r2 - r3).lo;
+    p.has_cover = 0;
+    p.trapped = 0;
+    double lb_w3 = add_dn(mul_dn(4.0, r3.lo), -1.0);
+    if (lb_w3 <= 0.0) {
+        p.strips_state = 0;
+    } else {
+        lb_w3 = sqrt_dn(lb_w3);
+        double lb_w2 = sqrt_dn(add_dn(mul_dn(4.0, r2.lo), -1.0));
+        double lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
+        double lb_cov = add_dn(lb_w1, add_dn(lb_w2, lb_w3));
+        double ub_rem = add_up(la.hi, -lb_cov);
+        if (ub_rem <= 0.0) {
+            p.strips_state = 1;
+            return p;
+        }
+        p.strips_state = 2;
+        p.strips = cr_prepare(ub_rem, 1.0);
+    }
+    if (cover_strip_enters(r1.lo, r2.lo, r3.lo)) {
+        uint32_t saved = trap_status();
+        trap_clear();
+        double width = cover_strip_width(la.hi, r1.lo, r2.lo, r3.lo);
+        p.trapped = trap_status() != TRAP_NONE;
+        if (saved != TRAP_NONE) trap(saved);
+        p.cover = cr_prepare(add_up(la.hi, -width), 1.0);
+        p.has_cover = 1;
+    }
+    return p;
+}
+CC_FN bool r123_check(const R123Prep& p, double ub_r4) {
+    if (p.trapped) trap(TRAP_BISECTION_CAP);
+    if (p.strips_state == 1) return true;
+    if (p.strips_state == 2 && cr_check(p.strips, ub_r4, p.lb_R4)) return true;
+    return p.has_cover && cr_check(p.cover, ub_r4, p.lb_R4);
+}
+
+// criteria with the reference's signatures (weight computed inside)
+CC_FN_INL bool r1_strategies(Iv la, Iv r1, double ub_r2) { return r1_strategies(la, required_weight_for(la), r1, ub_r2); }
+CC_FN_INL bool r1_r2_strategies(Iv la, Iv r1, Iv r2, double ub_r3) {
+    return r1_r2_strategies(la, required_weight_for(la), r1, r2, ub_r3);
+}
+CC_FN_INL bool r1_r2_r3_strategies(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4) {
+    return r1_r2_r3_strategies(la, required_weight_for(la), r1, r2, r3, ub_r4);
 }
 
 }  // namespace tight

@@ -4,22 +4,29 @@
 // The reference launches one kernel per lambda box, each a fixed
 // (r1,r2)-blocks x (r3,r4)-threads grid in which every thread re-evaluates
 // the outer checks, with a host synchronisation after every launch.  Here all
-// lambda boxes ("tasks") of a generation go through the same five stages, one
+// lambda boxes ("tasks") of a generation go through the same stages, one
 // persistent-grid kernel each, in stream order without host synchronisation:
 //
 //   stage 1  (task, i1)        r1 cells:  r2 range, r1_strategies
 //   stage 2  (r1 cell, i2)     r2 cells:  r1_strategies, r3 range, r1_r2_strategies
 //   stage 3  (r2 cell, i3)     r3 cells:  r1_r2_strategies, r4 range, r1_r2_r3_strategies, R4
 //   stage 4a (r3 cell, i4)     leaves:    r1_r2_r3_strategies, R, two_by_two
-//   stage 4b (leaf queue)      leaves:    r1_r2_r3_strategies(box, R4), gaps
+//   stage 4b (leaf queue)      leaves:    r1_r2_r3_strategies(box, R4), gaps precondition
+//   stage 4c (gaps queue)      leaves:    gaps bisection
 //
 // Each stage reads its item count from device memory and appends survivors
 // to the next stage's queue with one atomic per warp (warp-aggregated
-// atomics).  The expensive leaf strategies run in stage 4b on a compacted
-// queue, so a warp evaluates them on 32 leaves that all need them.
-// Critical leaves carry their task index; the host merges them per task by r1
-// (merge_adjacent_r1, tight_rectangle.cu:121-159), which restores the
+// atomics), so every stage runs on full warps of items that need it.
+// Critical leaves carry their task index; the host merges them per task by
+// r1 (merge_adjacent_r1, tight_rectangle.cu:121-159), which restores the
 // reference's order exactly.
+//
+// Two forms (template parameter Hoist):
+//   plain  -- every cell calls the criteria as the reference does;
+//   hoist  -- a parent cell prepares the criteria its children evaluate with
+//             only their own upper bound changing (cc_tight.cuh, "prepared
+//             forms"), e.g. the cover-strip bisection runs once per r3 cell
+//             instead of once per leaf.  Identical verdicts.
 //
 // Every grid cell visited contributes one (level, outcome) count and
 // mix64(key) to a digest; the oracle computes the same trace.
@@ -41,21 +48,31 @@ struct Task {
 struct Cell2 {  // a surviving r1 cell
     Iv r1, r2r;
     int task, i1;
+    tight::R1Prep p1;
 };
 
 struct Cell3 {  // a surviving r2 cell
     Iv r1, r2, r3r;
     int task;
     int16_t i1, i2;
+    tight::R12Prep p2;
 };
 
 struct Cell4 {  // a surviving r3 cell
     Iv r1, r2, r3, r4r, R4;
     int task;
     int16_t i1, i2, i3, pad;
+    tight::R123Prep p3;
 };
 
 struct Leaf {  // a leaf that survived stage 4a
+    uint32_t cell4;
+    uint16_t i4;
+    uint16_t trapped;
+};
+
+struct GapsLeaf {  // a leaf that needs the gaps bisection
+    tight::GapsJob job;
     uint32_t cell4;
     uint16_t i4;
     uint16_t trapped;
@@ -68,7 +85,7 @@ struct Critical {
 };
 
 struct Counters {
-    unsigned long long n_cell2, n_cell3, n_cell4, n_leaf, n_crit;
+    unsigned long long n_cell2, n_cell3, n_cell4, n_leaf, n_gaps, n_crit;
     unsigned long long overflow;
     unsigned long long leaf_evals;
     unsigned long long digest;
@@ -76,7 +93,7 @@ struct Counters {
 };
 
 struct Caps {
-    unsigned long long cell2, cell3, cell4, leaf, crit;
+    unsigned long long cell2, cell3, cell4, leaf, gaps, crit;
 };
 
 CC_FN uint64_t mix64(uint64_t x) {
@@ -144,6 +161,12 @@ __device__ __forceinline__ unsigned long long warp_append(unsigned long long* co
     return slot;
 }
 
+// warp-uniform grid-stride loop over [0, total): all 32 lanes enter every
+// iteration (lanes past the end with valid = false), so warp collectives are safe
+#define CC_WARP_LOOP(total)                                                                              \
+    for (unsigned long long base_ = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); \
+         base_ < (total); base_ += (unsigned long long)gridDim.x * blockDim.x)
+
 // stage 0: one thread per task
 __global__ void k_tasks(const Box* __restrict__ parents, int n_parents, int la_splits, Task* __restrict__ tasks) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -161,6 +184,7 @@ __global__ void k_tasks(const Box* __restrict__ parents, int n_parents, int la_s
 }
 
 // stage 1: r1 cells (tight_rectangle.cu:182-191)
+template <bool Hoist>
 __global__ void __launch_bounds__(128) k_stage1(const Box* __restrict__ parents, const Task* __restrict__ tasks, int n_tasks,
                                                 int s1, Cell2* __restrict__ out, Caps caps, Counters* c,
                                                 unsigned long long task_base) {
@@ -168,17 +192,15 @@ __global__ void __launch_bounds__(128) k_stage1(const Box* __restrict__ parents,
     trace_init(bt);
     trap_clear();
     const unsigned long long total = (unsigned long long)n_tasks * s1;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
-         base += stride) {
-        unsigned long long idx = base + (threadIdx.x & 31);
+    CC_WARP_LOOP(total) {
+        unsigned long long idx = base_ + (threadIdx.x & 31);
         bool valid = idx < total;
         int task = valid ? (int)(idx / s1) : 0;
         int i1 = valid ? (int)(idx % s1) : 0;
         int outcome = -1;
         Cell2 cell;
         if (valid) {
-            Task tk = tasks[task];
+            const Task tk = tasks[task];
             if (!tk.live) {
                 valid = false;  // the reference returns before its r1 loop
             } else {
@@ -186,9 +208,18 @@ __global__ void __launch_bounds__(128) k_stage1(const Box* __restrict__ parents,
                 cell.r2r = intersect(tight::r2_range(tk.weight, cell.r1), parents[tk.parent].r[1]);
                 cell.task = task;
                 cell.i1 = i1;
-                if (empty(cell.r2r)) outcome = CC_T_L1_EMPTY;
-                else if (tight::r1_strategies(tk.la, cell.r1, cell.r2r.hi)) outcome = CC_T_L1_R1;
-                else outcome = CC_T_L1_SPLIT;
+                if (empty(cell.r2r)) {
+                    outcome = CC_T_L1_EMPTY;
+                } else {
+                    bool ok;
+                    if (Hoist) {
+                        cell.p1 = tight::r1_prepare(tk.la, tk.weight, cell.r1);
+                        ok = tight::r1_check(cell.p1, cell.r2r.hi);
+                    } else {
+                        ok = tight::r1_strategies(tk.la, tk.weight, cell.r1, cell.r2r.hi);
+                    }
+                    outcome = ok ? CC_T_L1_R1 : CC_T_L1_SPLIT;
+                }
             }
         }
         __syncwarp();
@@ -200,6 +231,7 @@ __global__ void __launch_bounds__(128) k_stage1(const Box* __restrict__ parents,
 }
 
 // stage 2: r2 cells (tight_rectangle.cu:193-206)
+template <bool Hoist>
 __global__ void __launch_bounds__(128) k_stage2(const Box* __restrict__ parents, const Task* __restrict__ tasks,
                                                 const Cell2* __restrict__ in, int s2, Cell3* __restrict__ out, Caps caps,
                                                 Counters* c, unsigned long long task_base) {
@@ -208,35 +240,44 @@ __global__ void __launch_bounds__(128) k_stage2(const Box* __restrict__ parents,
     trap_clear();
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cell2;
     const unsigned long long total = (n_in < caps.cell2 ? n_in : caps.cell2) * s2;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
-         base += stride) {
-        unsigned long long idx = base + (threadIdx.x & 31);
+    CC_WARP_LOOP(total) {
+        unsigned long long idx = base_ + (threadIdx.x & 31);
         bool valid = idx < total;
         int outcome = -1;
         Cell3 cell;
-        int i2 = 0;
-        Cell2 p;
+        int i2 = 0, task = 0, i1 = 0;
         if (valid) {
-            p = in[idx / s2];
+            const Cell2& p = in[idx / s2];
             i2 = (int)(idx % s2);
-            const Task tk = tasks[p.task];
+            task = p.task;
+            i1 = p.i1;
+            const Task tk = tasks[task];
             cell.r1 = p.r1;
             cell.r2 = subinterval(p.r2r, i2, s2);
-            cell.task = p.task;
-            cell.i1 = (int16_t)p.i1;
+            cell.task = task;
+            cell.i1 = (int16_t)i1;
             cell.i2 = (int16_t)i2;
-            if (tight::r1_strategies(tk.la, p.r1, cell.r2.hi)) {
+            bool r1_ok = Hoist ? tight::r1_check(p.p1, cell.r2.hi) : tight::r1_strategies(tk.la, tk.weight, p.r1, cell.r2.hi);
+            if (r1_ok) {
                 outcome = CC_T_L2_R1;
             } else {
-                cell.r3r = intersect(tight::r3_range(tk.weight, p.r1, cell.r2), parents[tk.parent].r[2]);
-                if (empty(cell.r3r)) outcome = CC_T_L2_EMPTY;
-                else if (tight::r1_r2_strategies(tk.la, p.r1, cell.r2, cell.r3r.hi)) outcome = CC_T_L2_R12;
-                else outcome = CC_T_L2_SPLIT;
+                cell.r3r = intersect(tight::r3_range(tk.weight, cell.r1, cell.r2), parents[tk.parent].r[2]);
+                if (empty(cell.r3r)) {
+                    outcome = CC_T_L2_EMPTY;
+                } else {
+                    bool ok;
+                    if (Hoist) {
+                        cell.p2 = tight::r12_prepare(tk.la, tk.weight, cell.r1, cell.r2);
+                        ok = tight::r12_check(cell.p2, cell.r3r.hi);
+                    } else {
+                        ok = tight::r1_r2_strategies(tk.la, tk.weight, cell.r1, cell.r2, cell.r3r.hi);
+                    }
+                    outcome = ok ? CC_T_L2_R12 : CC_T_L2_SPLIT;
+                }
             }
         }
         __syncwarp();
-        trace_note(bt, valid, valid ? trace_key(task_base + p.task, 1, p.i1, i2, 0, 0, outcome) : 0, outcome);
+        trace_note(bt, valid, valid ? trace_key(task_base + task, 1, i1, i2, 0, 0, outcome) : 0, outcome);
         unsigned long long slot = warp_append(&c->n_cell3, valid && outcome == CC_T_L2_SPLIT, caps.cell3, &c->overflow);
         if (slot != ~0ULL) out[slot] = cell;
     }
@@ -244,6 +285,7 @@ __global__ void __launch_bounds__(128) k_stage2(const Box* __restrict__ parents,
 }
 
 // stage 3: r3 cells (tight_rectangle.cu:208-227)
+template <bool Hoist>
 __global__ void __launch_bounds__(128) k_stage3(const Box* __restrict__ parents, const Task* __restrict__ tasks,
                                                 const Cell3* __restrict__ in, int s3, Cell4* __restrict__ out, Caps caps,
                                                 Counters* c, unsigned long long task_base) {
@@ -252,51 +294,62 @@ __global__ void __launch_bounds__(128) k_stage3(const Box* __restrict__ parents,
     trap_clear();
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cell3;
     const unsigned long long total = (n_in < caps.cell3 ? n_in : caps.cell3) * s3;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
-         base += stride) {
-        unsigned long long idx = base + (threadIdx.x & 31);
+    CC_WARP_LOOP(total) {
+        unsigned long long idx = base_ + (threadIdx.x & 31);
         bool valid = idx < total;
         int outcome = -1;
         Cell4 cell;
-        int i3 = 0;
-        Cell3 p;
+        int i3 = 0, task = 0, i1 = 0, i2 = 0;
         if (valid) {
-            p = in[idx / s3];
+            const Cell3& p = in[idx / s3];
             i3 = (int)(idx % s3);
-            const Task tk = tasks[p.task];
+            task = p.task;
+            i1 = p.i1;
+            i2 = p.i2;
+            const Task tk = tasks[task];
             cell.r1 = p.r1;
             cell.r2 = p.r2;
             cell.r3 = subinterval(p.r3r, i3, s3);
-            cell.task = p.task;
+            cell.task = task;
             cell.i1 = p.i1;
             cell.i2 = p.i2;
             cell.i3 = (int16_t)i3;
-            if (tight::r1_r2_strategies(tk.la, p.r1, p.r2, cell.r3.hi)) {
+            bool r12_ok = Hoist ? tight::r12_check(p.p2, cell.r3.hi)
+                                : tight::r1_r2_strategies(tk.la, tk.weight, p.r1, p.r2, cell.r3.hi);
+            if (r12_ok) {
                 outcome = CC_T_L3_R12;
             } else {
                 cell.r4r = intersect(tight::r4_range(tk.weight, p.r1, p.r2, cell.r3), parents[tk.parent].r[3]);
                 if (empty(cell.r4r)) {
                     outcome = CC_T_L3_EMPTY;
-                } else if (tight::r1_r2_r3_strategies(tk.la, p.r1, p.r2, cell.r3, cell.r4r.hi)) {
-                    outcome = CC_T_L3_R123;
                 } else {
-                    cell.R4 = tk.weight - p.r1 - p.r2 - cell.r3;
-                    tighten_lb(cell.R4, 0.0);
-                    outcome = empty(cell.R4) ? CC_T_L3_R4EMPTY : CC_T_L3_SPLIT;
+                    bool ok;
+                    if (Hoist) {
+                        cell.p3 = tight::r123_prepare(tk.la, tk.weight, cell.r1, cell.r2, cell.r3);
+                        ok = tight::r123_check(cell.p3, cell.r4r.hi);
+                    } else {
+                        ok = tight::r1_r2_r3_strategies(tk.la, tk.weight, cell.r1, cell.r2, cell.r3, cell.r4r.hi);
+                    }
+                    if (ok) {
+                        outcome = CC_T_L3_R123;
+                    } else {
+                        cell.R4 = tk.weight - cell.r1 - cell.r2 - cell.r3;
+                        tighten_lb(cell.R4, 0.0);
+                        outcome = empty(cell.R4) ? CC_T_L3_R4EMPTY : CC_T_L3_SPLIT;
+                    }
                 }
             }
         }
         __syncwarp();
-        trace_note(bt, valid, valid ? trace_key(task_base + p.task, 2, p.i1, p.i2, i3, 0, outcome) : 0, outcome);
+        trace_note(bt, valid, valid ? trace_key(task_base + task, 2, i1, i2, i3, 0, outcome) : 0, outcome);
         unsigned long long slot = warp_append(&c->n_cell4, valid && outcome == CC_T_L3_SPLIT, caps.cell4, &c->overflow);
         if (slot != ~0ULL) out[slot] = cell;
     }
     trace_flush(bt, c, 2);
 }
 
-__device__ __forceinline__ Box leaf_box(const Cell4& p, Iv r4) {
-    Box v{Iv{0, 0}, {p.r1, p.r2, p.r3, r4}};
+__device__ __forceinline__ Box leaf_box(const Cell4& p, Iv la, Iv r4) {
+    Box v{la, {p.r1, p.r2, p.r3, r4}};
     tighten_lb(v.r[2], v.r[3].lo);
     tighten_lb(v.r[1], v.r[2].lo);
     tighten_lb(v.r[0], v.r[1].lo);
@@ -304,6 +357,7 @@ __device__ __forceinline__ Box leaf_box(const Cell4& p, Iv r4) {
 }
 
 // stage 4a: leaves, the cheap checks (tight_rectangle.cu:229-246)
+template <bool Hoist>
 __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks, const Cell4* __restrict__ in, int s4,
                                                  Leaf* __restrict__ out, Caps caps, Counters* c,
                                                  unsigned long long task_base) {
@@ -311,31 +365,32 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
     trace_init(bt);
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cell4;
     const unsigned long long total = (n_in < caps.cell4 ? n_in : caps.cell4) * s4;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     unsigned long long evals = 0;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
-         base += stride) {
-        unsigned long long idx = base + (threadIdx.x & 31);
+    CC_WARP_LOOP(total) {
+        unsigned long long idx = base_ + (threadIdx.x & 31);
         bool valid = idx < total;
         int outcome = -1;
         uint32_t pidx = 0;
-        int i4 = 0;
-        Cell4 p;
-        Box v;
+        int i4 = 0, task = 0, i1 = 0, i2 = 0, i3 = 0;
         bool trapped = false;
         if (valid) {
             evals += 1;
             pidx = (uint32_t)(idx / s4);
             i4 = (int)(idx % s4);
-            p = in[pidx];
-            const Task tk = tasks[p.task];
+            const Cell4& p = in[pidx];
+            task = p.task;
+            i1 = p.i1;
+            i2 = p.i2;
+            i3 = p.i3;
+            const Task tk = tasks[task];
             trap_clear();
             Iv r4 = subinterval(p.r4r, i4, s4);
-            if (tight::r1_r2_r3_strategies(tk.la, p.r1, p.r2, p.r3, r4.hi)) {
+            bool r123_ok = Hoist ? tight::r123_check(p.p3, r4.hi)
+                                 : tight::r1_r2_r3_strategies(tk.la, tk.weight, p.r1, p.r2, p.r3, r4.hi);
+            if (r123_ok) {
                 outcome = CC_T_L4_R123;
             } else {
-                v = leaf_box(p, r4);
-                v.la = tk.la;
+                Box v = leaf_box(p, tk.la, r4);
                 Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
                 tighten_lb(R, 0.0);
                 if (empty(R)) {
@@ -343,14 +398,13 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
                 } else {
                     bool ok = tight::two_by_two_strategies(v, R);
                     trapped = trap_status() != TRAP_NONE;
-                    if (ok && !trapped) outcome = CC_T_L4_2X2;
-                    else outcome = -2;  // undecided: goes on to stage 4b
+                    outcome = (ok && !trapped) ? CC_T_L4_2X2 : -2;  // -2: on to stage 4b
                 }
             }
         }
         __syncwarp();
         bool decided = valid && outcome >= 0;
-        trace_note(bt, decided, decided ? trace_key(task_base + p.task, 3, p.i1, p.i2, p.i3, i4, outcome) : 0, decided ? outcome : 0);
+        trace_note(bt, decided, decided ? trace_key(task_base + task, 3, i1, i2, i3, i4, outcome) : 0, decided ? outcome : 0);
         unsigned long long slot = warp_append(&c->n_leaf, valid && outcome == -2, caps.leaf, &c->overflow);
         if (slot != ~0ULL) out[slot] = Leaf{pidx, (uint16_t)i4, (uint16_t)(trapped ? 1 : 0)};
     }
@@ -359,46 +413,106 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
     trace_flush(bt, c, 3);
 }
 
-// stage 4b: leaves that need the expensive strategies (tight_rectangle.cu:246-255)
+__device__ __forceinline__ void push_critical(Critical* crit, unsigned long long slot, const Box& v, int task, bool trapped) {
+    if (slot != ~0ULL) crit[slot] = Critical{v, task, trapped ? 1u : 0u};
+}
+
+// stage 4b: r1_r2_r3_strategies(box, R4); leaves that reach the gaps strategy
+// go on to its bisection in stage 4c (tight_rectangle.cu:246-255)
 __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
-                                                 const Leaf* __restrict__ in, int s4, Critical* __restrict__ crit, Caps caps,
-                                                 Counters* c, unsigned long long task_base) {
+                                                 const Leaf* __restrict__ in, int s4, GapsLeaf* __restrict__ gq,
+                                                 Critical* __restrict__ crit, Caps caps, Counters* c,
+                                                 unsigned long long task_base) {
     __shared__ BlockTrace bt;
     trace_init(bt);
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_leaf;
     const unsigned long long total = n_in < caps.leaf ? n_in : caps.leaf;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
-         base += stride) {
-        unsigned long long idx = base + (threadIdx.x & 31);
+    CC_WARP_LOOP(total) {
+        unsigned long long idx = base_ + (threadIdx.x & 31);
         bool valid = idx < total;
         int outcome = -1;
-        Cell4 p;
-        Leaf lf;
+        Leaf lf{0, 0, 0};
         Box v;
-        bool trapped = false;
+        int task = 0, i1 = 0, i2 = 0, i3 = 0;
+        bool trapped = false, need_gaps = false;
+        GapsLeaf gl;
         if (valid) {
             lf = in[idx];
-            p = cells[lf.cell4];
-            const Task tk = tasks[p.task];
+            const Cell4& p = cells[lf.cell4];
+            task = p.task;
+            i1 = p.i1;
+            i2 = p.i2;
+            i3 = p.i3;
+            const Task tk = tasks[task];
             trap_clear();
             if (lf.trapped) trap(TRAP_BISECTION_CAP);
             Iv r4 = subinterval(p.r4r, lf.i4, s4);
-            v = leaf_box(p, r4);
-            v.la = tk.la;
+            v = leaf_box(p, tk.la, r4);
             Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
             tighten_lb(R, 0.0);
-            if (tight::r1_r2_r3_strategies(v, p.R4)) outcome = CC_T_L4_R123LEAF;
-            else if (tight::r1_r2_large_r3_r4_gaps_strategy(v, R)) outcome = CC_T_L4_GAPS;
-            else outcome = CC_T_L4_CRITICAL;
+            tight::GapsStart g;
+            if (tight::r1_r2_r3_strategies(v, p.R4)) {
+                outcome = CC_T_L4_R123LEAF;
+            } else if (tight::gaps_enters(v.r[0].lo, v.r[1].lo, g)) {
+                need_gaps = true;
+                gl.job = tight::GapsJob{tk.la.hi, v.r[0].lo, v.r[1].lo, v.r[3].lo, v.r[3].hi, g.w1, g.w2, R.lo, R.hi};
+                gl.cell4 = lf.cell4;
+                gl.i4 = lf.i4;
+            } else {
+                outcome = CC_T_L4_CRITICAL;
+            }
             trapped = trap_status() != TRAP_NONE;
-            if (trapped) outcome = CC_T_L4_TRAPPED;
+            gl.trapped = trapped ? 1 : 0;
+            if (trapped && !need_gaps) outcome = CC_T_L4_TRAPPED;
         }
         __syncwarp();
-        trace_note(bt, valid, valid ? trace_key(task_base + p.task, 3, p.i1, p.i2, p.i3, lf.i4, outcome) : 0, valid ? outcome : 0);
+        bool decided = valid && !need_gaps;
+        trace_note(bt, decided, decided ? trace_key(task_base + task, 3, i1, i2, i3, lf.i4, outcome) : 0,
+                   decided ? outcome : 0);
+        unsigned long long slot = warp_append(&c->n_gaps, valid && need_gaps, caps.gaps, &c->overflow);
+        if (slot != ~0ULL) gq[slot] = gl;
+        bool keep = decided && (outcome == CC_T_L4_CRITICAL || outcome == CC_T_L4_TRAPPED);
+        push_critical(crit, warp_append(&c->n_crit, keep, caps.crit, &c->overflow), v, task, trapped);
+    }
+    trace_flush(bt, c, 3);
+}
+
+// stage 4c: the gaps bisection on full warps of leaves that need it
+// (r1_r2_large_r3_r4_gaps_strategy.cu:61-98)
+__global__ void __launch_bounds__(128) k_stage4c(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
+                                                 const GapsLeaf* __restrict__ gq, int s4, Critical* __restrict__ crit,
+                                                 Caps caps, Counters* c, unsigned long long task_base) {
+    __shared__ BlockTrace bt;
+    trace_init(bt);
+    const unsigned long long n_in = *(volatile unsigned long long*)&c->n_gaps;
+    const unsigned long long total = n_in < caps.gaps ? n_in : caps.gaps;
+    CC_WARP_LOOP(total) {
+        unsigned long long idx = base_ + (threadIdx.x & 31);
+        bool valid = idx < total;
+        int outcome = -1;
+        Box v;
+        int task = 0, i1 = 0, i2 = 0, i3 = 0, i4 = 0;
+        bool trapped = false;
+        if (valid) {
+            const GapsLeaf& gl = gq[idx];
+            const Cell4& p = cells[gl.cell4];
+            task = p.task;
+            i1 = p.i1;
+            i2 = p.i2;
+            i3 = p.i3;
+            i4 = gl.i4;
+            uint32_t m = tight::gaps_pass(gl.job);
+            trapped = gl.trapped || (m >> 31);
+            outcome = trapped ? CC_T_L4_TRAPPED : ((m & (1u << 5)) ? CC_T_L4_GAPS : CC_T_L4_CRITICAL);
+            if (outcome != CC_T_L4_GAPS) {
+                const Task tk = tasks[task];
+                v = leaf_box(p, tk.la, subinterval(p.r4r, i4, s4));
+            }
+        }
+        __syncwarp();
+        trace_note(bt, valid, valid ? trace_key(task_base + task, 3, i1, i2, i3, i4, outcome) : 0, valid ? outcome : 0);
         bool keep = valid && (outcome == CC_T_L4_CRITICAL || outcome == CC_T_L4_TRAPPED);
-        unsigned long long slot = warp_append(&c->n_crit, keep, caps.crit, &c->overflow);
-        if (slot != ~0ULL) crit[slot] = Critical{v, p.task, trapped ? 1u : 0u};
+        push_critical(crit, warp_append(&c->n_crit, keep, caps.crit, &c->overflow), v, task, trapped);
     }
     trace_flush(bt, c, 3);
 }

@@ -168,6 +168,14 @@ uint64_t cc_last_launch_count(cc_handle* h);
 int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, cc_tight_box** criticals,
                    size_t* n_crit, cc_prove_stats* stats);
 
+/* cc_tight_prove with options.  CC_PROVE_PLAIN evaluates every criterion in
+ * every grid cell as the reference does; the default (0) prepares the parts
+ * of a criterion that do not depend on the child cell's bound once per parent
+ * cell.  Both give identical criticals and traces. */
+#define CC_PROVE_PLAIN 1
+int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, int flags,
+                      cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats);
+
 /* Summary of a critical set vs the 2- and 3-disk worst cases
  * (kernel_compute_distance_from_theoretical_worst_cases). */
 int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_tight_summary_t* out);

@@ -129,6 +129,43 @@ int ccport_tight_prove(const cc_tight_box* root, const cc_tight_grid* grid, int 
 
 void ccport_free(void* p) { std::free(p); }
 
+/* Prepared (hoisted) criteria vs the plain ones: for every box and n_ub upper
+ * bounds spread over (and just outside) the next radius' interval, compare
+ * r1_check / r12_check / r123_check with r1_strategies / r1_r2_strategies /
+ * r1_r2_r3_strategies.  Returns the number of disagreements. */
+size_t ccport_prepared_mismatches(const cc_tight_box* boxes, size_t n, int n_ub) {
+    size_t bad = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const cc_tight_box& b = boxes[i];
+        Iv la = to_iv(b.la), r1 = to_iv(b.r[0]), r2 = to_iv(b.r[1]), r3 = to_iv(b.r[2]), r4 = to_iv(b.r[3]);
+        Iv w = ct::required_weight_for(la);
+        ct::R1Prep p1 = ct::r1_prepare(la, w, r1);
+        ct::R12Prep p2 = ct::r12_prepare(la, w, r1, r2);
+        ct::R123Prep p3 = ct::r123_prepare(la, w, r1, r2, r3);
+        const Iv next[3] = {r2, r3, r4};
+        for (int k = 0; k < 3; ++k) {
+            for (int j = 0; j < n_ub; ++j) {
+                double t = n_ub > 1 ? (double)j / (n_ub - 1) : 1.0;
+                double ub = next[k].lo + (next[k].hi - next[k].lo) * (1.25 * t - 0.125);
+                if (!(ub >= 0)) ub = next[k].hi;
+                bool a, c;
+                if (k == 0) {
+                    a = ct::r1_check(p1, ub);
+                    c = ct::r1_strategies(la, w, r1, ub);
+                } else if (k == 1) {
+                    a = ct::r12_check(p2, ub);
+                    c = ct::r1_r2_strategies(la, w, r1, r2, ub);
+                } else {
+                    a = ct::r123_check(p3, ub);
+                    c = ct::r1_r2_r3_strategies(la, w, r1, r2, r3, ub);
+                }
+                bad += a != c;
+            }
+        }
+    }
+    return bad;
+}
+
 /* the rounding layer itself, for the primitive tests (op: 0 add, 1 mul, 2 div, 3 sqrt, 4 rcp) */
 void ccport_round(int op, int up, int exact_fenv, const double* a, const double* b, double* out, size_t n) {
     for (size_t i = 0; i < n; ++i) {

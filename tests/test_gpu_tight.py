@@ -87,11 +87,12 @@ def test_eval_empty_and_ragged(prover, port):
         assert np.array_equal(prover.tight_eval(boxes), port.tight_eval(boxes))
 
 
+@pytest.mark.parametrize("plain", [False, True])
 @pytest.mark.parametrize("case", range(4))
-def test_prove_matches_golden(prover, golden_prove, case):
+def test_prove_matches_golden(prover, golden_prove, case, plain):
     c = golden_prove[case]
     g = cg.make_grid(c["la_init"], c["r_init"], c["gens"], c["r_gen"])
-    crit, st = prover.tight_find_critical_intervals(box_from_hex(c["root"]), g)
+    crit, st = prover.tight_find_critical_intervals(box_from_hex(c["root"]), g, plain=plain)
     want = boxes_from_hex(c["criticals"])
     assert len(crit) == len(want)
     assert np.array_equal(crit.view(np.uint64), want.view(np.uint64))
@@ -102,14 +103,16 @@ def test_prove_matches_golden(prover, golden_prove, case):
     assert st["kernel_launches"] > 0
 
 
-def test_prove_matches_port_bigger(prover, port):
-    root = W.tight_root(1.0, 1.0 + 0.1 / 64)
+@pytest.mark.parametrize("la", [(1.0, 1.0 + 0.1 / 64), (1.03, 1.04), (1.6, 1.62)])
+def test_prove_matches_port_bigger(prover, port, la):
+    root = W.tight_root(*la)
     gg = dict(la_init=2, r_init=(32, 64, 32, 32), gens=(1, 2), r_gen=(32, 32, 32, 16))
-    crit, st = prover.tight_find_critical_intervals(root, cg.make_grid(**gg))
     pc, ps = port.tight_prove(root, O.make_grid(**gg), threads=16)
-    assert np.array_equal(crit.view(np.uint64), pc.view(np.uint64))
-    for k in ("digest", "counts", "gen_sizes", "leaf_evals"):
-        assert st[k] == ps[k], k
+    for plain in (False, True):
+        crit, st = prover.tight_find_critical_intervals(root, cg.make_grid(**gg), plain=plain)
+        assert np.array_equal(crit.view(np.uint64), pc.view(np.uint64))
+        for k in ("digest", "counts", "gen_sizes", "leaf_evals"):
+            assert st[k] == ps[k], k
 
 
 def test_prove_rejects_bad_grid(prover):

@@ -160,3 +160,21 @@ def test_theory_constants(ref):
     three = (3 / 256) / l2 * (16 * l2 * l2 + 40 + 9 / (l2 * l2))
     two = l2 / 4 + 1 / (2 * l2)
     assert abs(three - two) < 1e-12
+
+
+def test_prepared_criteria_equal_plain(port):
+    """The proof engine's hoisted criteria (prepare once per parent cell, check
+    per child bound) agree with the plain criteria for every bound."""
+    import ctypes
+    lib = port.lib
+    lib.ccport_prepared_mismatches.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    lib.ccport_prepared_mismatches.restype = ctypes.c_size_t
+    for gen, seed in [(W.tight_microbench, 61), (W.tight_near_critical, 62)]:
+        boxes = np.ascontiguousarray(gen(20000, seed=seed))
+        assert lib.ccport_prepared_mismatches(boxes.ctypes.data, len(boxes), 9) == 0
+    # boxes from the proof's own grid near lambda = 1 (where most strategies are close calls)
+    root = W.tight_root(1.0, 1.02)
+    g = O.make_grid(2, (8, 8, 8, 8), (), (8, 8, 8, 8))
+    crit, st = port.tight_prove(root, g, threads=4)
+    edge = np.ascontiguousarray(np.concatenate([crit, W.tight_near_critical(5000, seed=63)]))
+    assert lib.ccport_prepared_mismatches(edge.ctypes.data, len(edge), 17) == 0
