@@ -70,11 +70,31 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    build_prover()
     if verbose:
         for name, _ in UNITS:
             log = os.path.join(OUT, name.replace(".cu", ".o.log"))
             sys.stdout.write(open(log).read())
     return LIB
+
+
+PROVER = os.path.join(OUT, "circlecover_prover")
+
+
+def build_prover():
+    """The C++ host driver (drop-in for the reference's prover.cpp and its
+    find_critical_intervals()) linked against the library."""
+    host = os.path.join(PKG, "host")
+    srcs = [os.path.join(host, f) for f in sorted(os.listdir(host)) if f.endswith(".cpp")]
+    cxx = os.environ.get("CXX", "g++")
+    tmp = PROVER + ".tmp%d" % os.getpid()
+    cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include")] + srcs + [
+        "-L" + OUT, "-lcirclecover_gb300", "-Wl,-rpath,$ORIGIN", "-pthread", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("host driver build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, PROVER)
+    return PROVER
 
 
 if __name__ == "__main__":

@@ -1,0 +1,13 @@
+// Entry point with the reference's shape (reference: prover.cpp:23-37): runs
+// the tight-rectangle proof on the GB300 through the drop-in driver.  argv is
+// ignored, as in the reference.
+namespace circlecover {
+namespace tight_rectangle {
+void find_critical_intervals();
+}
+}  // namespace circlecover
+
+int main(int, const char*[]) {
+    circlecover::tight_rectangle::find_critical_intervals();
+    return 0;
+}
