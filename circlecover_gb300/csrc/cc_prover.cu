@@ -19,6 +19,7 @@
 #include "cc_tight_summary.cuh"
 
 #include <algorithm>
+#include <mutex>
 
 using cc::Iv;
 namespace ct = cc::tight;
@@ -232,6 +233,7 @@ const char* cc_status_str(int s) {
         case CC_ERR_INTERRUPTED: return "interrupted";
         case CC_ERR_NO_DEVICE: return "no usable CUDA device";
         case CC_ERR_OOM: return "out of memory";
+        case CC_ERR_TOO_LARGE: return "batch larger than the entry point's fixed capacity";
         default: return "unknown status";
     }
 }
@@ -292,6 +294,85 @@ int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* ma
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     CC_CUDA(h, cudaSetDevice(h->device));
     return eval_batch<Layout::SoA>(h, soa, n, masks, s);
+}
+
+// ---- allocation-free evaluation ---------------------------------------------
+// For callers that must not allocate device memory once they are running:
+// code that executes inside a host framework owning every device allocation
+// (an arena or pool it hands out itself), latency-critical loops where a
+// cudaMalloc would block on device-wide synchronisation, and processes that
+// run close to the memory limit and pre-reserve everything at start-up.
+// cc_tight_eval_device_static evaluates a batch already in device memory
+// with the same three passes as cc_tight_eval_device, but keeps its
+// bisection queues in the fixed array below instead of handle-owned buffers,
+// and needs no handle.  The array is part of the library image: every GPU
+// that loads the library holds CC_STATIC_EVAL_SCRATCH_BYTES for it until
+// the process exits.
+static constexpr size_t kStaticMaxBoxes = CC_STATIC_EVAL_MAX_BOXES;
+static constexpr size_t kStaticCountersBytes = 256;
+static constexpr size_t kStaticScratchBytes =
+    kStaticCountersBytes + kStaticMaxBoxes * (sizeof(ct::CoverJob) + sizeof(uint32_t) + sizeof(ct::GapsJob) + sizeof(uint32_t));
+static_assert(kStaticScratchBytes <= CC_STATIC_EVAL_SCRATCH_BYTES, "static scratch larger than advertised");
+static __device__ __align__(256) unsigned char cc_static_eval_scratch[CC_STATIC_EVAL_SCRATCH_BYTES];
+
+namespace {
+constexpr int kStaticMaxDevices = 64;
+std::once_flag g_static_once[kStaticMaxDevices];
+void* g_static_scratch[kStaticMaxDevices];  // device address of the array on each device
+int g_static_sms[kStaticMaxDevices];
+int g_static_setup[kStaticMaxDevices];      // cc_status of the one-time set-up
+
+// once per device, with that device current: the array's device address (its
+// name in host code is only a host-side stand-in) and the SM count
+void static_setup(int dev) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, cc_static_eval_scratch);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_static_sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        g_static_setup[dev] = CC_ERR_CUDA;
+        return;
+    }
+    g_static_scratch[dev] = p;
+    g_static_setup[dev] = CC_OK;
+}
+}  // namespace
+
+extern "C" int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t* masks, void* stream) {
+    if (n && (!soa || !masks)) return CC_ERR_PARAM;
+    if (n > kStaticMaxBoxes) return CC_ERR_TOO_LARGE;
+    if (n == 0) return CC_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kStaticMaxDevices) {
+        cudaGetLastError();
+        return CC_ERR_NO_DEVICE;
+    }
+    std::call_once(g_static_once[dev], static_setup, dev);
+    if (g_static_setup[dev] != CC_OK) return g_static_setup[dev];
+    unsigned char* base = (unsigned char*)g_static_scratch[dev];
+    EvalQueues q;
+    q.counts = (unsigned long long*)base;
+    unsigned char* p = base + kStaticCountersBytes;
+    q.cover = (ct::CoverJob*)p;
+    p += kStaticMaxBoxes * sizeof(ct::CoverJob);
+    q.gaps = (ct::GapsJob*)p;
+    p += kStaticMaxBoxes * sizeof(ct::GapsJob);
+    q.cover_box = (uint32_t*)p;
+    p += kStaticMaxBoxes * sizeof(uint32_t);
+    q.gaps_box = (uint32_t*)p;
+    q.cap = kStaticMaxBoxes;
+    cudaStream_t s = (cudaStream_t)stream;
+    // the queue counters are the only state that must start at zero
+    if (cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s) != cudaSuccess) {
+        cudaGetLastError();
+        return CC_ERR_CUDA;
+    }
+    const int g = g_static_sms[dev] * 8;
+    k_eval_main<Layout::SoA><<<g, 128, 0, s>>>(soa, n, masks, q);
+    k_eval_cover<<<g, 128, 0, s>>>(q, masks);
+    k_eval_gaps<<<g, 128, 0, s>>>(q, masks);
+    if (cudaGetLastError() != cudaSuccess) return CC_ERR_CUDA;
+    return CC_OK;
 }
 
 // Host-memory entry point: boxes are staged through pinned memory in chunks,

@@ -63,7 +63,8 @@ enum cc_status {
     CC_ERR_TIMEOUT = 4,        /* a bounded device wait ran out */
     CC_ERR_INTERRUPTED = 5,    /* cc_interrupt() was called during a proof */
     CC_ERR_NO_DEVICE = 6,      /* no CUDA device / not built for this device */
-    CC_ERR_OOM = 7             /* device or host allocation failed */
+    CC_ERR_OOM = 7,            /* device or host allocation failed */
+    CC_ERR_TOO_LARGE = 8       /* batch larger than a fixed-capacity entry point accepts */
 };
 
 /* ---- per-box verdict mask of cc_tight_eval ------------------------------- */
@@ -158,6 +159,29 @@ int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* m
  * `stream` (a cudaStream_t; NULL = the handle's stream) and does not
  * synchronise. */
 int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* masks, void* stream);
+
+/* Allocation-free variant of cc_tight_eval_device.  It has no counterpart in
+ * the reference.  It is for callers that cannot allocate device memory while
+ * they run -- a host framework that owns every device allocation, a
+ * latency-critical loop in which cudaMalloc's implicit synchronisation is not
+ * acceptable, a process that reserves all memory at start-up -- and so cannot
+ * create a handle either.  Same inputs, outputs and results as
+ * cc_tight_eval_device; it works on the calling thread's current device and
+ * launches on `stream` (a cudaStream_t; NULL = the legacy default stream)
+ * without synchronising.
+ *   - Its scratch is a fixed array inside the library image,
+ *     CC_STATIC_EVAL_SCRATCH_BYTES per GPU, held until the process exits;
+ *     batches of more than CC_STATIC_EVAL_MAX_BOXES boxes are rejected with
+ *     CC_ERR_TOO_LARGE (split larger batches into several calls).
+ *   - The first call on a device looks up that array's device address; make
+ *     that first call before any stream capture.
+ *   - All calls on a device share the array: calls that can overlap on the
+ *     GPU (different streams, or other threads) race and give wrong masks;
+ *     serialise them (one stream, or events).
+ *   - It calls no cudaMalloc, cudaFree or allocating library routine. */
+#define CC_STATIC_EVAL_MAX_BOXES 65536
+#define CC_STATIC_EVAL_SCRATCH_BYTES (256 + 65536 * 128) /* 8 MiB + 256 bytes */
+int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t* masks, void* stream);
 
 /* Number of kernels the last call on this handle launched. */
 uint64_t cc_last_launch_count(cc_handle* h);
