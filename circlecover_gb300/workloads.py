@@ -125,6 +125,51 @@ def tight_near_critical(n, seed=5, start=0, frac_near=0.9):
     return base
 
 
+SB_UB_DISK_WEIGHT = 9.0 / 64.0
+SB_CRITICAL_RATIO = 0.61
+
+
+def sb_boxes(n, seed=3, start=0, la_lo=1.0, la_hi=2.5, heavy=0.7):
+    """Boxes of the size-bound proof: lambda ~ U[la_lo, la_hi]; six weights
+    r1 >= ... >= r6 <= 9/64.  A fraction `heavy` of the boxes has large
+    disks (each weight u * 9/64 with u^(1/4), u ~ U(0,1], so most are close
+    to the bound) and a remaining weight R = 0.61 lambda - sum near 0, where
+    the expensive strategies are reached; the rest has uniform weights.
+    Interval widths log-uniform in [2**-20, 2**-6]; lower bounds >= 0."""
+    idx = np.arange(start, start + n, dtype=np.uint64)
+    lam = la_lo + (la_hi - la_lo) * uniform(seed, idx, 0)
+    pick = uniform(seed, idx, 1) < heavy
+    w = []
+    for k in range(6):
+        u = 1.0 - uniform(seed, idx, 2 + k)
+        heavy_w = np.sqrt(np.sqrt(u)) * SB_UB_DISK_WEIGHT
+        w.append(np.where(pick, heavy_w, u * SB_UB_DISK_WEIGHT))
+    w = -np.sort(-np.stack(w), axis=0)  # descending per box
+    out = np.zeros(n, dtype=SB_BOX)
+    wl = exp2(-20.0 + 14.0 * uniform(seed, idx, 8))
+    out["la"][:, 0] = np.maximum(1.0, lam - 0.5 * wl)
+    out["la"][:, 1] = lam + 0.5 * wl
+    for k in range(6):
+        wk = exp2(-20.0 + 14.0 * uniform(seed, idx, 9 + k))
+        out["r"][:, k, 0] = np.maximum(0.0, w[k] - 0.5 * wk)
+        out["r"][:, k, 1] = np.minimum(SB_UB_DISK_WEIGHT, w[k] + 0.5 * wk)
+    # scale heavy boxes so that the six disks nearly exhaust 0.61 lambda
+    total = SB_CRITICAL_RATIO * lam
+    s = w.sum(axis=0)
+    scale = np.where(pick & (s > total), total / s * (1.0 - 1e-3 * uniform(seed, idx, 16)), 1.0)
+    out["r"] *= scale[:, None, None]
+    return out
+
+
+def sb_root(la_lo=1.0, la_hi=2.5):
+    """Root box of the size-bound proof (rectangle_size_bound.cu:317-320)."""
+    b = np.zeros(1, dtype=SB_BOX)
+    b["la"][0] = (la_lo, la_hi)
+    for k in range(6):
+        b["r"][0, k] = (0.0, SB_UB_DISK_WEIGHT)
+    return b[0]
+
+
 def tight_root(la_lo=1.0, la_hi=TIGHT_LAMBDA_MAX):
     """Root box of the tight proof (reference: tight_rectangle.cu:461-464)."""
     b = np.zeros(1, dtype=TIGHT_BOX)

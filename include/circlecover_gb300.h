@@ -77,6 +77,23 @@ enum cc_status {
 #define CC_TV_R_EMPTY (1u << 6)     /* R or R4 is empty: the reference's leaf skips the box */
 #define CC_TV_TRAPPED (1u << 31)    /* a criterion hit a reference trap site */
 
+/* ---- per-box verdict mask of cc_sb_eval ---------------------------------- */
+/* bit k (0..13) = the k-th criterion of the size-bound cascade certified the
+ * tightened box (rectangle_size_bound/rectangle_size_bound.cu:201-229, in
+ * that order: even split, uneven split, multi-disk strip, wall building, r1
+ * in corner (explicit), r1/r2 opposite corners, r1/r2 vertical strip, 2x2
+ * cover (with strip and recursion), L-shaped, r1 in corner (wall building),
+ * advanced multi-disk strip, five-disk cover, six-disk cover, seven-disk
+ * strategies); bit 14 = box or R empty (the reference's leaf skips it);
+ * bits 15..19 = the kernel's shortcuts on the untightened box
+ * (rectangle_size_bound.cu:162-177): even split (la,r1,r2), uneven split
+ * (la,r1,r2), uneven split (la,r1,r2,r3), opposite corners, vertical strip;
+ * bit 31 = a criterion reached a trap site. */
+#define CC_SV_CRITERIA_MASK 0x3fffu
+#define CC_SV_EMPTY (1u << 14)
+#define CC_SV_SHORTCUTS_MASK (0x1fu << 15)
+#define CC_SV_TRAPPED (1u << 31)
+
 /* ---- outcome codes of the proof trace (one per grid cell visited) -------- */
 enum cc_trace_outcome {
     /* level 0: r1 cells */

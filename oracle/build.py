@@ -43,7 +43,8 @@ def _stale(target, deps):
 
 def _port_deps():
     deps = [os.path.join(HERE, "port", "port.cpp"), os.path.join(HERE, "tight_driver.hpp"),
-            os.path.join(HERE, "shim", "cc_rounding.h"), os.path.join(ROOT, "include", "circlecover_gb300.h")]
+            os.path.join(HERE, "shim", "cc_rounding.h"), os.path.join(ROOT, "include", "circlecover_gb300.h"),
+            os.path.join(HERE, "sb_driver.hpp")]
     csrc = os.path.join(ROOT, "circlecover_gb300", "csrc")
     deps += [os.path.join(csrc, f) for f in os.listdir(csrc) if f.endswith(".cuh")]
     return deps

@@ -19,7 +19,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
 TIGHT_BOX = np.dtype([("la", "<f8", (2,)), ("r", "<f8", (4, 2))])
-assert TIGHT_BOX.itemsize == 80
+SB_BOX = np.dtype([("la", "<f8", (2,)), ("r", "<f8", (6, 2))])
+assert TIGHT_BOX.itemsize == 80 and SB_BOX.itemsize == 112
 
 
 class CcIv(ctypes.Structure):
@@ -111,6 +112,16 @@ class _Lib:
         ops = np.zeros(n, dtype=np.uint64) if count_ops else None
         getattr(self.lib, self.prefix + "_tight_eval")(
             boxes.ctypes.data, n, masks.ctypes.data, ops.ctypes.data if ops is not None else None, threads)
+        return (masks, ops) if count_ops else masks
+
+    def sb_eval(self, boxes, threads=1, count_ops=False):
+        boxes = np.ascontiguousarray(boxes, dtype=SB_BOX)
+        n = len(boxes)
+        masks = np.zeros(n, dtype=np.uint32)
+        ops = np.zeros(n, dtype=np.uint64) if count_ops else None
+        f = getattr(self.lib, self.prefix + "_sb_eval")
+        f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        f(boxes.ctypes.data, n, masks.ctypes.data, ops.ctypes.data if ops is not None else None, threads)
         return (masks, ops) if count_ops else masks
 
     def tight_prove(self, root, grid, threads=1):

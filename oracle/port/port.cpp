@@ -26,6 +26,7 @@ thread_local unsigned long long cc_port_op_count = 0;
 
 #define CC_HOST_PORT 1
 #include "../../circlecover_gb300/csrc/cc_tight.cuh"
+#include "../../circlecover_gb300/csrc/cc_sb_eval.cuh"
 
 namespace cc {
 thread_local uint32_t cc_port_trap_word = 0;
@@ -128,6 +129,44 @@ int ccport_tight_prove(const cc_tight_box* root, const cc_tight_grid* grid, int 
 }
 
 void ccport_free(void* p) { std::free(p); }
+
+int ccport_sb_eval(const cc_sb_box* boxes, size_t n, uint32_t* masks, uint64_t* ops, int threads) {
+    auto body = [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+            unsigned long long before = cc_port_op_count;
+            cc::sb::Box6 x;
+            x.la = to_iv(boxes[i].la);
+            for (int k = 0; k < 6; ++k) x.r[k] = to_iv(boxes[i].r[k]);
+            masks[i] = cc::sb::sb_eval_all(x);
+            if (ops) ops[i] = cc_port_op_count - before;
+        }
+    };
+    if (threads <= 1 || n < 64) {
+        body(0, n);
+        return 0;
+    }
+    std::vector<std::thread> pool;
+    size_t chunk = (n + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) {
+        size_t b = t * chunk, e = b + chunk < n ? b + chunk : n;
+        if (b >= e) break;
+        pool.emplace_back(body, b, e);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+/* the size-bound proof constants from their formulas, for the constant check */
+void ccport_sb_constants(double* out) {
+    cc::sb::ValsConstants c = cc::sb::vals_constants_formula();
+    out[0] = c.weight_bound_wall_building;
+    out[1] = c.width_fraction_incomplete;
+    out[2] = c.lb_w_infty_denom;
+    out[3] = c.phase_factor.lo;
+    out[4] = c.phase_factor.hi;
+    out[5] = cc::tight::break_even_lo_formula();
+    out[6] = cc::tight::break_even_hi_formula();
+}
 
 /* Prepared (hoisted) criteria vs the plain ones: for every box and n_ub upper
  * bounds spread over (and just outside) the next radius' interval, compare

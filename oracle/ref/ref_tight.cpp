@@ -33,6 +33,26 @@ void algcuda::trap() noexcept {
     std::abort();
 }
 
+/* run f(ctx); a reference trap() inside it lands here: the call counts as
+   "not certified" and *trapped is set */
+bool cc_ref_guarded_call(bool (*f)(void*), void* ctx, uint32_t* trapped) {
+    jmp_buf env;
+    jmp_buf* prev = cc_ref_trap_target;
+    uint32_t before = cc_ref_trapped;
+    cc_ref_trapped = 0;
+    cc_ref_trap_target = &env;
+    bool r = false;
+    if (setjmp(env) == 0) {
+        r = f(ctx);
+    } else {
+        r = false;
+    }
+    cc_ref_trap_target = prev;
+    *trapped = cc_ref_trapped;
+    cc_ref_trapped = before | cc_ref_trapped;
+    return r;
+}
+
 extern "C" int cc_ref_printf(const char* fmt, ...) {
     ++cc_ref_printf_count;
     if (std::getenv("CC_REF_PRINTF")) {
