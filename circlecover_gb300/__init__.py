@@ -100,6 +100,7 @@ _lib = None
 EXPORTS = [
     "cc_create", "cc_destroy", "cc_status_str", "cc_last_error", "cc_tight_eval", "cc_tight_eval_device",
     "cc_last_launch_count", "cc_tight_prove", "cc_tight_prove_ex", "cc_tight_summary", "cc_interrupt", "cc_free",
+    "cc_sb_eval", "cc_sb_eval_device",
 ]
 
 
@@ -130,6 +131,8 @@ def load_library(path=LIB_PATH):
     lib.cc_tight_prove_ex.argtypes = [vp, ctypes.POINTER(CcTightBox), ctypes.POINTER(CcTightGrid), ctypes.c_int,
                                       ctypes.POINTER(vp), ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
     lib.cc_tight_summary.argtypes = [vp, vp, sz, vp]
+    lib.cc_sb_eval.argtypes = [vp, vp, sz, vp]
+    lib.cc_sb_eval_device.argtypes = [vp, vp, sz, vp, vp]
     lib.cc_interrupt.argtypes = [vp]
     lib.cc_free.argtypes = [vp]
     if hasattr(lib, "cc_selftest_round"):
@@ -191,6 +194,19 @@ class Prover:
         self._check(self.lib.cc_tight_eval_device(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
                                                   ctypes.c_void_p(stream_ptr) if stream_ptr else None),
                     "cc_tight_eval_device")
+
+    def sb_eval(self, boxes):
+        """Size-bound verdict masks (CC_SV_* bits) of host boxes (SB_BOX records)."""
+        boxes = np.ascontiguousarray(boxes, dtype=SB_BOX)
+        masks = np.zeros(len(boxes), dtype=np.uint32)
+        self._check(self.lib.cc_sb_eval(self.h, boxes.ctypes.data, len(boxes), masks.ctypes.data), "cc_sb_eval")
+        return masks
+
+    def sb_eval_device(self, soa_ptr, n, masks_ptr, stream_ptr=None):
+        """Device-resident size-bound evaluation: SoA (14 x n float64) in."""
+        self._check(self.lib.cc_sb_eval_device(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
+                                               ctypes.c_void_p(stream_ptr) if stream_ptr else None),
+                    "cc_sb_eval_device")
 
     def tight_find_critical_intervals(self, root, grid, plain=False):
         """The tight proof from `root` (a TIGHT_BOX record) with split counts

@@ -22,6 +22,7 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcom
                  "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 UNITS = [
     ("cc_prover.cu", ["-fmad=false", "-Xptxas", "-v"]),
+    ("cc_sb_kernels.cu", ["-fmad=false", "-Xptxas", "-v"]),
     ("cc_selftest_fmad.cu", []),
 ]
 

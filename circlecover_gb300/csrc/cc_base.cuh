@@ -84,7 +84,7 @@ enum TrapSite : uint32_t {
 // one status byte per thread, kept in shared memory so that any device
 // function can set it without threading a context argument through every
 // criterion; 1024 threads per block at most.
-__shared__ uint8_t cc_trap_words[1024];
+static __shared__ uint8_t cc_trap_words[1024];
 CC_FN void trap(uint32_t site) { cc_trap_words[threadIdx.x] = (uint8_t)site; }
 CC_FN uint32_t trap_status() { return cc_trap_words[threadIdx.x]; }
 CC_FN void trap_clear() { cc_trap_words[threadIdx.x] = TRAP_NONE; }

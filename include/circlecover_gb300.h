@@ -200,6 +200,15 @@ int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* ma
 #define CC_STATIC_EVAL_SCRATCH_BYTES (256 + 65536 * 128) /* 8 MiB + 256 bytes */
 int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t* masks, void* stream);
 
+/* Evaluate the size-bound criteria on n boxes in HOST memory (AoS, 112-byte
+ * boxes); verdict masks (CC_SV_*) to host memory.  Replaces the criteria of
+ * rectangle_size_bound/strategies.cuh:32-147 as the reference's leaf calls
+ * them (rectangle_size_bound/rectangle_size_bound.cu:189-231). */
+int cc_sb_eval(cc_handle* h, const cc_sb_box* boxes, size_t n, uint32_t* masks);
+/* Same on DEVICE memory: 14 arrays of n doubles (la.lb, la.ub, r1.lb, ...,
+ * r6.ub); asynchronous on `stream` (NULL = the handle's stream). */
+int cc_sb_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* masks, void* stream);
+
 /* Number of kernels the last call on this handle launched. */
 uint64_t cc_last_launch_count(cc_handle* h);
 

@@ -60,6 +60,35 @@ def edge_boxes():
     return np.array(rows, dtype=W.TIGHT_BOX)
 
 
+def sb_edge_boxes():
+    """Size-bound boxes at the edges: all radii at the bound 9/64, point
+    intervals, zero radii, lambda at 1, 2.5 and 8, R close to 0."""
+    rows = []
+    ub = 9.0 / 64.0
+
+    def box(la, r):
+        b = np.zeros(1, dtype=W.SB_BOX)
+        b["la"][0] = la
+        b["r"][0] = r
+        rows.append(b[0])
+
+    for la in [(1.0, 1.0), (1.0, 1.0 + 2 ** -20), (2.5, 2.5), (1.5, 1.6), (8.0, 8.0), (2.4, 2.5)]:
+        lam = la[1]
+        box(la, [(0.0, ub)] * 6)
+        box(la, [(ub, ub)] * 6)
+        box(la, [(ub - 1e-3, ub)] * 6)
+        box(la, [(0.0, 0.0)] * 6)
+        box(la, [(ub, ub), (ub, ub), (0.1, 0.1), (0.05, 0.05), (0.01, 0.02), (0.0, 0.01)])
+        w = 0.61 * lam / 6.0
+        w = min(w, ub)
+        box(la, [(w - 1e-6, w)] * 6)
+        box(la, [(0.13, 0.14), (0.12, 0.13), (0.11, 0.12), (0.1, 0.11), (0.09, 0.1), (0.08, 0.09)])
+        box(la, [(0.2, 0.1)] + [(0.0, 0.01)] * 5)  # empty r1
+        for r3 in (0.0, 0.002):  # r1, r2 in opposite corners, a tiny rest
+            box(la, [(0.119, 0.12), (0.119, 0.12)] + [(r3, r3)] + [(0.0, r3)] * 3)
+    return np.array(rows, dtype=W.SB_BOX)
+
+
 PROOF_CASES = [
     # (name, la range, la_init, r_init, gens, r_gen)
     ("near_one", (1.0, 1.0 + 0.1 / 256), 2, (16, 16, 16, 16), (1, 2), (16, 16, 16, 8)),
@@ -92,6 +121,14 @@ def main():
     assert bops.max() < 65536
     np.savez_compressed(os.path.join(HERE, "tight_bench_ops.npz"), ops=bops.astype(np.uint16), masks=bm)
     print("bench sample: mean ops/box %.1f" % bops.mean())
+
+    # size-bound criteria: per-box masks of the reference's code
+    sb_parts = [W.sb_boxes(2000, seed=3, la_hi=2.5), W.sb_boxes(1500, seed=4, la_hi=8.0), sb_edge_boxes()]
+    sbb = np.concatenate(sb_parts)
+    sbm, sbops = ref.sb_eval(sbb, threads=8, count_ops=True)
+    np.savez_compressed(os.path.join(HERE, "sb_eval_golden.npz"), boxes=sbb.view(np.float64).reshape(len(sbb), 14),
+                        masks=sbm, ops=sbops, parts=np.array([len(p) for p in sb_parts]))
+    print("size-bound eval fixtures:", len(sbb), "boxes, mean ops %.0f" % sbops.mean())
 
     cases = []
     for name, la, la_init, r_init, gens, r_gen in PROOF_CASES:
