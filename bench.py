@@ -83,18 +83,26 @@ class ClockSampler:
 def algorithmic_ops_per_box():
     """Mean number of FP64 directed-rounding operations the REFERENCE's code
     executes per box of this workload (shim counters on the reference built
-    for the host; first 2**16 boxes of the 2**24-box set)."""
+    for the host; first 2**16 boxes of the 2**24-box set), split by the kernel
+    that executes them: the strip-width and gap-width bisection loops (counted
+    on the port, whose loops execute the reference's operations one for one)
+    and the main pass (the rest of the reference's count)."""
     z = np.load(os.path.join(ROOT, "tests", "golden", "tight_bench_ops.npz"))
-    return float(z["ops"].astype(np.float64).mean()), z["masks"]
+    total = float(z["ops"].astype(np.float64).mean())
+    cover = float(z["cover_ops"].astype(np.float64).mean())
+    gaps = float(z["gaps_ops"].astype(np.float64).mean())
+    return total, {"k_eval_main": total - cover - gaps, "k_eval_cover": cover, "k_eval_gaps": gaps}, z["masks"]
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the eval kernel from the committed ncu summary."""
+def ncu_traffic(kernel):
+    """DRAM bytes (read + write) per full-size launch of `kernel` from the
+    committed ncu summary (a line `traffic_bytes_per_launch[<kernel>]: B`)."""
     p = os.path.join(ROOT, "profiles", "tight_eval_microbench_2e24.md")
     if not os.path.exists(p):
         return None
+    key = "traffic_bytes_per_launch[%s]:" % kernel
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
+        if line.startswith(key):
             try:
                 return float(line.split(":", 1)[1])
             except ValueError:
@@ -102,10 +110,14 @@ def ncu_traffic():
     return None
 
 
+_CPU_BOXES = {}
+
+
 def cpu_baseline(n_sample, seed=1):
     """The CPU implementation on all host cores over a bounded sample of the
-    workload: the reference's own criteria code if it was built on this host,
-    else the oracle's port of it."""
+    workload (about 10 s of CPU work at the default sample): the reference's
+    own criteria code if it was built on this host, else the oracle's port
+    of it."""
     from circlecover_gb300 import workloads as W
     from oracle import oracle as O
     O.ensure_built()
@@ -114,7 +126,9 @@ def cpu_baseline(n_sample, seed=1):
         impl, kind = O.Ref(), "reference"
     else:
         impl, kind = O.Port(), "port"
-    boxes = W.tight_microbench(n_sample, seed=seed)
+    if (n_sample, seed) not in _CPU_BOXES:
+        _CPU_BOXES[(n_sample, seed)] = W.tight_microbench(n_sample, seed=seed)
+    boxes = _CPU_BOXES[(n_sample, seed)]
     impl.tight_eval(boxes[:4096], threads=cores)
     t0 = time.perf_counter()
     impl.tight_eval(boxes, threads=cores)
@@ -178,6 +192,9 @@ def run_ours(args, ws, rank, local):
         step()
     barrier()
     launches_per_step = prover.last_launch_count
+    # per-kernel CUDA events (recorded by the library on the same stream)
+    prover.set_stage_timing(True)
+    stage_ms = np.zeros(3)
     clocks = ClockSampler(local)
     clocks.start()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -185,10 +202,13 @@ def run_ours(args, ws, rank, local):
     e0.record(stream)
     for _ in range(args.steps):
         step()
+        stage_ms += np.array(prover.stage_times())
     e1.record(stream)
     barrier()
     ck = clocks.stop()
+    prover.set_stage_timing(False)
     ms = e0.elapsed_time(e1) / args.steps
+    stage_ms /= args.steps
     if ws > 1:
         t = torch.tensor([ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -197,7 +217,7 @@ def run_ours(args, ws, rank, local):
 
     # correctness of the timed output: the sampled boxes' masks equal the
     # reference's (golden) masks
-    ops_per_box, ref_masks = algorithmic_ops_per_box()
+    ops_per_box, stage_ops, ref_masks = algorithmic_ops_per_box()
     got = masks[: len(ref_masks)].cpu().numpy().view(np.uint32)
     verified = bool(rank != 0 or np.array_equal(got, ref_masks))
 
@@ -222,7 +242,13 @@ def run_ours(args, ws, rank, local):
         prover.close()
         return
     peak = ctypes_peak(prover)
-    achieved = ops_per_box * n / (ms * 1e-3)
+    names = ["k_eval_main", "k_eval_cover", "k_eval_gaps"]
+    stages = {k: {"ms": float(stage_ms[i]), "ops_per_box": stage_ops[k],
+                  "achieved": stage_ops[k] * n / (stage_ms[i] * 1e-3) / 1e12,
+                  "frac": stage_ops[k] * n / (stage_ms[i] * 1e-3) / peak} for i, k in enumerate(names)}
+    dom = names[int(np.argmax(stage_ms))]
+    achieved = stage_ops[dom] * n / (stage_ms[names.index(dom)] * 1e-3)
+    step_achieved = ops_per_box * n / (ms * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -232,11 +258,15 @@ def run_ours(args, ws, rank, local):
                    "boxes_per_gpu": n, "l2_flush": "not needed: inputs (%.2f GB) exceed L2" % (n * 80 / 1e9),
                    "layout": "SoA, 10 x n float64"},
         "verified_vs_reference_masks": verified,
-        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "Top/s (FP64 ops)",
-                     "frac": achieved / peak, "traffic": ncu_traffic(),
-                     "ops_per_box": ops_per_box,
-                     "note": "achieved = reference's directed-rounding ops per box (shim-counted) x boxes / kernel "
-                             "time; peak = measured FP64 directed add/mul instruction rate of this GPU"},
+        "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved / 1e12, "peak": peak / 1e12,
+                     "unit": "Top/s (FP64 ops)", "frac": achieved / peak, "traffic": ncu_traffic(dom),
+                     "ops_per_box": stage_ops[dom], "stages": stages,
+                     "step": {"achieved": step_achieved / 1e12, "frac": step_achieved / peak,
+                              "ops_per_box": ops_per_box},
+                     "note": "achieved = the reference's directed-rounding ops per box that this kernel executes "
+                             "(shim-counted) x boxes / the kernel's mean CUDA-event time; peak = FP64 directed "
+                             "add/mul instruction rate measured by this bench on this GPU (MEASURED_PEAKS.json "
+                             "holds no FP64 figure); traffic = ncu DRAM bytes per launch (profiles/)"},
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": ck,
         "e2e": e2e,
@@ -265,7 +295,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--log2n", type=int, default=24)
-    ap.add_argument("--cpu-sample", type=int, default=1 << 20)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 23)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -100,7 +100,7 @@ _lib = None
 EXPORTS = [
     "cc_create", "cc_destroy", "cc_status_str", "cc_last_error", "cc_tight_eval", "cc_tight_eval_device",
     "cc_last_launch_count", "cc_tight_prove", "cc_tight_prove_ex", "cc_tight_summary", "cc_interrupt", "cc_free",
-    "cc_sb_eval", "cc_sb_eval_device",
+    "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times",
 ]
 
 
@@ -134,6 +134,8 @@ def load_library(path=LIB_PATH):
     lib.cc_sb_eval.argtypes = [vp, vp, sz, vp]
     lib.cc_sb_eval_device.argtypes = [vp, vp, sz, vp, vp]
     lib.cc_interrupt.argtypes = [vp]
+    lib.cc_set_stage_timing.argtypes = [vp, ctypes.c_int]
+    lib.cc_last_stage_times.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     lib.cc_free.argtypes = [vp]
     if hasattr(lib, "cc_selftest_round"):
         lib.cc_selftest_round.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, sz]
@@ -194,6 +196,18 @@ class Prover:
         self._check(self.lib.cc_tight_eval_device(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
                                                   ctypes.c_void_p(stream_ptr) if stream_ptr else None),
                     "cc_tight_eval_device")
+
+    def set_stage_timing(self, enable=True):
+        """Record a CUDA event around each evaluation kernel (see stage_times)."""
+        self._check(self.lib.cc_set_stage_timing(self.h, int(bool(enable))), "cc_set_stage_timing")
+
+    def stage_times(self):
+        """Milliseconds of k_eval_main, k_eval_cover, k_eval_gaps in the last
+        timed evaluation (waits for it to finish)."""
+        ms = np.zeros(3, dtype=np.float32)
+        n = ctypes.c_int()
+        self._check(self.lib.cc_last_stage_times(self.h, ms.ctypes.data, 3, ctypes.byref(n)), "cc_last_stage_times")
+        return [float(x) for x in ms[: n.value]]
 
     def sb_eval(self, boxes):
         """Size-bound verdict masks (CC_SV_* bits) of host boxes (SB_BOX records)."""

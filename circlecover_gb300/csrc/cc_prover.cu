@@ -147,12 +147,20 @@ static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks,
     if (st) return st;
     CC_CUDA(h, cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s));
     const int g = h->sm_count * 8;
+    h->stages_recorded = 0;
+    if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[0], s));
     k_eval_main<L><<<g, 128, 0, s>>>(in, n, masks, q);
     CC_LAUNCHED(h);
+    if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[1], s));
     k_eval_cover<<<g, 128, 0, s>>>(q, masks);
     CC_LAUNCHED(h);
+    if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[2], s));
     k_eval_gaps<<<g, 128, 0, s>>>(q, masks);
     CC_LAUNCHED(h);
+    if (h->timing) {
+        CC_CUDA(h, cudaEventRecord(h->stage_ev[3], s));
+        h->stages_recorded = CC_EVAL_STAGES;
+    }
     return CC_OK;
 }
 
@@ -275,8 +283,32 @@ int cc_destroy(cc_handle* h) {
     for (auto& b : h->bufs)
         if (b.ptr) cudaFree(b.ptr);
     if (h->pinned) cudaFreeHost(h->pinned);
+    for (auto& e : h->stage_ev)
+        if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
+    return CC_OK;
+}
+
+int cc_set_stage_timing(cc_handle* h, int enable) {
+    if (!h) return CC_ERR_PARAM;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    if (enable && !h->stage_ev[0])
+        for (auto& e : h->stage_ev) CC_CUDA(h, cudaEventCreate(&e));
+    h->timing = enable != 0;
+    h->stages_recorded = 0;
+    return CC_OK;
+}
+
+int cc_last_stage_times(cc_handle* h, float* ms, int max_stages, int* n_stages) {
+    if (!h || !ms || !n_stages || max_stages < 0) return ccrt::fail(h, CC_ERR_PARAM, "cc_last_stage_times: bad argument");
+    *n_stages = 0;
+    if (!h->stages_recorded) return ccrt::fail(h, CC_ERR_PARAM, "cc_last_stage_times: no timed call recorded");
+    CC_CUDA(h, cudaSetDevice(h->device));
+    CC_CUDA(h, cudaEventSynchronize(h->stage_ev[h->stages_recorded]));
+    int k = h->stages_recorded < max_stages ? h->stages_recorded : max_stages;
+    for (int i = 0; i < k; ++i) CC_CUDA(h, cudaEventElapsedTime(&ms[i], h->stage_ev[i], h->stage_ev[i + 1]));
+    *n_stages = k;
     return CC_OK;
 }
 

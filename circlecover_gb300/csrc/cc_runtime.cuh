@@ -31,6 +31,10 @@ struct cc_handle {
     // pinned host staging for the host-memory entry points
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
+    // per-stage events of the evaluation (cc_set_stage_timing)
+    bool timing = false;
+    cudaEvent_t stage_ev[CC_EVAL_STAGES + 1] = {};
+    int stages_recorded = 0;
 };
 
 namespace ccrt {

@@ -212,6 +212,19 @@ int cc_sb_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* masks
 /* Number of kernels the last call on this handle launched. */
 uint64_t cc_last_launch_count(cc_handle* h);
 
+/* Per-stage device timing (no reference counterpart; a measurement aid).
+ * While enabled, cc_tight_eval_device records a CUDA event around each of
+ * its three kernels on the stream it launches on:
+ *   stage 0 = k_eval_main  (all criteria except the two bisections),
+ *   stage 1 = k_eval_cover (strip-width bisection of the compacted queue),
+ *   stage 2 = k_eval_gaps  (gap-width bisection of the compacted queue).
+ * cc_last_stage_times waits for the last recorded event and writes the
+ * elapsed milliseconds of each stage of the most recent call (at most
+ * max_stages values; *n_stages = how many were written). */
+#define CC_EVAL_STAGES 3
+int cc_set_stage_timing(cc_handle* h, int enable);
+int cc_last_stage_times(cc_handle* h, float* ms, int max_stages, int* n_stages);
+
 /* Run the tight proof from `root` with split counts `grid`.  On success
  * *criticals points to *n_crit boxes (release with cc_free), in the order the
  * reference's driver produces them; stats may be NULL. */

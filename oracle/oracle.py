@@ -162,6 +162,16 @@ class Port(_Lib):
         self.lib.ccport_subinterval.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_double)]
 
+    def tight_eval_passes(self, boxes):
+        """Per-box operation counts of the three evaluation passes (main,
+        strip-width bisection, gap-width bisection); counting build only."""
+        boxes = np.ascontiguousarray(boxes, dtype=TIGHT_BOX)
+        ops3 = np.zeros((len(boxes), 3), dtype=np.uint64)
+        f = self.lib.ccport_tight_eval_passes
+        f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        f(boxes.ctypes.data, len(boxes), ops3.ctypes.data)
+        return ops3
+
     def round(self, op, up, a, b=None, exact_fenv=False):
         a = np.ascontiguousarray(a, dtype=np.float64)
         bb = np.ascontiguousarray(b, dtype=np.float64) if b is not None else None

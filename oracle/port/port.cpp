@@ -106,6 +106,31 @@ int ccport_tight_eval(const cc_tight_box* boxes, size_t n, uint32_t* masks, uint
     return 0;
 }
 
+/* Operation counts of the three evaluation passes (main, strip-width
+ * bisection, gap-width bisection) per box: ops3[3*i + k].  Meaningful in the
+ * counting build only.  Used to attribute the algorithmic work of a box to
+ * the GPU kernel that executes each pass. */
+int ccport_tight_eval_passes(const cc_tight_box* boxes, size_t n, uint64_t* ops3) {
+    for (size_t i = 0; i < n; ++i) {
+        const cc_tight_box& in = boxes[i];
+        ct::Box b{to_iv(in.la), {to_iv(in.r[0]), to_iv(in.r[1]), to_iv(in.r[2]), to_iv(in.r[3])}};
+        bool need_cover, need_gaps;
+        ct::CoverJob cj;
+        ct::GapsJob gj;
+        unsigned long long c0 = cc_port_op_count;
+        ct::eval_main(b, need_cover, cj, need_gaps, gj);
+        unsigned long long c1 = cc_port_op_count;
+        if (need_cover) ct::cover_pass(cj);
+        unsigned long long c2 = cc_port_op_count;
+        if (need_gaps) ct::gaps_pass(gj);
+        unsigned long long c3 = cc_port_op_count;
+        ops3[3 * i] = c1 - c0;
+        ops3[3 * i + 1] = c2 - c1;
+        ops3[3 * i + 2] = c3 - c2;
+    }
+    return 0;
+}
+
 int ccport_tight_prove(const cc_tight_box* root, const cc_tight_grid* grid, int threads, cc_tight_box** out, size_t* n_out,
                        cc_prove_stats* stats) {
     Driver::Box r{to_iv(root->la), {to_iv(root->r[0]), to_iv(root->r[1]), to_iv(root->r[2]), to_iv(root->r[3])}};

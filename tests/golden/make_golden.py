@@ -119,8 +119,16 @@ def main():
     bench = W.tight_microbench(1 << 16, seed=1)
     bm, bops = ref.tight_eval(bench, threads=8, count_ops=True)
     assert bops.max() < 65536
-    np.savez_compressed(os.path.join(HERE, "tight_bench_ops.npz"), ops=bops.astype(np.uint16), masks=bm)
-    print("bench sample: mean ops/box %.1f" % bops.mean())
+    # the share of each box's work done by the two bisection passes (the
+    # strip-width and gap-width kernels): the port's count of those loops,
+    # which execute the reference's operations one for one; the main pass
+    # gets the rest of the reference's count
+    p3 = O.Port(count=True).tight_eval_passes(bench)
+    assert np.all(p3[:, 1] + p3[:, 2] <= bops)
+    np.savez_compressed(os.path.join(HERE, "tight_bench_ops.npz"), ops=bops.astype(np.uint16), masks=bm,
+                        cover_ops=p3[:, 1].astype(np.uint16), gaps_ops=p3[:, 2].astype(np.uint16))
+    print("bench sample: mean ops/box %.1f (strip bisection %.1f, gap bisection %.1f)"
+          % (bops.mean(), p3[:, 1].mean(), p3[:, 2].mean()))
 
     # size-bound criteria: per-box masks of the reference's code
     sb_parts = [W.sb_boxes(2000, seed=3, la_hi=2.5), W.sb_boxes(1500, seed=4, la_hi=8.0), sb_edge_boxes()]

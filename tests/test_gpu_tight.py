@@ -73,6 +73,22 @@ def test_eval_device_soa(prover, port):
     assert np.array_equal(got, port.tight_eval(boxes, threads=16))
 
 
+def test_stage_timing_times_three_kernels_without_changing_masks(prover, port):
+    import torch
+    boxes = W.tight_microbench(40_000, seed=32)
+    soa = torch.from_numpy(W.to_soa(boxes)).cuda()
+    masks = torch.zeros(len(boxes), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    with pytest.raises(Exception):
+        prover.stage_times()  # nothing timed yet
+    prover.set_stage_timing(True)
+    prover.tight_eval_device(soa.data_ptr(), len(boxes), masks.data_ptr())
+    ms = prover.stage_times()
+    prover.set_stage_timing(False)
+    assert len(ms) == 3 and all(t > 0 for t in ms)
+    assert np.array_equal(masks.cpu().numpy().view(np.uint32), port.tight_eval(boxes, threads=16))
+
+
 def cc_stream_sync(prover):
     import torch
     torch.cuda.synchronize()
