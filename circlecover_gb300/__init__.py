@@ -32,6 +32,13 @@ REFERENCE_GRID = dict(la_init=256, r_init=(128, 128, 128, 128), gens=(1, 2, 2, 2
                       r_gen=(128, 128, 128, 64))
 
 
+# reference split counts of the size-bound proof (rectangle_size_bound.cu:36-62)
+REFERENCE_SB_GRID = dict(la_init=256, r_init=(128, 128, 64, 64, 64, 64), la_gen=64, r_gen=(32, 32, 16, 16, 16, 32),
+                         gens=1)
+SB_LEAF_OUTCOMES = 17
+SBT_LEAF_EMPTY, SBT_LEAF_CRITICAL, SBT_LEAF_TRAPPED = 14, 15, 16
+
+
 class CudaError(RuntimeError):
     pass
 
@@ -68,6 +75,59 @@ class CcProveStats(ctypes.Structure):
     ]
 
 
+class CcSbGrid(ctypes.Structure):
+    _fields_ = [
+        ("la_splits_init", ctypes.c_int),
+        ("r_splits_init", ctypes.c_int * 6),
+        ("la_splits_gen", ctypes.c_int),
+        ("r_splits_gen", ctypes.c_int * 6),
+        ("num_generations", ctypes.c_int),
+    ]
+
+
+class CcSbProveStats(ctypes.Structure):
+    _fields_ = [
+        ("task_counts", ctypes.c_uint64 * 4),
+        ("cell_counts", ctypes.c_uint64 * 4),
+        ("leaf_counts", ctypes.c_uint64 * SB_LEAF_OUTCOMES),
+        ("digest", ctypes.c_uint64),
+        ("leaf_evals", ctypes.c_uint64),
+        ("trapped_leaves", ctypes.c_uint64),
+        ("trapped_shortcuts", ctypes.c_uint64),
+        ("gen_sizes", ctypes.c_uint64 * (MAX_GEN + 1)),
+        ("generations_run", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("seconds", ctypes.c_double),
+        ("kernel_launches", ctypes.c_uint64),
+    ]
+
+
+def make_sb_grid(la_init, r_init, la_gen=64, r_gen=(32, 32, 16, 16, 16, 32), gens=0):
+    """Split counts of the size-bound proof (cc_sb_grid)."""
+    g = CcSbGrid()
+    g.la_splits_init = la_init
+    g.la_splits_gen = la_gen
+    for k in range(6):
+        g.r_splits_init[k] = r_init[k]
+        g.r_splits_gen[k] = r_gen[k]
+    g.num_generations = gens
+    return g
+
+
+def sb_stats_to_dict(s):
+    return {
+        "task_counts": [int(x) for x in s.task_counts],
+        "cell_counts": [int(x) for x in s.cell_counts],
+        "leaf_counts": [int(x) for x in s.leaf_counts],
+        "digest": int(s.digest),
+        "leaf_evals": int(s.leaf_evals),
+        "trapped_leaves": int(s.trapped_leaves),
+        "trapped_shortcuts": int(s.trapped_shortcuts),
+        "gen_sizes": [int(s.gen_sizes[g]) for g in range(int(s.generations_run) + 1)],
+        "generations_run": int(s.generations_run),
+    }
+
+
 def make_grid(la_init, r_init, gens=(), r_gen=(128, 128, 128, 64)):
     g = CcTightGrid()
     g.la_splits_init = int(la_init)
@@ -100,7 +160,7 @@ _lib = None
 EXPORTS = [
     "cc_create", "cc_destroy", "cc_status_str", "cc_last_error", "cc_tight_eval", "cc_tight_eval_device",
     "cc_last_launch_count", "cc_tight_prove", "cc_tight_prove_ex", "cc_tight_summary", "cc_interrupt", "cc_free",
-    "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times",
+    "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove",
 ]
 
 
@@ -134,6 +194,8 @@ def load_library(path=LIB_PATH):
     lib.cc_sb_eval.argtypes = [vp, vp, sz, vp]
     lib.cc_sb_eval_device.argtypes = [vp, vp, sz, vp, vp]
     lib.cc_interrupt.argtypes = [vp]
+    lib.cc_sb_prove.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.POINTER(vp), ctypes.POINTER(sz),
+                                ctypes.POINTER(vp), ctypes.POINTER(CcSbProveStats)]
     lib.cc_set_stage_timing.argtypes = [vp, ctypes.c_int]
     lib.cc_last_stage_times.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     lib.cc_free.argtypes = [vp]
@@ -238,6 +300,30 @@ class Prover:
             ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)
         self.lib.cc_free(out)
         return arr, stats_to_dict(st)
+
+    def sb_find_critical_intervals(self, root, grid):
+        """The size-bound proof from `root` (an SB_BOX record) with split counts
+        `grid` (make_sb_grid); returns (criticals, flags, stats).  Criticals
+        are in the reference's final order (sorted and merged); flags bit 0 =
+        kept because a criterion reached a trap site."""
+        root = np.ascontiguousarray(np.asarray(root, dtype=SB_BOX).reshape(1))
+        out = ctypes.c_void_p()
+        flags = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcSbProveStats()
+        self._check(self.lib.cc_sb_prove(self.h, root.ctypes.data, ctypes.byref(grid), ctypes.byref(out),
+                                         ctypes.byref(n), ctypes.byref(flags), ctypes.byref(st)), "cc_sb_prove")
+        arr = np.zeros(n.value, dtype=SB_BOX)
+        fl = np.zeros(n.value, dtype=np.uint32)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * SB_BOX.itemsize)
+            ctypes.memmove(fl.ctypes.data, flags.value, n.value * 4)
+        self.lib.cc_free(out)
+        self.lib.cc_free(flags)
+        d = sb_stats_to_dict(st)
+        d["seconds"] = float(st.seconds)
+        d["kernel_launches"] = int(st.kernel_launches)
+        return arr, fl, d
 
     def interrupt(self):
         self.lib.cc_interrupt(self.h)

@@ -1,8 +1,8 @@
 """In-tree build of the prover's CUDA library for sm_103a.
 
 ``libcirclecover_gb300.so`` (under ``circlecover_gb300/_build/``) exports the C
-ABI of ``include/circlecover_gb300.h``.  Two translation units are compiled in
-parallel with nvcc and linked as a shared library; the main one with
+ABI of ``include/circlecover_gb300.h``.  The translation units are compiled in
+parallel with nvcc and linked as a shared library; the prover's with
 ``-fmad=false`` (no implicit FMA contraction), the diagnostic one with nvcc's
 default contraction on purpose.
 """
@@ -23,6 +23,7 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcom
 UNITS = [
     ("cc_prover.cu", ["-fmad=false", "-Xptxas", "-v"]),
     ("cc_sb_kernels.cu", ["-fmad=false", "-Xptxas", "-v"]),
+    ("cc_sb_prove.cu", ["-fmad=false", "-Xptxas", "-v"]),
     ("cc_selftest_fmad.cu", []),
 ]
 

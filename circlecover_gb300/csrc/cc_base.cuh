@@ -16,7 +16,7 @@
 #if defined(__CUDACC__) && !defined(CC_HOST_PORT)
 #define CC_DEVICE_BUILD 1
 #define CC_FN __device__ __forceinline__
-#define CC_FN_NOINLINE __device__ __noinline__
+#define CC_FN_NOINLINE static __device__ __noinline__
 #define CC_FN_INL __device__ inline
 #else
 #define CC_FN static inline
@@ -89,7 +89,11 @@ CC_FN void trap(uint32_t site) { cc_trap_words[threadIdx.x] = (uint8_t)site; }
 CC_FN uint32_t trap_status() { return cc_trap_words[threadIdx.x]; }
 CC_FN void trap_clear() { cc_trap_words[threadIdx.x] = TRAP_NONE; }
 #else
-extern thread_local uint32_t cc_port_trap_word;
+// host build: per-thread status (initial-exec TLS: a plain load per access)
+#ifndef CC_HOST_TLS
+#define CC_HOST_TLS thread_local __attribute__((tls_model("initial-exec")))
+#endif
+extern CC_HOST_TLS uint32_t cc_port_trap_word;
 CC_FN void trap(uint32_t site) { cc_port_trap_word = site; }
 CC_FN uint32_t trap_status() { return cc_port_trap_word; }
 CC_FN void trap_clear() { cc_port_trap_word = TRAP_NONE; }

@@ -1,0 +1,723 @@
+// Device engine of the size-bound proof (reference:
+// rectangle_size_bound/rectangle_size_bound.cu:132-382) and its C ABI entry
+// point cc_sb_prove.
+//
+// The reference enumerates the (lambda, r1, r2) tasks of a parent box on the
+// host and launches one kernel per task (about 4.2 million synchronous
+// launches for its initial pass), each a (r3, r4)-blocks x (r5, r6)-threads
+// grid in which every thread runs the whole criteria cascade on its leaf.
+// Here the tasks of a generation go through device stages in stream order:
+//
+//   tasks   one thread per task: its box (running r1 tightening,
+//           from_la_r1_r2), empty check, whole-task shortcuts
+//   cells   one thread per (task, r3 piece): the three r3 shortcuts
+//   leaves  one thread per (cell, r4, r5, r6 piece): leaf box, tighten, R,
+//           empty check, the first criterion of the cascade
+//   pass K  one thread per leaf still undecided: criterion K (K = 1..12),
+//           survivors compacted into the next pass's queue
+//   seven   the seven-disk strategies, the costliest criterion, in three
+//           kernels: one thread per leaf for the r7-range prefix, one thread
+//           per (leaf, r7 piece) for the 16 pieces, one thread per leaf to
+//           combine the pieces' outcomes as the sequential loop would
+//
+// so that every kernel runs one criterion on full warps of leaves that need
+// it, instead of warps in which one lane runs the seven-disk strategies while
+// 31 lanes wait.  Survivors of the last criterion and leaves whose cascade
+// reached a trap site are the critical boxes; the host merges them per
+// generation exactly as merge_critical_intervals<N> does.  Queues are sized
+// so that they cannot overflow: a task chunk bounds the cell count, and a
+// leaf slice whose undecided leaves would not fit the pass queues is undone
+// (counters restored from a snapshot) and redone in halves.  The slice
+// length adapts to the share of leaves that the first criterion leaves
+// undecided, so that few slices (and few kernel tails) cover a task chunk.
+//
+// Every task, r3 cell and leaf visited contributes one count and one mixed
+// key to the trace (cc_sb_prove_stats), computed the same way by the oracle.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "cc_runtime.cuh"
+#include "cc_sb_proof.cuh"
+
+using cc::Iv;
+namespace sb = cc::sb;
+using sb::Box6;
+
+namespace {
+
+struct SbTask {  // a task that passed the whole-task shortcuts
+    Box6 box;
+    uint64_t id;
+    uint64_t pad;
+};
+static_assert(sizeof(SbTask) == 128, "task record");
+
+struct SbCell {  // an r3 cell that passed the r3 shortcuts
+    Iv r3;
+    uint32_t task;
+    uint32_t i3;
+};
+
+struct SbLeaf {  // an undecided or critical leaf
+    Box6 box;
+    uint64_t id;   // task id
+    uint64_t idx;  // i3 | i4 << 11 | i5 << 22 | i6 << 33 | trapped << 63
+};
+static_assert(sizeof(SbLeaf) == 128, "leaf record");
+
+struct SbCounters {
+    unsigned long long n_task, n_cell, n_q[2], n_crit;
+    unsigned long long overflow;
+    unsigned long long leaf_evals, trapped_shortcuts;
+    unsigned long long digest;
+    unsigned long long task_counts[4], cell_counts[4], leaf_counts[CC_SBT_LEAF_OUTCOMES];
+};
+
+struct SevenJob {  // a leaf whose seven-disk prefix left r7 pieces to check
+    sb::SevenPrefix pre;
+    uint32_t leaf;  // index in the pass queue
+    uint32_t fail_mask, trap_mask, pad;
+};
+
+constexpr int kThreads = 128;
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ unsigned long long warp_append(unsigned long long* counter, bool want, unsigned long long cap,
+                                                          unsigned long long* overflow) {
+    const unsigned lane = threadIdx.x & 31;
+    unsigned ballot = __ballot_sync(0xffffffffu, want);
+    if (ballot == 0) return ~0ULL;
+    unsigned long long base = 0;
+    if (lane == (unsigned)(__ffs(ballot) - 1)) base = atomicAdd(counter, (unsigned long long)__popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
+    unsigned long long slot = base + __popc(ballot & ((1u << lane) - 1));
+    if (!want) return ~0ULL;
+    if (slot >= cap) {
+        atomicExch(overflow, 1ULL);
+        return ~0ULL;
+    }
+    return slot;
+}
+
+// warp-uniform grid-stride loop: all 32 lanes enter every iteration
+#define SB_WARP_LOOP(total)                                                                              \
+    for (unsigned long long base_ = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); \
+         base_ < (total); base_ += (unsigned long long)gridDim.x * blockDim.x)
+
+template <int N>
+struct BlockTrace {
+    unsigned long long counts[N];
+    unsigned long long digest;
+    unsigned long long extra;  // leaf evaluations or trapped shortcuts
+};
+
+template <int N>
+__device__ __forceinline__ void trace_init(BlockTrace<N>& bt) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) bt.counts[i] = 0;
+    if (threadIdx.x == 0) bt.digest = 0, bt.extra = 0;
+    __syncthreads();
+}
+
+template <int N>
+__device__ __forceinline__ void trace_note(BlockTrace<N>& bt, bool valid, uint64_t key, int outcome) {
+    uint64_t d = valid ? key : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if ((threadIdx.x & 31) == 0 && d) atomicAdd(&bt.digest, (unsigned long long)d);
+    if (valid) atomicAdd(&bt.counts[outcome], 1ULL);
+}
+
+template <int N>
+__device__ __forceinline__ void trace_flush(BlockTrace<N>& bt, unsigned long long* counts, SbCounters* c,
+                                            unsigned long long* extra) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+        if (bt.counts[i]) atomicAdd(&counts[i], bt.counts[i]);
+    if (threadIdx.x == 0) {
+        if (bt.digest) atomicAdd(&c->digest, bt.digest);
+        if (bt.extra && extra) atomicAdd(extra, bt.extra);
+    }
+}
+
+__device__ __forceinline__ uint64_t pack_idx(int i3, int i4, int i5, int i6) {
+    return (uint64_t)i3 | ((uint64_t)i4 << 11) | ((uint64_t)i5 << 22) | ((uint64_t)i6 << 33);
+}
+
+__device__ __forceinline__ uint64_t leaf_key(int gen, const SbLeaf& l, int outcome) {
+    const uint64_t x = l.idx;
+    return sb::sb_trace_key(gen, l.id, 2, (int)(x & 2047), (int)((x >> 11) & 2047), (int)((x >> 22) & 2047),
+                            (int)((x >> 33) & 2047), outcome);
+}
+
+// ---------------------------------------------------------------- stages
+struct TaskGrid {
+    int gen, nla, n1, n2;
+    unsigned long long per_parent;
+};
+
+// tasks [t0, t1) of the generation (rectangle_size_bound.cu:281-296, 161-164)
+__global__ void __launch_bounds__(kThreads) k_sbp_tasks(const Box6* __restrict__ parents, unsigned long long t0,
+                                                         unsigned long long t1, TaskGrid g, SbTask* __restrict__ out,
+                                                         unsigned long long cap, SbCounters* c) {
+    __shared__ BlockTrace<4> bt;
+    trace_init(bt);
+    SB_WARP_LOOP(t1 - t0) {
+        const unsigned long long idx = t0 + base_ + (threadIdx.x & 31);
+        const bool valid = idx < t1;
+        int outcome = CC_SBT_TASK_EMPTY;
+        Box6 tb;
+        if (valid) {
+            const unsigned long long p = idx / g.per_parent, rem = idx % g.per_parent;
+            const int r2_i = (int)(rem % g.n2);
+            const int r1_i = (int)((rem / g.n2) % g.n1);
+            const int la_i = (int)(rem / ((unsigned long long)g.n2 * g.n1));
+            tb = sb::task_box(parents[p], la_i, g.nla, r1_i, g.n1, r2_i, g.n2);
+            bool trapped = false;
+            outcome = sb::task_outcome(tb, trapped);
+            if (trapped) atomicAdd(&bt.extra, 1ULL);
+        }
+        trace_note(bt, valid, sb::sb_trace_key(g.gen, idx, 0, 0, 0, 0, 0, outcome), outcome);
+        unsigned long long slot = warp_append(&c->n_task, valid && outcome == CC_SBT_TASK_SPLIT, cap, &c->overflow);
+        if (slot != ~0ULL) {
+            out[slot].box = tb;
+            out[slot].id = idx;
+        }
+    }
+    trace_flush(bt, c->task_counts, c, &c->trapped_shortcuts);
+}
+
+// r3 cells of the queued tasks (rectangle_size_bound.cu:171-178)
+__global__ void __launch_bounds__(kThreads) k_sbp_cells(const SbTask* __restrict__ tasks, int gen, int n3,
+                                                         SbCell* __restrict__ out, unsigned long long cap,
+                                                         SbCounters* c) {
+    __shared__ BlockTrace<4> bt;
+    trace_init(bt);
+    const unsigned long long total = c->n_task * (unsigned long long)n3;
+    SB_WARP_LOOP(total) {
+        const unsigned long long idx = base_ + (threadIdx.x & 31);
+        const bool valid = idx < total;
+        int outcome = CC_SBT_CELL_SPLIT;
+        uint32_t t = 0;
+        int i3 = 0;
+        Iv r3{0.0, 0.0};
+        uint64_t key = 0;
+        if (valid) {
+            t = (uint32_t)(idx / n3);
+            i3 = (int)(idx % n3);
+            const Box6 tb = tasks[t].box;
+            r3 = cc::subinterval(tb.r[2], i3, n3);
+            bool trapped = false;
+            outcome = sb::cell_outcome(tb, r3, trapped);
+            if (trapped) atomicAdd(&bt.extra, 1ULL);
+            key = sb::sb_trace_key(gen, tasks[t].id, 1, i3, 0, 0, 0, outcome);
+        }
+        trace_note(bt, valid, key, outcome);
+        unsigned long long slot = warp_append(&c->n_cell, valid && outcome == CC_SBT_CELL_SPLIT, cap, &c->overflow);
+        if (slot != ~0ULL) out[slot] = SbCell{r3, t, (uint32_t)i3};
+    }
+    trace_flush(bt, c->cell_counts, c, &c->trapped_shortcuts);
+}
+
+struct LeafGrid {
+    int gen, n4, n5, n6;
+};
+
+// Leaves [l0, l1) of the cell grid (rectangle_size_bound.cu:180-205): box,
+// tighten, R and the empty checks, then criterion 0 of the cascade.
+// Undecided leaves go to queue `q`, trapped ones to the criticals.
+__global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restrict__ tasks,
+                                                          const SbCell* __restrict__ cells, unsigned long long l0,
+                                                          unsigned long long l1, LeafGrid g, SbLeaf* __restrict__ q,
+                                                          unsigned long long* n_q, unsigned long long q_cap,
+                                                          SbLeaf* __restrict__ crit, unsigned long long crit_cap,
+                                                          SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    const unsigned long long n456 = (unsigned long long)g.n4 * g.n5 * g.n6;
+    SB_WARP_LOOP(l1 - l0) {
+        const unsigned long long idx = l0 + base_ + (threadIdx.x & 31);
+        const bool valid = idx < l1;
+        int outcome = CC_SBT_LEAF_EMPTY;
+        SbLeaf leaf;
+        if (valid) {
+            const SbCell cell = cells[idx / n456];
+            const unsigned long long rem = idx % n456;
+            const int i6 = (int)(rem % g.n6);
+            const int i5 = (int)((rem / g.n6) % g.n5);
+            const int i4 = (int)(rem / ((unsigned long long)g.n6 * g.n5));
+            const SbTask& task = tasks[cell.task];
+            leaf.box = sb::leaf_box(task.box, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6);
+            leaf.id = task.id;
+            leaf.idx = pack_idx((int)cell.i3, i4, i5, i6);
+            sb::Vals v;
+            v.R = sb::remaining_weight(leaf.box);
+            if (sb::box_empty(leaf.box) || cc::empty(v.R)) {
+                outcome = CC_SBT_LEAF_EMPTY;
+            } else {
+                cc::trap_clear();
+                const bool ok = sb::sb_criterion(0, leaf.box, v);
+                if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
+                else outcome = ok ? 0 : CC_SBT_LEAF_CRITICAL;  // CRITICAL here = undecided
+                cc::trap_clear();
+            }
+        }
+        const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
+        trace_note(bt, valid && !undecided, valid ? leaf_key(g.gen, leaf, outcome) : 0, outcome);
+        const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
+        if ((threadIdx.x & 31) == 0) atomicAdd(&bt.extra, (unsigned long long)nv);
+        unsigned long long slot = warp_append(n_q, undecided, q_cap, &c->overflow);
+        if (slot != ~0ULL) q[slot] = leaf;
+        const bool trapped = valid && outcome == CC_SBT_LEAF_TRAPPED;
+        slot = warp_append(&c->n_crit, trapped, crit_cap, &c->overflow);
+        if (slot != ~0ULL) {
+            leaf.idx |= 1ULL << 63;
+            crit[slot] = leaf;
+        }
+    }
+    trace_flush(bt, c->leaf_counts, c, &c->leaf_evals);
+}
+
+// Criterion K on the undecided leaves of `qin` (rectangle_size_bound.cu:
+// 199-231).  Undecided leaves go to `qout`, or to the criticals after the
+// last criterion; a trap sends the leaf to the criticals, flagged.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_sbp_pass(const SbLeaf* __restrict__ qin, const unsigned long long* n_in,
+                                                        SbLeaf* __restrict__ qout, unsigned long long* n_out,
+                                                        unsigned long long q_cap, SbLeaf* __restrict__ crit,
+                                                        unsigned long long crit_cap, int gen, SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    const unsigned long long total = *n_in;
+    constexpr bool kLast = K == sb::SB_NUM_CRITERIA - 1;
+    SB_WARP_LOOP(total) {
+        const unsigned long long idx = base_ + (threadIdx.x & 31);
+        const bool valid = idx < total;
+        int outcome = CC_SBT_LEAF_CRITICAL;
+        SbLeaf leaf;
+        if (valid) {
+            leaf = qin[idx];
+            sb::Vals v;
+            v.R = sb::remaining_weight(leaf.box);
+            cc::trap_clear();
+            const bool ok = sb::sb_criterion(K, leaf.box, v);
+            if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
+            else if (ok) outcome = K;
+            cc::trap_clear();
+        }
+        const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
+        const bool decided = valid && (!undecided || kLast);
+        trace_note(bt, decided, decided ? leaf_key(gen, leaf, outcome) : 0, outcome);
+        if (!kLast) {
+            unsigned long long slot = warp_append(n_out, undecided, q_cap, &c->overflow);
+            if (slot != ~0ULL) qout[slot] = leaf;
+        }
+        const bool to_crit = valid && (outcome == CC_SBT_LEAF_TRAPPED || (kLast && undecided));
+        unsigned long long slot = warp_append(&c->n_crit, to_crit, crit_cap, &c->overflow);
+        if (slot != ~0ULL) {
+            if (outcome == CC_SBT_LEAF_TRAPPED) leaf.idx |= 1ULL << 63;
+            crit[slot] = leaf;
+        }
+    }
+    trace_flush(bt, c->leaf_counts, c, nullptr);
+}
+
+// Seven-disk strategies, prefix (seven_disk_strategies.cu:1397-1432): decided
+// leaves are traced here, the others become jobs of 16 r7 pieces.
+__global__ void __launch_bounds__(kThreads) k_sbp_seven_prefix(const SbLeaf* __restrict__ qin,
+                                                                const unsigned long long* n_in, SevenJob* __restrict__ jobs,
+                                                                unsigned long long* n_jobs, unsigned long long job_cap,
+                                                                SbLeaf* __restrict__ crit, unsigned long long crit_cap,
+                                                                int gen, SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    const unsigned long long total = *n_in;
+    SB_WARP_LOOP(total) {
+        const unsigned long long idx = base_ + (threadIdx.x & 31);
+        const bool valid = idx < total;
+        int outcome = CC_SBT_LEAF_CRITICAL;  // here: pieces to check
+        SbLeaf leaf;
+        sb::SevenPrefix pre;
+        if (valid) {
+            leaf = qin[idx];
+            sb::Vals v;
+            v.R = sb::remaining_weight(leaf.box);
+            cc::trap_clear();
+            const bool ok = sb::seven_disk_prefix(leaf.box, v, pre);
+            if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
+            else if (ok) outcome = sb::SB_SEVEN_DISK;
+            cc::trap_clear();
+        }
+        const bool open = valid && outcome == CC_SBT_LEAF_CRITICAL;
+        const bool decided = valid && !open;
+        trace_note(bt, decided, decided ? leaf_key(gen, leaf, outcome) : 0, outcome);
+        unsigned long long slot = warp_append(n_jobs, open, job_cap, &c->overflow);
+        if (slot != ~0ULL) jobs[slot] = SevenJob{pre, (uint32_t)idx, 0u, 0u, 0u};
+        slot = warp_append(&c->n_crit, valid && outcome == CC_SBT_LEAF_TRAPPED, crit_cap, &c->overflow);
+        if (slot != ~0ULL) {
+            leaf.idx |= 1ULL << 63;
+            crit[slot] = leaf;
+        }
+    }
+    trace_flush(bt, c->leaf_counts, c, nullptr);
+}
+
+// Seven-disk strategies, one r7 piece per thread (:1434-1493)
+__global__ void __launch_bounds__(kThreads) k_sbp_seven_pieces(const SbLeaf* __restrict__ qin,
+                                                                SevenJob* __restrict__ jobs,
+                                                                const unsigned long long* n_jobs) {
+    const unsigned long long total = *n_jobs * 16ULL;
+    for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (unsigned long long)gridDim.x * blockDim.x) {
+        SevenJob& job = jobs[idx >> 4];
+        const int k = (int)(idx & 15);
+        const Box6 box = qin[job.leaf].box;
+        sb::Vals v;
+        v.R = sb::remaining_weight(box);
+        cc::trap_clear();
+        const bool ok = sb::seven_disk_piece(box, v, job.pre, k);
+        const bool trapped = cc::trap_status() != cc::TRAP_NONE;
+        cc::trap_clear();
+        if (!ok) atomicOr(&job.fail_mask, 1u << k);
+        if (trapped) atomicOr(&job.trap_mask, 1u << k);
+    }
+}
+
+// Seven-disk strategies, the pieces' outcomes combined as the sequential loop
+// would: it stops at the first piece that is not covered, so only traps in
+// pieces up to that one count.
+__global__ void __launch_bounds__(kThreads) k_sbp_seven_resolve(const SbLeaf* __restrict__ qin,
+                                                                 const SevenJob* __restrict__ jobs,
+                                                                 const unsigned long long* n_jobs,
+                                                                 SbLeaf* __restrict__ crit, unsigned long long crit_cap,
+                                                                 int gen, SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    const unsigned long long total = *n_jobs;
+    SB_WARP_LOOP(total) {
+        const unsigned long long idx = base_ + (threadIdx.x & 31);
+        const bool valid = idx < total;
+        int outcome = sb::SB_SEVEN_DISK;
+        SbLeaf leaf;
+        if (valid) {
+            const SevenJob job = jobs[idx];
+            leaf = qin[job.leaf];
+            const uint32_t first_fail = job.fail_mask ? (uint32_t)(__ffs(job.fail_mask) - 1) : 15u;
+            const uint32_t seen = first_fail >= 15u ? 0xffffu : ((2u << first_fail) - 1u);
+            if (job.trap_mask & seen) outcome = CC_SBT_LEAF_TRAPPED;
+            else if (job.fail_mask) outcome = CC_SBT_LEAF_CRITICAL;
+        }
+        trace_note(bt, valid, valid ? leaf_key(gen, leaf, outcome) : 0, outcome);
+        const bool to_crit = valid && outcome != sb::SB_SEVEN_DISK;
+        unsigned long long slot = warp_append(&c->n_crit, to_crit, crit_cap, &c->overflow);
+        if (slot != ~0ULL) {
+            if (outcome == CC_SBT_LEAF_TRAPPED) leaf.idx |= 1ULL << 63;
+            crit[slot] = leaf;
+        }
+    }
+    trace_flush(bt, c->leaf_counts, c, nullptr);
+}
+
+// ---------------------------------------------------------------- host side
+enum Slot { S_PARENTS = 0, S_TASKS, S_CELLS, S_Q0, S_Q1, S_CRIT, S_COUNTERS, S_JOBS };
+constexpr int kSlotBase = 24;  // handle buffer slots 24..31
+
+struct Engine {
+    cc_handle* h;
+    cudaStream_t s;
+    int grid;
+    unsigned long long task_chunk, cell_cap, slice, crit_cap;
+    unsigned long long range;  // leaves per slice, adapted as the proof runs
+    Box6* parents = nullptr;
+    SbTask* tasks = nullptr;
+    SbCell* cells = nullptr;
+    SbLeaf* q[2] = {nullptr, nullptr};
+    SbLeaf* crit = nullptr;
+    SevenJob* jobs = nullptr;
+    SbCounters* dc = nullptr;
+    SbCounters* backup = nullptr;  // snapshot of dc taken before each slice
+    SbCounters* hc = nullptr;      // pinned
+    std::vector<SbLeaf> found;
+    uint64_t launches = 0;
+};
+
+// criteria K..12 as passes over the compacted queue, then the seven-disk
+// kernels; the undecided leaves of one pass are the next one's input
+template <int K>
+int launch_passes(Engine& e, int gen, int src) {
+    if constexpr (K < sb::SB_SEVEN_DISK) {
+        const int dst = src ^ 1;
+        CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
+        k_sbp_pass<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], e.q[dst], &e.dc->n_q[dst], e.slice,
+                                                     e.crit, e.crit_cap, gen, e.dc);
+        CC_LAUNCHED(e.h);
+        e.launches++;
+        return launch_passes<K + 1>(e, gen, dst);
+    } else {
+        static_assert(K == sb::SB_NUM_CRITERIA - 1, "the seven-disk strategies are the last criterion");
+        unsigned long long* n_jobs = &e.dc->n_q[src ^ 1];  // the free queue's counter counts the jobs
+        CC_CUDA(e.h, cudaMemsetAsync(n_jobs, 0, sizeof(unsigned long long), e.s));
+        k_sbp_seven_prefix<<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], e.jobs, n_jobs, e.slice, e.crit,
+                                                          e.crit_cap, gen, e.dc);
+        CC_LAUNCHED(e.h);
+        k_sbp_seven_pieces<<<e.grid, kThreads, 0, e.s>>>(e.q[src], e.jobs, n_jobs);
+        CC_LAUNCHED(e.h);
+        k_sbp_seven_resolve<<<e.grid, kThreads, 0, e.s>>>(e.q[src], e.jobs, n_jobs, e.crit, e.crit_cap, gen, e.dc);
+        CC_LAUNCHED(e.h);
+        e.launches += 3;
+        return CC_OK;
+    }
+}
+
+int sync_counters(Engine& e) {
+    CC_CUDA(e.h, cudaMemcpyAsync(e.hc, e.dc, sizeof(SbCounters), cudaMemcpyDeviceToHost, e.s));
+    CC_CUDA(e.h, cudaStreamSynchronize(e.s));
+    if (e.hc->overflow) return ccrt::fail(e.h, CC_ERR_QUEUE_OVERFLOW, "cc_sb_prove: queue overflow");
+    return CC_OK;
+}
+
+int drain_criticals(Engine& e) {
+    const unsigned long long n = e.hc->n_crit;
+    if (!n) return CC_OK;
+    size_t old = e.found.size();
+    e.found.resize(old + n);
+    CC_CUDA(e.h, cudaMemcpyAsync(e.found.data() + old, e.crit, n * sizeof(SbLeaf), cudaMemcpyDeviceToHost, e.s));
+    CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_crit, 0, sizeof(unsigned long long), e.s));
+    CC_CUDA(e.h, cudaStreamSynchronize(e.s));
+    e.hc->n_crit = 0;
+    return CC_OK;
+}
+
+// one generation: every task of every parent (find_critical_intervals_in)
+// A generation after the first stops at a chunk boundary when cc_interrupt
+// was called (the initial pass is not interruptible, as in the reference:
+// rectangle_size_bound.cu:325, 341).
+int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla, const int* rn) {
+    int st;
+    void* p;
+    if ((st = ccrt::ensure(e.h, kSlotBase + S_PARENTS, parents.size() * sizeof(Box6), &p))) return st;
+    e.parents = (Box6*)p;
+    CC_CUDA(e.h, cudaMemcpyAsync(e.parents, parents.data(), parents.size() * sizeof(Box6), cudaMemcpyHostToDevice, e.s));
+    const unsigned long long per_parent = (unsigned long long)nla * rn[0] * rn[1];
+    const unsigned long long ntasks = parents.size() * per_parent;
+    const unsigned long long n456 = (unsigned long long)rn[3] * rn[4] * rn[5];
+    // a chunk's cells must fit the cell queue even if every task survives
+    unsigned long long chunk = e.cell_cap / (unsigned long long)rn[2];
+    if (chunk > e.task_chunk) chunk = e.task_chunk;
+    if (chunk < 1) chunk = 1;
+    TaskGrid tg{gen, nla, rn[0], rn[1], per_parent};
+    LeafGrid lg{gen, rn[3], rn[4], rn[5]};
+    for (unsigned long long t0 = 0; t0 < ntasks; t0 += chunk) {
+        if (gen > 0 && e.h->interrupt.load()) return CC_ERR_INTERRUPTED;
+        const unsigned long long t1 = t0 + chunk < ntasks ? t0 + chunk : ntasks;
+        CC_CUDA(e.h, cudaMemsetAsync(e.dc, 0, 2 * sizeof(unsigned long long), e.s));  // n_task, n_cell
+        int tgrid = (int)std::min<unsigned long long>((t1 - t0 + kThreads - 1) / kThreads, (unsigned long long)e.grid);
+        k_sbp_tasks<<<tgrid, kThreads, 0, e.s>>>(e.parents, t0, t1, tg, e.tasks, chunk, e.dc);
+        CC_LAUNCHED(e.h);
+        k_sbp_cells<<<e.grid, kThreads, 0, e.s>>>(e.tasks, gen, rn[2], e.cells, e.cell_cap, e.dc);
+        CC_LAUNCHED(e.h);
+        e.launches += 2;
+        if ((st = sync_counters(e))) return st;
+        const unsigned long long n_leaves = e.hc->n_cell * n456;
+        unsigned long long l0 = 0;
+        while (l0 < n_leaves) {
+            // room for the criticals of a full pass queue
+            if (e.hc->n_crit > e.crit_cap - e.slice && (st = drain_criticals(e))) return st;
+            const unsigned long long l1 = n_leaves - l0 > e.range ? l0 + e.range : n_leaves;
+            CC_CUDA(e.h, cudaMemcpyAsync(e.backup, e.dc, sizeof(SbCounters), cudaMemcpyDeviceToDevice, e.s));
+            CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[0], 0, sizeof(unsigned long long), e.s));
+            int lgrid = (int)std::min<unsigned long long>((l1 - l0 + kThreads - 1) / kThreads, (unsigned long long)e.grid);
+            k_sbp_leaves<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, e.q[0], &e.dc->n_q[0], e.slice,
+                                                      e.crit, e.crit_cap, e.dc);
+            CC_LAUNCHED(e.h);
+            e.launches++;
+            CC_CUDA(e.h, cudaMemcpyAsync(e.hc, e.dc, sizeof(SbCounters), cudaMemcpyDeviceToHost, e.s));
+            CC_CUDA(e.h, cudaStreamSynchronize(e.s));
+            if (e.hc->overflow) {  // undo the slice and retry with half of it
+                if (e.range == 1) return ccrt::fail(e.h, CC_ERR_QUEUE_OVERFLOW, "cc_sb_prove: queue overflow");
+                CC_CUDA(e.h, cudaMemcpyAsync(e.dc, e.backup, sizeof(SbCounters), cudaMemcpyDeviceToDevice, e.s));
+                if ((st = sync_counters(e))) return st;
+                e.range /= 2;
+                continue;
+            }
+            // aim the next slice at half of the pass queue
+            const unsigned long long open = e.hc->n_q[0] ? e.hc->n_q[0] : 1;
+            unsigned long long next = (unsigned long long)((double)(l1 - l0) * (double)(e.slice / 2) / (double)open);
+            e.range = std::max<unsigned long long>(std::min<unsigned long long>(1024, e.slice),
+                                                   std::min<unsigned long long>(next, 1ULL << 31));
+            if ((st = launch_passes<1>(e, gen, 0))) return st;
+            if ((st = sync_counters(e))) return st;
+            l0 = l1;
+        }
+    }
+    return drain_criticals(e);
+}
+
+// Variables::operator< (rectangle_size_bound/variables.hpp:82-94)
+bool iv_less(const Iv& a, const Iv& b) { return a.lo < b.lo || (a.lo == b.lo && a.hi < b.hi); }
+bool box_less(const Box6& a, const Box6& b) {
+    if (iv_less(a.la, b.la)) return true;
+    if (iv_less(b.la, a.la)) return false;
+    for (int i = 0; i < 6; ++i) {
+        if (iv_less(a.r[i], b.r[i])) return true;
+        if (iv_less(b.r[i], a.r[i])) return false;
+    }
+    return false;
+}
+bool iv_same(const Iv& a, const Iv& b) { return a.lo == b.lo && a.hi == b.hi; }
+
+struct Crit {
+    Box6 box;
+    uint32_t trapped;
+};
+
+// merge_critical_intervals<N> (rectangle_size_bound.cu:103-130)
+std::vector<Crit> merge(std::vector<Crit>& v, int n_merged) {
+    std::vector<Crit> out;
+    if (v.empty()) return out;
+    std::sort(v.begin(), v.end(), [](const Crit& a, const Crit& b) { return box_less(a.box, b.box); });
+    out.push_back(v.front());
+    for (const Crit& x : v) {
+        Crit& p = out.back();
+        bool same = iv_same(x.box.la, p.box.la);
+        for (int i = 0; same && i < n_merged; ++i) same = iv_same(x.box.r[i], p.box.r[i]);
+        if (same) {
+            for (int i = n_merged; i < 6; ++i) {  // Interval::do_join
+                if (x.box.r[i].lo < p.box.r[i].lo) p.box.r[i].lo = x.box.r[i].lo;
+                if (x.box.r[i].hi > p.box.r[i].hi) p.box.r[i].hi = x.box.r[i].hi;
+            }
+            p.trapped |= x.trapped;
+        } else {
+            out.push_back(x);
+        }
+    }
+    return out;
+}
+
+bool grid_ok(const cc_sb_grid* g) {
+    auto ok = [](int x) { return x >= 1 && x <= 2047; };
+    if (!ok(g->la_splits_init) || g->num_generations < 0 || g->num_generations > CC_MAX_GENERATIONS) return false;
+    if (g->num_generations > 0 && !ok(g->la_splits_gen)) return false;
+    for (int i = 0; i < 6; ++i) {
+        if (!ok(g->r_splits_init[i])) return false;
+        if (g->num_generations > 0 && !ok(g->r_splits_gen[i])) return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, cc_sb_box** criticals,
+                           size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats) {
+    if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
+    if (!grid_ok(grid)) return ccrt::fail(h, CC_ERR_PARAM, "cc_sb_prove: split counts must be in [1, 2047]");
+    const auto t_start = std::chrono::steady_clock::now();
+    h->launches = 0;
+    h->interrupt.store(0);
+    CC_CUDA(h, cudaSetDevice(h->device));
+    *criticals = nullptr;
+    *n_crit = 0;
+    if (flags) *flags = nullptr;
+
+    Engine e;
+    e.h = h;
+    e.s = h->stream;
+    e.grid = h->sm_count * 8;
+    // sizes of the work units (queue capacities follow from them); the
+    // environment can shrink them, which only changes how the same work is
+    // cut into launches
+    auto log2_env = [](const char* name, int dflt, int lo, int hi) {
+        const char* v = std::getenv(name);
+        int x = v ? std::atoi(v) : dflt;
+        return x < lo ? lo : (x > hi ? hi : x);
+    };
+    e.task_chunk = 1ULL << log2_env("CC_SB_TASK_CHUNK_LOG2", 18, 0, 18);
+    e.cell_cap = 1ULL << 22;
+    e.slice = 1ULL << log2_env("CC_SB_SLICE_LOG2", 22, 5, 26);
+    e.crit_cap = 2 * e.slice;
+    e.range = e.slice;
+    int st;
+    void* p;
+    if ((st = ccrt::ensure(h, kSlotBase + S_TASKS, e.task_chunk * sizeof(SbTask), &p))) return st;
+    e.tasks = (SbTask*)p;
+    if ((st = ccrt::ensure(h, kSlotBase + S_CELLS, e.cell_cap * sizeof(SbCell), &p))) return st;
+    e.cells = (SbCell*)p;
+    if ((st = ccrt::ensure(h, kSlotBase + S_Q0, e.slice * sizeof(SbLeaf), &p))) return st;
+    e.q[0] = (SbLeaf*)p;
+    if ((st = ccrt::ensure(h, kSlotBase + S_Q1, e.slice * sizeof(SbLeaf), &p))) return st;
+    e.q[1] = (SbLeaf*)p;
+    if ((st = ccrt::ensure(h, kSlotBase + S_CRIT, e.crit_cap * sizeof(SbLeaf), &p))) return st;
+    e.crit = (SbLeaf*)p;
+    if ((st = ccrt::ensure(h, kSlotBase + S_COUNTERS, 2 * sizeof(SbCounters), &p))) return st;
+    e.dc = (SbCounters*)p;
+    e.backup = e.dc + 1;
+    if ((st = ccrt::ensure(h, kSlotBase + S_JOBS, e.slice * sizeof(SevenJob), &p))) return st;
+    e.jobs = (SevenJob*)p;
+    if ((st = ccrt::ensure_pinned(h, sizeof(SbCounters)))) return st;
+    e.hc = (SbCounters*)h->pinned;
+    CC_CUDA(h, cudaMemsetAsync(e.dc, 0, sizeof(SbCounters), e.s));
+
+    std::vector<uint64_t> gen_sizes;
+    int generations_run = 0;
+    uint64_t trapped_leaves = 0;
+    std::vector<Box6> parents(1);
+    parents[0].la = Iv{root->la.lb, root->la.ub};
+    for (int i = 0; i < 6; ++i) parents[0].r[i] = Iv{root->r[i].lb, root->r[i].ub};
+    std::vector<Crit> cur;
+    int status = CC_OK;
+    for (int gen = 0; gen <= grid->num_generations; ++gen) {
+        if (gen > 0) {
+            if (cur.empty()) break;
+            parents.clear();
+            for (const Crit& c : cur) parents.push_back(c.box);
+        }
+        e.found.clear();
+        st = gen == 0 ? run_generation(e, parents, 0, grid->la_splits_init, grid->r_splits_init)
+                      : run_generation(e, parents, gen, grid->la_splits_gen, grid->r_splits_gen);
+        if (st == CC_ERR_INTERRUPTED) {  // keep the last complete generation's result
+            status = st;
+            break;
+        }
+        if (st) return st;
+        std::vector<Crit> found(e.found.size());
+        for (size_t i = 0; i < e.found.size(); ++i) {
+            found[i].box = e.found[i].box;
+            found[i].trapped = (uint32_t)(e.found[i].idx >> 63);
+            trapped_leaves += found[i].trapped;
+        }
+        const int n_merged = gen == 0 ? 0 : (gen % 3 == 0 ? 3 : (gen % 3 == 1 ? 2 : 1));
+        cur = merge(found, n_merged);
+        gen_sizes.push_back(cur.size());
+        if (gen > 0) generations_run = gen;
+    }
+
+    *n_crit = cur.size();
+    *criticals = (cc_sb_box*)std::malloc(sizeof(cc_sb_box) * (cur.size() + 1));
+    if (flags) *flags = (uint32_t*)std::malloc(sizeof(uint32_t) * (cur.size() + 1));
+    if (!*criticals || (flags && !*flags)) return ccrt::fail(h, CC_ERR_OOM, "cc_sb_prove: host allocation");
+    for (size_t i = 0; i < cur.size(); ++i) {
+        (*criticals)[i].la = cc_iv{cur[i].box.la.lo, cur[i].box.la.hi};
+        for (int k = 0; k < 6; ++k) (*criticals)[i].r[k] = cc_iv{cur[i].box.r[k].lo, cur[i].box.r[k].hi};
+        if (flags) (*flags)[i] = cur[i].trapped;
+    }
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        if ((st = sync_counters(e))) return st;
+        std::memcpy(stats->task_counts, e.hc->task_counts, sizeof(stats->task_counts));
+        std::memcpy(stats->cell_counts, e.hc->cell_counts, sizeof(stats->cell_counts));
+        std::memcpy(stats->leaf_counts, e.hc->leaf_counts, sizeof(stats->leaf_counts));
+        stats->digest = e.hc->digest;
+        stats->leaf_evals = e.hc->leaf_evals;
+        stats->trapped_leaves = trapped_leaves;
+        stats->trapped_shortcuts = e.hc->trapped_shortcuts;
+        for (size_t g = 0; g < gen_sizes.size() && g <= CC_MAX_GENERATIONS; ++g) stats->gen_sizes[g] = gen_sizes[g];
+        stats->generations_run = generations_run;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        stats->kernel_launches = h->launches;
+    }
+    return status;
+}

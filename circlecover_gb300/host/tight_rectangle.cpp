@@ -1,7 +1,7 @@
 // Drop-in replacement of the reference's tight-rectangle driver,
 // circlecover::tight_rectangle::find_critical_intervals()
 // (reference: tight_rectangle/tight_rectangle.cu:458-537, called from
-// prover.cpp:33), on top of the C ABI in include/circlecover_gb300.h.
+// prover.cpp:34), on top of the C ABI in include/circlecover_gb300.h.
 //
 // Same split counts, same stdout (banner, the two- and three-disk summaries
 // with 19-digit intervals), same Ctrl-C behaviour: the first SIGINT stops the
@@ -9,15 +9,7 @@
 // the second one exits (reference: interrupt.cpp:30-46).  Errors that the
 // reference reports by throwing std::system_error/std::logic_error are thrown
 // here as std::runtime_error with the library's message.
-#include <atomic>
-#include <csignal>
-#include <cstdlib>
-#include <iomanip>
-#include <iostream>
-#include <stdexcept>
-#include <string>
-
-#include "circlecover_gb300.h"
+#include "dropin.hpp"
 
 namespace circlecover {
 namespace tight_rectangle {
@@ -26,52 +18,11 @@ void find_critical_intervals();
 
 namespace dropin {
 
-static constexpr std::size_t kOutputWidth = 120;
-
-// 120-column banner (reference: output_case.hpp:35-54)
-void begin_case(const char* message) {
-    std::string m(message);
-    if (m.size() >= kOutputWidth - 2) {
-        std::cout << m << std::endl;
-        return;
-    }
-    std::size_t pre = (kOutputWidth - m.size() - 2) / 2;
-    std::size_t post = kOutputWidth - m.size() - 2 - pre;
-    std::cout << std::string(pre, '-') << ' ' << m << ' ' << std::string(post, '-') << std::endl;
-}
-
-void end_case() { std::cout << std::string(kOutputWidth, '-') << std::endl; }
-
-// interval as "[lb, ub]", 19 significant digits, width 26 (reference: interval.hpp:294-303)
-std::ostream& operator<<(std::ostream& o, const cc_iv& iv) {
-    std::ios_base::fmtflags f = o.flags(std::ios::right);
-    std::streamsize p = o.precision(19);
-    o << '[' << std::setw(26) << iv.lb << ", " << std::setw(26) << iv.ub << ']';
-    o.flags(f);
-    o.precision(p);
-    return o;
-}
-
 // reference: tight_rectangle.cu:539-545
 std::ostream& operator<<(std::ostream& o, const cc_tight_box& b) {
     o << "λ = " << b.la;
     for (int i = 0; i < 4; ++i) o << ", r²_" << (i + 1) << " = " << b.r[i];
     return o;
-}
-
-std::atomic<cc_handle*> g_active{nullptr};
-std::atomic<int> g_interrupts{0};
-
-extern "C" void on_sigint(int) {
-    if (g_interrupts.fetch_add(1) > 0) std::_Exit(SIGINT);
-    cc_handle* h = g_active.load();
-    if (h) cc_interrupt(h);
-}
-
-void check(cc_handle* h, int status, const char* what) {
-    if (status != CC_OK && status != CC_ERR_INTERRUPTED) {
-        throw std::runtime_error(std::string(what) + ": " + cc_status_str(status) + (h ? std::string(" (") + cc_last_error(h) + ")" : ""));
-    }
 }
 
 void print_summary(const cc_tight_summary_t& r) {

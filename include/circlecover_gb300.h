@@ -15,12 +15,20 @@
  *       (tight_rectangle/tight_rectangle.cu:229-248)
  *   cc_tight_prove
  *       circlecover::tight_rectangle::find_critical_intervals()
- *       (tight_rectangle/tight_rectangle.cu:458-537; called by prover.cpp:33),
+ *       (tight_rectangle/tight_rectangle.cu:458-537; called by prover.cpp:34),
  *       with the split counts as parameters instead of compile-time constants
  *       (tight_rectangle.cu:44-68)
  *   cc_tight_summary
  *       kernel_compute_distance_from_theoretical_worst_cases
  *       (tight_rectangle.cu:322-456)
+ *   cc_sb_eval / cc_sb_eval_device
+ *       the size-bound criteria and shortcuts, evaluated per box
+ *       (rectangle_size_bound/strategies.cuh:32-147, in the cascade of
+ *       rectangle_size_bound.cu:161-231)
+ *   cc_sb_prove
+ *       circlecover::rectangle_size_bound::find_critical_intervals()
+ *       (rectangle_size_bound/rectangle_size_bound.cu:312-382; called by
+ *       prover.cpp:35), split counts as parameters (:36-62)
  *
  * Conventions: plain C types, caller-owned buffers unless stated, status
  * codes instead of exceptions (the reference throws std::system_error or
@@ -133,6 +141,44 @@ typedef struct cc_prove_stats {
     uint64_t kernel_launches;  /* kernels launched by the call */
 } cc_prove_stats;
 
+/* ---- size-bound proof ------------------------------------------------------
+ * Trace outcomes by level: 0 = task (one lambda x r1 x r2 piece of a parent
+ * box), 1 = r3 cell of a task, 2 = leaf (an r4 x r5 x r6 cell). */
+enum cc_sb_trace_outcome {
+    CC_SBT_TASK_EMPTY = 0, CC_SBT_TASK_EVEN = 1, CC_SBT_TASK_UNEVEN = 2, CC_SBT_TASK_SPLIT = 3,
+    CC_SBT_CELL_UNEVEN = 0, CC_SBT_CELL_OPPOSITE = 1, CC_SBT_CELL_VSTRIP = 2, CC_SBT_CELL_SPLIT = 3,
+    /* leaves: 0..13 = the criterion (CC_SV_* bit order) that certified it */
+    CC_SBT_LEAF_EMPTY = 14, CC_SBT_LEAF_CRITICAL = 15, CC_SBT_LEAF_TRAPPED = 16
+};
+#define CC_SBT_LEAF_OUTCOMES 17
+
+/* Split counts of the size-bound proof.  The reference's values
+ * (rectangle_size_bound.cu:36-62): la_splits_init 256, r_splits_init
+ * {128,128,64,64,64,64}, la_splits_gen 64, r_splits_gen {32,32,16,16,16,32},
+ * num_generations 1.  Every count in [1, 2047]. */
+typedef struct cc_sb_grid {
+    int la_splits_init;
+    int r_splits_init[6];
+    int la_splits_gen;
+    int r_splits_gen[6];
+    int num_generations;
+} cc_sb_grid;
+
+typedef struct cc_sb_prove_stats {
+    uint64_t task_counts[4];                  /* by CC_SBT_TASK_* */
+    uint64_t cell_counts[4];                  /* by CC_SBT_CELL_* */
+    uint64_t leaf_counts[CC_SBT_LEAF_OUTCOMES];
+    uint64_t digest;                          /* sum of the mixed trace keys */
+    uint64_t leaf_evals;                      /* leaves visited */
+    uint64_t trapped_leaves;                  /* leaves kept because of a trap */
+    uint64_t trapped_shortcuts;               /* shortcuts not taken because of a trap */
+    uint64_t gen_sizes[CC_MAX_GENERATIONS + 1]; /* criticals after init (merged), gen 1, ... */
+    int32_t generations_run;
+    int32_t reserved;
+    double seconds;
+    uint64_t kernel_launches;
+} cc_sb_prove_stats;
+
 /* summary of the final criticals vs the theoretical worst cases;
  * == Max_distances (tight_rectangle.cu:322-341) */
 typedef struct cc_tight_summary_t {
@@ -243,8 +289,27 @@ int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_gri
  * (kernel_compute_distance_from_theoretical_worst_cases). */
 int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_tight_summary_t* out);
 
-/* Ask a running cc_tight_prove on this handle to stop after the current
- * generation (the reference's Ctrl-C behaviour, interrupt.cpp:30-46). */
+/* Run the size-bound proof from `root` (replaces the driver and kernel of
+ * rectangle_size_bound/rectangle_size_bound.cu:132-382: the (lambda, r1, r2)
+ * host loops of find_critical_intervals_in, one kernel launch per task
+ * there, the r3..r6 grid of kernel_find_critical_intervals_in with its
+ * shortcuts and cascade, and the generation loop with
+ * merge_critical_intervals<N>).  On success *criticals points to *n_crit
+ * boxes (release with cc_free) in the reference's final order (sorted and
+ * merged), each with a flag in *flags (NULL allowed; cc_free it): bit 0 =
+ * kept because a criterion reached a trap site.  stats may be NULL.
+ * Work units: tasks are processed in chunks of 2^18 and leaves in slices of
+ * 2^22; the environment variables CC_SB_TASK_CHUNK_LOG2 (0..18) and
+ * CC_SB_SLICE_LOG2 (5..26) change them (same results, other launches). */
+int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, cc_sb_box** criticals, size_t* n_crit,
+                uint32_t** flags, cc_sb_prove_stats* stats);
+
+/* Ask a running proof on this handle to stop (the reference's Ctrl-C
+ * behaviour, interrupt.cpp:30-46).  cc_tight_prove stops after the current
+ * generation; cc_sb_prove stops inside the current refinement generation and
+ * keeps the previous one's result (its initial pass is not interruptible,
+ * rectangle_size_bound.cu:325, 341).  Either returns CC_ERR_INTERRUPTED with
+ * *criticals and *n_crit set to the result so far. */
 void cc_interrupt(cc_handle* h);
 
 void cc_free(void* p);

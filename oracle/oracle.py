@@ -140,6 +140,31 @@ class _Lib:
         return arr, stats_to_dict(st)
 
 
+    def sb_prove(self, root, grid, threads=1):
+        """The size-bound proof on the host: (criticals SB_BOX array, flags, stats dict)."""
+        from circlecover_gb300 import CcSbProveStats, sb_stats_to_dict
+        root = np.ascontiguousarray(np.asarray(root, dtype=SB_BOX).reshape(1))
+        out = ctypes.c_void_p()
+        flags = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcSbProveStats()
+        f = getattr(self.lib, self.prefix + "_sb_prove")
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p]
+        rc = f(root.ctypes.data, ctypes.addressof(grid), threads, ctypes.byref(out), ctypes.byref(flags), ctypes.byref(n),
+               ctypes.addressof(st))
+        if rc != 0:
+            raise RuntimeError("sb prove failed %d" % rc)
+        arr = np.zeros(n.value, dtype=SB_BOX)
+        fl = np.zeros(n.value, dtype=np.uint32)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * SB_BOX.itemsize)
+            ctypes.memmove(fl.ctypes.data, flags.value, n.value * 4)
+        getattr(self.lib, self.prefix + "_free")(out)
+        getattr(self.lib, self.prefix + "_free")(flags)
+        return arr, fl, sb_stats_to_dict(st)
+
+
 class Ref(_Lib):
     """The reference's own criteria code, built for the host."""
     prefix = "ccref"

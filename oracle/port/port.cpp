@@ -17,7 +17,7 @@
 #include <thread>
 #include <vector>
 
-thread_local unsigned long long cc_port_op_count = 0;
+CC_HOST_TLS unsigned long long cc_port_op_count = 0;
 #ifdef CC_PORT_COUNT
 #define CC_PORT_TICK() (++cc_port_op_count)
 #else
@@ -26,13 +26,14 @@ thread_local unsigned long long cc_port_op_count = 0;
 
 #define CC_HOST_PORT 1
 #include "../../circlecover_gb300/csrc/cc_tight.cuh"
-#include "../../circlecover_gb300/csrc/cc_sb_eval.cuh"
+#include "../../circlecover_gb300/csrc/cc_sb_proof.cuh"
 
 namespace cc {
-thread_local uint32_t cc_port_trap_word = 0;
+CC_HOST_TLS uint32_t cc_port_trap_word = 0;
 }
 
 #include "../tight_driver.hpp"
+#include "../sb_driver.hpp"
 
 using cc::Iv;
 namespace ct = cc::tight;
@@ -73,6 +74,29 @@ struct PortCriteria {
 };
 
 using Driver = cc_oracle::TightDriver<PortCriteria>;
+
+namespace csb = cc::sb;
+
+struct PortSbC {
+    using Box = csb::Box6;
+    static double lo(const Iv& v) { return v.lo; }
+    static double hi(const Iv& v) { return v.hi; }
+    static void do_join(Iv& a, const Iv& b) { cc::do_join(a, b); }
+    static Iv& rad(Box& b, int i) { return b.r[i]; }
+    static const Iv& rad(const Box& b, int i) { return b.r[i]; }
+    static Box task_box(const Box& p, int la_i, int nla, int r1_i, int n1, int r2_i, int n2) {
+        return csb::task_box(p, la_i, nla, r1_i, n1, r2_i, n2);
+    }
+    static int task_outcome(const Box& t, bool& trapped) { return csb::task_outcome(t, trapped); }
+    static Iv r3_piece(const Box& t, int i, int n) { return cc::subinterval(t.r[2], i, n); }
+    static int cell_outcome(const Box& t, Iv r3, bool& trapped) { return csb::cell_outcome(t, r3, trapped); }
+    static Box leaf_box(const Box& t, Iv r3, int i4, int n4, int i5, int n5, int i6, int n6) {
+        return csb::leaf_box(t, r3, i4, n4, i5, n5, i6, n6);
+    }
+    static int leaf_outcome(const Box& b) { return csb::leaf_outcome(b); }
+};
+
+using SbDriver = cc_oracle::SbDriver<PortSbC>;
 
 static Iv to_iv(const cc_iv& x) { return Iv{x.lb, x.ub}; }
 
@@ -178,6 +202,37 @@ int ccport_sb_eval(const cc_sb_box* boxes, size_t n, uint32_t* masks, uint64_t* 
         pool.emplace_back(body, b, e);
     }
     for (auto& th : pool) th.join();
+    return 0;
+}
+
+int ccport_sb_prove(const cc_sb_box* root, const cc_sb_grid* grid, int threads, cc_sb_box** out, uint32_t** flags,
+                    size_t* n_out, cc_sb_prove_stats* stats) {
+    csb::Box6 r;
+    r.la = to_iv(root->la);
+    for (int i = 0; i < 6; ++i) r.r[i] = to_iv(root->r[i]);
+    SbDriver::Result res = SbDriver::prove(r, *grid, threads);
+    size_t n = res.criticals.size();
+    *n_out = n;
+    *out = (cc_sb_box*)std::malloc(sizeof(cc_sb_box) * (n + 1));
+    *flags = (uint32_t*)std::malloc(sizeof(uint32_t) * (n + 1));
+    for (size_t i = 0; i < n; ++i) {
+        const csb::Box6& b = res.criticals[i].box;
+        (*out)[i].la = cc_iv{b.la.lo, b.la.hi};
+        for (int k = 0; k < 6; ++k) (*out)[i].r[k] = cc_iv{b.r[k].lo, b.r[k].hi};
+        (*flags)[i] = res.criticals[i].trapped;
+    }
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        std::memcpy(stats->task_counts, res.trace.task_counts, sizeof(stats->task_counts));
+        std::memcpy(stats->cell_counts, res.trace.cell_counts, sizeof(stats->cell_counts));
+        std::memcpy(stats->leaf_counts, res.trace.leaf_counts, sizeof(stats->leaf_counts));
+        stats->digest = res.trace.digest;
+        stats->leaf_evals = res.trace.leaf_evals;
+        stats->trapped_leaves = res.trapped_leaves;
+        stats->trapped_shortcuts = res.trace.trapped_shortcuts;
+        for (size_t g = 0; g < res.gen_sizes.size() && g <= CC_MAX_GENERATIONS; ++g) stats->gen_sizes[g] = res.gen_sizes[g];
+        stats->generations_run = res.generations_run;
+    }
     return 0;
 }
 

@@ -22,10 +22,10 @@ using circlecover::IV;
 namespace tr = circlecover::tight_rectangle;
 
 /* ------------------------------------------------ shim runtime support */
-thread_local unsigned long long cc_shim_op_count = 0;
-static thread_local jmp_buf* cc_ref_trap_target = nullptr;
-static thread_local uint32_t cc_ref_trapped = 0;
-static thread_local unsigned long long cc_ref_printf_count = 0;
+CC_HOST_TLS unsigned long long cc_shim_op_count = 0;
+static CC_HOST_TLS jmp_buf* cc_ref_trap_target = nullptr;
+static CC_HOST_TLS uint32_t cc_ref_trapped = 0;
+static CC_HOST_TLS unsigned long long cc_ref_printf_count = 0;
 
 void algcuda::trap() noexcept {
     cc_ref_trapped = 1;

@@ -165,9 +165,20 @@ CC_SHIM_INLINE double cc_sw_rcp_ru(double a) { return cc_sw_div_ru(1.0, a); }
  * thread-local counter.  The count per box is the algorithmic work unit of
  * the roofline (one FP64 directed-rounding primitive = 1 op).
  */
+#ifdef __cplusplus
+/* Thread-local state of the host builds.  Initial-exec TLS makes every access
+ * a plain thread-pointer-relative load.  With the default model for
+ * shared libraries (TLS descriptors), the port loaded into Python crashed on
+ * an aarch64 host (GCC 13, glibc) inside a worker thread's TLS accesses;
+ * with initial-exec it runs and agrees bit for bit. */
+#ifndef CC_HOST_TLS
+#define CC_HOST_TLS thread_local __attribute__((tls_model("initial-exec")))
+#endif
+#endif
+
 #ifdef CC_SHIM_COUNT
 #ifdef __cplusplus
-extern thread_local unsigned long long cc_shim_op_count;
+extern CC_HOST_TLS unsigned long long cc_shim_op_count;
 #else
 extern _Thread_local unsigned long long cc_shim_op_count;
 #endif

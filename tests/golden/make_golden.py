@@ -9,6 +9,8 @@ Outputs (committed, small):
   tight_eval_golden.npz   boxes + verdict masks + per-box op counts
   tight_prove_golden.json small proofs: root, split counts, critical boxes
                           (hex floats), trace counts and digest
+  sb_eval_golden.npz      size-bound boxes + verdict masks + op counts
+  sb_prove_golden.json    small size-bound proofs (as tight_prove_golden)
 The boxes come from circlecover_gb300.workloads (seeded, platform-independent)
 plus hand-made edge cases.
 """
@@ -98,6 +100,32 @@ PROOF_CASES = [
 ]
 
 
+UB_W = 9.0 / 64.0
+# (name, lambda range, radius ranges (None = [0, 9/64] each), grid: la_init, r_init, la_gen, r_gen, gens)
+SB_PROOF_CASES = [
+    ("init_small", (1.0, 2.5), None, (4, (8, 8, 4, 4, 4, 4), 64, (32, 32, 16, 16, 16, 32), 0)),
+    ("three_generations", (1.0, 2.5), None, (4, (8, 8, 4, 4, 4, 4), 2, (2, 2, 2, 2, 2, 2), 3)),
+    ("wide_lambda", (2.5, 8.0), None, (4, (8, 8, 4, 4, 4, 4), 2, (2, 2, 2, 2, 2, 4), 1)),
+    ("mid_lambda", (1.2, 1.6), None, (4, (16, 16, 8, 6, 6, 6), 2, (2, 2, 2, 2, 2, 2), 1)),
+    ("large_disks", (1.0, 1.1), [(0.12, UB_W), (0.1, UB_W)] + [(0.0, UB_W)] * 4,
+     (2, (8, 8, 6, 6, 6, 6), 64, (32, 32, 16, 16, 16, 32), 0)),
+    ("mixed_disks", (1.2, 1.5), [(0.12, UB_W), (0.11, UB_W), (0.1, 0.13), (0.0, 0.12), (0.0, 0.1), (0.0, 0.1)],
+     (2, (4, 4, 4, 4, 4, 4), 2, (2, 2, 2, 2, 2, 2), 1)),
+]
+
+
+def sb_root_box(la, radii):
+    b = np.zeros(1, dtype=W.SB_BOX)
+    b["la"][0] = la
+    b["r"][0] = radii if radii is not None else [(0.0, UB_W)] * 6
+    return b[0]
+
+
+def hexbox6(b):
+    return [[float(b["la"][0]).hex(), float(b["la"][1]).hex()]] + [[float(b["r"][k][0]).hex(), float(b["r"][k][1]).hex()]
+                                                                   for k in range(6)]
+
+
 def hexbox(b):
     return [[float(b["la"][0]).hex(), float(b["la"][1]).hex()]] + [[float(b["r"][k][0]).hex(), float(b["r"][k][1]).hex()]
                                                                    for k in range(4)]
@@ -148,6 +176,20 @@ def main():
         print("proof", name, "criticals", len(crit), "gen sizes", st["gen_sizes"], "leaves", st["leaf_evals"])
     with open(os.path.join(HERE, "tight_prove_golden.json"), "w") as f:
         json.dump(dict(source="reference criteria built for the host (oracle/_ref)", cases=cases), f, indent=0)
+
+    from circlecover_gb300 import make_sb_grid
+    sb_cases = []
+    for name, la, radii, (la_init, r_init, la_gen, r_gen, gens) in SB_PROOF_CASES:
+        root = sb_root_box(la, radii)
+        g = make_sb_grid(la_init, r_init, la_gen, r_gen, gens)
+        crit, flags, st = ref.sb_prove(root, g, threads=8)
+        sb_cases.append(dict(name=name, root=hexbox6(root), la_init=la_init, r_init=list(r_init), la_gen=la_gen,
+                             r_gen=list(r_gen), gens=gens, criticals=[hexbox6(b) for b in crit],
+                             flags=[int(x) for x in flags], stats=st))
+        print("size-bound proof", name, "criticals", len(crit), "trapped", int(flags.sum()), "gen sizes",
+              st["gen_sizes"], "leaves", st["leaf_evals"])
+    with open(os.path.join(HERE, "sb_prove_golden.json"), "w") as f:
+        json.dump(dict(source="reference criteria built for the host (oracle/_ref)", cases=sb_cases), f, indent=0)
 
 
 if __name__ == "__main__":
