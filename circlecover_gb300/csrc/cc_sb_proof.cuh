@@ -95,6 +95,20 @@ CC_FN Box6 leaf_box(const Box6& t, Iv r3, int i4, int n4, int i5, int n5, int i6
     return tightened(b);
 }
 
+// leaf_box with the steps of the r4, r5, r6 splits precomputed per task
+// (subinterval_step): the same box
+CC_FN Box6 leaf_box_steps(const Box6& t, const double step[3], Iv r3, int i4, int n4, int i5, int n5, int i6, int n6) {
+    Box6 b;
+    b.la = t.la;
+    b.r[0] = t.r[0];
+    b.r[1] = t.r[1];
+    b.r[2] = r3;
+    b.r[3] = subinterval_with_step(t.r[3], step[0], i4, n4);
+    b.r[4] = subinterval_with_step(t.r[4], step[1], i5, n5);
+    b.r[5] = subinterval_with_step(t.r[5], step[2], i6, n6);
+    return tightened(b);
+}
+
 // The cascade on one leaf box in the kernel's order (:189-231); the first
 // criterion that certifies decides.  A trap ends the cascade: the reference
 // would have aborted the run there, here the leaf is reported (critical,

@@ -14,7 +14,8 @@
 //   leaves  one thread per (cell, r4, r5, r6 piece): leaf box, tighten, R,
 //           empty check, the first criterion of the cascade
 //   pass K  one thread per leaf still undecided: criterion K (K = 1..12),
-//           survivors compacted into the next pass's queue
+//           survivors compacted into the next pass's queue; the r1-in-corner
+//           criterion (K = 4) runs one thread per (leaf, placement)
 //   seven   the seven-disk strategies, the costliest criterion, in three
 //           kernels: one thread per leaf for the r7-range prefix, one thread
 //           per (leaf, r7 piece) for the 16 pieces, one thread per leaf to
@@ -53,9 +54,9 @@ namespace {
 struct SbTask {  // a task that passed the whole-task shortcuts
     Box6 box;
     uint64_t id;
-    uint64_t pad;
+    double step[3];  // steps of its r4, r5, r6 splits
 };
-static_assert(sizeof(SbTask) == 128, "task record");
+static_assert(sizeof(SbTask) == 144, "task record");
 
 struct SbCell {  // an r3 cell that passed the r3 shortcuts
     Iv r3;
@@ -156,7 +157,7 @@ __device__ __forceinline__ uint64_t leaf_key(int gen, const SbLeaf& l, int outco
 
 // ---------------------------------------------------------------- stages
 struct TaskGrid {
-    int gen, nla, n1, n2;
+    int gen, nla, n1, n2, n4, n5, n6;
     unsigned long long per_parent;
 };
 
@@ -186,6 +187,9 @@ __global__ void __launch_bounds__(kThreads) k_sbp_tasks(const Box6* __restrict__
         if (slot != ~0ULL) {
             out[slot].box = tb;
             out[slot].id = idx;
+            out[slot].step[0] = cc::subinterval_step(tb.r[3], g.n4);
+            out[slot].step[1] = cc::subinterval_step(tb.r[4], g.n5);
+            out[slot].step[2] = cc::subinterval_step(tb.r[5], g.n6);
         }
     }
     trace_flush(bt, c->task_counts, c, &c->trapped_shortcuts);
@@ -245,13 +249,26 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
         int outcome = CC_SBT_LEAF_EMPTY;
         SbLeaf leaf;
         if (valid) {
-            const SbCell cell = cells[idx / n456];
-            const unsigned long long rem = idx % n456;
-            const int i6 = (int)(rem % g.n6);
-            const int i5 = (int)((rem / g.n6) % g.n5);
-            const int i4 = (int)(rem / ((unsigned long long)g.n6 * g.n5));
+            unsigned long long ci;
+            int i4, i5, i6;
+            if (n456 <= 0xffffffffULL) {  // 32-bit index arithmetic where it fits
+                const unsigned long long q = idx / (uint32_t)n456;
+                const uint32_t rem = (uint32_t)(idx - q * n456);
+                const uint32_t r56 = rem / (uint32_t)g.n6;
+                ci = q;
+                i6 = (int)(rem - r56 * (uint32_t)g.n6);
+                i4 = (int)(r56 / (uint32_t)g.n5);
+                i5 = (int)(r56 - (uint32_t)i4 * (uint32_t)g.n5);
+            } else {
+                ci = idx / n456;
+                const unsigned long long rem = idx % n456;
+                i6 = (int)(rem % g.n6);
+                i5 = (int)((rem / g.n6) % g.n5);
+                i4 = (int)(rem / ((unsigned long long)g.n6 * g.n5));
+            }
+            const SbCell cell = cells[ci];
             const SbTask& task = tasks[cell.task];
-            leaf.box = sb::leaf_box(task.box, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6);
+            leaf.box = sb::leaf_box_steps(task.box, task.step, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6);
             leaf.id = task.id;
             leaf.idx = pack_idx((int)cell.i3, i4, i5, i6);
             sb::Vals v;
@@ -326,6 +343,81 @@ __global__ void __launch_bounds__(kThreads) k_sbp_pass(const SbLeaf* __restrict_
     trace_flush(bt, c->leaf_counts, c, nullptr);
 }
 
+// A criterion made of independent placements tried in order until one
+// works (r1 in a corner: nine placements) runs one placement per thread; the
+// resolve kernel then combines them as the sequential loop would: the first
+// placement that works decides, and only traps in placements up to that one
+// count.  masks[2 * leaf] = placements that worked, masks[2 * leaf + 1] =
+// placements that reached a trap site.
+template <int K>
+struct SplitCriterion;
+template <>
+struct SplitCriterion<sb::SB_R1_CORNER_EXPLICIT> {
+    static constexpr int kItems = sb::kR1CornerItems;
+    __device__ static bool item(const Box6& b, const sb::Vals& v, int i) { return sb::r1_corner_item(b, v, i); }
+};
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_sbp_split_items(const SbLeaf* __restrict__ qin,
+                                                               const unsigned long long* n_in, uint32_t* masks) {
+    constexpr int I = SplitCriterion<K>::kItems;
+    // placement-major order: the lanes of a warp try the same placement on
+    // consecutive leaves
+    const unsigned long long nl = *n_in, total = nl * (unsigned long long)I;
+    for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (unsigned long long)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / nl);
+        const unsigned long long leaf = idx - (unsigned long long)i * nl;
+        const Box6 box = qin[leaf].box;
+        sb::Vals v;
+        v.R = sb::remaining_weight(box);
+        cc::trap_clear();
+        const bool ok = SplitCriterion<K>::item(box, v, i);
+        const bool trapped = cc::trap_status() != cc::TRAP_NONE;
+        cc::trap_clear();
+        if (ok) atomicOr(&masks[2 * leaf], 1u << i);
+        if (trapped) atomicOr(&masks[2 * leaf + 1], 1u << i);
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_sbp_split_resolve(const SbLeaf* __restrict__ qin,
+                                                                 const unsigned long long* n_in,
+                                                                 const uint32_t* __restrict__ masks,
+                                                                 SbLeaf* __restrict__ qout, unsigned long long* n_out,
+                                                                 unsigned long long q_cap, SbLeaf* __restrict__ crit,
+                                                                 unsigned long long crit_cap, int gen, SbCounters* c) {
+    constexpr int I = SplitCriterion<K>::kItems;
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    const unsigned long long total = *n_in;
+    SB_WARP_LOOP(total) {
+        const unsigned long long idx = base_ + (threadIdx.x & 31);
+        const bool valid = idx < total;
+        int outcome = CC_SBT_LEAF_CRITICAL;  // here: undecided
+        SbLeaf leaf;
+        if (valid) {
+            leaf = qin[idx];
+            const uint32_t ok = masks[2 * idx], trapped = masks[2 * idx + 1];
+            const uint32_t first = ok ? (uint32_t)(__ffs(ok) - 1) : (uint32_t)(I - 1);
+            const uint32_t seen = (2u << first) - 1u;
+            if (trapped & seen) outcome = CC_SBT_LEAF_TRAPPED;
+            else if (ok) outcome = K;
+        }
+        const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
+        const bool decided = valid && !undecided;
+        trace_note(bt, decided, decided ? leaf_key(gen, leaf, outcome) : 0, outcome);
+        unsigned long long slot = warp_append(n_out, undecided, q_cap, &c->overflow);
+        if (slot != ~0ULL) qout[slot] = leaf;
+        slot = warp_append(&c->n_crit, valid && outcome == CC_SBT_LEAF_TRAPPED, crit_cap, &c->overflow);
+        if (slot != ~0ULL) {
+            leaf.idx |= 1ULL << 63;
+            crit[slot] = leaf;
+        }
+    }
+    trace_flush(bt, c->leaf_counts, c, nullptr);
+}
+
 // Seven-disk strategies, prefix (seven_disk_strategies.cu:1397-1432): decided
 // leaves are traced here, the others become jobs of 16 r7 pieces.
 __global__ void __launch_bounds__(kThreads) k_sbp_seven_prefix(const SbLeaf* __restrict__ qin,
@@ -370,11 +462,13 @@ __global__ void __launch_bounds__(kThreads) k_sbp_seven_prefix(const SbLeaf* __r
 __global__ void __launch_bounds__(kThreads) k_sbp_seven_pieces(const SbLeaf* __restrict__ qin,
                                                                 SevenJob* __restrict__ jobs,
                                                                 const unsigned long long* n_jobs) {
-    const unsigned long long total = *n_jobs * 16ULL;
+    // piece-major order: the lanes of a warp check the same piece of
+    // consecutive jobs, so they start on the same code path
+    const unsigned long long nj = *n_jobs, total = nj * 16ULL;
     for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (unsigned long long)gridDim.x * blockDim.x) {
-        SevenJob& job = jobs[idx >> 4];
-        const int k = (int)(idx & 15);
+        const int k = (int)(idx / nj);
+        SevenJob& job = jobs[idx - (unsigned long long)k * nj];
         const Box6 box = qin[job.leaf].box;
         sb::Vals v;
         v.R = sb::remaining_weight(box);
@@ -449,7 +543,19 @@ struct Engine {
 // kernels; the undecided leaves of one pass are the next one's input
 template <int K>
 int launch_passes(Engine& e, int gen, int src) {
-    if constexpr (K < sb::SB_SEVEN_DISK) {
+    if constexpr (K == sb::SB_R1_CORNER_EXPLICIT) {
+        const int dst = src ^ 1;
+        uint32_t* masks = reinterpret_cast<uint32_t*>(e.jobs);  // free until the seven-disk kernels
+        CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
+        CC_CUDA(e.h, cudaMemsetAsync(masks, 0, e.slice * 2 * sizeof(uint32_t), e.s));
+        k_sbp_split_items<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], masks);
+        CC_LAUNCHED(e.h);
+        k_sbp_split_resolve<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], masks, e.q[dst],
+                                                              &e.dc->n_q[dst], e.slice, e.crit, e.crit_cap, gen, e.dc);
+        CC_LAUNCHED(e.h);
+        e.launches += 2;
+        return launch_passes<K + 1>(e, gen, dst);
+    } else if constexpr (K < sb::SB_SEVEN_DISK) {
         const int dst = src ^ 1;
         CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
         k_sbp_pass<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], e.q[dst], &e.dc->n_q[dst], e.slice,
@@ -509,7 +615,7 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
     unsigned long long chunk = e.cell_cap / (unsigned long long)rn[2];
     if (chunk > e.task_chunk) chunk = e.task_chunk;
     if (chunk < 1) chunk = 1;
-    TaskGrid tg{gen, nla, rn[0], rn[1], per_parent};
+    TaskGrid tg{gen, nla, rn[0], rn[1], rn[3], rn[4], rn[5], per_parent};
     LeafGrid lg{gen, rn[3], rn[4], rn[5]};
     for (unsigned long long t0 = 0; t0 < ntasks; t0 += chunk) {
         if (gen > 0 && e.h->interrupt.load()) return CC_ERR_INTERRUPTED;
@@ -637,7 +743,7 @@ extern "C" int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid
     };
     e.task_chunk = 1ULL << log2_env("CC_SB_TASK_CHUNK_LOG2", 18, 0, 18);
     e.cell_cap = 1ULL << 22;
-    e.slice = 1ULL << log2_env("CC_SB_SLICE_LOG2", 22, 5, 26);
+    e.slice = 1ULL << log2_env("CC_SB_SLICE_LOG2", 24, 5, 26);
     e.crit_cap = 2 * e.slice;
     e.range = e.slice;
     int st;

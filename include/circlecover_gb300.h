@@ -298,8 +298,9 @@ int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_t
  * boxes (release with cc_free) in the reference's final order (sorted and
  * merged), each with a flag in *flags (NULL allowed; cc_free it): bit 0 =
  * kept because a criterion reached a trap site.  stats may be NULL.
- * Work units: tasks are processed in chunks of 2^18 and leaves in slices of
- * 2^22; the environment variables CC_SB_TASK_CHUNK_LOG2 (0..18) and
+ * Work units: tasks are processed in chunks of 2^18 and undecided leaves in
+ * queues of 2^24 (about 9 GB of device memory in all); the environment
+ * variables CC_SB_TASK_CHUNK_LOG2 (0..18) and
  * CC_SB_SLICE_LOG2 (5..26) change them (same results, other launches). */
 int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, cc_sb_box** criticals, size_t* n_crit,
                 uint32_t** flags, cc_sb_prove_stats* stats);
