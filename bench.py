@@ -275,6 +275,7 @@ def run_ours(args, ws, rank, local):
     }
     if ws == 1 and not args.no_proof:
         line["proof"] = proof_comparison(prover)
+        line["sb_proof"] = sb_proof_run(prover)
     if ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
     prover.close()
@@ -306,6 +307,29 @@ def proof_comparison(prover):
     return out
 
 
+SB_SLICE = dict(la=(1.0, 1.0 + 1.5 * 2 / 256), grid=(2, (32, 32, 64, 64, 64, 64)))
+
+
+def sb_proof_run(prover, warm=True):
+    """The size-bound proof on a slice of the reference's own initial pass:
+    lambda over two of its 256 pieces of [1, 2.5], r1 and r2 in 32 pieces
+    (the reference: 128), r3..r6 in 64 pieces (as the reference), every
+    squared radius in [0, 9/64]; one pass, no refinement generation."""
+    import circlecover_gb300 as cg
+    from circlecover_gb300 import workloads as W
+    root = W.sb_root(*SB_SLICE["la"])
+    la_n, rn = SB_SLICE["grid"]
+    if warm:  # buffers are allocated on the first call
+        prover.sb_find_critical_intervals(root, cg.make_sb_grid(1, (2, 2, 2, 2, 2, 2)))
+    t0 = time.perf_counter()
+    crit, flags, st = prover.sb_find_critical_intervals(root, cg.make_sb_grid(la_n, rn))
+    dt = time.perf_counter() - t0
+    return {"workload": "size-bound proof, initial pass: lambda [1, 1+3/256] x 2, r1 x 32, r2 x 32, r3..r6 x 64",
+            "seconds": dt, "leaves": st["leaf_evals"], "leaves_per_s": st["leaf_evals"] / dt,
+            "criticals": int(len(crit)), "trapped": int(flags.sum()), "kernel_launches": st["kernel_launches"],
+            "leaf_outcomes": st["leaf_counts"], "digest": st["digest"]}
+
+
 def ctypes_peak(prover):
     import ctypes
     lib = prover.lib
@@ -328,8 +352,19 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-proof", action="store_true")
+    ap.add_argument("--workload", default="tight_eval", choices=["tight_eval", "sb_proof"])
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "sb_proof":  # the size-bound proof slice alone (for profiling)
+        import __graft_entry__
+        __graft_entry__.build()
+        import circlecover_gb300 as cg
+        with cg.Prover(local) as prover:
+            for i in range(args.warmup + args.steps):
+                r = sb_proof_run(prover, warm=(i == 0))
+                if i >= args.warmup and rank == 0:
+                    print(json.dumps(r), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, ws, rank)
         return
