@@ -236,6 +236,23 @@ int ccport_sb_prove(const cc_sb_box* root, const cc_sb_grid* grid, int threads, 
     return 0;
 }
 
+/* interval times scalar, for the rounding test */
+void ccport_iv_mul_scalar(double lo, double hi, double s, double* out) {
+    Iv r = Iv{lo, hi} * s;
+    out[0] = r.lo;
+    out[1] = r.hi;
+}
+
+/* one task box of the size-bound driver */
+void ccport_sb_task_box(const cc_sb_box* parent, int la_i, int nla, int r1_i, int n1, int r2_i, int n2, cc_sb_box* out) {
+    csb::Box6 p;
+    p.la = to_iv(parent->la);
+    for (int i = 0; i < 6; ++i) p.r[i] = to_iv(parent->r[i]);
+    csb::Box6 t = csb::task_box(p, la_i, nla, r1_i, n1, r2_i, n2);
+    out->la = cc_iv{t.la.lo, t.la.hi};
+    for (int i = 0; i < 6; ++i) out->r[i] = cc_iv{t.r[i].lo, t.r[i].hi};
+}
+
 /* the size-bound proof constants from their formulas, for the constant check */
 void ccport_sb_constants(double* out) {
     cc::sb::ValsConstants c = cc::sb::vals_constants_formula();

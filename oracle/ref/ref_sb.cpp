@@ -270,3 +270,15 @@ extern "C" int ccref_sb_prove(const cc_sb_box* root, const cc_sb_grid* grid, int
     }
     return 0;
 }
+
+/* the box of one task of find_critical_intervals_in (r1 tightened across the
+ * r2 loop, from_la_r1_r2), for the driver-state test */
+extern "C" void ccref_sb_task_box(const cc_sb_box* parent, int la_i, int nla, int r1_i, int n1, int r2_i, int n2,
+                                  cc_sb_box* out) {
+    rsb::Variables p;
+    p.la = IV(parent->la.lb, parent->la.ub);
+    for (int i = 0; i < 6; ++i) p.radii[i] = IV(parent->r[i].lb, parent->r[i].ub);
+    rsb::Variables t = RefSbC::task_box(p, la_i, nla, r1_i, n1, r2_i, n2);
+    out->la = cc_iv{t.la.get_lb(), t.la.get_ub()};
+    for (int i = 0; i < 6; ++i) out->r[i] = cc_iv{t.radii[i].get_lb(), t.radii[i].get_ub()};
+}

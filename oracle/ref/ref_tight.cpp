@@ -243,4 +243,12 @@ int ccref_tight_can_recurse(double w, double h, double largest, double weight) {
     return tr::can_recurse(w, h, largest, weight) ? 1 : 0;
 }
 
+/* algcuda::Interval<double> * double (interval.cuh:185-197), for the
+ * interval-times-scalar rounding test */
+void ccref_iv_mul_scalar(double lo, double hi, double s, double* out) {
+    IV r = IV(lo, hi) * s;
+    out[0] = r.get_lb();
+    out[1] = r.get_ub();
+}
+
 }  // extern "C"
