@@ -276,6 +276,7 @@ def run_ours(args, ws, rank, local):
     if ws == 1 and not args.no_proof:
         line["proof"] = proof_comparison(prover)
         line["sb_proof"] = sb_proof_run(prover)
+        line["sb_forms"] = sb_forms(prover)
     if ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
     prover.close()
@@ -327,7 +328,35 @@ def sb_proof_run(prover, warm=True):
     return {"workload": "size-bound proof, initial pass: lambda [1, 1+3/256] x 2, r1 x 32, r2 x 32, r3..r6 x 64",
             "seconds": dt, "leaves": st["leaf_evals"], "leaves_per_s": st["leaf_evals"] / dt,
             "criticals": int(len(crit)), "trapped": int(flags.sum()), "kernel_launches": st["kernel_launches"],
-            "leaf_outcomes": st["leaf_counts"], "digest": st["digest"]}
+            "leaf_outcomes": st["leaf_counts"], "digest": st["digest"],
+            "fp32_prefilter": {"decided_empty": st["fp32_decided"],
+                               "decided_share": st["fp32_decided"] / max(1, st["leaf_evals"]),
+                               "widening_R_mean": st["widening_mean"], "widening_R_max": st["widening_max"],
+                               "widening_samples": st["widening_samples"]}}
+
+
+def sb_forms(prover):
+    """The size-bound proof in its three forms on a smaller workload (lambda
+    [1, 1.1] x 8, r1 x 32, r2 x 32, r3..r6 x 16): plain (one thread runs a
+    leaf's whole cascade, as the reference's kernel), batched without the
+    FP32 pre-filter, batched with it; identical criticals and traces."""
+    import circlecover_gb300 as cg
+    from circlecover_gb300 import workloads as W
+    root = W.sb_root(1.0, 1.1)
+    grid = cg.make_sb_grid(8, (32, 32, 16, 16, 16, 16))
+    res = {}
+    for name, kw in (("batched", {}), ("batched_no_fp32", {"fp32": False}), ("plain", {"plain": True})):
+        prover.sb_find_critical_intervals(root, cg.make_sb_grid(1, (2, 2, 2, 2, 2, 2)), **kw)
+        t0 = time.perf_counter()
+        crit, flags, st = prover.sb_find_critical_intervals(root, grid, **kw)
+        res[name] = (time.perf_counter() - t0, crit, flags, st)
+    keys = ("task_counts", "cell_counts", "leaf_counts", "digest", "leaf_evals")
+    b = res["batched"]
+    same = all(np.array_equal(r[1].view(np.uint64), b[1].view(np.uint64)) and np.array_equal(r[2], b[2])
+               and all(r[3][k] == b[3][k] for k in keys) for r in res.values())
+    return {"workload": "size-bound proof, initial pass: lambda [1,1.1] x 8, r1 x 32, r2 x 32, r3..r6 x 16",
+            "leaves": b[3]["leaf_evals"], "batched_s": b[0], "batched_no_fp32_s": res["batched_no_fp32"][0],
+            "plain_s": res["plain"][0], "speedup_vs_plain": res["plain"][0] / b[0], "identical": bool(same)}
 
 
 def ctypes_peak(prover):

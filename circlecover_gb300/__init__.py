@@ -99,6 +99,10 @@ class CcSbProveStats(ctypes.Structure):
         ("reserved", ctypes.c_int32),
         ("seconds", ctypes.c_double),
         ("kernel_launches", ctypes.c_uint64),
+        ("fp32_decided", ctypes.c_uint64),
+        ("widening_samples", ctypes.c_uint64),
+        ("widening_mean", ctypes.c_double),
+        ("widening_max", ctypes.c_double),
     ]
 
 
@@ -160,7 +164,7 @@ _lib = None
 EXPORTS = [
     "cc_create", "cc_destroy", "cc_status_str", "cc_last_error", "cc_tight_eval", "cc_tight_eval_device",
     "cc_last_launch_count", "cc_tight_prove", "cc_tight_prove_ex", "cc_tight_summary", "cc_interrupt", "cc_free",
-    "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove",
+    "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove", "cc_sb_prove_ex",
 ]
 
 
@@ -196,6 +200,8 @@ def load_library(path=LIB_PATH):
     lib.cc_interrupt.argtypes = [vp]
     lib.cc_sb_prove.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.POINTER(vp), ctypes.POINTER(sz),
                                 ctypes.POINTER(vp), ctypes.POINTER(CcSbProveStats)]
+    lib.cc_sb_prove_ex.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.c_int, ctypes.POINTER(vp),
+                                   ctypes.POINTER(sz), ctypes.POINTER(vp), ctypes.POINTER(CcSbProveStats)]
     lib.cc_set_stage_timing.argtypes = [vp, ctypes.c_int]
     lib.cc_last_stage_times.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     lib.cc_free.argtypes = [vp]
@@ -301,18 +307,22 @@ class Prover:
         self.lib.cc_free(out)
         return arr, stats_to_dict(st)
 
-    def sb_find_critical_intervals(self, root, grid):
+    def sb_find_critical_intervals(self, root, grid, plain=False, fp32=True):
         """The size-bound proof from `root` (an SB_BOX record) with split counts
         `grid` (make_sb_grid); returns (criticals, flags, stats).  Criticals
         are in the reference's final order (sorted and merged); flags bit 0 =
-        kept because a criterion reached a trap site."""
+        kept because a criterion reached a trap site.  plain=True runs the
+        plain form (one thread per leaf runs the whole cascade); fp32=False
+        turns off the FP32 emptiness pre-filter.  All forms give the same
+        criticals, flags and trace."""
         root = np.ascontiguousarray(np.asarray(root, dtype=SB_BOX).reshape(1))
         out = ctypes.c_void_p()
         flags = ctypes.c_void_p()
         n = ctypes.c_size_t()
         st = CcSbProveStats()
-        self._check(self.lib.cc_sb_prove(self.h, root.ctypes.data, ctypes.byref(grid), ctypes.byref(out),
-                                         ctypes.byref(n), ctypes.byref(flags), ctypes.byref(st)), "cc_sb_prove")
+        opts = (1 if plain else 0) | (0 if fp32 else 2)
+        self._check(self.lib.cc_sb_prove_ex(self.h, root.ctypes.data, ctypes.byref(grid), opts, ctypes.byref(out),
+                                            ctypes.byref(n), ctypes.byref(flags), ctypes.byref(st)), "cc_sb_prove_ex")
         arr = np.zeros(n.value, dtype=SB_BOX)
         fl = np.zeros(n.value, dtype=np.uint32)
         if n.value:
@@ -323,6 +333,10 @@ class Prover:
         d = sb_stats_to_dict(st)
         d["seconds"] = float(st.seconds)
         d["kernel_launches"] = int(st.kernel_launches)
+        d["fp32_decided"] = int(st.fp32_decided)
+        d["widening_samples"] = int(st.widening_samples)
+        d["widening_mean"] = float(st.widening_mean)
+        d["widening_max"] = float(st.widening_max)
         return arr, fl, d
 
     def interrupt(self):

@@ -77,6 +77,10 @@ struct SbCounters {
     unsigned long long leaf_evals, trapped_shortcuts;
     unsigned long long digest;
     unsigned long long task_counts[4], cell_counts[4], leaf_counts[CC_SBT_LEAF_OUTCOMES];
+    unsigned long long fp32_empty;      // leaves the FP32 pre-filter proved empty
+    unsigned long long widen_count;     // leaves with an FP64 R of nonzero width
+    double widen_sum;                   // sum of FP32 / FP64 width of R over them
+    unsigned long long widen_max_bits;  // bits of the largest ratio (positive doubles order as integers)
 };
 
 struct SevenJob {  // a leaf whose seven-disk prefix left r7 pieces to check
@@ -229,7 +233,80 @@ __global__ void __launch_bounds__(kThreads) k_sbp_cells(const SbTask* __restrict
 
 struct LeafGrid {
     int gen, n4, n5, n6;
+    int fp32;  // run the FP32 pre-filter
 };
+
+// ---------------------------------------------------------------- FP32 pre-filter
+// The leaf kernel skips a leaf (outcome EMPTY) when its tightened box or its
+// remaining weight R is empty (rectangle_size_bound.cu:196-198).  Most leaves
+// of a pass are empty, and the FP64 instructions that decide it dominate the
+// kernel.  The pre-filter decides the same question with outward-rounded FP32
+// bounds on the FP64 quantities themselves, and only where it proves the
+// FP64 answer "empty":
+//   * every FP64 value v the test reads gets FP32 bounds lo32 <= v <= hi32
+//     (a double converted with rounding down/up; an FMA piece bound
+//     fma(step, i, lo) from the rounded-down/up step and lo, with FMA rounded
+//     down/up: any float below/above the exact value is also below/above its
+//     FP64 rounding);
+//   * tightened lower bounds are maxima of lower bounds, so their FP32 lower
+//     bounds are maxima of FP32 lower bounds;
+//   * R's upper bound is a chain of FP64 round-up subtractions from
+//     la.hi * 0.61 (rounded down); the same chain in FP32 with round-up
+//     operations on upper/lower bounds is never below it.
+// So "FP32 says empty" implies "FP64 says empty"; otherwise the FP64 test
+// runs as before.  Verdicts and traces are unchanged; the pre-filter only
+// removes FP64 work.
+struct F32Piece {
+    float lo, hi;  // bounds of a piece's FP64 lower bound (lo) and upper bound (hi)
+};
+
+__device__ __forceinline__ F32Piece f32_piece(Iv a, double step, int i, int n) {
+    F32Piece p;
+    const float fi = (float)i;  // exact: i < 2^24
+    p.lo = __fmaf_rd(__double2float_rd(step), fi, __double2float_rd(a.lo));
+    p.hi = (i + 1 == n) ? __double2float_ru(a.hi)
+                        : __fmaf_ru(__double2float_ru(step), (float)(i + 1), __double2float_ru(a.lo));
+    return p;
+}
+
+// true only if the FP64 leaf test certainly finds the leaf empty; `ub_R`
+// receives the FP32 upper bound of R.hi and `lb_R` a lower bound of R.lo
+__device__ __forceinline__ bool f32_leaf_empty(const Box6& t, const double step[3], Iv r3, int i4, int n4, int i5,
+                                               int n5, int i6, int n6, float& lb_R, float& ub_R) {
+    float lo[6], hi[6];
+    lo[0] = __double2float_rd(t.r[0].lo);
+    hi[0] = __double2float_ru(t.r[0].hi);
+    lo[1] = __double2float_rd(t.r[1].lo);
+    hi[1] = __double2float_ru(t.r[1].hi);
+    lo[2] = __double2float_rd(r3.lo);
+    hi[2] = __double2float_ru(r3.hi);
+    F32Piece p4 = f32_piece(t.r[3], step[0], i4, n4);
+    F32Piece p5 = f32_piece(t.r[4], step[1], i5, n5);
+    F32Piece p6 = f32_piece(t.r[5], step[2], i6, n6);
+    lo[3] = p4.lo, hi[3] = p4.hi;
+    lo[4] = p5.lo, hi[4] = p5.hi;
+    lo[5] = p6.lo, hi[5] = p6.hi;
+    // tightened lower bounds (variables.hpp:53-65): running maximum from r6
+    // down to r2, starting at 0; r1 keeps its own
+    float m = 0.0f;
+    bool empty = lo[0] >= hi[0];
+    for (int k = 5; k >= 1; --k) {
+        m = fmaxf(m, lo[k]);
+        lo[k] = m;
+        empty = empty || (m >= hi[k]);
+    }
+    // R = la * 0.61 - r1 - ... - r6 (variables.cuh:32-36)
+    float u = __fmul_ru(__double2float_ru(t.la.hi), __double2float_ru(sb::kCriticalRatio));
+    float l = __fmul_rd(__double2float_rd(t.la.lo), __double2float_rd(sb::kCriticalRatio));
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        u = __fadd_ru(u, -lo[k]);
+        l = __fadd_rd(l, -hi[k]);
+    }
+    ub_R = u;
+    lb_R = l;
+    return empty || u < 0.0f;
+}
 
 // Leaves [l0, l1) of the cell grid (rectangle_size_bound.cu:180-205): box,
 // tighten, R and the empty checks, then criterion 0 of the cascade.
@@ -241,6 +318,10 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
                                                           SbLeaf* __restrict__ crit, unsigned long long crit_cap,
                                                           SbCounters* c) {
     __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    __shared__ unsigned int fp32_empty, widen_n;
+    __shared__ double widen_sum;
+    __shared__ unsigned long long widen_max;
+    if (threadIdx.x == 0) fp32_empty = 0, widen_n = 0, widen_sum = 0.0, widen_max = 0;
     trace_init(bt);
     const unsigned long long n456 = (unsigned long long)g.n4 * g.n5 * g.n6;
     SB_WARP_LOOP(l1 - l0) {
@@ -268,11 +349,24 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
             }
             const SbCell cell = cells[ci];
             const SbTask& task = tasks[cell.task];
-            leaf.box = sb::leaf_box_steps(task.box, task.step, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6);
             leaf.id = task.id;
             leaf.idx = pack_idx((int)cell.i3, i4, i5, i6);
+            float lb_R = 0.0f, ub_R = 0.0f;
+            if (g.fp32 && f32_leaf_empty(task.box, task.step, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6, lb_R, ub_R)) {
+                outcome = CC_SBT_LEAF_EMPTY;
+                atomicAdd(&fp32_empty, 1u);
+                goto decided;
+            }
+            leaf.box = sb::leaf_box_steps(task.box, task.step, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6);
+            {
             sb::Vals v;
             v.R = sb::remaining_weight(leaf.box);
+            if (g.fp32 && v.R.hi > v.R.lo) {  // widening of the FP32 bounds of R over FP64 R
+                const double w = ((double)ub_R - (double)(lb_R > 0.0f ? lb_R : 0.0f)) / (v.R.hi - v.R.lo);
+                atomicAdd(&widen_n, 1u);
+                atomicAdd(&widen_sum, w);
+                atomicMax(&widen_max, (unsigned long long)__double_as_longlong(w > 0.0 ? w : 0.0));
+            }
             if (sb::box_empty(leaf.box) || cc::empty(v.R)) {
                 outcome = CC_SBT_LEAF_EMPTY;
             } else {
@@ -282,7 +376,9 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
                 else outcome = ok ? 0 : CC_SBT_LEAF_CRITICAL;  // CRITICAL here = undecided
                 cc::trap_clear();
             }
+            }
         }
+    decided:
         const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
         trace_note(bt, valid && !undecided, valid ? leaf_key(g.gen, leaf, outcome) : 0, outcome);
         const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
@@ -293,6 +389,54 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
         slot = warp_append(&c->n_crit, trapped, crit_cap, &c->overflow);
         if (slot != ~0ULL) {
             leaf.idx |= 1ULL << 63;
+            crit[slot] = leaf;
+        }
+    }
+    trace_flush(bt, c->leaf_counts, c, &c->leaf_evals);
+    if (threadIdx.x == 0) {
+        if (fp32_empty) atomicAdd(&c->fp32_empty, (unsigned long long)fp32_empty);
+        if (widen_n) {
+            atomicAdd(&c->widen_count, (unsigned long long)widen_n);
+            atomicAdd(&c->widen_sum, widen_sum);
+            atomicMax(&c->widen_max_bits, widen_max);
+        }
+    }
+}
+
+// The plain form: one thread runs a leaf's whole cascade, as the reference's
+// kernel does (rectangle_size_bound.cu:180-231); no queues, no pre-filter.
+__global__ void __launch_bounds__(kThreads) k_sbp_leaves_plain(const SbTask* __restrict__ tasks,
+                                                                const SbCell* __restrict__ cells,
+                                                                unsigned long long l0, unsigned long long l1, LeafGrid g,
+                                                                SbLeaf* __restrict__ crit, unsigned long long crit_cap,
+                                                                SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    const unsigned long long n456 = (unsigned long long)g.n4 * g.n5 * g.n6;
+    SB_WARP_LOOP(l1 - l0) {
+        const unsigned long long idx = l0 + base_ + (threadIdx.x & 31);
+        const bool valid = idx < l1;
+        int outcome = CC_SBT_LEAF_EMPTY;
+        SbLeaf leaf;
+        if (valid) {
+            const unsigned long long ci = idx / n456, rem = idx % n456;
+            const int i6 = (int)(rem % g.n6);
+            const int i5 = (int)((rem / g.n6) % g.n5);
+            const int i4 = (int)(rem / ((unsigned long long)g.n6 * g.n5));
+            const SbCell cell = cells[ci];
+            const SbTask& task = tasks[cell.task];
+            leaf.box = sb::leaf_box(task.box, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6);
+            leaf.id = task.id;
+            leaf.idx = pack_idx((int)cell.i3, i4, i5, i6);
+            outcome = sb::leaf_outcome(leaf.box);
+        }
+        trace_note(bt, valid, valid ? leaf_key(g.gen, leaf, outcome) : 0, outcome);
+        const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
+        if ((threadIdx.x & 31) == 0) atomicAdd(&bt.extra, (unsigned long long)nv);
+        const bool to_crit = valid && (outcome == CC_SBT_LEAF_CRITICAL || outcome == CC_SBT_LEAF_TRAPPED);
+        unsigned long long slot = warp_append(&c->n_crit, to_crit, crit_cap, &c->overflow);
+        if (slot != ~0ULL) {
+            if (outcome == CC_SBT_LEAF_TRAPPED) leaf.idx |= 1ULL << 63;
             crit[slot] = leaf;
         }
     }
@@ -526,6 +670,8 @@ struct Engine {
     int grid;
     unsigned long long task_chunk, cell_cap, slice, crit_cap;
     unsigned long long range;  // leaves per slice, adapted as the proof runs
+    bool plain = false;        // one thread per leaf runs the whole cascade
+    bool fp32 = true;          // FP32 emptiness pre-filter in the leaf kernel
     Box6* parents = nullptr;
     SbTask* tasks = nullptr;
     SbCell* cells = nullptr;
@@ -616,7 +762,7 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
     if (chunk > e.task_chunk) chunk = e.task_chunk;
     if (chunk < 1) chunk = 1;
     TaskGrid tg{gen, nla, rn[0], rn[1], rn[3], rn[4], rn[5], per_parent};
-    LeafGrid lg{gen, rn[3], rn[4], rn[5]};
+    LeafGrid lg{gen, rn[3], rn[4], rn[5], e.fp32 ? 1 : 0};
     for (unsigned long long t0 = 0; t0 < ntasks; t0 += chunk) {
         if (gen > 0 && e.h->interrupt.load()) return CC_ERR_INTERRUPTED;
         const unsigned long long t1 = t0 + chunk < ntasks ? t0 + chunk : ntasks;
@@ -637,8 +783,12 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
             CC_CUDA(e.h, cudaMemcpyAsync(e.backup, e.dc, sizeof(SbCounters), cudaMemcpyDeviceToDevice, e.s));
             CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[0], 0, sizeof(unsigned long long), e.s));
             int lgrid = (int)std::min<unsigned long long>((l1 - l0 + kThreads - 1) / kThreads, (unsigned long long)e.grid);
-            k_sbp_leaves<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, e.q[0], &e.dc->n_q[0], e.slice,
-                                                      e.crit, e.crit_cap, e.dc);
+            if (e.plain) {
+                k_sbp_leaves_plain<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, e.crit, e.crit_cap, e.dc);
+            } else {
+                k_sbp_leaves<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, e.q[0], &e.dc->n_q[0],
+                                                          e.slice, e.crit, e.crit_cap, e.dc);
+            }
             CC_LAUNCHED(e.h);
             e.launches++;
             CC_CUDA(e.h, cudaMemcpyAsync(e.hc, e.dc, sizeof(SbCounters), cudaMemcpyDeviceToHost, e.s));
@@ -648,6 +798,11 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
                 CC_CUDA(e.h, cudaMemcpyAsync(e.dc, e.backup, sizeof(SbCounters), cudaMemcpyDeviceToDevice, e.s));
                 if ((st = sync_counters(e))) return st;
                 e.range /= 2;
+                continue;
+            }
+            if (e.plain) {  // every leaf was decided in place; at most `slice` criticals per slice
+                e.range = e.slice;
+                l0 = l1;
                 continue;
             }
             // aim the next slice at half of the pass queue
@@ -719,6 +874,11 @@ bool grid_ok(const cc_sb_grid* g) {
 
 extern "C" int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, cc_sb_box** criticals,
                            size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats) {
+    return cc_sb_prove_ex(h, root, grid, 0, criticals, n_crit, flags, stats);
+}
+
+extern "C" int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, int options,
+                              cc_sb_box** criticals, size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats) {
     if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
     if (!grid_ok(grid)) return ccrt::fail(h, CC_ERR_PARAM, "cc_sb_prove: split counts must be in [1, 2047]");
     const auto t_start = std::chrono::steady_clock::now();
@@ -731,6 +891,8 @@ extern "C" int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid
 
     Engine e;
     e.h = h;
+    e.plain = (options & CC_PROVE_PLAIN) != 0;
+    e.fp32 = !e.plain && !(options & CC_SB_NO_FP32_PREFILTER);
     e.s = h->stream;
     e.grid = h->sm_count * 8;
     // sizes of the work units (queue capacities follow from them); the
@@ -822,6 +984,12 @@ extern "C" int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid
         stats->trapped_shortcuts = e.hc->trapped_shortcuts;
         for (size_t g = 0; g < gen_sizes.size() && g <= CC_MAX_GENERATIONS; ++g) stats->gen_sizes[g] = gen_sizes[g];
         stats->generations_run = generations_run;
+        stats->fp32_decided = e.hc->fp32_empty;
+        stats->widening_samples = e.hc->widen_count;
+        stats->widening_mean = e.hc->widen_count ? e.hc->widen_sum / (double)e.hc->widen_count : 0.0;
+        double wmax;
+        std::memcpy(&wmax, &e.hc->widen_max_bits, sizeof(double));
+        stats->widening_max = wmax;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
         stats->kernel_launches = h->launches;
     }

@@ -177,6 +177,13 @@ typedef struct cc_sb_prove_stats {
     int32_t reserved;
     double seconds;
     uint64_t kernel_launches;
+    /* FP32 pre-filter: leaves it proved empty (no FP64 work for them), and
+     * over the other leaves with an FP64 R of nonzero width the mean and the
+     * largest ratio of the FP32 bounds' width to the FP64 width of R */
+    uint64_t fp32_decided;
+    uint64_t widening_samples;
+    double widening_mean;
+    double widening_max;
 } cc_sb_prove_stats;
 
 /* summary of the final criticals vs the theoretical worst cases;
@@ -304,6 +311,16 @@ int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_t
  * CC_SB_SLICE_LOG2 (5..26) change them (same results, other launches). */
 int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, cc_sb_box** criticals, size_t* n_crit,
                 uint32_t** flags, cc_sb_prove_stats* stats);
+
+/* cc_sb_prove with options: CC_PROVE_PLAIN runs the plain form (one thread
+ * per leaf runs the whole cascade, as the reference's kernel does; no
+ * pre-filter); CC_SB_NO_FP32_PREFILTER keeps the batched passes but decides
+ * every leaf's emptiness in FP64 only.  All forms give identical criticals,
+ * flags and traces (the pre-filter skips FP64 work only where its FP32
+ * bounds prove the FP64 test's answer). */
+#define CC_SB_NO_FP32_PREFILTER 2
+int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, int options, cc_sb_box** criticals,
+                   size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats);
 
 /* Ask a running proof on this handle to stop (the reference's Ctrl-C
  * behaviour, interrupt.cpp:30-46).  cc_tight_prove stops after the current

@@ -105,6 +105,30 @@ def test_gpu_sb_prove_matches_golden(prover, golden_sb_prove, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("form", ["plain", "no_fp32"])
+def test_gpu_sb_prove_other_forms_match_golden(prover, golden_sb_prove, form):
+    """The plain form (whole cascade per thread) and the batched form without
+    the FP32 pre-filter give the same criticals, flags and trace."""
+    for c in golden_sb_prove:
+        crit, flags, st = prover.sb_find_critical_intervals(box6_from_hex(c["root"]), grid_of(c),
+                                                            plain=form == "plain", fp32=False)
+        check_against(c, crit, flags, st)
+        assert st["fp32_decided"] == 0
+
+
+@pytest.mark.gpu
+def test_gpu_fp32_prefilter_decides_only_empty_leaves(prover, golden_sb_prove):
+    decided = 0
+    for c in golden_sb_prove:
+        crit, flags, st = prover.sb_find_critical_intervals(box6_from_hex(c["root"]), grid_of(c))
+        assert st["fp32_decided"] <= st["leaf_counts"][cg.SBT_LEAF_EMPTY]
+        decided += st["fp32_decided"]
+        if st["widening_samples"]:
+            assert 1.0 <= st["widening_mean"] <= st["widening_max"]
+    assert decided > 0
+
+
+@pytest.mark.gpu
 def test_gpu_sb_prove_matches_port_larger(prover, port):
     """Several leaf slices and task chunks: the reference's own initial grid
     restricted to a narrow lambda range, one generation."""
