@@ -51,17 +51,28 @@ using sb::Box6;
 
 namespace {
 
+// FP32 bounds of a task's FP64 values for the leaf pre-filter (rounded
+// down / up once per task instead of once per leaf)
+struct SbTaskF32 {
+    float la_lo_dn, la_hi_up;
+    float cr_dn, cr_up;                       // the critical ratio 0.61 (a double) rounded down / up
+    float r_lo_dn[2], r_hi_up[2];             // r1, r2
+    float step_dn[3], step_up[3];             // r4..r6 split steps
+    float base_dn[3], base_up[3], top_up[3];  // r4..r6 range lower bounds, upper bounds
+};
+
 struct SbTask {  // a task that passed the whole-task shortcuts
     Box6 box;
     uint64_t id;
     double step[3];  // steps of its r4, r5, r6 splits
+    SbTaskF32 f;
 };
-static_assert(sizeof(SbTask) == 144, "task record");
 
 struct SbCell {  // an r3 cell that passed the r3 shortcuts
     Iv r3;
     uint32_t task;
     uint32_t i3;
+    float r3_lo_dn, r3_hi_up;
 };
 
 struct SbLeaf {  // an undecided or critical leaf
@@ -128,13 +139,18 @@ __device__ __forceinline__ void trace_init(BlockTrace<N>& bt) {
     __syncthreads();
 }
 
+// every lane of the warp calls this; lanes with the same outcome are counted
+// by one shared-memory atomic (a warp whose leaves are all empty would
+// otherwise serialise 32 atomics on one address)
 template <int N>
 __device__ __forceinline__ void trace_note(BlockTrace<N>& bt, bool valid, uint64_t key, int outcome) {
     uint64_t d = valid ? key : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
     if ((threadIdx.x & 31) == 0 && d) atomicAdd(&bt.digest, (unsigned long long)d);
-    if (valid) atomicAdd(&bt.counts[outcome], 1ULL);
+    const unsigned same = __match_any_sync(0xffffffffu, valid ? outcome : -1);
+    if (valid && (threadIdx.x & 31) == (unsigned)(__ffs(same) - 1))
+        atomicAdd(&bt.counts[outcome], (unsigned long long)__popc(same));
 }
 
 template <int N>
@@ -194,6 +210,22 @@ __global__ void __launch_bounds__(kThreads) k_sbp_tasks(const Box6* __restrict__
             out[slot].step[0] = cc::subinterval_step(tb.r[3], g.n4);
             out[slot].step[1] = cc::subinterval_step(tb.r[4], g.n5);
             out[slot].step[2] = cc::subinterval_step(tb.r[5], g.n6);
+            SbTaskF32& f = out[slot].f;
+            f.la_lo_dn = __double2float_rd(tb.la.lo);
+            f.la_hi_up = __double2float_ru(tb.la.hi);
+            f.cr_dn = __double2float_rd(sb::kCriticalRatio);
+            f.cr_up = __double2float_ru(sb::kCriticalRatio);
+            for (int k = 0; k < 2; ++k) {
+                f.r_lo_dn[k] = __double2float_rd(tb.r[k].lo);
+                f.r_hi_up[k] = __double2float_ru(tb.r[k].hi);
+            }
+            for (int k = 0; k < 3; ++k) {
+                f.step_dn[k] = __double2float_rd(out[slot].step[k]);
+                f.step_up[k] = __double2float_ru(out[slot].step[k]);
+                f.base_dn[k] = __double2float_rd(tb.r[3 + k].lo);
+                f.base_up[k] = __double2float_ru(tb.r[3 + k].lo);
+                f.top_up[k] = __double2float_ru(tb.r[3 + k].hi);
+            }
         }
     }
     trace_flush(bt, c->task_counts, c, &c->trapped_shortcuts);
@@ -226,14 +258,16 @@ __global__ void __launch_bounds__(kThreads) k_sbp_cells(const SbTask* __restrict
         }
         trace_note(bt, valid, key, outcome);
         unsigned long long slot = warp_append(&c->n_cell, valid && outcome == CC_SBT_CELL_SPLIT, cap, &c->overflow);
-        if (slot != ~0ULL) out[slot] = SbCell{r3, t, (uint32_t)i3};
+        if (slot != ~0ULL) out[slot] = SbCell{r3, t, (uint32_t)i3, __double2float_rd(r3.lo), __double2float_ru(r3.hi)};
     }
     trace_flush(bt, c->cell_counts, c, &c->trapped_shortcuts);
 }
 
 struct LeafGrid {
     int gen, n4, n5, n6;
-    int fp32;  // run the FP32 pre-filter
+    int fp32;                  // run the FP32 pre-filter
+    uint32_t rem0;             // l0 % (n4 n5 n6), when that product is below 2^31
+    unsigned long long cell0;  // l0 / (n4 n5 n6)
 };
 
 // ---------------------------------------------------------------- FP32 pre-filter
@@ -256,48 +290,36 @@ struct LeafGrid {
 // So "FP32 says empty" implies "FP64 says empty"; otherwise the FP64 test
 // runs as before.  Verdicts and traces are unchanged; the pre-filter only
 // removes FP64 work.
-struct F32Piece {
-    float lo, hi;  // bounds of a piece's FP64 lower bound (lo) and upper bound (hi)
-};
-
-__device__ __forceinline__ F32Piece f32_piece(Iv a, double step, int i, int n) {
-    F32Piece p;
-    const float fi = (float)i;  // exact: i < 2^24
-    p.lo = __fmaf_rd(__double2float_rd(step), fi, __double2float_rd(a.lo));
-    p.hi = (i + 1 == n) ? __double2float_ru(a.hi)
-                        : __fmaf_ru(__double2float_ru(step), (float)(i + 1), __double2float_ru(a.lo));
-    return p;
-}
-
 // true only if the FP64 leaf test certainly finds the leaf empty; `ub_R`
 // receives the FP32 upper bound of R.hi and `lb_R` a lower bound of R.lo
-__device__ __forceinline__ bool f32_leaf_empty(const Box6& t, const double step[3], Iv r3, int i4, int n4, int i5,
-                                               int n5, int i6, int n6, float& lb_R, float& ub_R) {
+__device__ __forceinline__ bool f32_leaf_empty(const SbTaskF32& t, float r3_lo, float r3_hi, const int idx[3],
+                                               const int n[3], float& lb_R, float& ub_R) {
     float lo[6], hi[6];
-    lo[0] = __double2float_rd(t.r[0].lo);
-    hi[0] = __double2float_ru(t.r[0].hi);
-    lo[1] = __double2float_rd(t.r[1].lo);
-    hi[1] = __double2float_ru(t.r[1].hi);
-    lo[2] = __double2float_rd(r3.lo);
-    hi[2] = __double2float_ru(r3.hi);
-    F32Piece p4 = f32_piece(t.r[3], step[0], i4, n4);
-    F32Piece p5 = f32_piece(t.r[4], step[1], i5, n5);
-    F32Piece p6 = f32_piece(t.r[5], step[2], i6, n6);
-    lo[3] = p4.lo, hi[3] = p4.hi;
-    lo[4] = p5.lo, hi[4] = p5.hi;
-    lo[5] = p6.lo, hi[5] = p6.hi;
+    lo[0] = t.r_lo_dn[0];
+    hi[0] = t.r_hi_up[0];
+    lo[1] = t.r_lo_dn[1];
+    hi[1] = t.r_hi_up[1];
+    lo[2] = r3_lo;
+    hi[2] = r3_hi;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {  // bounds of fma(step, i, lo) and of the piece's upper bound
+        const int i = idx[k];
+        lo[3 + k] = __fmaf_rd(t.step_dn[k], (float)i, t.base_dn[k]);  // exact: i < 2^24
+        hi[3 + k] = (i + 1 == n[k]) ? t.top_up[k] : __fmaf_ru(t.step_up[k], (float)(i + 1), t.base_up[k]);
+    }
     // tightened lower bounds (variables.hpp:53-65): running maximum from r6
     // down to r2, starting at 0; r1 keeps its own
     float m = 0.0f;
     bool empty = lo[0] >= hi[0];
+#pragma unroll
     for (int k = 5; k >= 1; --k) {
         m = fmaxf(m, lo[k]);
         lo[k] = m;
         empty = empty || (m >= hi[k]);
     }
     // R = la * 0.61 - r1 - ... - r6 (variables.cuh:32-36)
-    float u = __fmul_ru(__double2float_ru(t.la.hi), __double2float_ru(sb::kCriticalRatio));
-    float l = __fmul_rd(__double2float_rd(t.la.lo), __double2float_rd(sb::kCriticalRatio));
+    float u = __fmul_ru(t.la_hi_up, t.cr_up);
+    float l = __fmul_rd(t.la_lo_dn, t.cr_dn);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         u = __fadd_ru(u, -lo[k]);
@@ -318,10 +340,12 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
                                                           SbLeaf* __restrict__ crit, unsigned long long crit_cap,
                                                           SbCounters* c) {
     __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
-    __shared__ unsigned int fp32_empty, widen_n;
-    __shared__ double widen_sum;
-    __shared__ unsigned long long widen_max;
-    if (threadIdx.x == 0) fp32_empty = 0, widen_n = 0, widen_sum = 0.0, widen_max = 0;
+    __shared__ unsigned long long fp32_empty_b, widen_n_b, widen_max_b;
+    __shared__ double widen_sum_b;
+    if (threadIdx.x == 0) fp32_empty_b = 0, widen_n_b = 0, widen_sum_b = 0.0, widen_max_b = 0;
+    // per-thread pre-filter statistics, reduced once per block
+    unsigned int fp32_empty = 0, widen_n = 0;
+    double widen_sum = 0.0, widen_max = 0.0;
     trace_init(bt);
     const unsigned long long n456 = (unsigned long long)g.n4 * g.n5 * g.n6;
     SB_WARP_LOOP(l1 - l0) {
@@ -332,11 +356,13 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
         if (valid) {
             unsigned long long ci;
             int i4, i5, i6;
-            if (n456 <= 0xffffffffULL) {  // 32-bit index arithmetic where it fits
-                const unsigned long long q = idx / (uint32_t)n456;
-                const uint32_t rem = (uint32_t)(idx - q * n456);
+            if (n456 < (1ULL << 31) && l1 - l0 < (1ULL << 31)) {
+                // 32-bit index arithmetic: offsets from the slice's first cell
+                const uint32_t off = g.rem0 + (uint32_t)(idx - l0);  // < 2^32
+                const uint32_t q = off / (uint32_t)n456;
+                const uint32_t rem = off - q * (uint32_t)n456;
                 const uint32_t r56 = rem / (uint32_t)g.n6;
-                ci = q;
+                ci = g.cell0 + q;
                 i6 = (int)(rem - r56 * (uint32_t)g.n6);
                 i4 = (int)(r56 / (uint32_t)g.n5);
                 i5 = (int)(r56 - (uint32_t)i4 * (uint32_t)g.n5);
@@ -352,9 +378,10 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
             leaf.id = task.id;
             leaf.idx = pack_idx((int)cell.i3, i4, i5, i6);
             float lb_R = 0.0f, ub_R = 0.0f;
-            if (g.fp32 && f32_leaf_empty(task.box, task.step, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6, lb_R, ub_R)) {
+            const int pidx[3] = {i4, i5, i6}, pn[3] = {g.n4, g.n5, g.n6};
+            if (g.fp32 && f32_leaf_empty(task.f, cell.r3_lo_dn, cell.r3_hi_up, pidx, pn, lb_R, ub_R)) {
                 outcome = CC_SBT_LEAF_EMPTY;
-                atomicAdd(&fp32_empty, 1u);
+                ++fp32_empty;
                 goto decided;
             }
             leaf.box = sb::leaf_box_steps(task.box, task.step, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6);
@@ -363,9 +390,9 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
             v.R = sb::remaining_weight(leaf.box);
             if (g.fp32 && v.R.hi > v.R.lo) {  // widening of the FP32 bounds of R over FP64 R
                 const double w = ((double)ub_R - (double)(lb_R > 0.0f ? lb_R : 0.0f)) / (v.R.hi - v.R.lo);
-                atomicAdd(&widen_n, 1u);
-                atomicAdd(&widen_sum, w);
-                atomicMax(&widen_max, (unsigned long long)__double_as_longlong(w > 0.0 ? w : 0.0));
+                ++widen_n;
+                widen_sum += w;
+                widen_max = w > widen_max ? w : widen_max;
             }
             if (sb::box_empty(leaf.box) || cc::empty(v.R)) {
                 outcome = CC_SBT_LEAF_EMPTY;
@@ -392,13 +419,19 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
             crit[slot] = leaf;
         }
     }
+    if (fp32_empty) atomicAdd(&fp32_empty_b, (unsigned long long)fp32_empty);
+    if (widen_n) {
+        atomicAdd(&widen_n_b, (unsigned long long)widen_n);
+        atomicAdd(&widen_sum_b, widen_sum);
+        atomicMax(&widen_max_b, (unsigned long long)__double_as_longlong(widen_max));
+    }
     trace_flush(bt, c->leaf_counts, c, &c->leaf_evals);
     if (threadIdx.x == 0) {
-        if (fp32_empty) atomicAdd(&c->fp32_empty, (unsigned long long)fp32_empty);
-        if (widen_n) {
-            atomicAdd(&c->widen_count, (unsigned long long)widen_n);
-            atomicAdd(&c->widen_sum, widen_sum);
-            atomicMax(&c->widen_max_bits, widen_max);
+        if (fp32_empty_b) atomicAdd(&c->fp32_empty, fp32_empty_b);
+        if (widen_n_b) {
+            atomicAdd(&c->widen_count, widen_n_b);
+            atomicAdd(&c->widen_sum, widen_sum_b);
+            atomicMax(&c->widen_max_bits, widen_max_b);
         }
     }
 }
@@ -762,7 +795,7 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
     if (chunk > e.task_chunk) chunk = e.task_chunk;
     if (chunk < 1) chunk = 1;
     TaskGrid tg{gen, nla, rn[0], rn[1], rn[3], rn[4], rn[5], per_parent};
-    LeafGrid lg{gen, rn[3], rn[4], rn[5], e.fp32 ? 1 : 0};
+    LeafGrid lg{gen, rn[3], rn[4], rn[5], e.fp32 ? 1 : 0, 0u, 0ULL};
     for (unsigned long long t0 = 0; t0 < ntasks; t0 += chunk) {
         if (gen > 0 && e.h->interrupt.load()) return CC_ERR_INTERRUPTED;
         const unsigned long long t1 = t0 + chunk < ntasks ? t0 + chunk : ntasks;
@@ -783,6 +816,8 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
             CC_CUDA(e.h, cudaMemcpyAsync(e.backup, e.dc, sizeof(SbCounters), cudaMemcpyDeviceToDevice, e.s));
             CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[0], 0, sizeof(unsigned long long), e.s));
             int lgrid = (int)std::min<unsigned long long>((l1 - l0 + kThreads - 1) / kThreads, (unsigned long long)e.grid);
+            lg.cell0 = l0 / n456;
+            lg.rem0 = (uint32_t)(l0 % n456);
             if (e.plain) {
                 k_sbp_leaves_plain<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, e.crit, e.crit_cap, e.dc);
             } else {

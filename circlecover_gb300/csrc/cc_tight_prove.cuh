@@ -127,12 +127,15 @@ __device__ __forceinline__ void trace_init(BlockTrace& bt) {
 }
 
 __device__ __forceinline__ void trace_note(BlockTrace& bt, bool valid, uint64_t key, int outcome) {
-    // warp-reduce the digest, shared atomics for the counts
+    // warp-reduce the digest; one shared atomic per distinct outcome in the
+    // warp for the counts (lanes with equal outcomes would serialise)
     uint64_t d = valid ? key : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(&bt.digest, (unsigned long long)d);
-    if (valid) atomicAdd(&bt.counts[outcome], 1ULL);
+    const unsigned same = __match_any_sync(0xffffffffu, valid ? outcome : -1);
+    if (valid && (threadIdx.x & 31) == (unsigned)(__ffs(same) - 1))
+        atomicAdd(&bt.counts[outcome], (unsigned long long)__popc(same));
 }
 
 __device__ __forceinline__ void trace_flush(BlockTrace& bt, Counters* c, int level) {
