@@ -534,22 +534,67 @@ struct SplitCriterion<sb::SB_R1_CORNER_EXPLICIT> {
     __device__ static bool item(const Box6& b, const sb::Vals& v, int i) { return sb::r1_corner_item(b, v, i); }
 };
 
-template <int K>
-__global__ void __launch_bounds__(kThreads) k_sbp_split_items(const SbLeaf* __restrict__ qin,
-                                                               const unsigned long long* n_in, uint32_t* masks) {
-    constexpr int I = SplitCriterion<K>::kItems;
-    // placement-major order: the lanes of a warp try the same placement on
-    // consecutive leaves
+// r1 in a corner, first half: every (leaf, placement), placement-major.
+// Placement 8 runs whole here; placements 0..7 run their start (the weight
+// bound and the corner disk) and, where that does not already fail, become
+// a job for the backtracking kernel, so that the backtracking (93 % of the
+// criterion's operations, reached by about a fifth of the placements) runs
+// on full warps.  A job is (leaf << 4) | placement.
+__global__ void __launch_bounds__(kThreads) k_sbp_r1c_start(const SbLeaf* __restrict__ qin,
+                                                             const unsigned long long* n_in, uint32_t* masks,
+                                                             unsigned long long* jobs, unsigned long long* n_jobs,
+                                                             unsigned long long job_cap, SbCounters* c) {
+    constexpr int I = sb::kR1CornerItems;
     const unsigned long long nl = *n_in, total = nl * (unsigned long long)I;
+    SB_WARP_LOOP(total) {
+        const unsigned long long idx = base_ + (threadIdx.x & 31);
+        const bool valid = idx < total;
+        bool job = false;
+        unsigned long long leaf = 0;
+        int i = 0;
+        if (valid) {
+            i = (int)(idx / nl);
+            leaf = idx - (unsigned long long)i * nl;
+            const Box6 box = qin[leaf].box;
+            sb::Vals v;
+            v.R = sb::remaining_weight(box);
+            cc::trap_clear();
+            bool ok;
+            if (i == 8) {
+                ok = sb::r1_corner_r34_and_r2(box);
+            } else {
+                sb::CornerStart st;
+                job = sb::r1_corner_start(box, v, i, st);
+                ok = false;
+            }
+            const bool trapped = cc::trap_status() != cc::TRAP_NONE;
+            cc::trap_clear();
+            if (ok) atomicOr(&masks[2 * leaf], 1u << i);
+            if (trapped) atomicOr(&masks[2 * leaf + 1], 1u << i);
+        }
+        unsigned long long slot = warp_append(n_jobs, job, job_cap, &c->overflow);
+        if (slot != ~0ULL) jobs[slot] = (leaf << 4) | (unsigned long long)i;
+    }
+}
+
+// r1 in a corner, second half: the backtracking of the jobs (the start is
+// recomputed; same operations, same values)
+__global__ void __launch_bounds__(kThreads) k_sbp_r1c_reach(const SbLeaf* __restrict__ qin,
+                                                             const unsigned long long* __restrict__ jobs,
+                                                             const unsigned long long* n_jobs, uint32_t* masks) {
+    const unsigned long long total = *n_jobs;
     for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (unsigned long long)gridDim.x * blockDim.x) {
-        const int i = (int)(idx / nl);
-        const unsigned long long leaf = idx - (unsigned long long)i * nl;
+        const unsigned long long job = jobs[idx];
+        const unsigned long long leaf = job >> 4;
+        const int i = (int)(job & 15);
         const Box6 box = qin[leaf].box;
         sb::Vals v;
         v.R = sb::remaining_weight(box);
         cc::trap_clear();
-        const bool ok = SplitCriterion<K>::item(box, v, i);
+        sb::CornerStart st;
+        bool ok = sb::r1_corner_start(box, v, i, st);
+        ok = ok && sb::corner_groups_reach(box, 2 + i / 2, st.cross, st.first, st.limit);
         const bool trapped = cc::trap_status() != cc::TRAP_NONE;
         cc::trap_clear();
         if (ok) atomicOr(&masks[2 * leaf], 1u << i);
@@ -725,14 +770,22 @@ int launch_passes(Engine& e, int gen, int src) {
     if constexpr (K == sb::SB_R1_CORNER_EXPLICIT) {
         const int dst = src ^ 1;
         uint32_t* masks = reinterpret_cast<uint32_t*>(e.jobs);  // free until the seven-disk kernels
+        // the jobs live in the output queue's memory until the resolve kernel
+        // writes the queue; n_q[dst] counts them until then
+        unsigned long long* r1c_jobs = reinterpret_cast<unsigned long long*>(e.q[dst]);
+        static_assert(sizeof(SbLeaf) >= 8 * sizeof(unsigned long long), "8 jobs per queue record");
         CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
         CC_CUDA(e.h, cudaMemsetAsync(masks, 0, e.slice * 2 * sizeof(uint32_t), e.s));
-        k_sbp_split_items<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], masks);
+        k_sbp_r1c_start<<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], masks, r1c_jobs, &e.dc->n_q[dst],
+                                                       e.slice * 8, e.dc);
         CC_LAUNCHED(e.h);
+        k_sbp_r1c_reach<<<e.grid, kThreads, 0, e.s>>>(e.q[src], r1c_jobs, &e.dc->n_q[dst], masks);
+        CC_LAUNCHED(e.h);
+        CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
         k_sbp_split_resolve<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], masks, e.q[dst],
                                                               &e.dc->n_q[dst], e.slice, e.crit, e.crit_cap, gen, e.dc);
         CC_LAUNCHED(e.h);
-        e.launches += 2;
+        e.launches += 3;
         return launch_passes<K + 1>(e, gen, dst);
     } else if constexpr (K < sb::SB_SEVEN_DISK) {
         const int dst = src ^ 1;
