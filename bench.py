@@ -285,26 +285,43 @@ def run_ours(args, ws, rank, local):
 
 def proof_comparison(prover):
     """Wall time of the tight proof's initial pass on the small plain-method
-    workload (lambda in [1, 1.1] in 256 pieces, r1 in 64, r2..r4 in 128 each)
-    in the batched form (criteria prepared once per parent cell) and in the
-    plain form (every criterion re-evaluated in every cell, as the reference
-    does); both must give identical criticals and traces."""
+    workload (lambda in [1, 1.1] in 256 pieces, r1 in 64, r2..r4 in 128
+    each) in three forms, all with identical criticals:
+      plain    -- every criterion re-evaluated in every cell, the reference's
+                  leaf order;
+      batched  -- criteria prepared once per parent cell, compacted stages;
+      learned  -- batched, with the leaf criteria ordered per r3 cell by the
+                  network, trained first (by the library's kernels) on
+                  records from this workload's own plain-order cells."""
     import circlecover_gb300 as cg
+    from circlecover_gb300 import learn
     from circlecover_gb300 import workloads as W
     root = W.tight_root(1.0, 1.1)
     grid = cg.make_grid(256, (64, 128, 128, 128))
     out = {"workload": "tight proof, initial pass: lambda [1,1.1] x 256, r1 x 64, r2..r4 x 128"}
+    prover.tight_find_critical_intervals(W.tight_root(1.0, 1.0001), cg.make_grid(2, (8, 8, 8, 8)))  # buffers
+    t0 = time.perf_counter()
+    prover.mlp_init(3)
+    rec, ncells = learn.proof_records(prover, root, grid, per_cell=16)
+    hist = learn.train(prover, rec, epochs=4, batch=8192)
+    train_s = time.perf_counter() - t0
+    rep = learn.prediction_report(learn.predict(prover, rec), rec.labels_np)
     res = {}
-    for name, plain in (("batched", False), ("plain", True)):
+    for name, kw in (("batched", {}), ("learned", {"learned": True}), ("plain", {"plain": True})):
         t0 = time.perf_counter()
-        crit, st = prover.tight_find_critical_intervals(root, grid, plain=plain)
+        crit, st = prover.tight_find_critical_intervals(root, grid, **kw)
         res[name] = (time.perf_counter() - t0, crit, st)
     bt, bc, bs = res["batched"]
-    pt, pc, ps = res["plain"]
-    out.update({"batched_s": bt, "plain_s": pt, "speedup": pt / bt, "leaves": bs["leaf_evals"],
-                "leaves_per_s_batched": bs["leaf_evals"] / bt, "criticals": len(bc),
-                "identical": bool(np.array_equal(bc.view(np.uint64), pc.view(np.uint64))
-                                  and all(bs[k] == ps[k] for k in ("counts", "digest", "leaf_evals", "gen_sizes")))})
+    keys = ("gen_sizes", "leaf_evals", "trapped_leaves")
+    same = all(np.array_equal(r[1].view(np.uint64), bc.view(np.uint64)) and all(r[2][k] == bs[k] for k in keys)
+               for r in res.values())
+    out.update({"plain_s": res["plain"][0], "batched_s": bt, "learned_s": res["learned"][0],
+                "speedup_batched": res["plain"][0] / bt, "speedup_learned": res["plain"][0] / res["learned"][0],
+                "leaves": bs["leaf_evals"], "criticals": len(bc), "identical_criticals": bool(same),
+                "identical_trace_plain_batched": bool(res["plain"][2]["digest"] == bs["digest"]),
+                "training": {"cells_logged": ncells, "records": rec.n, "seconds": train_s, "loss": hist,
+                             "error_rate_per_output": rep["error_rate_per_output"]},
+                "leaf_outcomes": {k: res[k][2]["counts"][3][:7] for k in res}})
     return out
 
 

@@ -165,7 +165,12 @@ EXPORTS = [
     "cc_create", "cc_destroy", "cc_status_str", "cc_last_error", "cc_tight_eval", "cc_tight_eval_device",
     "cc_last_launch_count", "cc_tight_prove", "cc_tight_prove_ex", "cc_tight_summary", "cc_interrupt", "cc_free",
     "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove", "cc_sb_prove_ex",
+    "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
+    "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log",
 ]
+
+MLP_PARAMS = 5319
+MLP_FEATURES = 10
 
 
 def load_library(path=LIB_PATH):
@@ -198,6 +203,15 @@ def load_library(path=LIB_PATH):
     lib.cc_sb_eval.argtypes = [vp, vp, sz, vp]
     lib.cc_sb_eval_device.argtypes = [vp, vp, sz, vp, vp]
     lib.cc_interrupt.argtypes = [vp]
+    lib.cc_mlp_init.argtypes = [vp, ctypes.c_uint64]
+    lib.cc_mlp_set_weights.argtypes = [vp, vp]
+    lib.cc_mlp_get_weights.argtypes = [vp, vp]
+    lib.cc_mlp_features.argtypes = [vp, vp, sz, ctypes.c_float, vp]
+    lib.cc_mlp_gradients.argtypes = [vp, vp, vp, sz, vp, ctypes.POINTER(ctypes.c_float)]
+    lib.cc_mlp_train_step.argtypes = [vp, vp, vp, sz, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
+    lib.cc_mlp_infer.argtypes = [vp, vp, sz, vp]
+    lib.cc_tight_first.argtypes = [vp, vp, sz, ctypes.c_int, vp, vp]
+    lib.cc_tight_cell_log.argtypes = [vp, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_int)]
     lib.cc_sb_prove.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.POINTER(vp), ctypes.POINTER(sz),
                                 ctypes.POINTER(vp), ctypes.POINTER(CcSbProveStats)]
     lib.cc_sb_prove_ex.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.c_int, ctypes.POINTER(vp),
@@ -290,15 +304,29 @@ class Prover:
                                                ctypes.c_void_p(stream_ptr) if stream_ptr else None),
                     "cc_sb_eval_device")
 
-    def tight_find_critical_intervals(self, root, grid, plain=False):
+    def tight_cell_log(self):
+        """(cells, r4_splits) logged by the last proof run with log_cells=True."""
+        n = ctypes.c_size_t()
+        s4 = ctypes.c_int()
+        self._check(self.lib.cc_tight_cell_log(self.h, None, 0, ctypes.byref(n), ctypes.byref(s4)), "cc_tight_cell_log")
+        out = np.zeros(n.value, dtype=TIGHT_BOX)
+        if n.value:
+            self._check(self.lib.cc_tight_cell_log(self.h, out.ctypes.data, n.value, ctypes.byref(n), ctypes.byref(s4)),
+                        "cc_tight_cell_log")
+        return out, int(s4.value)
+
+    def tight_find_critical_intervals(self, root, grid, plain=False, learned=False, log_cells=False):
         """The tight proof from `root` (a TIGHT_BOX record) with split counts
         `grid` (make_grid); returns (criticals, stats).  plain=True runs the
-        plain form (every criterion re-evaluated in every cell)."""
+        plain form (every criterion re-evaluated in every cell); learned=True
+        lets the trained network order the leaf criteria (CC_PROVE_LEARNED);
+        log_cells=True keeps a sample of r3 cells for tight_cell_log()."""
         rs = box_struct(root)
         out = ctypes.c_void_p()
         n = ctypes.c_size_t()
         st = CcProveStats()
-        self._check(self.lib.cc_tight_prove_ex(self.h, ctypes.byref(rs), ctypes.byref(grid), 1 if plain else 0,
+        flags = (1 if plain else 0) | (4 if learned else 0) | (8 if log_cells else 0)
+        self._check(self.lib.cc_tight_prove_ex(self.h, ctypes.byref(rs), ctypes.byref(grid), flags,
                                                ctypes.byref(out), ctypes.byref(n), ctypes.byref(st)),
                     "cc_tight_prove_ex")
         arr = np.zeros(n.value, dtype=TIGHT_BOX)
@@ -338,6 +366,48 @@ class Prover:
         d["widening_mean"] = float(st.widening_mean)
         d["widening_max"] = float(st.widening_max)
         return arr, fl, d
+
+    # ---- learned strategy ordering (device pointers are raw ints, e.g.
+    # torch.Tensor.data_ptr())
+    def mlp_init(self, seed=0):
+        self._check(self.lib.cc_mlp_init(self.h, seed), "cc_mlp_init")
+
+    def mlp_weights(self):
+        w = np.zeros(MLP_PARAMS, dtype=np.float32)
+        self._check(self.lib.cc_mlp_get_weights(self.h, w.ctypes.data), "cc_mlp_get_weights")
+        return w
+
+    def mlp_set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == MLP_PARAMS
+        self._check(self.lib.cc_mlp_set_weights(self.h, w.ctypes.data), "cc_mlp_set_weights")
+
+    def mlp_features(self, soa_ptr, n, feat_ptr, depth=0.0):
+        self._check(self.lib.cc_mlp_features(self.h, ctypes.c_void_p(soa_ptr), n, depth, ctypes.c_void_p(feat_ptr)),
+                    "cc_mlp_features")
+
+    def mlp_gradients(self, feat_ptr, labels_ptr, n):
+        g = np.zeros(MLP_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        self._check(self.lib.cc_mlp_gradients(self.h, ctypes.c_void_p(feat_ptr), ctypes.c_void_p(labels_ptr), n,
+                                              g.ctypes.data, ctypes.byref(loss)), "cc_mlp_gradients")
+        return g, float(loss.value)
+
+    def mlp_train_step(self, feat_ptr, labels_ptr, n, lr):
+        loss = ctypes.c_float()
+        self._check(self.lib.cc_mlp_train_step(self.h, ctypes.c_void_p(feat_ptr), ctypes.c_void_p(labels_ptr), n,
+                                               lr, ctypes.byref(loss)), "cc_mlp_train_step")
+        return float(loss.value)
+
+    def mlp_infer(self, feat_ptr, n, logits_ptr):
+        self._check(self.lib.cc_mlp_infer(self.h, ctypes.c_void_p(feat_ptr), n, ctypes.c_void_p(logits_ptr)),
+                    "cc_mlp_infer")
+
+    def tight_first(self, soa_ptr, n, outcome_ptr, evals_ptr=None, learned=False):
+        """First-success evaluation (see cc_tight_first); device pointers."""
+        self._check(self.lib.cc_tight_first(self.h, ctypes.c_void_p(soa_ptr), n, 1 if learned else 0,
+                                            ctypes.c_void_p(outcome_ptr),
+                                            ctypes.c_void_p(evals_ptr) if evals_ptr else None), "cc_tight_first")
 
     def interrupt(self):
         self.lib.cc_interrupt(self.h)

@@ -24,6 +24,7 @@ UNITS = [
     ("cc_prover.cu", ["-fmad=false", "-Xptxas", "-v"]),
     ("cc_sb_kernels.cu", ["-fmad=false", "-Xptxas", "-v"]),
     ("cc_sb_prove.cu", ["-fmad=false", "-Xptxas", "-v"]),
+    ("cc_mlp.cu", ["-fmad=false", "-Xptxas", "-v"]),
     ("cc_selftest_fmad.cu", []),
 ]
 

@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <vector>
 
+#include "cc_mlp.cuh"
 #include "cc_runtime.cuh"
 #include "cc_tight.cuh"
 #include "cc_tight_prove.cuh"
@@ -283,6 +284,7 @@ int cc_destroy(cc_handle* h) {
     for (auto& b : h->bufs)
         if (b.ptr) cudaFree(b.ptr);
     if (h->pinned) cudaFreeHost(h->pinned);
+    if (h->mlp_free) h->mlp_free(h);
     for (auto& e : h->stage_ev)
         if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -559,8 +561,8 @@ namespace {
 using namespace cc::prove;
 
 // buffer slots in the handle
-enum Slot { S_PARENTS = 6, S_TASKS, S_CELL2, S_CELL3, S_CELL4, S_LEAF, S_CRIT, S_COUNTERS, S_GAPS };
-static_assert(S_GAPS < 16, "proof buffers overlap the evaluation queues");
+enum Slot { S_PARENTS = 6, S_TASKS, S_CELL2, S_CELL3, S_CELL4, S_LEAF, S_CRIT, S_COUNTERS, S_GAPS, S_LEAF2 };
+static_assert(S_LEAF2 < 16, "proof buffers overlap the evaluation queues");
 
 struct GenTotals {
     unsigned long long counts[4][8] = {};
@@ -594,14 +596,69 @@ void merge_by_r1(std::vector<cc_tight_box>& v, std::vector<cc_tight_box>& out) {
     (void)first;
 }
 
+// ---- learned leaf order ------------------------------------------------------
+// Before the leaves of an r3 cell are checked, the network looks at the cell
+// (its r4 range in place of a leaf's r4) and predicts whether the leaf
+// criterion r1_r2_r3_strategies(box, R4) will certify its leaves.  If so,
+// stage 4a tries that criterion (about 31 directed-rounding operations on
+// the microbench) before the 2x2 criterion (about 116, six bisections) that
+// the reference's order puts first.  The threshold -1.0 on the logit
+// (probability 0.27) is about the ratio of the two costs: above it, trying
+// the cheap criterion first saves more than it wastes.
+constexpr float kLeafFirstLogit = -1.0f;
+constexpr unsigned long long kCellLogRate = 64;      // log one cell in 64
+constexpr unsigned long long kCellLogCap = 1 << 20;  // cells logged per proof at most
+
+__global__ void k_cell_features(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
+                                const unsigned long long* n_dev, unsigned long long cap, float* __restrict__ feat) {
+    const unsigned long long n = *n_dev < cap ? *n_dev : cap;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const Cell4& c = cells[i];
+        const Task& t = tasks[c.task];
+        const double v[10] = {t.la.lo, t.la.hi, c.r1.lo, c.r1.hi, c.r2.lo, c.r2.hi, c.r3.lo, c.r3.hi, c.r4r.lo, c.r4r.hi};
+        cc::mlp::features(v, t.weight, 0.0f, feat + i * cc::mlp::kFeatures);
+    }
+}
+
+__global__ void k_cell_order(Cell4* __restrict__ cells, const unsigned long long* n_dev, unsigned long long cap,
+                             const float* __restrict__ logits) {
+    const unsigned long long n = *n_dev < cap ? *n_dev : cap;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        cells[i].order = logits[i * 8 + 4] > kLeafFirstLogit ? 1 : 0;
+}
+
+// a sample of the r3 cells (la, r1, r2, r3, r4 range) for training records
+__global__ void k_cell_log(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
+                           const unsigned long long* n_dev, unsigned long long cap, unsigned long long salt,
+                           cc_tight_box* __restrict__ log, unsigned long long* n_log) {
+    const unsigned long long n = *n_dev < cap ? *n_dev : cap;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        if (mix64(i ^ salt) % kCellLogRate) continue;
+        const unsigned long long slot = atomicAdd(n_log, 1ULL);
+        if (slot >= kCellLogCap) continue;
+        const Cell4& c = cells[i];
+        const Task& t = tasks[c.task];
+        log[slot] = cc_tight_box{{t.la.lo, t.la.hi}, {{c.r1.lo, c.r1.hi}, {c.r2.lo, c.r2.hi}, {c.r3.lo, c.r3.hi},
+                                                      {c.r4r.lo, c.r4r.hi}}};
+    }
+}
+
+enum { S_CELL_FEAT = 32, S_CELL_LOGITS, S_CELL_LOG };
+
 // One chunk of parents [a, b) of a generation; returns CC_QUEUE_OVERFLOW
 // (without side effects on `out`/`tot`) when a device queue ran full.
 int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, size_t b, int k, const int s[4], Caps caps,
-              std::vector<cc_tight_box>& out, GenTotals& tot, unsigned long long task_base, bool hoist) {
+              std::vector<cc_tight_box>& out, GenTotals& tot, unsigned long long task_base, bool hoist, int flags) {
+    const bool learned = hoist && (flags & CC_PROVE_LEARNED);
+    const bool log_cells = hoist && (flags & CC_PROVE_LOG_CELLS);
     const size_t np = b - a;
     const size_t ntasks = np * (size_t)k;
-    void *d_par, *d_tasks, *d_c2, *d_c3, *d_c4, *d_leaf, *d_gaps, *d_crit, *d_cnt;
+    void *d_par, *d_tasks, *d_c2, *d_c3, *d_c4, *d_leaf, *d_gaps, *d_crit, *d_cnt, *d_leaf2 = nullptr;
     int st;
+    if (hoist && (st = ccrt::ensure(h, S_LEAF2, caps.leaf2 * sizeof(Leaf2), &d_leaf2))) return st;
     if ((st = ccrt::ensure(h, S_GAPS, caps.gaps * sizeof(GapsLeaf), &d_gaps))) return st;
     if ((st = ccrt::ensure(h, S_PARENTS, np * sizeof(cc_tight_box), &d_par))) return st;
     if ((st = ccrt::ensure(h, S_TASKS, ntasks * sizeof(Task), &d_tasks))) return st;
@@ -628,7 +685,46 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
         k_stage3<true><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell3*)d_c3, s[2], (Cell4*)d_c4, caps,
                                           cnt, task_base);
         CC_LAUNCHED(h);
-        k_stage4a<true><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf, caps, cnt, task_base);
+        if (learned) {
+            void *d_feat, *d_logits;
+            if ((st = ccrt::ensure(h, S_CELL_FEAT, caps.cell4 * cc::mlp::kFeatures * sizeof(float), &d_feat))) return st;
+            if ((st = ccrt::ensure(h, S_CELL_LOGITS, caps.cell4 * 8 * sizeof(float), &d_logits))) return st;
+            k_cell_features<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, &cnt->n_cell4, caps.cell4,
+                                               (float*)d_feat);
+            CC_LAUNCHED(h);
+            if ((st = cc_mlp_infer_async(h, (const float*)d_feat, &cnt->n_cell4, caps.cell4, (float*)d_logits, sm)))
+                return st;
+            k_cell_order<<<g, 128, 0, sm>>>((Cell4*)d_c4, &cnt->n_cell4, caps.cell4, (const float*)d_logits);
+            CC_LAUNCHED(h);
+        }
+        if (log_cells) {
+            void* d_log;
+            if ((st = ccrt::ensure(h, S_CELL_LOG, kCellLogCap * sizeof(cc_tight_box) + 64, &d_log))) return st;
+            unsigned long long* n_log = (unsigned long long*)((char*)d_log + kCellLogCap * sizeof(cc_tight_box));
+            CC_CUDA(h, cudaMemsetAsync(n_log, 0, sizeof(unsigned long long), sm));
+            k_cell_log<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, &cnt->n_cell4, caps.cell4,
+                                          task_base * 0x9e3779b97f4a7c15ULL, (cc_tight_box*)d_log, n_log);
+            CC_LAUNCHED(h);
+            unsigned long long nl = 0;
+            CC_CUDA(h, cudaMemcpyAsync(&nl, n_log, sizeof(nl), cudaMemcpyDeviceToHost, sm));
+            CC_CUDA(h, cudaStreamSynchronize(sm));
+            nl = std::min<unsigned long long>(nl, kCellLogCap);
+            const size_t room = kCellLogCap - std::min<size_t>(h->cell_log.size(), kCellLogCap);
+            const size_t take = std::min<size_t>(nl, room);
+            if (take) {
+                const size_t old = h->cell_log.size();
+                h->cell_log.resize(old + take);
+                CC_CUDA(h, cudaMemcpyAsync(h->cell_log.data() + old, d_log, take * sizeof(cc_tight_box),
+                                           cudaMemcpyDeviceToHost, sm));
+                CC_CUDA(h, cudaStreamSynchronize(sm));
+            }
+            h->cell_log_splits = s[3];
+        }
+        k_stage4a<true, true><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf,
+                                                 (Leaf2*)d_leaf2, caps, cnt, task_base);
+        CC_LAUNCHED(h);
+        k_stage4a2<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf2*)d_leaf2, (Leaf*)d_leaf, caps,
+                                      cnt, task_base);
         CC_LAUNCHED(h);
     } else {
         k_stage1<false><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (int)ntasks, s[0], (Cell2*)d_c2, caps, cnt,
@@ -640,8 +736,8 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
         k_stage3<false><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell3*)d_c3, s[2], (Cell4*)d_c4,
                                            caps, cnt, task_base);
         CC_LAUNCHED(h);
-        k_stage4a<false><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf, caps, cnt,
-                                            task_base);
+        k_stage4a<false, false><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf,
+                                                   nullptr, caps, cnt, task_base);
         CC_LAUNCHED(h);
     }
     k_stage4b<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3], (GapsLeaf*)d_gaps,
@@ -689,7 +785,7 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
 
 // all tasks of one generation, in parent chunks that fit the device queues
 int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k, const int s[4],
-                   std::vector<cc_tight_box>& out, GenTotals& tot, Caps& caps, bool hoist) {
+                   std::vector<cc_tight_box>& out, GenTotals& tot, Caps& caps, bool hoist, int flags) {
     const size_t max_tasks_chunk = 1 << 16;
     size_t a = 0;
     size_t chunk = std::max<size_t>(1, max_tasks_chunk / (size_t)k);
@@ -699,7 +795,7 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
         cp.cell2 = (unsigned long long)(b - a) * k * s[0];
         std::vector<cc_tight_box> part;
         GenTotals t;
-        int st = run_chunk(h, parents, a, b, k, s, cp, part, t, (unsigned long long)a * k, hoist);
+        int st = run_chunk(h, parents, a, b, k, s, cp, part, t, (unsigned long long)a * k, hoist, flags);
         if (st == CC_ERR_QUEUE_OVERFLOW) {
             if (b - a > 1) {
                 chunk = std::max<size_t>(1, (b - a) / 2);
@@ -707,6 +803,7 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
                 caps.cell3 *= 2;
                 caps.cell4 *= 2;
                 caps.leaf *= 2;
+                caps.leaf2 *= 2;
                 caps.gaps *= 2;
                 caps.crit *= 2;
                 if (caps.cell4 > (1ULL << 31)) return ccrt::fail(h, CC_ERR_QUEUE_OVERFLOW, "tight proof: one box exceeds the queue limit");
@@ -730,6 +827,9 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
 extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, int flags,
                                  cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats) {
     const bool hoist = !(flags & CC_PROVE_PLAIN);
+    if ((flags & CC_PROVE_LEARNED) && !h->mlp)
+        return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_prove_ex: CC_PROVE_LEARNED needs a network (cc_mlp_init)");
+    if (flags & CC_PROVE_LOG_CELLS) h->cell_log.clear();
     if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
     if (grid->la_splits_init < 1 || grid->num_generations < 0 || grid->num_generations > CC_MAX_GENERATIONS)
         return ccrt::fail(h, CC_ERR_PARAM, "grid: bad lambda splits or generation count");
@@ -745,7 +845,7 @@ extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const c
     CC_CUDA(h, cudaSetDevice(h->device));
     auto t0 = std::chrono::steady_clock::now();
 
-    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 22, 1ULL << 20};
+    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 22, 1ULL << 20, 1ULL << 26};
     GenTotals tot;
     std::vector<cc_tight_box> cur{*root}, next;
     uint64_t gen_sizes[CC_MAX_GENERATIONS + 1] = {};
@@ -756,7 +856,7 @@ extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const c
         const int k = g == 0 ? grid->la_splits_init : grid->la_splits_gen[g - 1];
         const int* s = g == 0 ? grid->r_splits_init : grid->r_splits_gen;
         next.clear();
-        int st = run_generation(h, cur, k, s, next, tot, caps, hoist);
+        int st = run_generation(h, cur, k, s, next, tot, caps, hoist, flags);
         if (st) return st;
         cur.swap(next);
         gen_sizes[g] = cur.size();
@@ -787,6 +887,15 @@ extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const c
 extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, cc_tight_box** criticals,
                               size_t* n_crit, cc_prove_stats* stats) {
     return cc_tight_prove_ex(h, root, grid, 0, criticals, n_crit, stats);
+}
+
+extern "C" int cc_tight_cell_log(cc_handle* h, cc_tight_box* out, size_t cap, size_t* n, int* r4_splits) {
+    if (!h || !n || (cap && !out)) return CC_ERR_PARAM;
+    *n = h->cell_log.size();
+    if (r4_splits) *r4_splits = h->cell_log_splits;
+    const size_t k = std::min(cap, h->cell_log.size());
+    if (k) std::memcpy(out, h->cell_log.data(), k * sizeof(cc_tight_box));
+    return CC_OK;
 }
 
 extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_tight_summary_t* out) {

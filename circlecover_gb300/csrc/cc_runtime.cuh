@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/circlecover_gb300.h"
 
@@ -27,10 +28,16 @@ struct cc_handle {
         void* ptr = nullptr;
         size_t bytes = 0;
     };
-    Buf bufs[32];
+    Buf bufs[40];
     // pinned host staging for the host-memory entry points
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
+    // sample of r3 cells logged by the last tight proof (CC_PROVE_LOG_CELLS)
+    std::vector<cc_tight_box> cell_log;
+    int cell_log_splits = 0;
+    // learned-ordering network (cc_mlp_*), owned by the handle
+    void* mlp = nullptr;
+    void (*mlp_free)(cc_handle*) = nullptr;
     // per-stage events of the evaluation (cc_set_stage_timing)
     bool timing = false;
     cudaEvent_t stage_ev[CC_EVAL_STAGES + 1] = {};

@@ -11,6 +11,8 @@
 //   stage 2  (r1 cell, i2)     r2 cells:  r1_strategies, r3 range, r1_r2_strategies
 //   stage 3  (r2 cell, i3)     r3 cells:  r1_r2_strategies, r4 range, r1_r2_r3_strategies, R4
 //   stage 4a (r3 cell, i4)     leaves:    r1_r2_r3_strategies, R, two_by_two
+//                                         (prepared form: two_by_two in stage
+//                                         4a2 on the compacted leaves that need it)
 //   stage 4b (leaf queue)      leaves:    r1_r2_r3_strategies(box, R4), gaps precondition
 //   stage 4c (gaps queue)      leaves:    gaps bisection
 //
@@ -61,14 +63,15 @@ struct Cell3 {  // a surviving r2 cell
 struct Cell4 {  // a surviving r3 cell
     Iv r1, r2, r3, r4r, R4;
     int task;
-    int16_t i1, i2, i3, pad;
+    int16_t i1, i2, i3;
+    int16_t order;  // learned order: 1 = try the r1_r2_r3 leaf criterion before 2x2
     tight::R123Prep p3;
 };
 
 struct Leaf {  // a leaf that survived stage 4a
     uint32_t cell4;
     uint16_t i4;
-    uint16_t trapped;
+    uint16_t trapped;  // bit 0: a trap site was reached; bit 1: the leaf criterion already failed
 };
 
 struct GapsLeaf {  // a leaf that needs the gaps bisection
@@ -90,10 +93,19 @@ struct Counters {
     unsigned long long leaf_evals;
     unsigned long long digest;
     unsigned long long counts[4][8];
+    unsigned long long n_leaf2;  // leaves waiting for the 2x2 criterion (split stage 4a)
+};
+
+struct Leaf2 {  // a leaf that needs the 2x2 criterion
+    Iv r4;
+    uint32_t cell4;
+    uint16_t i4;
+    uint16_t pad;  // bits as Leaf::trapped
 };
 
 struct Caps {
     unsigned long long cell2, cell3, cell4, leaf, gaps, crit;
+    unsigned long long leaf2;  // leaves waiting for the 2x2 criterion (about half of all leaves)
 };
 
 CC_FN uint64_t mix64(uint64_t x) {
@@ -317,6 +329,7 @@ __global__ void __launch_bounds__(128) k_stage3(const Box* __restrict__ parents,
             cell.i1 = p.i1;
             cell.i2 = p.i2;
             cell.i3 = (int16_t)i3;
+            cell.order = 0;
             bool r12_ok = Hoist ? tight::r12_check(p.p2, cell.r3.hi)
                                 : tight::r1_r2_strategies(tk.la, tk.weight, p.r1, p.r2, cell.r3.hi);
             if (r12_ok) {
@@ -359,10 +372,13 @@ __device__ __forceinline__ Box leaf_box(const Cell4& p, Iv la, Iv r4) {
     return v;
 }
 
-// stage 4a: leaves, the cheap checks (tight_rectangle.cu:229-246)
-template <bool Hoist>
+// stage 4a: leaves, the cheap checks (tight_rectangle.cu:229-246).  Split
+// form: the leaves that reach the 2x2 criterion (about half of them; its six
+// bisections are the stage's main cost) are compacted into a queue for
+// stage 4a2 instead of being checked here next to lanes that have finished.
+template <bool Hoist, bool Split>
 __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks, const Cell4* __restrict__ in, int s4,
-                                                 Leaf* __restrict__ out, Caps caps, Counters* c,
+                                                 Leaf* __restrict__ out, Leaf2* __restrict__ out2, Caps caps, Counters* c,
                                                  unsigned long long task_base) {
     __shared__ BlockTrace bt;
     trace_init(bt);
@@ -375,7 +391,8 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
         int outcome = -1;
         uint32_t pidx = 0;
         int i4 = 0, task = 0, i1 = 0, i2 = 0, i3 = 0;
-        bool trapped = false;
+        bool trapped = false, leaf_tried = false;
+        Iv r4{0.0, 0.0};
         if (valid) {
             evals += 1;
             pidx = (uint32_t)(idx / s4);
@@ -387,7 +404,7 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
             i3 = p.i3;
             const Task tk = tasks[task];
             trap_clear();
-            Iv r4 = subinterval(p.r4r, i4, s4);
+            r4 = subinterval(p.r4r, i4, s4);
             bool r123_ok = Hoist ? tight::r123_check(p.p3, r4.hi)
                                  : tight::r1_r2_r3_strategies(tk.la, tk.weight, p.r1, p.r2, p.r3, r4.hi);
             if (r123_ok) {
@@ -398,21 +415,77 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
                 tighten_lb(R, 0.0);
                 if (empty(R)) {
                     outcome = CC_T_L4_REMPTY;
+                } else if (Split) {
+                    outcome = -3;  // on to stage 4a2
+                    if (p.order) {  // learned order: the cheap leaf criterion first
+                        const bool ok4 = tight::r1_r2_r3_strategies(v, p.R4);
+                        if (ok4 && trap_status() == TRAP_NONE) outcome = CC_T_L4_R123LEAF;
+                        else if (!ok4) leaf_tried = true;  // (a trap leaves it to the plain order)
+                    }
                 } else {
                     bool ok = tight::two_by_two_strategies(v, R);
                     trapped = trap_status() != TRAP_NONE;
                     outcome = (ok && !trapped) ? CC_T_L4_2X2 : -2;  // -2: on to stage 4b
                 }
             }
+            if (Split) trapped = trap_status() != TRAP_NONE;
         }
         __syncwarp();
         bool decided = valid && outcome >= 0;
         trace_note(bt, decided, decided ? trace_key(task_base + task, 3, i1, i2, i3, i4, outcome) : 0, decided ? outcome : 0);
-        unsigned long long slot = warp_append(&c->n_leaf, valid && outcome == -2, caps.leaf, &c->overflow);
-        if (slot != ~0ULL) out[slot] = Leaf{pidx, (uint16_t)i4, (uint16_t)(trapped ? 1 : 0)};
+        if (Split) {
+            unsigned long long slot = warp_append(&c->n_leaf2, valid && outcome == -3, caps.leaf2, &c->overflow);
+            if (slot != ~0ULL)
+                out2[slot] = Leaf2{r4, pidx, (uint16_t)i4, (uint16_t)((trapped ? 1 : 0) | (leaf_tried ? 2 : 0))};
+        } else {
+            unsigned long long slot = warp_append(&c->n_leaf, valid && outcome == -2, caps.leaf, &c->overflow);
+            if (slot != ~0ULL) out[slot] = Leaf{pidx, (uint16_t)i4, (uint16_t)(trapped ? 1 : 0)};
+        }
     }
     for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
     if ((threadIdx.x & 31) == 0 && evals) atomicAdd(&c->leaf_evals, evals);
+    trace_flush(bt, c, 3);
+}
+
+// stage 4a2 (split form): the 2x2 criterion on the compacted leaves
+// (tight_rectangle.cu:246); failures go on to stage 4b
+__global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
+                                                  const Leaf2* __restrict__ in, Leaf* __restrict__ out, Caps caps,
+                                                  Counters* c, unsigned long long task_base) {
+    __shared__ BlockTrace bt;
+    trace_init(bt);
+    const unsigned long long n_in = *(volatile unsigned long long*)&c->n_leaf2;
+    const unsigned long long total = n_in < caps.leaf2 ? n_in : caps.leaf2;
+    CC_WARP_LOOP(total) {
+        unsigned long long idx = base_ + (threadIdx.x & 31);
+        bool valid = idx < total;
+        int outcome = -1;
+        Leaf2 lf{Iv{0.0, 0.0}, 0, 0, 0};
+        int task = 0, i1 = 0, i2 = 0, i3 = 0;
+        bool trapped = false;
+        if (valid) {
+            lf = in[idx];
+            const Cell4& p = cells[lf.cell4];
+            task = p.task;
+            i1 = p.i1;
+            i2 = p.i2;
+            i3 = p.i3;
+            const Task tk = tasks[task];
+            trap_clear();
+            Box v = leaf_box(p, tk.la, lf.r4);
+            Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+            tighten_lb(R, 0.0);
+            bool ok = tight::two_by_two_strategies(v, R);
+            trapped = (lf.pad & 1) != 0 || trap_status() != TRAP_NONE;
+            outcome = (ok && !trapped) ? CC_T_L4_2X2 : -2;
+        }
+        __syncwarp();
+        bool decided = valid && outcome >= 0;
+        trace_note(bt, decided, decided ? trace_key(task_base + task, 3, i1, i2, i3, lf.i4, outcome) : 0,
+                   decided ? outcome : 0);
+        unsigned long long slot = warp_append(&c->n_leaf, valid && outcome == -2, caps.leaf, &c->overflow);
+        if (slot != ~0ULL) out[slot] = Leaf{lf.cell4, lf.i4, (uint16_t)((trapped ? 1 : 0) | (lf.pad & 2))};
+    }
     trace_flush(bt, c, 3);
 }
 
@@ -448,13 +521,13 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
             i3 = p.i3;
             const Task tk = tasks[task];
             trap_clear();
-            if (lf.trapped) trap(TRAP_BISECTION_CAP);
+            if (lf.trapped & 1) trap(TRAP_BISECTION_CAP);
             Iv r4 = subinterval(p.r4r, lf.i4, s4);
             v = leaf_box(p, tk.la, r4);
             Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
             tighten_lb(R, 0.0);
             tight::GapsStart g;
-            if (tight::r1_r2_r3_strategies(v, p.R4)) {
+            if (!(lf.trapped & 2) && tight::r1_r2_r3_strategies(v, p.R4)) {
                 outcome = CC_T_L4_R123LEAF;
             } else if (tight::gaps_enters(v.r[0].lo, v.r[1].lo, g)) {
                 need_gaps = true;

@@ -289,8 +289,26 @@ int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* 
  * of a criterion that do not depend on the child cell's bound once per parent
  * cell.  Both give identical criticals and traces. */
 #define CC_PROVE_PLAIN 1
+/* Learned leaf order (prepared form only): per r3 cell the network
+ * (cc_mlp_*) predicts whether the leaf criterion r1_r2_r3_strategies(box,
+ * R4) certifies the cell's leaves; where it does, that criterion is tried
+ * before the 2x2 criterion.  The criticals are the same as without it (a box
+ * is critical when no criterion certifies it, in any order; only a leaf that
+ * reaches a trap site in one order and is certified earlier in the other
+ * could differ); the trace then records the criterion that certified in the
+ * order used. */
+#define CC_PROVE_LEARNED 4
+/* Log a sample (1 in 64, at most 2^20) of the r3 cells the proof splits,
+ * as boxes with r4 = the cell's r4 range, for training records
+ * (cc_tight_cell_log). */
+#define CC_PROVE_LOG_CELLS 8
 int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, int flags,
                       cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats);
+
+/* The cells logged by the last cc_tight_prove_ex with CC_PROVE_LOG_CELLS:
+ * *n = how many (at most cap copied into out), *r4_splits = the r4 split
+ * count of their leaves (may be NULL). */
+int cc_tight_cell_log(cc_handle* h, cc_tight_box* out, size_t cap, size_t* n, int* r4_splits);
 
 /* Summary of a critical set vs the 2- and 3-disk worst cases
  * (kernel_compute_distance_from_theoretical_worst_cases). */
@@ -321,6 +339,37 @@ int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, cc_
 #define CC_SB_NO_FP32_PREFILTER 2
 int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, int options, cc_sb_box** criticals,
                    size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats);
+
+/* ---- learned strategy ordering (no reference counterpart) ------------------
+ * A 10 -> 64 -> 64 -> 7 perceptron per handle: 6 logits, "criterion k
+ * certifies the box" (CC_TV_* order), and 1 logit, "no criterion certifies
+ * it" (the box must be split).  Parameters, FP32, in this order: W1[10][64],
+ * b1[64], W2[64][64], b2[64], W3[64][7], b3[7].  Trained on the GPU by the
+ * library's own kernels (Adam on the mean summed binary cross-entropy);
+ * inference with BF16 weights and activations, FP32 accumulation, tensor
+ * cores.  All array arguments except the weights are DEVICE pointers. */
+#define CC_MLP_FEATURES 10
+#define CC_MLP_OUTPUTS 7
+#define CC_MLP_PARAMS 5319
+int cc_mlp_init(cc_handle* h, uint64_t seed);            /* He initialisation, Adam state cleared */
+int cc_mlp_set_weights(cc_handle* h, const float* w);    /* host array of CC_MLP_PARAMS */
+int cc_mlp_get_weights(cc_handle* h, float* w);          /* host array of CC_MLP_PARAMS */
+/* features of n tight boxes (SoA, 10 x n doubles) -> feat[n][10] */
+int cc_mlp_features(cc_handle* h, const double* soa, size_t n, float depth, float* feat);
+/* gradient of the mean loss over n <= 65536 samples (labels: bit k = target
+ * of output k) into grad (host, CC_MLP_PARAMS floats); *loss = the mean loss */
+int cc_mlp_gradients(cc_handle* h, const float* feat, const uint32_t* labels, size_t n, float* grad, float* loss);
+/* one Adam step (learning rate lr) on the mean loss over n <= 65536 samples */
+int cc_mlp_train_step(cc_handle* h, const float* feat, const uint32_t* labels, size_t n, float lr, float* loss);
+/* logits[n][8] (column 7 unused) */
+int cc_mlp_infer(cc_handle* h, const float* feat, size_t n, float* logits);
+/* First-success evaluation of n tight boxes (SoA on the device): the steps
+ * of the reference's nesting (r1, r1+r2, r1+r2+r3 criteria, R4/R empty,
+ * 2x2, r1+r2+r3 leaf, gaps) until one decides; with learned != 0 the
+ * network's most likely criterion runs first and the plain order follows.
+ * outcome[i] = deciding step (0..5 criterion, 6 R empty, 7 none: critical)
+ * | 0x80 if a trap site was reached; evals[i] (may be NULL) = steps run. */
+int cc_tight_first(cc_handle* h, const double* soa, size_t n, int learned, uint8_t* outcome, uint8_t* evals);
 
 /* Ask a running proof on this handle to stop (the reference's Ctrl-C
  * behaviour, interrupt.cpp:30-46).  cc_tight_prove stops after the current

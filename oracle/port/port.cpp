@@ -155,6 +155,45 @@ int ccport_tight_eval_passes(const cc_tight_box* boxes, size_t n, uint64_t* ops3
     return 0;
 }
 
+/* Operation counts of each tight criterion evaluated on its own at the leaf
+ * arguments (CC_TV_* order; counting build only): ops7[7*i + k], k = 6 the
+ * R4/R emptiness test.  For the cost side of strategy ordering. */
+int ccport_tight_criterion_ops(const cc_tight_box* boxes, size_t n, uint64_t* ops7) {
+    for (size_t i = 0; i < n; ++i) {
+        const cc_tight_box& in = boxes[i];
+        const Iv la = to_iv(in.la), r1 = to_iv(in.r[0]), r2 = to_iv(in.r[1]), r3 = to_iv(in.r[2]), r4 = to_iv(in.r[3]);
+        unsigned long long c = cc_port_op_count;
+        const Iv weight = ct::required_weight_for(la);
+        auto tick = [&](int k) {
+            ops7[7 * i + k] = cc_port_op_count - c;
+            c = cc_port_op_count;
+        };
+        c = cc_port_op_count;
+        ct::r1_strategies(la, weight, r1, r2.hi);
+        tick(0);
+        ct::r1_r2_strategies(la, weight, r1, r2, r3.hi);
+        tick(1);
+        ct::r1_r2_r3_strategies(la, weight, r1, r2, r3, r4.hi);
+        tick(2);
+        Iv R4 = weight - r1 - r2 - r3;
+        cc::tighten_lb(R4, 0.0);
+        ct::Box v{la, {r1, r2, r3, r4}};
+        cc::tighten_lb(v.r[2], v.r[3].lo);
+        cc::tighten_lb(v.r[1], v.r[2].lo);
+        cc::tighten_lb(v.r[0], v.r[1].lo);
+        Iv R = weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+        cc::tighten_lb(R, 0.0);
+        tick(6);
+        ct::two_by_two_strategies(v, R);
+        tick(3);
+        ct::r1_r2_r3_strategies(v, R4);
+        tick(4);
+        ct::r1_r2_large_r3_r4_gaps_strategy(v, R);
+        tick(5);
+    }
+    return 0;
+}
+
 int ccport_tight_prove(const cc_tight_box* root, const cc_tight_grid* grid, int threads, cc_tight_box** out, size_t* n_out,
                        cc_prove_stats* stats) {
     Driver::Box r{to_iv(root->la), {to_iv(root->r[0]), to_iv(root->r[1]), to_iv(root->r[2]), to_iv(root->r[3])}};
