@@ -190,6 +190,14 @@ def run_ours(args, ws, rank, local):
         torch.cuda.synchronize()
 
     barrier()  # inputs were copied on the default stream
+    tune = None
+    if not args.no_autotune:  # register budget and grid of each pass, on a 2^20-box sample
+        m = min(n, 1 << 20)
+        sample = torch.from_numpy(W.to_soa(boxes[:m])).to("cuda")
+        smask = torch.empty(m, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        tune = prover.autotune_eval(sample.data_ptr(), m, smask.data_ptr())
+        del sample, smask
     for _ in range(args.warmup):
         step()
     barrier()
@@ -258,7 +266,7 @@ def run_ours(args, ws, rank, local):
         "config": {"workload": "tight criteria microbench: 2^24 boxes per GPU, lambda~U[1,4], log-uniform widths "
                                "2^-20..2^-4, total weight critical*(1+eps), eps log-uniform 1e-6..1e-1",
                    "boxes_per_gpu": n, "l2_flush": "not needed: inputs (%.2f GB) exceed L2" % (n * 80 / 1e9),
-                   "layout": "SoA, 10 x n float64"},
+                   "layout": "SoA, 10 x n float64", "autotune": tune},
         "verified_vs_reference_masks": verified,
         "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved / 1e12, "peak": peak / 1e12,
                      "unit": "Top/s (FP64 ops)", "frac": achieved / peak, "traffic": ncu_traffic(dom),
@@ -277,6 +285,7 @@ def run_ours(args, ws, rank, local):
         line["proof"] = proof_comparison(prover)
         line["sb_proof"] = sb_proof_run(prover)
         line["sb_forms"] = sb_forms(prover)
+        line["near_critical"] = near_critical_run(prover)
     if ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
     prover.close()
@@ -323,6 +332,44 @@ def proof_comparison(prover):
                              "error_rate_per_output": rep["error_rate_per_output"]},
                 "leaf_outcomes": {k: res[k][2]["counts"][3][:7] for k in res}})
     return out
+
+
+def near_critical_run(prover, n=1 << 22):
+    """Near-critical stress: 2^22 boxes, 90 % with total weight within 1e-4
+    (relative) of the critical weight, 10 % drawn as the microbench.  Verdict
+    masks of all six criteria (boxes/s, device-resident, CUDA events on the
+    launching stream), and the first-success evaluation in the plain order
+    and with the trained network's choice first (same decisions)."""
+    import torch
+    from circlecover_gb300 import learn
+    from circlecover_gb300 import workloads as W
+    boxes = W.tight_near_critical(n, seed=5)
+    soa = torch.from_numpy(W.to_soa(boxes)).cuda()
+    masks = torch.empty(n, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    for _ in range(3):
+        prover.tight_eval_device(soa.data_ptr(), n, masks.data_ptr(), stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    steps = 5
+    for _ in range(steps):
+        prover.tight_eval_device(soa.data_ptr(), n, masks.data_ptr(), stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    m = masks.cpu().numpy().view(np.uint32)
+    prover.mlp_init(5)
+    train_rec = learn.Records(prover, W.tight_near_critical(1 << 20, seed=77))
+    learn.train(prover, train_rec, epochs=4, batch=8192)
+    rec = learn.Records(prover, boxes)
+    cmp = learn.compare_orders(prover, rec)
+    cmp.pop("outcomes_plain")
+    cmp.pop("outcomes_learned")
+    return {"workload": "near-critical stress: 2^22 boxes, 90% within 1e-4 of the critical weight",
+            "masks_boxes_per_s": n / (ms * 1e-3), "ms": ms,
+            "gaps_certified_share": float(((m >> 5) & 1).mean()),
+            "critical_share": float(((m & 0x7F) == 0).mean()), "first_success": cmp}
 
 
 SB_SLICE = dict(la=(1.0, 1.0 + 1.5 * 2 / 256), grid=(2, (32, 32, 64, 64, 64, 64)))
@@ -398,6 +445,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-proof", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="tight_eval", choices=["tight_eval", "sb_proof"])
     args = ap.parse_args()
     ws, rank, local = dist_env()

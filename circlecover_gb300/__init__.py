@@ -75,6 +75,11 @@ class CcProveStats(ctypes.Structure):
     ]
 
 
+class CcTuneResult(ctypes.Structure):
+    _fields_ = [("min_blocks", ctypes.c_int * 3), ("blocks_per_sm", ctypes.c_int * 3), ("ms", ctypes.c_float * 3),
+                ("ms_default", ctypes.c_float * 3)]
+
+
 class CcSbGrid(ctypes.Structure):
     _fields_ = [
         ("la_splits_init", ctypes.c_int),
@@ -166,7 +171,7 @@ EXPORTS = [
     "cc_last_launch_count", "cc_tight_prove", "cc_tight_prove_ex", "cc_tight_summary", "cc_interrupt", "cc_free",
     "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove", "cc_sb_prove_ex",
     "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
-    "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log",
+    "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
 ]
 
 MLP_PARAMS = 5319
@@ -212,6 +217,7 @@ def load_library(path=LIB_PATH):
     lib.cc_mlp_infer.argtypes = [vp, vp, sz, vp]
     lib.cc_tight_first.argtypes = [vp, vp, sz, ctypes.c_int, vp, vp]
     lib.cc_tight_cell_log.argtypes = [vp, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_int)]
+    lib.cc_autotune_eval.argtypes = [vp, vp, sz, vp, ctypes.POINTER(CcTuneResult)]
     lib.cc_sb_prove.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.POINTER(vp), ctypes.POINTER(sz),
                                 ctypes.POINTER(vp), ctypes.POINTER(CcSbProveStats)]
     lib.cc_sb_prove_ex.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.c_int, ctypes.POINTER(vp),
@@ -278,6 +284,16 @@ class Prover:
         self._check(self.lib.cc_tight_eval_device(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
                                                   ctypes.c_void_p(stream_ptr) if stream_ptr else None),
                     "cc_tight_eval_device")
+
+    def autotune_eval(self, soa_ptr, n, masks_ptr):
+        """Tune the evaluation passes on a device sample (cc_autotune_eval);
+        the choice stays in this handle.  Returns the report as a dict."""
+        r = CcTuneResult()
+        self._check(self.lib.cc_autotune_eval(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
+                                              ctypes.byref(r)), "cc_autotune_eval")
+        names = ("k_eval_main", "k_eval_cover", "k_eval_gaps")
+        return {names[i]: {"min_blocks": r.min_blocks[i], "blocks_per_sm": r.blocks_per_sm[i],
+                           "ms": float(r.ms[i]), "ms_default": float(r.ms_default[i])} for i in range(3)}
 
     def set_stage_timing(self, enable=True):
         """Record a CUDA event around each evaluation kernel (see stage_times)."""

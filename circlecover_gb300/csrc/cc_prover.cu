@@ -80,9 +80,12 @@ struct EvalQueues {
     unsigned long long cap;
 };
 
-template <Layout L>
-__global__ void __launch_bounds__(128) k_eval_main(const double* __restrict__ in, size_t n, uint32_t* __restrict__ masks,
-                                                   EvalQueues q) {
+// MinB: the register budget (__launch_bounds__ minimum resident blocks per
+// SM: 1 = up to 255 registers per thread, 4 = 128, 8 = 64), chosen per
+// kernel by the autotuner (cc_autotune_eval) together with the grid size.
+template <Layout L, int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_main(const double* __restrict__ in, size_t n,
+                                                         uint32_t* __restrict__ masks, EvalQueues q) {
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n;
          base += stride) {
@@ -109,7 +112,8 @@ __global__ void __launch_bounds__(128) k_eval_main(const double* __restrict__ in
     }
 }
 
-__global__ void __launch_bounds__(128) k_eval_cover(EvalQueues q, uint32_t* __restrict__ masks) {
+template <int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_cover(EvalQueues q, uint32_t* __restrict__ masks) {
     const unsigned long long n = q.counts[0] < q.cap ? q.counts[0] : q.cap;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -118,7 +122,8 @@ __global__ void __launch_bounds__(128) k_eval_cover(EvalQueues q, uint32_t* __re
     }
 }
 
-__global__ void __launch_bounds__(128) k_eval_gaps(EvalQueues q, uint32_t* __restrict__ masks) {
+template <int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_gaps(EvalQueues q, uint32_t* __restrict__ masks) {
     const unsigned long long n = q.counts[1] < q.cap ? q.counts[1] : q.cap;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -140,6 +145,25 @@ static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
     return CC_OK;
 }
 
+// launches of the three passes with a tuned register budget and grid
+// (the AoS main pass, used by the host-memory entry point, keeps MinB 1)
+template <Layout L>
+static void launch_main(int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks, EvalQueues q) {
+    if (L == Layout::SoA && minb == 4) k_eval_main<L, 4><<<g, 128, 0, s>>>(in, n, masks, q);
+    else if (L == Layout::SoA && minb == 8) k_eval_main<L, 8><<<g, 128, 0, s>>>(in, n, masks, q);
+    else k_eval_main<L, 1><<<g, 128, 0, s>>>(in, n, masks, q);
+}
+static void launch_cover(int minb, int g, cudaStream_t s, EvalQueues q, uint32_t* masks) {
+    if (minb == 4) k_eval_cover<4><<<g, 128, 0, s>>>(q, masks);
+    else if (minb == 8) k_eval_cover<8><<<g, 128, 0, s>>>(q, masks);
+    else k_eval_cover<1><<<g, 128, 0, s>>>(q, masks);
+}
+static void launch_gaps(int minb, int g, cudaStream_t s, EvalQueues q, uint32_t* masks) {
+    if (minb == 4) k_eval_gaps<4><<<g, 128, 0, s>>>(q, masks);
+    else if (minb == 8) k_eval_gaps<8><<<g, 128, 0, s>>>(q, masks);
+    else k_eval_gaps<1><<<g, 128, 0, s>>>(q, masks);
+}
+
 // the three passes on one batch already on the device
 template <Layout L>
 static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks, cudaStream_t s) {
@@ -147,16 +171,15 @@ static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks,
     int st = eval_queues(h, n, &q);
     if (st) return st;
     CC_CUDA(h, cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s));
-    const int g = h->sm_count * 8;
     h->stages_recorded = 0;
     if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[0], s));
-    k_eval_main<L><<<g, 128, 0, s>>>(in, n, masks, q);
+    launch_main<L>(h->tune_minb[0], h->sm_count * h->tune_grid[0], s, in, n, masks, q);
     CC_LAUNCHED(h);
     if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[1], s));
-    k_eval_cover<<<g, 128, 0, s>>>(q, masks);
+    launch_cover(h->tune_minb[1], h->sm_count * h->tune_grid[1], s, q, masks);
     CC_LAUNCHED(h);
     if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[2], s));
-    k_eval_gaps<<<g, 128, 0, s>>>(q, masks);
+    launch_gaps(h->tune_minb[2], h->sm_count * h->tune_grid[2], s, q, masks);
     CC_LAUNCHED(h);
     if (h->timing) {
         CC_CUDA(h, cudaEventRecord(h->stage_ev[3], s));
@@ -330,6 +353,69 @@ int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* ma
     return eval_batch<Layout::SoA>(h, soa, n, masks, s);
 }
 
+// ---- autotuner ------------------------------------------------------------------
+// For each of the three evaluation passes, every register budget (MinB 1, 4,
+// 8) and grid size (2, 4, 8, 16 blocks of 128 per SM) is timed with CUDA
+// events on the caller's sample batch (the main pass first; the bisection
+// passes then rerun on the queues it filled: they only OR bits into the
+// masks, so reruns change nothing); the fastest setting of each pass is kept
+// in the handle for later cc_tight_eval_device / cc_tight_eval calls.
+extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint32_t* masks, cc_tune_result* out) {
+    if (!h || !soa || !masks || !n) return CC_ERR_PARAM;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    EvalQueues q;
+    int st = eval_queues(h, n, &q);
+    if (st) return st;
+    cudaStream_t s = h->stream;
+    cudaEvent_t e0, e1;
+    CC_CUDA(h, cudaEventCreate(&e0));
+    CC_CUDA(h, cudaEventCreate(&e1));
+    const int minbs[3] = {1, 4, 8}, grids[4] = {2, 4, 8, 16};
+    cc_tune_result r{};
+    auto time_stage = [&](int stage, int minb, int grid, float* ms) -> int {
+        const int g = h->sm_count * grid;
+        float best = 1e30f;
+        for (int rep = 0; rep < 2; ++rep) {
+            if (stage == 0) CC_CUDA(h, cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s));
+            CC_CUDA(h, cudaEventRecord(e0, s));
+            if (stage == 0) launch_main<Layout::SoA>(minb, g, s, soa, n, masks, q);
+            else if (stage == 1) launch_cover(minb, g, s, q, masks);
+            else launch_gaps(minb, g, s, q, masks);
+            CC_LAUNCHED(h);
+            CC_CUDA(h, cudaEventRecord(e1, s));
+            CC_CUDA(h, cudaEventSynchronize(e1));
+            float t;
+            CC_CUDA(h, cudaEventElapsedTime(&t, e0, e1));
+            best = t < best ? t : best;
+        }
+        *ms = best;
+        return CC_OK;
+    };
+    for (int stage = 0; stage < 3; ++stage) {
+        float best = 1e30f;
+        int bm = 1, bg = 8;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 4; ++b) {
+                float t;
+                if ((st = time_stage(stage, minbs[a], grids[b], &t))) return st;
+                if (minbs[a] == 1 && grids[b] == 8) r.ms_default[stage] = t;
+                if (t < best) best = t, bm = minbs[a], bg = grids[b];
+            }
+        // leave the queues filled by the chosen main pass for the later stages
+        float rerun;
+        if (stage == 0 && (st = time_stage(0, bm, bg, &rerun))) return st;
+        h->tune_minb[stage] = bm;
+        h->tune_grid[stage] = bg;
+        r.min_blocks[stage] = bm;
+        r.blocks_per_sm[stage] = bg;
+        r.ms[stage] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (out) *out = r;
+    return CC_OK;
+}
+
 // ---- allocation-free evaluation ---------------------------------------------
 // For callers that must not allocate device memory once they are running:
 // code that executes inside a host framework owning every device allocation
@@ -402,9 +488,9 @@ extern "C" int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t
         return CC_ERR_CUDA;
     }
     const int g = g_static_sms[dev] * 8;
-    k_eval_main<Layout::SoA><<<g, 128, 0, s>>>(soa, n, masks, q);
-    k_eval_cover<<<g, 128, 0, s>>>(q, masks);
-    k_eval_gaps<<<g, 128, 0, s>>>(q, masks);
+    k_eval_main<Layout::SoA, 1><<<g, 128, 0, s>>>(soa, n, masks, q);
+    k_eval_cover<1><<<g, 128, 0, s>>>(q, masks);
+    k_eval_gaps<1><<<g, 128, 0, s>>>(q, masks);
     if (cudaGetLastError() != cudaSuccess) return CC_ERR_CUDA;
     return CC_OK;
 }

@@ -32,6 +32,9 @@ struct cc_handle {
     // pinned host staging for the host-memory entry points
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
+    // evaluation passes' register budget and grid (blocks per SM), set by cc_autotune_eval
+    int tune_minb[3] = {1, 1, 1};
+    int tune_grid[3] = {8, 8, 8};
     // sample of r3 cells logged by the last tight proof (CC_PROVE_LOG_CELLS)
     std::vector<cc_tight_box> cell_log;
     int cell_log_splits = 0;

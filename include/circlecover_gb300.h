@@ -265,6 +265,21 @@ int cc_sb_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* masks
 /* Number of kernels the last call on this handle launched. */
 uint64_t cc_last_launch_count(cc_handle* h);
 
+/* Autotuner (no reference counterpart).  Times each of the three
+ * evaluation passes of cc_tight_eval_device with every register budget
+ * (minimum resident blocks 1, 4, 8: at most 255, 128, 64 registers per
+ * thread) and grid size (2, 4, 8, 16 blocks of 128 threads per SM) on the
+ * caller's sample (device SoA boxes and a masks array), and keeps the
+ * fastest per pass in the handle for later evaluation calls.  The defaults
+ * are 1 and 8. */
+typedef struct cc_tune_result {
+    int min_blocks[3];     /* chosen register budget of main, strip-width, gap-width pass */
+    int blocks_per_sm[3];  /* chosen grid */
+    float ms[3];           /* time of each pass with the chosen setting */
+    float ms_default[3];   /* time with the defaults */
+} cc_tune_result;
+int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint32_t* masks, cc_tune_result* out);
+
 /* Per-stage device timing (no reference counterpart; a measurement aid).
  * While enabled, cc_tight_eval_device records a CUDA event around each of
  * its three kernels on the stream it launches on:

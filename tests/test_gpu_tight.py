@@ -146,3 +146,18 @@ def test_prove_empty_root(prover):
     crit, st = prover.tight_find_critical_intervals(root, cg.make_grid(2, (8, 8, 8, 8), (1,)))
     assert len(crit) == 0
     assert st["leaf_evals"] == 0
+
+
+def test_autotuned_passes_give_the_same_masks(prover, port):
+    import torch
+    boxes = W.tight_microbench(1 << 16, seed=44)
+    soa = torch.from_numpy(W.to_soa(boxes)).cuda()
+    masks = torch.zeros(len(boxes), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    rep = prover.autotune_eval(soa.data_ptr(), len(boxes), masks.data_ptr())
+    assert set(rep) == {"k_eval_main", "k_eval_cover", "k_eval_gaps"}
+    for r in rep.values():
+        assert r["min_blocks"] in (1, 4, 8) and r["blocks_per_sm"] in (2, 4, 8, 16)
+        assert r["ms"] <= r["ms_default"] * 1.0001
+    got = prover.tight_eval(boxes)  # runs with the tuned settings
+    assert np.array_equal(got, port.tight_eval(boxes, threads=16))
