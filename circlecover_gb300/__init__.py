@@ -172,6 +172,7 @@ EXPORTS = [
     "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove", "cc_sb_prove_ex",
     "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
+    "cc_tight_generation",
 ]
 
 MLP_PARAMS = 5319
@@ -218,6 +219,8 @@ def load_library(path=LIB_PATH):
     lib.cc_tight_first.argtypes = [vp, vp, sz, ctypes.c_int, vp, vp]
     lib.cc_tight_cell_log.argtypes = [vp, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_int)]
     lib.cc_autotune_eval.argtypes = [vp, vp, sz, vp, ctypes.POINTER(CcTuneResult)]
+    lib.cc_tight_generation.argtypes = [vp, vp, sz, ctypes.c_int, vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                                        ctypes.POINTER(vp), ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
     lib.cc_sb_prove.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.POINTER(vp), ctypes.POINTER(sz),
                                 ctypes.POINTER(vp), ctypes.POINTER(CcSbProveStats)]
     lib.cc_sb_prove_ex.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.c_int, ctypes.POINTER(vp),
@@ -319,6 +322,23 @@ class Prover:
         self._check(self.lib.cc_sb_eval_device(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
                                                ctypes.c_void_p(stream_ptr) if stream_ptr else None),
                     "cc_sb_eval_device")
+
+    def tight_generation(self, parents, la_splits, r_splits, lo=0, hi=(1 << 64) - 1, learned=False):
+        """One generation of the tight proof over the tasks [lo, hi)
+        (cc_tight_generation): (criticals in task order, stats)."""
+        parents = np.ascontiguousarray(parents, dtype=TIGHT_BOX)
+        rs = (ctypes.c_int * 4)(*r_splits)
+        out = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcProveStats()
+        self._check(self.lib.cc_tight_generation(self.h, parents.ctypes.data if len(parents) else None, len(parents),
+                                                 la_splits, rs, lo, hi, 4 if learned else 0, ctypes.byref(out),
+                                                 ctypes.byref(n), ctypes.byref(st)), "cc_tight_generation")
+        arr = np.zeros(n.value, dtype=TIGHT_BOX)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)
+        self.lib.cc_free(out)
+        return arr, stats_to_dict(st)
 
     def tight_cell_log(self):
         """(cells, r4_splits) logged by the last proof run with log_cells=True."""

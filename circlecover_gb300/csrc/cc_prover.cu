@@ -173,7 +173,9 @@ static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks,
     CC_CUDA(h, cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s));
     h->stages_recorded = 0;
     if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[0], s));
-    launch_main<L>(h->tune_minb[0], h->sm_count * h->tune_grid[0], s, in, n, masks, q);
+    // the tuned setting applies to the device (SoA) batches it was tuned on
+    launch_main<L>(L == Layout::SoA ? h->tune_minb[0] : 1, h->sm_count * (L == Layout::SoA ? h->tune_grid[0] : 8), s,
+                   in, n, masks, q);
     CC_LAUNCHED(h);
     if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[1], s));
     launch_cover(h->tune_minb[1], h->sm_count * h->tune_grid[1], s, q, masks);
@@ -737,7 +739,8 @@ enum { S_CELL_FEAT = 32, S_CELL_LOGITS, S_CELL_LOG };
 // One chunk of parents [a, b) of a generation; returns CC_QUEUE_OVERFLOW
 // (without side effects on `out`/`tot`) when a device queue ran full.
 int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, size_t b, int k, const int s[4], Caps caps,
-              std::vector<cc_tight_box>& out, GenTotals& tot, unsigned long long task_base, bool hoist, int flags) {
+              std::vector<cc_tight_box>& out, GenTotals& tot, unsigned long long task_base, bool hoist, int flags,
+              unsigned long long task_lo, unsigned long long task_hi) {
     const bool learned = hoist && (flags & CC_PROVE_LEARNED);
     const bool log_cells = hoist && (flags & CC_PROVE_LOG_CELLS);
     const size_t np = b - a;
@@ -759,7 +762,8 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
     CC_CUDA(h, cudaMemcpyAsync(d_par, parents.data() + a, np * sizeof(cc_tight_box), cudaMemcpyHostToDevice, sm));
     CC_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(Counters), sm));
     const int g = stage_grid(h);
-    k_tasks<<<(unsigned)((ntasks + 127) / 128), 128, 0, sm>>>((const Box*)d_par, (int)np, k, (Task*)d_tasks);
+    k_tasks<<<(unsigned)((ntasks + 127) / 128), 128, 0, sm>>>((const Box*)d_par, (int)np, k, (Task*)d_tasks, task_base,
+                                                              task_lo, task_hi);
     CC_LAUNCHED(h);
     if (hoist) {
         k_stage1<true><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (int)ntasks, s[0], (Cell2*)d_c2, caps, cnt,
@@ -871,17 +875,21 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
 
 // all tasks of one generation, in parent chunks that fit the device queues
 int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k, const int s[4],
-                   std::vector<cc_tight_box>& out, GenTotals& tot, Caps& caps, bool hoist, int flags) {
+                   std::vector<cc_tight_box>& out, GenTotals& tot, Caps& caps, bool hoist, int flags,
+                   unsigned long long task_lo = 0, unsigned long long task_hi = ~0ULL) {
     const size_t max_tasks_chunk = 1 << 16;
-    size_t a = 0;
+    // parents whose tasks meet [task_lo, task_hi)
+    size_t a = (size_t)std::min<unsigned long long>(task_lo / (unsigned long long)k, parents.size());
+    const size_t a_end = (size_t)std::min<unsigned long long>(
+        task_hi == ~0ULL ? parents.size() : (task_hi + (unsigned long long)k - 1) / (unsigned long long)k, parents.size());
     size_t chunk = std::max<size_t>(1, max_tasks_chunk / (size_t)k);
-    while (a < parents.size()) {
-        size_t b = std::min(parents.size(), a + chunk);
+    while (a < a_end) {
+        size_t b = std::min(a_end, a + chunk);
         Caps cp = caps;
         cp.cell2 = (unsigned long long)(b - a) * k * s[0];
         std::vector<cc_tight_box> part;
         GenTotals t;
-        int st = run_chunk(h, parents, a, b, k, s, cp, part, t, (unsigned long long)a * k, hoist, flags);
+        int st = run_chunk(h, parents, a, b, k, s, cp, part, t, (unsigned long long)a * k, hoist, flags, task_lo, task_hi);
         if (st == CC_ERR_QUEUE_OVERFLOW) {
             if (b - a > 1) {
                 chunk = std::max<size_t>(1, (b - a) / 2);
@@ -973,6 +981,42 @@ extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const c
 extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, cc_tight_box** criticals,
                               size_t* n_crit, cc_prove_stats* stats) {
     return cc_tight_prove_ex(h, root, grid, 0, criticals, n_crit, stats);
+}
+
+extern "C" int cc_tight_generation(cc_handle* h, const cc_tight_box* parents, size_t n_parents, int la_splits,
+                                   const int r_splits[4], uint64_t task_lo, uint64_t task_hi, int flags,
+                                   cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats) {
+    if (!h || (n_parents && !parents) || !r_splits || !criticals || !n_crit || task_lo > task_hi) return CC_ERR_PARAM;
+    if (!valid_split(la_splits)) return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_generation: bad lambda splits");
+    for (int k = 0; k < 4; ++k)
+        if (!valid_split(r_splits[k])) return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_generation: splits in [1, 2047]");
+    if ((flags & CC_PROVE_LEARNED) && !h->mlp)
+        return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_generation: CC_PROVE_LEARNED needs a network (cc_mlp_init)");
+    *criticals = nullptr;
+    *n_crit = 0;
+    h->launches = 0;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    auto t0 = std::chrono::steady_clock::now();
+    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 22, 1ULL << 20, 1ULL << 26};
+    GenTotals tot;
+    std::vector<cc_tight_box> in(parents, parents + n_parents), out;
+    int st = run_generation(h, in, la_splits, r_splits, out, tot, caps, !(flags & CC_PROVE_PLAIN), flags, task_lo, task_hi);
+    if (st) return st;
+    *n_crit = out.size();
+    *criticals = (cc_tight_box*)std::malloc(sizeof(cc_tight_box) * (out.size() + 1));
+    if (!*criticals) return ccrt::fail(h, CC_ERR_OOM, "malloc criticals");
+    if (!out.empty()) std::memcpy(*criticals, out.data(), sizeof(cc_tight_box) * out.size());
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        std::memcpy(stats->counts, tot.counts, sizeof(stats->counts));
+        stats->digest = tot.digest;
+        stats->leaf_evals = tot.leaf_evals;
+        stats->trapped_leaves = tot.trapped;
+        stats->gen_sizes[0] = out.size();
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        stats->kernel_launches = h->launches;
+    }
+    return CC_OK;
 }
 
 extern "C" int cc_tight_cell_log(cc_handle* h, cc_tight_box* out, size_t cap, size_t* n, int* r4_splits) {

@@ -183,7 +183,10 @@ __device__ __forceinline__ unsigned long long warp_append(unsigned long long* co
          base_ < (total); base_ += (unsigned long long)gridDim.x * blockDim.x)
 
 // stage 0: one thread per task
-__global__ void k_tasks(const Box* __restrict__ parents, int n_parents, int la_splits, Task* __restrict__ tasks) {
+// tasks whose generation-wide index (task_base + t) lies outside [lo, hi)
+// belong to another shard: they are marked dead and contribute nothing
+__global__ void k_tasks(const Box* __restrict__ parents, int n_parents, int la_splits, Task* __restrict__ tasks,
+                        unsigned long long task_base, unsigned long long lo, unsigned long long hi) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_parents * la_splits) return;
     trap_clear();
@@ -194,7 +197,8 @@ __global__ void k_tasks(const Box* __restrict__ parents, int n_parents, int la_s
     tk.weight = tight::required_weight_for(tk.la);
     tk.r1r = intersect(tight::r1_range(tk.la), parents[p].r[0]);
     tk.parent = p;
-    tk.live = !empty(tk.r1r);
+    const unsigned long long g = task_base + (unsigned long long)t;
+    tk.live = !empty(tk.r1r) && g >= lo && g < hi;
     tasks[t] = tk;
 }
 

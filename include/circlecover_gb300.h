@@ -320,6 +320,18 @@ int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* 
 int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, int flags,
                       cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats);
 
+/* One generation of the tight proof restricted to the tasks [task_lo,
+ * task_hi) of that generation (task = parent index * la_splits + lambda
+ * piece; tasks outside the range contribute nothing).  Criticals are
+ * returned in task order, merged per task as the reference does; the
+ * concatenation over consecutive ranges equals the whole generation's
+ * output, and the stats (counts, digest, leaves) add up.  This is the unit a
+ * process group shards (one range per rank, the criticals all-gathered in
+ * rank order as the next generation's parents).  flags as cc_tight_prove_ex. */
+int cc_tight_generation(cc_handle* h, const cc_tight_box* parents, size_t n_parents, int la_splits,
+                        const int r_splits[4], uint64_t task_lo, uint64_t task_hi, int flags,
+                        cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats);
+
 /* The cells logged by the last cc_tight_prove_ex with CC_PROVE_LOG_CELLS:
  * *n = how many (at most cap copied into out), *r4_splits = the r4 split
  * count of their leaves (may be NULL). */

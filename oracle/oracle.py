@@ -187,6 +187,25 @@ class Port(_Lib):
         self.lib.ccport_subinterval.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_double)]
 
+    def tight_generation(self, parents, la_splits, r_splits, lo=0, hi=(1 << 64) - 1, threads=4):
+        """One generation over the tasks [lo, hi) on the CPU (sharding tests)."""
+        parents = np.ascontiguousarray(parents, dtype=TIGHT_BOX)
+        rs = (ctypes.c_int * 4)(*r_splits)
+        out = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcProveStats()
+        f = self.lib.ccport_tight_generation
+        f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                      ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t),
+                      ctypes.POINTER(CcProveStats)]
+        f(parents.ctypes.data if len(parents) else None, len(parents), la_splits, rs, lo, hi, threads,
+          ctypes.byref(out), ctypes.byref(n), ctypes.byref(st))
+        arr = np.zeros(n.value, dtype=TIGHT_BOX)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)
+        self.lib.ccport_free(out)
+        return arr, stats_to_dict(st)
+
     def tight_eval_passes(self, boxes):
         """Per-box operation counts of the three evaluation passes (main,
         strip-width bisection, gap-width bisection); counting build only."""

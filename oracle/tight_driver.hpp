@@ -170,7 +170,8 @@ struct TightDriver {
 
     /* one generation: every (box, lambda piece) is a task; results are appended in task order */
     static void generation(const std::vector<Box>& in, int la_splits, const int splits[4], int threads,
-                           std::vector<Box>& out, Trace& trace, uint64_t& trapped) {
+                           std::vector<Box>& out, Trace& trace, uint64_t& trapped, uint64_t lo = 0,
+                           uint64_t hi = ~0ULL) {
         size_t ntasks = in.size() * (size_t)la_splits;
         std::vector<std::vector<Box>> per_task(ntasks);
         std::vector<Trace> traces(threads > 0 ? threads : 1);
@@ -183,6 +184,7 @@ struct TightDriver {
             for (;;) {
                 size_t task = next.fetch_add(1);
                 if (task >= ntasks) break;
+                if (task < lo || task >= hi) continue;  // another shard's task
                 const Box& s = in[task / la_splits];
                 int k = (int)(task % la_splits);
                 Box sub{C::subinterval(s.la, k, la_splits), {s.r[0], s.r[1], s.r[2], s.r[3]}};
