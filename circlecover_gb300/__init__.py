@@ -75,6 +75,23 @@ class CcProveStats(ctypes.Structure):
     ]
 
 
+class CcTightSummary(ctypes.Structure):
+    """cc_tight_summary_t (Max_distances, tight_rectangle.cu:322-341)."""
+    _fields_ = [
+        ("have_range_2d", ctypes.c_int32), ("have_range_3d", ctypes.c_int32),
+        ("la_range_2d", CcIv), ("la_range_3d", CcIv),
+        ("dist_r1_2d", CcIv), ("dist_r1_2d_criticals", CcTightBox * 2),
+        ("dist_r2_2d", CcIv), ("dist_r2_2d_criticals", CcTightBox * 2),
+        ("lb_h1_2d", ctypes.c_double), ("ub_la_by_S1", ctypes.c_double), ("ub_R3_2d", ctypes.c_double),
+        ("dist_r1_3d", CcIv), ("dist_r1_3d_criticals", CcTightBox * 2),
+        ("dist_r2_3d", CcIv), ("dist_r2_3d_criticals", CcTightBox * 2),
+        ("dist_r3_3d", CcIv), ("dist_r3_3d_criticals", CcTightBox * 2),
+        ("ub_R4_3d", ctypes.c_double),
+        ("S1", CcIv), ("h2", CcIv), ("S3", CcIv),
+        ("pocket_width_3d", ctypes.c_double),
+    ]
+
+
 class CcTuneResult(ctypes.Structure):
     _fields_ = [("min_blocks", ctypes.c_int * 3), ("blocks_per_sm", ctypes.c_int * 3), ("ms", ctypes.c_float * 3),
                 ("ms_default", ctypes.c_float * 3)]
@@ -205,7 +222,7 @@ def load_library(path=LIB_PATH):
                                    ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
     lib.cc_tight_prove_ex.argtypes = [vp, ctypes.POINTER(CcTightBox), ctypes.POINTER(CcTightGrid), ctypes.c_int,
                                       ctypes.POINTER(vp), ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
-    lib.cc_tight_summary.argtypes = [vp, vp, sz, vp]
+    lib.cc_tight_summary.argtypes = [vp, vp, sz, ctypes.POINTER(CcTightSummary)]
     lib.cc_sb_eval.argtypes = [vp, vp, sz, vp]
     lib.cc_sb_eval_device.argtypes = [vp, vp, sz, vp, vp]
     lib.cc_interrupt.argtypes = [vp]
@@ -444,6 +461,15 @@ class Prover:
         self._check(self.lib.cc_tight_first(self.h, ctypes.c_void_p(soa_ptr), n, 1 if learned else 0,
                                             ctypes.c_void_p(outcome_ptr),
                                             ctypes.c_void_p(evals_ptr) if evals_ptr else None), "cc_tight_first")
+
+    def tight_summary(self, criticals):
+        """Max_distances of a critical set (cc_tight_summary), as the raw
+        cc_tight_summary_t structure."""
+        crit = np.ascontiguousarray(criticals, dtype=TIGHT_BOX)
+        out = CcTightSummary()
+        self._check(self.lib.cc_tight_summary(self.h, crit.ctypes.data if len(crit) else None, len(crit),
+                                              ctypes.byref(out)), "cc_tight_summary")
+        return out
 
     def interrupt(self):
         self.lib.cc_interrupt(self.h)

@@ -1037,7 +1037,16 @@ extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, siz
     if ((st = ccrt::ensure(h, 0, (n + 1) * sizeof(cc_tight_box), &d_in))) return st;
     if ((st = ccrt::ensure(h, 1, sizeof(cc_tight_summary_t), &d_out))) return st;
     if (n) CC_CUDA(h, cudaMemcpyAsync(d_in, criticals, n * sizeof(cc_tight_box), cudaMemcpyHostToDevice, h->stream));
-    cc::summary::k_summary<<<1, 1, 0, h->stream>>>((const cc::tight::Box*)d_in, n, (cc_tight_summary_t*)d_out);
+    void* d_items;
+    if ((st = ccrt::ensure(h, 2, (n + 1) * sizeof(cc::summary::Item), &d_items))) return st;
+    if (n) {
+        const int g = (int)std::min<size_t>((n + 127) / 128, (size_t)h->sm_count * 8);
+        cc::summary::k_summary_items<<<g, 128, 0, h->stream>>>((const cc::tight::Box*)d_in, n,
+                                                              (cc::summary::Item*)d_items);
+        CC_LAUNCHED(h);
+    }
+    cc::summary::k_summary_fold<<<1, 1, 0, h->stream>>>((const cc::summary::Item*)d_items, (const cc::tight::Box*)d_in,
+                                                        n, (cc_tight_summary_t*)d_out);
     CC_LAUNCHED(h);
     CC_CUDA(h, cudaMemcpyAsync(out, d_out, sizeof(cc_tight_summary_t), cudaMemcpyDeviceToHost, h->stream));
     CC_CUDA(h, cudaStreamSynchronize(h->stream));

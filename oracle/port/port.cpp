@@ -27,6 +27,7 @@ CC_HOST_TLS unsigned long long cc_port_op_count = 0;
 #define CC_HOST_PORT 1
 #include "../../circlecover_gb300/csrc/cc_tight.cuh"
 #include "../../circlecover_gb300/csrc/cc_sb_proof.cuh"
+#include "../../circlecover_gb300/csrc/cc_tight_summary.cuh"
 
 namespace cc {
 CC_HOST_TLS uint32_t cc_port_trap_word = 0;
@@ -243,6 +244,19 @@ int ccport_tight_generation(const cc_tight_box* parents, size_t n, int la_splits
         stats->gen_sizes[0] = res.size();
     }
     return 0;
+}
+
+/* Max_distances through the prover's own per-box items and in-order fold */
+void ccport_tight_summary(const cc_tight_box* crit, size_t n, cc_tight_summary_t* out) {
+    std::vector<cc::summary::Item> items(n);
+    std::vector<ct::Box> boxes(n);
+    for (size_t i = 0; i < n; ++i) {
+        boxes[i] = ct::Box{to_iv(crit[i].la), {to_iv(crit[i].r[0]), to_iv(crit[i].r[1]), to_iv(crit[i].r[2]),
+                                                to_iv(crit[i].r[3])}};
+        cc::trap_clear();
+        items[i] = cc::summary::summary_item(boxes[i]);
+    }
+    cc::summary::summary_fold(items.data(), boxes.data(), n, out);
 }
 
 void ccport_free(void* p) { std::free(p); }

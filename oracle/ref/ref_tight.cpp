@@ -243,6 +243,117 @@ int ccref_tight_can_recurse(double w, double h, double largest, double weight) {
     return tr::can_recurse(w, h, largest, weight) ? 1 : 0;
 }
 
+/* Max_distances of a critical set: a restatement of the reference's
+ * kernel_compute_distance_from_theoretical_worst_cases
+ * (tight_rectangle/tight_rectangle.cu:343-456; a one-thread CUDA kernel
+ * there) on the reference's own interval type and required_weight_for.
+ * Deviation: the reference starts S1/h2/S3 from uninitialised device memory
+ * and only overwrites them at the first box whose pocket width exceeds the
+ * running one while that is negative; they start at zero here. */
+static cc_iv civ(const IV& x) { return cc_iv{x.get_lb(), x.get_ub()}; }
+static IV fiv(const cc_iv& x) { return IV(x.lb, x.ub); }
+static cc_tight_box cbox(const tr::Variables& v) {
+    cc_tight_box b;
+    b.la = civ(v.la);
+    for (int k = 0; k < 4; ++k) b.r[k] = civ(v.radii[k]);
+    return b;
+}
+
+void ccref_tight_summary(const cc_tight_box* crit, size_t n, cc_tight_summary_t* out) {
+    cc_tight_summary_t o;
+    std::memset(&o, 0, sizeof(o));
+    o.la_range_3d = cc_iv{1.0, 1.0};
+    o.la_range_2d = cc_iv{2.0, 2.0};
+    o.pocket_width_3d = -1.0;
+    o.lb_h1_2d = 1.0;
+    o.ub_la_by_S1 = 1.0;
+    for (size_t i = 0; i < n; ++i) {
+        tr::Variables v;
+        v.la = fiv(crit[i].la);
+        for (int k = 0; k < 4; ++k) v.radii[k] = fiv(crit[i].r[k]);
+        auto track = [&](cc_iv& acc, const IV& d, cc_tight_box* dom) {
+            if (d.get_lb() < acc.lb) dom[0] = cbox(v);
+            if (d.get_ub() > acc.ub) dom[1] = cbox(v);
+        };
+        if (v.radii[2].get_ub() < 0.1) {
+            o.have_range_2d = 1;
+            IV lr = fiv(o.la_range_2d);
+            lr.do_join(v.la);
+            o.la_range_2d = civ(lr);
+            IV r1_t = 0.25 * (v.la.square() + 1.0);
+            IV r2_t{0.25, 0.25};
+            IV d1 = v.radii[0] - r1_t, d2 = v.radii[1] - r2_t;
+            track(o.dist_r1_2d, d1, o.dist_r1_2d_criticals);
+            IV j1 = fiv(o.dist_r1_2d);
+            j1.do_join(d1);
+            o.dist_r1_2d = civ(j1);
+            track(o.dist_r2_2d, d2, o.dist_r2_2d_criticals);
+            IV j2 = fiv(o.dist_r2_2d);
+            j2.do_join(d2);
+            o.dist_r2_2d = civ(j2);
+            IV R3 = tr::required_weight_for(v.la) - v.radii[0] - v.radii[1];
+            if (R3.get_ub() > o.ub_R3_2d) o.ub_R3_2d = R3.get_ub();
+            double lb_S1 = __dmul_rd(2.0, __dsqrt_rd(__dadd_rd(v.radii[0].get_lb(), -0.25)));
+            double la_by_S1 = __ddiv_ru(v.la.get_ub(), lb_S1);
+            if (la_by_S1 > o.ub_la_by_S1) o.ub_la_by_S1 = la_by_S1;
+            double t = __dadd_ru(v.la.get_ub(), -__dmul_rd(0.5, lb_S1));
+            double lb_h1 = __dmul_rd(2.0, __dsqrt_rd(__dadd_rd(v.radii[0].get_lb(), -__dmul_ru(t, t))));
+            if (lb_h1 < o.lb_h1_2d) o.lb_h1_2d = lb_h1;
+        } else {
+            o.have_range_3d = 1;
+            IV lr = fiv(o.la_range_3d);
+            lr.do_join(v.la);
+            o.la_range_3d = civ(lr);
+            IV la2 = v.la.square();
+            IV la4 = la2.square();
+            IV theory = (16.0 * la4 + 40.0 * la2 + 9.0) / (256.0 * la2);
+            IV d1 = v.radii[0] - theory, d2 = v.radii[1] - theory, d3 = v.radii[2] - theory;
+            track(o.dist_r1_3d, d1, o.dist_r1_3d_criticals);
+            track(o.dist_r2_3d, d2, o.dist_r2_3d_criticals);
+            track(o.dist_r3_3d, d3, o.dist_r3_3d_criticals);
+            IV j1 = fiv(o.dist_r1_3d), j2 = fiv(o.dist_r2_3d), j3 = fiv(o.dist_r3_3d);
+            j1.do_join(d1);
+            j2.do_join(d2);
+            j3.do_join(d3);
+            o.dist_r1_3d = civ(j1);
+            o.dist_r2_3d = civ(j2);
+            o.dist_r3_3d = civ(j3);
+            IV R4 = tr::required_weight_for(v.la) - v.radii[0] - v.radii[1] - v.radii[2];
+            if (R4.get_ub() > o.ub_R4_3d) o.ub_R4_3d = R4.get_ub();
+            uint32_t trapped = 0;
+            struct Ctx {
+                const tr::Variables* v;
+                IV S1, h2, S3;
+            } cx{&v, IV(0.0, 0.0), IV(0.0, 0.0), IV(0.0, 0.0)};
+            // the square roots trap on a negative lower bound (interval.cuh:339-346)
+            cc_ref_guarded_call([](void* p) {
+                Ctx& c = *(Ctx*)p;
+                c.S1 = sqrt(4.0 * c.v->radii[0] - 1.0);
+                c.h2 = sqrt(4.0 * c.v->radii[1] - (c.v->la - c.S1).square());
+                c.S3 = sqrt(4.0 * c.v->radii[2] - (1.0 - c.h2).square());
+                return true;
+            }, &cx, &trapped);
+            double pocket = (v.la - cx.S1 - cx.S3).get_ub();
+            if (pocket > o.pocket_width_3d) {
+                if (o.pocket_width_3d < 0.0) {
+                    o.S1 = civ(cx.S1);
+                    o.h2 = civ(cx.h2);
+                    o.S3 = civ(cx.S3);
+                }
+                o.pocket_width_3d = pocket;
+            }
+            IV a = fiv(o.S1), c = fiv(o.h2), e = fiv(o.S3);
+            a.do_join(cx.S1);
+            c.do_join(cx.h2);
+            e.do_join(cx.S3);
+            o.S1 = civ(a);
+            o.h2 = civ(c);
+            o.S3 = civ(e);
+        }
+    }
+    *out = o;
+}
+
 /* algcuda::Interval<double> * double (interval.cuh:185-197), for the
  * interval-times-scalar rounding test */
 void ccref_iv_mul_scalar(double lo, double hi, double s, double* out) {
