@@ -189,7 +189,7 @@ EXPORTS = [
     "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove", "cc_sb_prove_ex",
     "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
-    "cc_tight_generation",
+    "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume",
 ]
 
 MLP_PARAMS = 5319
@@ -236,6 +236,9 @@ def load_library(path=LIB_PATH):
     lib.cc_tight_first.argtypes = [vp, vp, sz, ctypes.c_int, vp, vp]
     lib.cc_tight_cell_log.argtypes = [vp, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_int)]
     lib.cc_autotune_eval.argtypes = [vp, vp, sz, vp, ctypes.POINTER(CcTuneResult)]
+    lib.cc_set_checkpoint.argtypes = [vp, ctypes.c_char_p]
+    lib.cc_tight_resume.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(CcTightGrid), ctypes.c_int, ctypes.POINTER(vp),
+                                    ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
     lib.cc_tight_generation.argtypes = [vp, vp, sz, ctypes.c_int, vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
                                         ctypes.POINTER(vp), ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
     lib.cc_sb_prove.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.POINTER(vp), ctypes.POINTER(sz),
@@ -351,6 +354,25 @@ class Prover:
         self._check(self.lib.cc_tight_generation(self.h, parents.ctypes.data if len(parents) else None, len(parents),
                                                  la_splits, rs, lo, hi, 4 if learned else 0, ctypes.byref(out),
                                                  ctypes.byref(n), ctypes.byref(st)), "cc_tight_generation")
+        arr = np.zeros(n.value, dtype=TIGHT_BOX)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)
+        self.lib.cc_free(out)
+        return arr, stats_to_dict(st)
+
+    def set_checkpoint(self, path):
+        """Write the tight proof's state after every generation to `path`
+        (None: off)."""
+        self._check(self.lib.cc_set_checkpoint(self.h, path.encode() if path else None), "cc_set_checkpoint")
+
+    def tight_resume(self, path, grid=None, learned=False):
+        """Continue a tight proof from a checkpoint: (criticals, stats)."""
+        out = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcProveStats()
+        self._check(self.lib.cc_tight_resume(self.h, path.encode(), ctypes.byref(grid) if grid is not None else None,
+                                             4 if learned else 0, ctypes.byref(out), ctypes.byref(n), ctypes.byref(st)),
+                    "cc_tight_resume")
         arr = np.zeros(n.value, dtype=TIGHT_BOX)
         if n.value:
             ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)

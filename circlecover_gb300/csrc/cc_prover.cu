@@ -916,15 +916,53 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
     return CC_OK;
 }
 
-}  // namespace
 
-extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, int flags,
-                                 cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats) {
-    const bool hoist = !(flags & CC_PROVE_PLAIN);
-    if ((flags & CC_PROVE_LEARNED) && !h->mlp)
-        return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_prove_ex: CC_PROVE_LEARNED needs a network (cc_mlp_init)");
-    if (flags & CC_PROVE_LOG_CELLS) h->cell_log.clear();
-    if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
+// ---- checkpoints --------------------------------------------------------------
+// State after a completed generation: the grid, the next generation's index,
+// the running trace totals and generation sizes, and the parents of the next
+// generation (the criticals so far).  Written to `path.tmp` and renamed, so
+// a checkpoint file is always complete.
+struct CkptHeader {
+    char magic[8];
+    uint32_t version;
+    int32_t next_gen;
+    int32_t flags;
+    int32_t pad;
+    cc_tight_grid grid;
+    unsigned long long counts[4][8];
+    unsigned long long digest, leaf_evals, trapped;
+    uint64_t gen_sizes[CC_MAX_GENERATIONS + 1];
+    uint64_t n_parents;
+};
+static const char kCkptMagic[8] = {'C', 'C', 'T', 'I', 'G', 'H', 'T', '1'};
+
+static int write_checkpoint(cc_handle* h, const cc_tight_grid* grid, int next_gen, int flags, const GenTotals& tot,
+                            const uint64_t* gen_sizes, const std::vector<cc_tight_box>& parents) {
+    CkptHeader hd;
+    std::memset(&hd, 0, sizeof(hd));
+    std::memcpy(hd.magic, kCkptMagic, 8);
+    hd.version = 1;
+    hd.next_gen = next_gen;
+    hd.flags = flags;
+    hd.grid = *grid;
+    std::memcpy(hd.counts, tot.counts, sizeof(hd.counts));
+    hd.digest = tot.digest;
+    hd.leaf_evals = tot.leaf_evals;
+    hd.trapped = tot.trapped;
+    std::memcpy(hd.gen_sizes, gen_sizes, sizeof(hd.gen_sizes));
+    hd.n_parents = parents.size();
+    const std::string tmp = h->checkpoint_path + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return ccrt::fail(h, CC_ERR_PARAM, "checkpoint: cannot open the file for writing");
+    bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1;
+    if (ok && !parents.empty()) ok = std::fwrite(parents.data(), sizeof(cc_tight_box), parents.size(), f) == parents.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), h->checkpoint_path.c_str()) != 0)
+        return ccrt::fail(h, CC_ERR_PARAM, "checkpoint: write failed");
+    return CC_OK;
+}
+
+static int check_grid(cc_handle* h, const cc_tight_grid* grid) {
     if (grid->la_splits_init < 1 || grid->num_generations < 0 || grid->num_generations > CC_MAX_GENERATIONS)
         return ccrt::fail(h, CC_ERR_PARAM, "grid: bad lambda splits or generation count");
     for (int k = 0; k < 4; ++k)
@@ -932,20 +970,23 @@ extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const c
             return ccrt::fail(h, CC_ERR_PARAM, "grid: radius splits must be in [1, 2047]");
     for (int g = 0; g < grid->num_generations; ++g)
         if (grid->la_splits_gen[g] < 1) return ccrt::fail(h, CC_ERR_PARAM, "grid: bad lambda splits");
-    *criticals = nullptr;
-    *n_crit = 0;
+    return CC_OK;
+}
+
+// generations start_gen..num_generations from `cur`
+static int prove_generations(cc_handle* h, const cc_tight_grid* grid, int flags, int start_gen,
+                             std::vector<cc_tight_box>& cur, GenTotals& tot, uint64_t* gen_sizes,
+                             cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats) {
+    const bool hoist = !(flags & CC_PROVE_PLAIN);
     h->launches = 0;
     h->interrupt.store(0);
     CC_CUDA(h, cudaSetDevice(h->device));
     auto t0 = std::chrono::steady_clock::now();
-
     Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 22, 1ULL << 20, 1ULL << 26};
-    GenTotals tot;
-    std::vector<cc_tight_box> cur{*root}, next;
-    uint64_t gen_sizes[CC_MAX_GENERATIONS + 1] = {};
-    int gens_run = 0;
+    std::vector<cc_tight_box> next;
+    int gens_run = start_gen > 0 ? start_gen - 1 : 0;
     int status = CC_OK;
-    for (int g = 0; g <= grid->num_generations; ++g) {
+    for (int g = start_gen; g <= grid->num_generations; ++g) {
         if (g > 0 && cur.empty()) break;
         const int k = g == 0 ? grid->la_splits_init : grid->la_splits_gen[g - 1];
         const int* s = g == 0 ? grid->r_splits_init : grid->r_splits_gen;
@@ -955,6 +996,8 @@ extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const c
         cur.swap(next);
         gen_sizes[g] = cur.size();
         gens_run = g;
+        if (!h->checkpoint_path.empty() && (st = write_checkpoint(h, grid, g + 1, flags, tot, gen_sizes, cur)))
+            return st;
         if (h->interrupt.load()) {
             status = CC_ERR_INTERRUPTED;
             break;
@@ -970,12 +1013,74 @@ extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const c
         stats->digest = tot.digest;
         stats->leaf_evals = tot.leaf_evals;
         stats->trapped_leaves = tot.trapped;
-        std::memcpy(stats->gen_sizes, gen_sizes, sizeof(gen_sizes));
+        std::memcpy(stats->gen_sizes, gen_sizes, sizeof(uint64_t) * (CC_MAX_GENERATIONS + 1));
         stats->generations_run = gens_run;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         stats->kernel_launches = h->launches;
     }
     return status;
+}
+
+}  // namespace
+
+extern "C" int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, int flags,
+                                 cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats) {
+    if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
+    if ((flags & CC_PROVE_LEARNED) && !h->mlp)
+        return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_prove_ex: CC_PROVE_LEARNED needs a network (cc_mlp_init)");
+    int st = check_grid(h, grid);
+    if (st) return st;
+    if (flags & CC_PROVE_LOG_CELLS) h->cell_log.clear();
+    *criticals = nullptr;
+    *n_crit = 0;
+    GenTotals tot;
+    std::vector<cc_tight_box> cur{*root};
+    uint64_t gen_sizes[CC_MAX_GENERATIONS + 1] = {};
+    return prove_generations(h, grid, flags, 0, cur, tot, gen_sizes, criticals, n_crit, stats);
+}
+
+extern "C" int cc_set_checkpoint(cc_handle* h, const char* path) {
+    if (!h) return CC_ERR_PARAM;
+    h->checkpoint_path = path ? path : "";
+    return CC_OK;
+}
+
+extern "C" int cc_tight_resume(cc_handle* h, const char* path, const cc_tight_grid* grid, int flags,
+                               cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats) {
+    if (!h || !path || !criticals || !n_crit) return CC_ERR_PARAM;
+    *criticals = nullptr;
+    *n_crit = 0;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_resume: cannot open the checkpoint");
+    CkptHeader hd;
+    bool ok = std::fread(&hd, sizeof(hd), 1, f) == 1 && std::memcmp(hd.magic, kCkptMagic, 8) == 0 && hd.version == 1 &&
+              hd.next_gen >= 1 && hd.next_gen <= CC_MAX_GENERATIONS + 1 && hd.n_parents < (1ULL << 40);
+    std::vector<cc_tight_box> cur;
+    if (ok) {
+        cur.resize(hd.n_parents);
+        ok = hd.n_parents == 0 || std::fread(cur.data(), sizeof(cc_tight_box), hd.n_parents, f) == hd.n_parents;
+    }
+    std::fclose(f);
+    if (!ok) return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_resume: not a complete checkpoint");
+    cc_tight_grid g = grid ? *grid : hd.grid;
+    int st = check_grid(h, &g);
+    if (st) return st;
+    // the run so far must be the start of the requested schedule
+    bool same = g.la_splits_init == hd.grid.la_splits_init && g.num_generations >= hd.next_gen - 1;
+    for (int k = 0; k < 4 && same; ++k) same = g.r_splits_init[k] == hd.grid.r_splits_init[k];
+    for (int k = 0; k < 4 && same && hd.next_gen > 1; ++k) same = g.r_splits_gen[k] == hd.grid.r_splits_gen[k];
+    for (int i = 0; i + 1 < hd.next_gen && same; ++i) same = g.la_splits_gen[i] == hd.grid.la_splits_gen[i];
+    if (!same) return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_resume: the checkpoint's schedule is not a prefix of the grid");
+    if ((flags & CC_PROVE_LEARNED) && !h->mlp)
+        return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_resume: CC_PROVE_LEARNED needs a network (cc_mlp_init)");
+    GenTotals tot;
+    std::memcpy(tot.counts, hd.counts, sizeof(tot.counts));
+    tot.digest = hd.digest;
+    tot.leaf_evals = hd.leaf_evals;
+    tot.trapped = hd.trapped;
+    uint64_t gen_sizes[CC_MAX_GENERATIONS + 1];
+    std::memcpy(gen_sizes, hd.gen_sizes, sizeof(gen_sizes));
+    return prove_generations(h, &g, flags, hd.next_gen, cur, tot, gen_sizes, criticals, n_crit, stats);
 }
 
 extern "C" int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, cc_tight_box** criticals,

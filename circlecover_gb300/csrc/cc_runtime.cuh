@@ -35,6 +35,8 @@ struct cc_handle {
     // evaluation passes' register budget and grid (blocks per SM), set by cc_autotune_eval
     int tune_minb[3] = {1, 1, 1};
     int tune_grid[3] = {8, 8, 8};
+    // where the tight proof writes its state after each generation (empty: off)
+    std::string checkpoint_path;
     // sample of r3 cells logged by the last tight proof (CC_PROVE_LOG_CELLS)
     std::vector<cc_tight_box> cell_log;
     int cell_log_splits = 0;

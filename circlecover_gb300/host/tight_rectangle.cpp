@@ -6,9 +6,13 @@
 // Same split counts, same stdout (banner, the two- and three-disk summaries
 // with 19-digit intervals), same Ctrl-C behaviour: the first SIGINT stops the
 // refinement after the current generation and the result so far is used,
-// the second one exits (reference: interrupt.cpp:30-46).  Errors that the
+// the second one exits (reference: interrupt.cpp:30-46).  With
+// CC_TIGHT_CHECKPOINT=<file> the state is saved after every generation and
+// a later run resumes from it.  Errors that the
 // reference reports by throwing std::system_error/std::logic_error are thrown
 // here as std::runtime_error with the library's message.
+#include <cstdio>
+
 #include "dropin.hpp"
 
 namespace circlecover {
@@ -94,7 +98,22 @@ void circlecover::tight_rectangle::find_critical_intervals() {
     cc_tight_box* crit = nullptr;
     size_t n = 0;
     cc_prove_stats stats;
-    int st = cc_tight_prove(h, &root, &grid, &crit, &n, &stats);
+    // CC_TIGHT_CHECKPOINT=<file>: state written after every generation; an
+    // existing file is resumed from
+    const char* ckpt = std::getenv("CC_TIGHT_CHECKPOINT");
+    int st;
+    if (ckpt && *ckpt) {
+        check(h, cc_set_checkpoint(h, ckpt), "cc_set_checkpoint");
+        if (FILE* f = std::fopen(ckpt, "rb")) {
+            std::fclose(f);
+            std::cerr << "Resuming from " << ckpt << std::endl;
+            st = cc_tight_resume(h, ckpt, &grid, 0, &crit, &n, &stats);
+        } else {
+            st = cc_tight_prove(h, &root, &grid, &crit, &n, &stats);
+        }
+    } else {
+        st = cc_tight_prove(h, &root, &grid, &crit, &n, &stats);
+    }
     std::signal(SIGINT, previous);
     g_active.store(nullptr);
     check(h, st, "cc_tight_prove");

@@ -320,6 +320,18 @@ int cc_tight_prove(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* 
 int cc_tight_prove_ex(cc_handle* h, const cc_tight_box* root, const cc_tight_grid* grid, int flags,
                       cc_tight_box** criticals, size_t* n_crit, cc_prove_stats* stats);
 
+/* Checkpoints of the tight proof (no reference counterpart; the reference
+ * can only be interrupted).  With a path set, cc_tight_prove_ex writes the
+ * state after every completed generation (grid, next generation, trace
+ * totals, generation sizes, the criticals so far) to `path` (atomically:
+ * written to path.tmp, then renamed).  cc_tight_resume continues from such a
+ * file with `grid` (NULL: the saved one), which must extend the saved
+ * schedule; the result and stats equal those of an uninterrupted run.
+ * cc_set_checkpoint(h, NULL) turns checkpoints off. */
+int cc_set_checkpoint(cc_handle* h, const char* path);
+int cc_tight_resume(cc_handle* h, const char* path, const cc_tight_grid* grid, int flags, cc_tight_box** criticals,
+                    size_t* n_crit, cc_prove_stats* stats);
+
 /* One generation of the tight proof restricted to the tasks [task_lo,
  * task_hi) of that generation (task = parent index * la_splits + lambda
  * piece; tasks outside the range contribute nothing).  Criticals are

@@ -161,3 +161,22 @@ def test_autotuned_passes_give_the_same_masks(prover, port):
         assert r["ms"] <= r["ms_default"] * 1.0001
     got = prover.tight_eval(boxes)  # runs with the tuned settings
     assert np.array_equal(got, port.tight_eval(boxes, threads=16))
+
+
+def test_checkpoint_resume_equals_uninterrupted_run(prover, golden_prove, tmp_path):
+    c = golden_prove[3]  # three refinement generations
+    full = cg.make_grid(c["la_init"], c["r_init"], c["gens"], c["r_gen"])
+    first = cg.make_grid(c["la_init"], c["r_init"], c["gens"][:1], c["r_gen"])
+    path = str(tmp_path / "tight.ckpt")
+    prover.set_checkpoint(path)
+    try:
+        prover.tight_find_critical_intervals(box_from_hex(c["root"]), first)  # init + generation 1
+    finally:
+        prover.set_checkpoint(None)
+    crit, st = prover.tight_resume(path, full)
+    want = boxes_from_hex(c["criticals"])
+    assert np.array_equal(crit.view(np.uint64), want.view(np.uint64))
+    for k in ("digest", "counts", "gen_sizes", "leaf_evals"):
+        assert st[k] == c["stats"][k], k
+    with pytest.raises(cg.CudaError):  # a schedule that does not extend the checkpoint's
+        prover.tight_resume(path, cg.make_grid(c["la_init"] * 2, c["r_init"], c["gens"], c["r_gen"]))
