@@ -446,9 +446,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-proof", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", default="tight_eval", choices=["tight_eval", "sb_proof"])
+    ap.add_argument("--workload", default="tight_eval", choices=["tight_eval", "sb_proof", "tight_proof"])
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "tight_proof":  # the tight proof forms alone (for profiling)
+        import __graft_entry__
+        __graft_entry__.build()
+        import circlecover_gb300 as cg
+        with cg.Prover(local) as prover:
+            r = proof_comparison(prover)
+            if rank == 0:
+                print(json.dumps(r), flush=True)
+        return
     if args.workload == "sb_proof":  # the size-bound proof slice alone (for profiling)
         import __graft_entry__
         __graft_entry__.build()
