@@ -251,6 +251,8 @@ def load_library(path=LIB_PATH):
     if hasattr(lib, "cc_selftest_round"):
         lib.cc_selftest_round.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, sz]
         lib.cc_selftest_subinterval.argtypes = [vp, vp, vp, vp, vp, sz, vp, vp]
+        lib.cc_selftest_bisection_f32.argtypes = [vp, ctypes.c_int, vp, sz, vp, vp]
+        lib.cc_selftest_bisection_width.argtypes = [vp, ctypes.c_int, vp, sz, vp, vp]
     _lib = lib
     return lib
 
@@ -517,3 +519,25 @@ class Prover:
                                                      cnt.ctypes.data, len(lo), a.ctypes.data, b.ctypes.data),
                     "cc_selftest_subinterval")
         return a.reshape(-1, 2), b.reshape(-1, 2)
+
+    def selftest_bisection_f32(self, which, args):
+        """Bisection predicate decided by the FP32 enclosure over [lo, hi]
+        (-1 undecided, 0, 1) and by the FP64 predicate at lo (0, 1; +2 on a
+        trap), per row of 8 args (cc_selftest_bisection_f32; which 0 = cover
+        strip, 1 = gaps; lo, hi in columns 6 and 7)."""
+        args = np.ascontiguousarray(args, dtype=np.float64).reshape(-1, 8)
+        f32 = np.empty(len(args), dtype=np.int8)
+        f64 = np.empty(len(args), dtype=np.int8)
+        self._check(self.lib.cc_selftest_bisection_f32(self.h, int(which), args.ctypes.data, len(args),
+                                                       f32.ctypes.data, f64.ctypes.data), "cc_selftest_bisection_f32")
+        return f32, f64
+
+    def selftest_bisection_width(self, which, args):
+        """The device's whole bisection per row (cc_selftest_bisection_width):
+        (widths, trapped)."""
+        args = np.ascontiguousarray(args, dtype=np.float64).reshape(-1, 8)
+        out = np.empty(len(args))
+        tr = np.empty(len(args), dtype=np.int8)
+        self._check(self.lib.cc_selftest_bisection_width(self.h, int(which), args.ctypes.data, len(args),
+                                                         out.ctypes.data, tr.ctypes.data), "cc_selftest_bisection_width")
+        return out, tr

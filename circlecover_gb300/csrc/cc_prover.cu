@@ -254,6 +254,38 @@ __global__ void k_selftest_subinterval(const double* lo, const double* hi, const
     out[2 * i + 1] = r.hi;
 }
 
+// one bisection step decided both ways: the FP32 enclosure's outcome over a
+// range of the bisection variable (-1 undecided, 0, 1) and the FP64
+// predicate's (0, 1) at the range's lower end
+__global__ void k_selftest_bisection_f32(int which, const double* __restrict__ args, size_t n, int8_t* f32_out,
+                                         int8_t* f64_out) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* a = args + 8 * i;
+    const cc::f32::Fv range{__double2float_rd(a[6]), __double2float_ru(a[7])};
+    cc::trap_clear();
+    if (which == 0) {  // r1, r2, r3; w in [a6, a7]
+        f32_out[i] = (int8_t)ct::strip_width_realizable_f32(ct::strip_f32_prepare(a[0], a[1], a[2]), range);
+        f64_out[i] = ct::strip_width_realizable(a[0], a[1], a[2], a[6]) ? 1 : 0;
+    } else {  // r1, r2, w1, w2, r4; g in [a6, a7]
+        f32_out[i] = (int8_t)ct::gap_width_realizable_f32(range, ct::gaps_f32_prepare(a[0], a[1], a[2], a[3], a[4]));
+        f64_out[i] = ct::gap_width_realizable(a[6], a[0], a[2], a[1], a[3], a[4]) ? 1 : 0;
+    }
+    if (cc::trap_status() != cc::TRAP_NONE) f64_out[i] |= 2;
+}
+
+// the whole bisection (with the FP32 shortcuts) of each row
+__global__ void k_selftest_bisection_width(int which, const double* __restrict__ args, size_t n, double* out,
+                                           int8_t* trapped) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* a = args + 8 * i;
+    cc::trap_clear();
+    if (which == 0) out[i] = ct::cover_strip_width(a[6], a[0], a[1], a[2]);  // la_hi in column 6
+    else out[i] = ct::gaps_width(a[0], a[1], a[4], ct::GapsStart{a[2], a[3]});
+    trapped[i] = cc::trap_status() != cc::TRAP_NONE ? 1 : 0;
+}
+
 // ============================================================== C ABI
 extern "C" {
 
@@ -637,6 +669,48 @@ int cc_selftest_subinterval(cc_handle* h, const double* lo, const double* hi, co
     h->launches += 1;
     CC_CUDA(h, cudaMemcpyAsync(out_a, da, n * 16, cudaMemcpyDeviceToHost, h->stream));
     CC_CUDA(h, cudaMemcpyAsync(out_b, db, n * 16, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CC_OK;
+}
+
+int cc_selftest_bisection_f32(cc_handle* h, int which, const double* args, size_t n, int8_t* f32_out,
+                              int8_t* f64_out) {
+    if (!h || !args || !f32_out || !f64_out || (which != 0 && which != 1)) return CC_ERR_PARAM;
+    h->launches = 0;
+    if (n == 0) return CC_OK;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    void *da, *d32, *d64;
+    int st = ccrt::ensure(h, 0, n * 64, &da);
+    if (!st) st = ccrt::ensure(h, 1, n, &d32);
+    if (!st) st = ccrt::ensure(h, 2, n, &d64);
+    if (st) return st;
+    CC_CUDA(h, cudaMemcpyAsync(da, args, n * 64, cudaMemcpyHostToDevice, h->stream));
+    k_selftest_bisection_f32<<<(unsigned)((n + 127) / 128), 128, 0, h->stream>>>(which, (const double*)da, n,
+                                                                                 (int8_t*)d32, (int8_t*)d64);
+    CC_LAUNCHED(h);
+    CC_CUDA(h, cudaMemcpyAsync(f32_out, d32, n, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaMemcpyAsync(f64_out, d64, n, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CC_OK;
+}
+
+int cc_selftest_bisection_width(cc_handle* h, int which, const double* args, size_t n, double* out,
+                                int8_t* trapped) {
+    if (!h || !args || !out || !trapped || (which != 0 && which != 1)) return CC_ERR_PARAM;
+    h->launches = 0;
+    if (n == 0) return CC_OK;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    void *da, *dout, *dtr;
+    int st = ccrt::ensure(h, 0, n * 64, &da);
+    if (!st) st = ccrt::ensure(h, 1, n * 8, &dout);
+    if (!st) st = ccrt::ensure(h, 2, n, &dtr);
+    if (st) return st;
+    CC_CUDA(h, cudaMemcpyAsync(da, args, n * 64, cudaMemcpyHostToDevice, h->stream));
+    k_selftest_bisection_width<<<(unsigned)((n + 127) / 128), 128, 0, h->stream>>>(which, (const double*)da, n,
+                                                                                   (double*)dout, (int8_t*)dtr);
+    CC_LAUNCHED(h);
+    CC_CUDA(h, cudaMemcpyAsync(out, dout, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaMemcpyAsync(trapped, dtr, n, cudaMemcpyDeviceToHost, h->stream));
     CC_CUDA(h, cudaStreamSynchronize(h->stream));
     return CC_OK;
 }

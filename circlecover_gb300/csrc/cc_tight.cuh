@@ -11,6 +11,7 @@
 #pragma once
 
 #include "cc_sb_common.cuh"
+#include "cc_f32.cuh"
 
 namespace cc {
 namespace tight {
@@ -295,6 +296,34 @@ CC_FN bool strip_width_realizable(double r1, double r2, double r3, double w) {
     return add_dn(w2, w3) >= w;
 }
 
+#if CC_DEVICE_BUILD
+// strip_width_realizable decided with FP32 enclosures of its FP64 values
+// (cc_f32.cuh), for every w in the enclosure W at once: YES / NO are the FP64
+// predicate's outcome at each such w, UNKNOWN leaves it to the FP64
+// predicate.  The operands that do not change during the bisection are
+// enclosed once.
+struct StripF32 {
+    f32::Fv a1, a2, a3;  // 4 r1, 4 r2, 4 r3
+};
+CC_FN StripF32 strip_f32_prepare(double r1, double r2, double r3) {
+    return StripF32{f32::scale(f32::of(r1), 4.0f), f32::scale(f32::of(r2), 4.0f), f32::scale(f32::of(r3), 4.0f)};
+}
+CC_FN int strip_width_realizable_f32(const StripF32& p, f32::Fv W) {
+    using namespace f32;
+    const Fv h1 = sub(p.a1, sqr(W));
+    if (h1.hi <= 0.0f) return NO;
+    if (!(h1.lo > 0.0f)) return UNKNOWN;
+    const Fv h_sq = sqr(sub(point(1.0f), sqrt_nn(h1)));
+    const Fv w2 = sub(p.a2, h_sq), w3 = sub(p.a3, h_sq);
+    if (w3.hi <= 0.0f || w2.hi <= 0.0f) return NO;
+    if (!(w3.lo > 0.0f && w2.lo > 0.0f)) return UNKNOWN;
+    const Fv sum = add(sqrt_nn(w2), sqrt_nn(w3));
+    if (sum.lo >= W.hi) return YES;
+    if (sum.hi < W.lo) return NO;
+    return UNKNOWN;
+}
+#endif
+
 // The cover-strip strategy (r1_r2_r3_strategies.cu:69-94) in three pieces,
 // so that the bisection can run as its own pass over the boxes that need it:
 //   enters: the strip of width 0.3 is realizable (else the strategy fails);
@@ -302,9 +331,24 @@ CC_FN bool strip_width_realizable(double r1, double r2, double r3, double w) {
 //   finish: recursion on the rest of the rectangle.
 CC_FN bool cover_strip_enters(double r1, double r2, double r3) { return strip_width_realizable(r1, r2, r3, 0.3); }
 
-CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
-    double lo = 0.3;
-    double hi = la_hi;
+// The reference's bisections (cover strip, gaps) run to the FP64 fixpoint:
+// mid = 0.5 * (lo + hi) until mid is no longer strictly between lo and hi,
+// with a trap after CC_BISECTION_CAP steps.  On the device two FP32 shortcuts
+// come first, both giving the same lo and the same trap status:
+//   * the predicate decided for the whole range [lo, hi] at once (an FP32
+//     enclosure of [lo, hi] contains every later mid, and the enclosures are
+//     inclusion-isotone).  If it is false everywhere, every step lowers hi and
+//     the result is lo; from 0 <= lo < hi <= DBL_MAX that takes fewer than
+//     2,100 steps (about 1,075 halvings down to the subnormals, 1,024 more at
+//     most for the exponent of hi), so the cap cannot trap.  If it is true
+//     everywhere, the steps raise lo and bisect_all_true replays them;
+//   * the leading steps decided by the FP32 enclosure of mid, as long as it
+//     decides the step for every lane of the warp (a warp vote, so the warp
+//     leaves the FP32 steps together); from the first step some lane cannot
+//     decide, every step runs the FP64 predicate.  A warp pays for an FP64
+//     step if any of its lanes needs one, so per-lane FP32 steps after that
+//     would only add work.
+CC_FN double bisect_all_true(double lo, double hi) {
     for (int it = 0;; ++it) {
         double mid = 0.5 * (lo + hi);
         if (mid <= lo || mid >= hi) {
@@ -314,7 +358,50 @@ CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
             trap(TRAP_BISECTION_CAP);
             break;
         }
-        if (strip_width_realizable(r1, r2, r3, mid)) {
+        lo = mid;
+    }
+    return lo;
+}
+
+#if CC_DEVICE_BUILD
+// true while the FP32 decision d may stand for every converged lane
+__device__ __forceinline__ bool f32_step_for_all(int d) { return __all_sync(__activemask(), d != f32::UNKNOWN); }
+#endif
+
+CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
+    double lo = 0.3;
+    double hi = la_hi;
+#if CC_DEVICE_BUILD
+    const StripF32 pf = strip_f32_prepare(r1, r2, r3);
+    if (lo < hi && hi <= CC_DBL_MAX) {
+        int whole = strip_width_realizable_f32(pf, f32::Fv{__double2float_rd(lo), __double2float_ru(hi)});
+        if (whole == f32::NO) return lo;
+        if (whole == f32::YES) return bisect_all_true(lo, hi);
+    }
+    bool f32_steps = true;
+#endif
+    for (int it = 0;; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) {
+            break;
+        }
+        if (it >= CC_BISECTION_CAP) {
+            trap(TRAP_BISECTION_CAP);
+            break;
+        }
+#if CC_DEVICE_BUILD
+        bool ok;
+        int d = f32_steps ? strip_width_realizable_f32(pf, f32::of(mid)) : f32::UNKNOWN;
+        if (f32_steps && f32_step_for_all(d)) {
+            ok = d == f32::YES;
+        } else {
+            f32_steps = false;
+            ok = strip_width_realizable(r1, r2, r3, mid);
+        }
+#else
+        bool ok = strip_width_realizable(r1, r2, r3, mid);
+#endif
+        if (ok) {
             lo = mid;
         } else {
             hi = mid;
@@ -575,6 +662,73 @@ CC_FN bool gap_width_realizable(double g, double r1, double w1, double r2, doubl
     return definitely(squared_distance(p4, px) <= r4);
 }
 
+#if CC_DEVICE_BUILD
+// gap_width_realizable decided with FP32 enclosures of its FP64 values
+// (cc_f32.cuh), operation for operation, for every g in the enclosure G at
+// once: the same quantities, each enclosed by the FP32 interval of the exact
+// operation on the enclosures of its operands (`Iv * scalar`, which rounds
+// both FP64 bounds down, stays inside that enclosure too).  YES / NO are the
+// FP64 predicate's outcome at each such g; UNKNOWN leaves it to the FP64
+// predicate.  In the FP64 code the centres' y difference is
+// [-0, +0] exactly, so the order of the two intersection points depends on
+// dx.lo >= 0 only.
+struct GapsF32 {
+    f32::Fv w1, x1, hw2, rdiff, rdiff_sq, s2, r4;
+};
+CC_FN GapsF32 gaps_f32_prepare(double r1, double r2, double w1, double w2, double r4) {
+    using namespace f32;
+    GapsF32 p;
+    const Fv R1 = of(r1), R2 = of(r2);
+    p.w1 = of(w1);
+    p.x1 = scale(p.w1, 0.5f);
+    p.hw2 = scale(of(w2), 0.5f);
+    p.rdiff = sub(R1, R2);
+    p.rdiff_sq = sqr(p.rdiff);
+    p.s2 = scale(add(R1, R2), 2.0f);
+    p.r4 = of(r4);
+    return p;
+}
+CC_FN int gap_width_realizable_f32(f32::Fv G, const GapsF32& p) {
+    using namespace f32;
+    const Fv y4 = sub(p.r4, mul(scale(G, 0.25f), G));
+    if (y4.hi <= 0.0f) return NO;
+    if (!(y4.lo > 0.0f)) return UNKNOWN;
+    const Fv x2 = add(add(p.hw2, G), p.w1);
+    // intersection(c1, c2)
+    const Fv d2 = sqr(sub(p.x1, x2));
+    if (d2.hi == 0.0f) return NO;
+    if (!(d2.lo > 0.0f)) return UNKNOWN;
+    const Fv d2_sq = sqr(d2);
+    if (!(d2_sq.lo > 0.0f)) return UNKNOWN;
+    const Fv t = sub(sub(div_pos(p.s2, d2), point(1.0f)), div_pos(p.rdiff_sq, d2_sq));
+    if (t.hi < 0.0f) return NO;
+    if (!(t.lo >= 0.0f)) return UNKNOWN;
+    const Fv half_chord = scale(sqrt_nn(t), 0.5f);
+    const Fv shift = div_pos(scale(p.rdiff, 0.5f), d2);
+    const Fv dx = sub(x2, p.x1);
+    const Fv dy = sub(point(0.5f), point(0.5f));
+    const Fv mx = add(scale(add(p.x1, x2), 0.5f), mul(shift, dx));
+    const Fv my = add(point(0.5f), mul(shift, dy));
+    const Fv ax = add(mx, mul(half_chord, dy)), ay = sub(my, mul(half_chord, dx));
+    const Fv bx = sub(mx, mul(half_chord, dy)), by = add(my, mul(half_chord, dx));
+    bool a_first;
+    if (dx.lo >= 0.0f) a_first = true;
+    else if (dx.hi < 0.0f) a_first = false;
+    else return UNKNOWN;
+    const Fv p0y = a_first ? ay : by, p1y = a_first ? by : ay;
+    bool take_a;
+    if (p0y.hi <= p1y.lo) take_a = a_first;         // first_lower certainly true: p[0]
+    else if (p0y.lo > p1y.hi) take_a = !a_first;    // certainly false: p[1]
+    else return UNKNOWN;
+    const Fv px = take_a ? ax : bx, py = take_a ? ay : by;
+    const Fv x4 = add(scale(G, 0.5f), p.w1);
+    const Fv dist = add(sqr(sub(x4, px)), sqr(sub(sqrt_nn(y4), py)));
+    if (dist.hi <= p.r4.lo) return YES;
+    if (dist.lo > p.r4.hi) return NO;
+    return UNKNOWN;
+}
+#endif
+
 // The gaps strategy (r1_r2_large_r3_r4_gaps_strategy.cu:61-98) in three
 // pieces, so that the bisection can run as its own pass over the boxes that
 // need it:
@@ -599,6 +753,16 @@ CC_FN bool gaps_enters(double r1, double r2, GapsStart& g) {
 CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
     const double w1 = g.w1, w2 = g.w2;
     double lo = 0.0, hi = add_dn(sqrt_dn(r1), sqrt_dn(r2));
+#if CC_DEVICE_BUILD
+    // FP32 shortcuts: see bisect_all_true
+    const GapsF32 pf = gaps_f32_prepare(r1, r2, w1, w2, r4);
+    if (lo < hi && hi <= CC_DBL_MAX) {
+        int whole = gap_width_realizable_f32(f32::Fv{0.0f, __double2float_ru(hi)}, pf);
+        if (whole == f32::NO) return lo;
+        if (whole == f32::YES) return bisect_all_true(lo, hi);
+    }
+    bool f32_steps = true;
+#endif
     for (int it = 0;; ++it) {
         double mid = 0.5 * (lo + hi);
         if (mid <= lo || mid >= hi) {
@@ -608,7 +772,19 @@ CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
             trap(TRAP_BISECTION_CAP);
             break;
         }
-        if (gap_width_realizable(mid, r1, w1, r2, w2, r4)) {
+#if CC_DEVICE_BUILD
+        bool ok;
+        int d = f32_steps ? gap_width_realizable_f32(f32::of(mid), pf) : f32::UNKNOWN;
+        if (f32_steps && f32_step_for_all(d)) {
+            ok = d == f32::YES;
+        } else {
+            f32_steps = false;
+            ok = gap_width_realizable(mid, r1, w1, r2, w2, r4);
+        }
+#else
+        bool ok = gap_width_realizable(mid, r1, w1, r2, w2, r4);
+#endif
+        if (ok) {
             lo = mid;
         } else {
             hi = mid;

@@ -431,6 +431,26 @@ int cc_selftest_round(cc_handle* h, int op, int up, const double* a, const doubl
  * 2n doubles each (reference: subintervals.hpp:33-43). */
 int cc_selftest_subinterval(cc_handle* h, const double* lo, const double* hi, const int* idx, const int* cnt, size_t n,
                             double* out_a, double* out_b);
+/* One step of the cover-strip (which = 0) or gaps (which = 1) bisection
+ * decided by the FP32 enclosure that runs before the FP64 predicate and by
+ * the FP64 predicate itself, for checking that every decided FP32 outcome
+ * equals the FP64 one.  args: n rows of 8 doubles, (r1, r2, r3, -, -, -, lo,
+ * hi) for strip_width_realizable (r1_r2_r3_strategies.cu:49-67) and (r1, r2,
+ * w1, w2, r4, -, lo, hi) for the gap width check
+ * (r1_r2_large_r3_r4_gaps_strategy.cu:29-59).  f32_out: the FP32 decision
+ * for every width in [lo, hi] at once (-1 undecided, 0 false, 1 true);
+ * f64_out: the FP64 predicate at the width lo (0 / 1, plus 2 if it reached a
+ * trap site). */
+int cc_selftest_bisection_f32(cc_handle* h, int which, const double* args, size_t n, int8_t* f32_out,
+                              int8_t* f64_out);
+/* The whole cover-strip (which = 0) or gaps (which = 1) bisection of each
+ * row, FP32 shortcuts included: rows of 8 doubles as for
+ * cc_selftest_bisection_f32, with la_hi in column 6 for the cover strip
+ * (r1_r2_r3_strategies.cu:69-94) and (r1, r2, w1, w2, r4) for the gaps
+ * (r1_r2_large_r3_r4_gaps_strategy.cu:61-98).  out: the widths; trapped: 1
+ * where the bisection reached its iteration cap. */
+int cc_selftest_bisection_width(cc_handle* h, int which, const double* args, size_t n, double* out,
+                                int8_t* trapped);
 /* Measured FP64 instruction throughput of the device (ops/s; one FP64
  * instruction = one op): chains of directed-rounding add/mul, or of FMA. */
 int cc_selftest_fp64_peak(cc_handle* h, int use_fma, double* ops_per_s);

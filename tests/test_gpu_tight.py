@@ -180,3 +180,114 @@ def test_checkpoint_resume_equals_uninterrupted_run(prover, golden_prove, tmp_pa
         assert st[k] == c["stats"][k], k
     with pytest.raises(cg.CudaError):  # a schedule that does not extend the checkpoint's
         prover.tight_resume(path, cg.make_grid(c["la_init"] * 2, c["r_init"], c["gens"], c["r_gen"]))
+
+
+def _bisection_rows(prover, which, rows, lo, hi, rounds=2200):
+    """Runs the bisection of every row to its FP64 fixpoint on the host,
+    each step decided by the device's FP64 predicate; checks every step the
+    FP32 enclosure of the step's point decides against it.  Returns (steps,
+    FP32-decided steps, final lo per row)."""
+    steps = decided = 0
+    for _ in range(rounds):
+        mid = 0.5 * (lo + hi)
+        act = (mid > lo) & (mid < hi)
+        if not act.any():
+            break
+        args = rows[act].copy()
+        args[:, 6] = args[:, 7] = mid[act]
+        f32, f64 = prover.selftest_bisection_f32(which, args)
+        assert not (f64 & 2).any()  # no trap site on these inputs
+        ok = f32 >= 0
+        assert np.array_equal(f32[ok], f64[ok] & 1), "an FP32 decision differs from the FP64 predicate"
+        steps += int(act.sum())
+        decided += int(ok.sum())
+        yes = np.zeros(len(rows), dtype=bool)
+        yes[np.nonzero(act)[0]] = (f64 & 1) == 1
+        lo = np.where(act & yes, mid, lo)
+        hi = np.where(act & ~yes, mid, hi)
+    return steps, decided, lo
+
+
+def _check_ranges(prover, which, rows, lo, hi, points=33):
+    """FP32 decisions over whole ranges [lo, hi]: where one is made, the FP64
+    predicate has that outcome at points spread over the range and at its
+    ends.  Returns how many ranges were decided."""
+    args = rows.copy()
+    args[:, 6], args[:, 7] = lo, hi
+    f32, _ = prover.selftest_bisection_f32(which, args)
+    dec = f32 >= 0
+    if not dec.any():
+        return 0
+    sub = args[dec]
+    for k in range(points):
+        t = args.copy()[dec]
+        t[:, 6] = sub[:, 6] + (sub[:, 7] - sub[:, 6]) * (k / (points - 1))
+        t[:, 6] = np.minimum(np.maximum(t[:, 6], sub[:, 6]), sub[:, 7])
+        t[:, 7] = t[:, 6]
+        _, f64 = prover.selftest_bisection_f32(which, t)
+        assert np.array_equal(f64 & 1, f32[dec]), "a whole-range FP32 decision differs from the FP64 predicate"
+    return int(dec.sum())
+
+
+def _gaps_rows(n, seed):
+    b = W.tight_microbench(n, seed=seed)
+    r = b["r"][:, :, 0].copy()
+    r[:, 2] = np.maximum(r[:, 2], r[:, 3])
+    r[:, 1] = np.maximum(r[:, 1], r[:, 2])
+    r[:, 0] = np.maximum(r[:, 0], r[:, 1])
+    keep = (4 * r[:, 0] - 1 > 0) & (4 * r[:, 1] - 1 > 0)
+    r = r[keep]
+    rows = np.zeros((len(r), 8))
+    rows[:, 0], rows[:, 1] = r[:, 0], r[:, 1]
+    rows[:, 2], rows[:, 3] = np.sqrt(4 * r[:, 0] - 1), np.sqrt(4 * r[:, 1] - 1)
+    rows[:, 4] = r[:, 3]
+    return rows
+
+
+def _cover_rows(prover, n, seed):
+    b = W.tight_microbench(n, seed=seed)
+    rows = np.zeros((len(b), 8))
+    rows[:, :3] = b["r"][:, :3, 0]
+    rows[:, 6] = rows[:, 7] = 0.3
+    _, f64 = prover.selftest_bisection_f32(0, rows)
+    keep = (f64 & 1) == 1  # the boxes whose strip of width 0.3 is realizable
+    return rows[keep], b["la"][keep, 1].copy()
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_fp32_bisection_decisions_equal_fp64(prover, which):
+    """The FP32 enclosures that decide bisection steps, and whole ranges of
+    steps, before the FP64 predicate runs never contradict it: along the
+    bisection paths of microbench boxes to their fixpoints, at points
+    scattered around each fixpoint, and over the starting ranges and ranges
+    around the fixpoints.  The device's whole bisection (shortcuts included)
+    returns the host-driven FP64 bisection's result bit for bit."""
+    if which == 1:
+        rows = _gaps_rows(1 << 14, seed=61)
+        lo0, hi0 = np.zeros(len(rows)), np.sqrt(rows[:, 0]) + np.sqrt(rows[:, 1])
+    else:
+        rows, la = _cover_rows(prover, 1 << 15, seed=62)
+        lo0, hi0 = np.full(len(rows), 0.3), la
+    steps, decided, fix = _bisection_rows(prover, which, rows, lo0.copy(), hi0.copy())
+    assert steps > 0 and decided >= 0.25 * steps, (steps, decided)
+    rng = np.random.default_rng(63 + which)
+    for scale in [0.5, 2.0 ** -10, 2.0 ** -20, 2.0 ** -26, 2.0 ** -40]:
+        args = rows.copy()
+        args[:, 6] = args[:, 7] = np.maximum(fix * (1 + scale * rng.uniform(-1, 1, len(rows))), 0.0)
+        f32, f64 = prover.selftest_bisection_f32(which, args)
+        ok = f32 >= 0
+        assert np.array_equal(f32[ok], f64[ok] & 1)
+    n_dec = _check_ranges(prover, which, rows, lo0, hi0)
+    for scale in [2.0 ** -4, 2.0 ** -12]:
+        lo = np.maximum(fix * (1 - scale), lo0)
+        hi = np.minimum(fix * (1 + scale), hi0)
+        good = lo < hi
+        n_dec += _check_ranges(prover, which, rows[good], lo[good], hi[good])
+    assert n_dec > 0
+    # the device's bisection with its shortcuts lands where the FP64 one does
+    args = rows.copy()
+    if which == 0:
+        args[:, 6] = hi0
+    got, trapped = prover.selftest_bisection_width(which, args)
+    assert not trapped.any()
+    assert np.array_equal(got.view(np.uint64), fix.view(np.uint64))
