@@ -93,7 +93,10 @@ def algorithmic_ops_per_box():
     total = float(z["ops"].astype(np.float64).mean())
     cover = float(z["cover_ops"].astype(np.float64).mean())
     gaps = float(z["gaps_ops"].astype(np.float64).mean())
-    return total, {"k_eval_main": total - cover - gaps, "k_eval_cover": cover, "k_eval_gaps": gaps}, z["masks"]
+    # the main criteria's operations are decided by the FP32 pass, or by the
+    # FP64 pass for the boxes the FP32 pass leaves to it: counted at the FP32 pass
+    return total, {"k_eval_f32": total - cover - gaps, "k_eval_main": 0.0, "k_eval_cover": cover,
+                   "k_eval_gaps": gaps}, z["masks"]
 
 
 def ncu_traffic(kernel):
@@ -204,7 +207,7 @@ def run_ours(args, ws, rank, local):
     launches_per_step = prover.last_launch_count
     # per-kernel CUDA events (recorded by the library on the same stream)
     prover.set_stage_timing(True)
-    stage_ms = np.zeros(3)
+    stage_ms = np.zeros(len(cg.EVAL_PASSES))
     clocks = ClockSampler(local)
     clocks.start()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -252,7 +255,7 @@ def run_ours(args, ws, rank, local):
         prover.close()
         return
     peak = ctypes_peak(prover)
-    names = ["k_eval_main", "k_eval_cover", "k_eval_gaps"]
+    names = list(cg.EVAL_PASSES)
     stages = {k: {"ms": float(stage_ms[i]), "ops_per_box": stage_ops[k],
                   "achieved": stage_ops[k] * n / (stage_ms[i] * 1e-3) / 1e12,
                   "frac": stage_ops[k] * n / (stage_ms[i] * 1e-3) / peak} for i, k in enumerate(names)}

@@ -93,8 +93,11 @@ class CcTightSummary(ctypes.Structure):
 
 
 class CcTuneResult(ctypes.Structure):
-    _fields_ = [("min_blocks", ctypes.c_int * 3), ("blocks_per_sm", ctypes.c_int * 3), ("ms", ctypes.c_float * 3),
-                ("ms_default", ctypes.c_float * 3)]
+    _fields_ = [("min_blocks", ctypes.c_int * 4), ("blocks_per_sm", ctypes.c_int * 4), ("ms", ctypes.c_float * 4),
+                ("ms_default", ctypes.c_float * 4)]
+
+
+EVAL_PASSES = ("k_eval_f32", "k_eval_main", "k_eval_cover", "k_eval_gaps")
 
 
 class CcSbGrid(ctypes.Structure):
@@ -189,7 +192,7 @@ EXPORTS = [
     "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove", "cc_sb_prove_ex",
     "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
-    "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume",
+    "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume", "cc_last_eval_counts",
 ]
 
 MLP_PARAMS = 5319
@@ -236,6 +239,7 @@ def load_library(path=LIB_PATH):
     lib.cc_tight_first.argtypes = [vp, vp, sz, ctypes.c_int, vp, vp]
     lib.cc_tight_cell_log.argtypes = [vp, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_int)]
     lib.cc_autotune_eval.argtypes = [vp, vp, sz, vp, ctypes.POINTER(CcTuneResult)]
+    lib.cc_last_eval_counts.argtypes = [vp, vp]
     lib.cc_set_checkpoint.argtypes = [vp, ctypes.c_char_p]
     lib.cc_tight_resume.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(CcTightGrid), ctypes.c_int, ctypes.POINTER(vp),
                                     ctypes.POINTER(sz), ctypes.POINTER(CcProveStats)]
@@ -316,21 +320,28 @@ class Prover:
         r = CcTuneResult()
         self._check(self.lib.cc_autotune_eval(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
                                               ctypes.byref(r)), "cc_autotune_eval")
-        names = ("k_eval_main", "k_eval_cover", "k_eval_gaps")
-        return {names[i]: {"min_blocks": r.min_blocks[i], "blocks_per_sm": r.blocks_per_sm[i],
-                           "ms": float(r.ms[i]), "ms_default": float(r.ms_default[i])} for i in range(3)}
+        return {k: {"min_blocks": r.min_blocks[i], "blocks_per_sm": r.blocks_per_sm[i],
+                    "ms": float(r.ms[i]), "ms_default": float(r.ms_default[i])} for i, k in enumerate(EVAL_PASSES)}
 
     def set_stage_timing(self, enable=True):
         """Record a CUDA event around each evaluation kernel (see stage_times)."""
         self._check(self.lib.cc_set_stage_timing(self.h, int(bool(enable))), "cc_set_stage_timing")
 
     def stage_times(self):
-        """Milliseconds of k_eval_main, k_eval_cover, k_eval_gaps in the last
-        timed evaluation (waits for it to finish)."""
-        ms = np.zeros(3, dtype=np.float32)
+        """Milliseconds of the evaluation passes (EVAL_PASSES order) in the
+        last timed evaluation (waits for it to finish)."""
+        ms = np.zeros(len(EVAL_PASSES), dtype=np.float32)
         n = ctypes.c_int()
-        self._check(self.lib.cc_last_stage_times(self.h, ms.ctypes.data, 3, ctypes.byref(n)), "cc_last_stage_times")
+        self._check(self.lib.cc_last_stage_times(self.h, ms.ctypes.data, len(ms), ctypes.byref(n)),
+                    "cc_last_stage_times")
         return [float(x) for x in ms[: n.value]]
+
+    def eval_counts(self):
+        """Queue sizes of the last evaluation batch (cc_last_eval_counts):
+        boxes left to the FP64 pass, strip-width and gap-width jobs."""
+        c = (ctypes.c_ulonglong * 4)()
+        self._check(self.lib.cc_last_eval_counts(self.h, c), "cc_last_eval_counts")
+        return {"fp64_boxes": int(c[0]), "cover_jobs": int(c[1]), "gaps_jobs": int(c[2]), "overflow": int(c[3])}
 
     def sb_eval(self, boxes):
         """Size-bound verdict masks (CC_SV_* bits) of host boxes (SB_BOX records)."""

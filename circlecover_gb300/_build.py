@@ -20,10 +20,12 @@ LIB = os.path.join(OUT, "libcirclecover_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
                  "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
+# --split-compile=0: the device code of a unit is compiled in parallel
+# pieces (one process per core), the units themselves in parallel too
 UNITS = [
-    ("cc_prover.cu", ["-fmad=false", "-Xptxas", "-v"]),
-    ("cc_sb_kernels.cu", ["-fmad=false", "-Xptxas", "-v"]),
-    ("cc_sb_prove.cu", ["-fmad=false", "-Xptxas", "-v"]),
+    ("cc_prover.cu", ["-fmad=false", "-Xptxas", "-v", "--split-compile=0"]),
+    ("cc_sb_kernels.cu", ["-fmad=false", "-Xptxas", "-v", "--split-compile=0"]),
+    ("cc_sb_prove.cu", ["-fmad=false", "-Xptxas", "-v", "--split-compile=0"]),
     ("cc_mlp.cu", ["-fmad=false", "-Xptxas", "-v"]),
     ("cc_selftest_fmad.cu", []),
 ]

@@ -73,6 +73,7 @@ enum TrapSite : uint32_t {
     TRAP_SEVEN_DISK_B = 6,     // rectangle_size_bound/seven_disk_strategies.cu:409
     TRAP_SEVEN_DISK_C = 7,     // rectangle_size_bound/seven_disk_strategies.cu:456
     TRAP_SEVEN_DISK_D = 8,     // rectangle_size_bound/seven_disk_strategies.cu:971
+    TRAP_F32_UNDECIDED = 9,    // not a reference trap: an FP32 enclosure could not decide (cc_f32.cuh)
 };
 
 // A bisection on doubles halves its bracket every step; from any finite

@@ -23,6 +23,7 @@
 namespace cc {
 
 struct Iv {
+    using S = double;  // scalar type of the bounds (criteria are templates over Iv and its FP32 enclosure)
     double lo, hi;
 };
 

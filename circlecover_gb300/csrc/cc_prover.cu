@@ -51,140 +51,198 @@ __device__ __forceinline__ ct::Box load_box(const double* __restrict__ in, size_
     return b;
 }
 
-// One box per thread, grid-stride over the batch.  FP64-pipe bound: each box
-// costs hundreds to thousands of directed-rounding operations against 80 bytes
-// loaded, so memory is irrelevant and the grid is sized to keep every SM's
-// FP64 units fed (a multiple of the SM count).
-template <Layout L>
-__global__ void __launch_bounds__(128) k_tight_eval(const double* __restrict__ in, size_t n, uint32_t* __restrict__ masks) {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        ct::Box b = load_box<L>(in, n, i);
-        masks[i] = ct::eval_all(b);
-    }
-}
-
-// ---- three-pass evaluation ------------------------------------------------
-// A warp pays for every path any of its lanes takes.  The two bisections
-// (cover strip: ~19% of boxes, ~700 operations; gaps: ~30% of boxes, ~6000
-// operations) would make almost every warp wait for one lane, so the main
-// pass only decides whether a box needs them and appends the box's inputs
-// to a queue (one atomic per warp); each bisection then runs as its own pass
-// over full warps of boxes that all need it.
+// ---- four-pass evaluation -------------------------------------------------
+// GB300 issues FP32 instructions at many times the FP64 rate, and a warp pays
+// for every path any of its lanes takes.  So:
+//   pass 0  every box: the criteria on FP32 enclosures of the FP64 values
+//           (ct::eval_group_f32), one kernel per criterion group (the whole
+//           FP32 evaluation does not fit the instruction cache), each ORing
+//           its bits into the box's mask; then k_eval_collect appends the
+//           boxes some group could not decide to the `full` queue and the
+//           boxes that need a bisection to its queue (one atomic per warp);
+//   pass 1  k_eval_main on the `full` queue: the FP64 criteria (ct::eval_main);
+//   pass 2  k_eval_cover: boxes that need the strip-width bisection (~19% of
+//           the microbench: ~700 operations each), on full warps;
+//   pass 3  k_eval_gaps: boxes that need the gap-width bisection (~30%).
+// The queues hold box indices; each pass reads the box itself.
 struct EvalQueues {
-    ct::CoverJob* cover;
+    uint32_t* full;
     uint32_t* cover_box;
-    ct::GapsJob* gaps;
     uint32_t* gaps_box;
-    unsigned long long* counts;  // [0] cover, [1] gaps, [2] overflow
+    unsigned long long* counts;  // [0] cover, [1] gaps, [2] overflow, [3] full
     unsigned long long cap;
 };
+static constexpr int kEvalCounters = 4;
 
 // MinB: the register budget (__launch_bounds__ minimum resident blocks per
 // SM: 1 = up to 255 registers per thread, 4 = 128, 8 = 64), chosen per
-// kernel by the autotuner (cc_autotune_eval) together with the grid size.
-template <Layout L, int MinB = 1>
-__global__ void __launch_bounds__(128, MinB) k_eval_main(const double* __restrict__ in, size_t n,
-                                                         uint32_t* __restrict__ masks, EvalQueues q) {
+// pass by the autotuner (cc_autotune_eval) together with the grid size.
+template <Layout L, int G, int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_f32(const double* __restrict__ in, size_t n,
+                                                        uint32_t* __restrict__ masks) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (G == 0) {
+            masks[i] = ct::eval_group_f32<G>(load_box<L>(in, n, i));
+        } else {
+            const uint32_t prev = masks[i];
+            if (prev & ct::kF32Undecided) continue;  // left to the FP64 pass anyway
+            masks[i] = prev | ct::eval_group_f32<G>(load_box<L>(in, n, i));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_eval_collect(size_t n, uint32_t* __restrict__ masks, EvalQueues q) {
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n;
          base += stride) {
         unsigned long long i = base + (threadIdx.x & 31);
         bool valid = i < n;
+        uint32_t m = valid ? masks[i] : 0u;
+        const bool undecided = (m & ct::kF32Undecided) != 0;
+        const bool need_cover = !undecided && (m & ct::kF32Cover);
+        const bool need_gaps = !undecided && (m & ct::kF32Gaps);
+        if (valid && (m & (ct::kF32Undecided | ct::kF32Cover | ct::kF32Gaps)))
+            masks[i] = m & ~(ct::kF32Undecided | ct::kF32Cover | ct::kF32Gaps);
+        unsigned long long s = cc::prove::warp_append(&q.counts[3], valid && undecided, q.cap, &q.counts[2]);
+        if (s != ~0ULL) q.full[s] = (uint32_t)i;
+        s = cc::prove::warp_append(&q.counts[0], valid && need_cover, q.cap, &q.counts[2]);
+        if (s != ~0ULL) q.cover_box[s] = (uint32_t)i;
+        s = cc::prove::warp_append(&q.counts[1], valid && need_gaps, q.cap, &q.counts[2]);
+        if (s != ~0ULL) q.gaps_box[s] = (uint32_t)i;
+    }
+}
+
+template <Layout L, int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_main(const double* __restrict__ in, size_t n,
+                                                         uint32_t* __restrict__ masks, EvalQueues q) {
+    const unsigned long long nq = q.counts[3] < q.cap ? q.counts[3] : q.cap;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nq;
+         base += stride) {
+        unsigned long long j = base + (threadIdx.x & 31);
+        bool valid = j < nq;
         bool need_cover = false, need_gaps = false;
-        ct::CoverJob cj;
-        ct::GapsJob gj;
+        uint32_t i = 0;
         if (valid) {
+            i = q.full[j];
             ct::Box b = load_box<L>(in, n, i);
+            ct::CoverJob cj;
+            ct::GapsJob gj;
             masks[i] = ct::eval_main(b, need_cover, cj, need_gaps, gj);
         }
         __syncwarp();
         unsigned long long s = cc::prove::warp_append(&q.counts[0], valid && need_cover, q.cap, &q.counts[2]);
-        if (s != ~0ULL) {
-            q.cover[s] = cj;
-            q.cover_box[s] = (uint32_t)i;
-        }
+        if (s != ~0ULL) q.cover_box[s] = i;
         s = cc::prove::warp_append(&q.counts[1], valid && need_gaps, q.cap, &q.counts[2]);
-        if (s != ~0ULL) {
-            q.gaps[s] = gj;
-            q.gaps_box[s] = (uint32_t)i;
-        }
+        if (s != ~0ULL) q.gaps_box[s] = i;
     }
 }
 
-template <int MinB = 1>
-__global__ void __launch_bounds__(128, MinB) k_eval_cover(EvalQueues q, uint32_t* __restrict__ masks) {
-    const unsigned long long n = q.counts[0] < q.cap ? q.counts[0] : q.cap;
-    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        uint32_t m = ct::cover_pass(q.cover[i]);
-        if (m) masks[q.cover_box[i]] |= m;
+template <Layout L, int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_cover(const double* __restrict__ in, size_t n, EvalQueues q,
+                                                          uint32_t* __restrict__ masks) {
+    const unsigned long long nq = q.counts[0] < q.cap ? q.counts[0] : q.cap;
+    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < nq;
+         j += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t i = q.cover_box[j];
+        uint32_t m = ct::cover_pass_box(load_box<L>(in, n, i));
+        if (m) masks[i] |= m;
     }
 }
 
-template <int MinB = 1>
-__global__ void __launch_bounds__(128, MinB) k_eval_gaps(EvalQueues q, uint32_t* __restrict__ masks) {
-    const unsigned long long n = q.counts[1] < q.cap ? q.counts[1] : q.cap;
-    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        uint32_t m = ct::gaps_pass(q.gaps[i]);
-        if (m) masks[q.gaps_box[i]] |= m;
+template <Layout L, int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_gaps(const double* __restrict__ in, size_t n, EvalQueues q,
+                                                         uint32_t* __restrict__ masks) {
+    const unsigned long long nq = q.counts[1] < q.cap ? q.counts[1] : q.cap;
+    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < nq;
+         j += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t i = q.gaps_box[j];
+        uint32_t m = ct::gaps_pass_box(load_box<L>(in, n, i));
+        if (m) masks[i] |= m;
     }
 }
 
-// queue buffers for up to `cap` boxes in handle slots 16..20
+// queue buffers for up to `cap` boxes in handle slots 16..19
 static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
-    void *a, *b, *c, *d, *e;
+    void *a, *b, *c, *e;
     int st;
-    if ((st = ccrt::ensure(h, 16, cap * sizeof(ct::CoverJob), &a))) return st;
+    if ((st = ccrt::ensure(h, 16, cap * sizeof(uint32_t), &a))) return st;
     if ((st = ccrt::ensure(h, 17, cap * sizeof(uint32_t), &b))) return st;
-    if ((st = ccrt::ensure(h, 18, cap * sizeof(ct::GapsJob), &c))) return st;
-    if ((st = ccrt::ensure(h, 19, cap * sizeof(uint32_t), &d))) return st;
-    if ((st = ccrt::ensure(h, 20, 4 * sizeof(unsigned long long), &e))) return st;
-    *q = EvalQueues{(ct::CoverJob*)a, (uint32_t*)b, (ct::GapsJob*)c, (uint32_t*)d, (unsigned long long*)e, cap};
+    if ((st = ccrt::ensure(h, 18, cap * sizeof(uint32_t), &c))) return st;
+    if ((st = ccrt::ensure(h, 19, kEvalCounters * sizeof(unsigned long long), &e))) return st;
+    *q = EvalQueues{(uint32_t*)a, (uint32_t*)b, (uint32_t*)c, (unsigned long long*)e, cap};
     return CC_OK;
 }
 
-// launches of the three passes with a tuned register budget and grid
-// (the AoS main pass, used by the host-memory entry point, keeps MinB 1)
+// launch of pass k (0 FP32, 1 FP64 main, 2 cover, 3 gaps) with a register
+// budget and grid
+// (the register budgets are tuned on device (SoA) batches; the host entry
+// point's AoS batches use the default budget)
+#define CC_EVAL_LAUNCH(KERNEL, ...)                                                                   \
+    template <Layout L>                                                                               \
+    static void launch_##KERNEL(int minb, int g, cudaStream_t s, const double* in, size_t n,          \
+                                uint32_t* masks, EvalQueues q) {                                      \
+        if constexpr (L == Layout::SoA) {                                                             \
+            if (minb == 4) KERNEL<L, 4><<<g, 128, 0, s>>>(__VA_ARGS__);                               \
+            else if (minb == 8) KERNEL<L, 8><<<g, 128, 0, s>>>(__VA_ARGS__);                          \
+            else KERNEL<L, 1><<<g, 128, 0, s>>>(__VA_ARGS__);                                         \
+        } else {                                                                                      \
+            KERNEL<L, 1><<<g, 128, 0, s>>>(__VA_ARGS__);                                              \
+        }                                                                                             \
+    }
+// pass 0: the FP32 group kernels, then the collection of the queues
 template <Layout L>
-static void launch_main(int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks, EvalQueues q) {
-    if (L == Layout::SoA && minb == 4) k_eval_main<L, 4><<<g, 128, 0, s>>>(in, n, masks, q);
-    else if (L == Layout::SoA && minb == 8) k_eval_main<L, 8><<<g, 128, 0, s>>>(in, n, masks, q);
-    else k_eval_main<L, 1><<<g, 128, 0, s>>>(in, n, masks, q);
+static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks,
+                              EvalQueues q) {
+#define CC_F32_GROUP(G)                                                                         \
+    if constexpr (L == Layout::SoA) {                                                           \
+        if (minb == 4) k_eval_f32<L, G, 4><<<g, 128, 0, s>>>(in, n, masks);                     \
+        else if (minb == 8) k_eval_f32<L, G, 8><<<g, 128, 0, s>>>(in, n, masks);                \
+        else k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks);                               \
+    } else {                                                                                    \
+        k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks);                                    \
+    }
+    CC_F32_GROUP(0)
+    CC_F32_GROUP(1)
+    CC_F32_GROUP(2)
+    CC_F32_GROUP(3)
+    CC_F32_GROUP(4)
+#undef CC_F32_GROUP
+    k_eval_collect<<<g, 128, 0, s>>>(n, masks, q);
 }
-static void launch_cover(int minb, int g, cudaStream_t s, EvalQueues q, uint32_t* masks) {
-    if (minb == 4) k_eval_cover<4><<<g, 128, 0, s>>>(q, masks);
-    else if (minb == 8) k_eval_cover<8><<<g, 128, 0, s>>>(q, masks);
-    else k_eval_cover<1><<<g, 128, 0, s>>>(q, masks);
-}
-static void launch_gaps(int minb, int g, cudaStream_t s, EvalQueues q, uint32_t* masks) {
-    if (minb == 4) k_eval_gaps<4><<<g, 128, 0, s>>>(q, masks);
-    else if (minb == 8) k_eval_gaps<8><<<g, 128, 0, s>>>(q, masks);
-    else k_eval_gaps<1><<<g, 128, 0, s>>>(q, masks);
+CC_EVAL_LAUNCH(k_eval_main, in, n, masks, q)
+CC_EVAL_LAUNCH(k_eval_cover, in, n, q, masks)
+CC_EVAL_LAUNCH(k_eval_gaps, in, n, q, masks)
+#undef CC_EVAL_LAUNCH
+
+template <Layout L>
+static void launch_pass(int pass, int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks,
+                        EvalQueues q) {
+    switch (pass) {
+        case 0: launch_k_eval_f32<L>(minb, g, s, in, n, masks, q); break;
+        case 1: launch_k_eval_main<L>(minb, g, s, in, n, masks, q); break;
+        case 2: launch_k_eval_cover<L>(minb, g, s, in, n, masks, q); break;
+        default: launch_k_eval_gaps<L>(minb, g, s, in, n, masks, q); break;
+    }
 }
 
-// the three passes on one batch already on the device
+// the four passes on one batch already on the device
 template <Layout L>
 static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks, cudaStream_t s) {
     EvalQueues q;
     int st = eval_queues(h, n, &q);
     if (st) return st;
-    CC_CUDA(h, cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s));
+    CC_CUDA(h, cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s));
     h->stages_recorded = 0;
-    if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[0], s));
-    // the tuned setting applies to the device (SoA) batches it was tuned on
-    launch_main<L>(L == Layout::SoA ? h->tune_minb[0] : 1, h->sm_count * (L == Layout::SoA ? h->tune_grid[0] : 8), s,
-                   in, n, masks, q);
-    CC_LAUNCHED(h);
-    if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[1], s));
-    launch_cover(h->tune_minb[1], h->sm_count * h->tune_grid[1], s, q, masks);
-    CC_LAUNCHED(h);
-    if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[2], s));
-    launch_gaps(h->tune_minb[2], h->sm_count * h->tune_grid[2], s, q, masks);
-    CC_LAUNCHED(h);
+    h->eval_counts = q.counts;
+    for (int pass = 0; pass < CC_EVAL_STAGES; ++pass) {
+        if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[pass], s));
+        launch_pass<L>(pass, h->tune_minb[pass], h->sm_count * h->tune_grid[pass], s, in, n, masks, q);
+        CC_LAUNCHED(h);
+        if (pass == 0) h->launches += ct::F32_GROUPS;  // the group kernels and the collection
+    }
     if (h->timing) {
-        CC_CUDA(h, cudaEventRecord(h->stage_ev[3], s));
+        CC_CUDA(h, cudaEventRecord(h->stage_ev[CC_EVAL_STAGES], s));
         h->stages_recorded = CC_EVAL_STAGES;
     }
     return CC_OK;
@@ -324,7 +382,7 @@ int cc_create(cc_handle** out, int device) {
     }
     // the kernels must exist for this device (built for sm_103a only)
     cudaFuncAttributes attr;
-    if (cudaFuncGetAttributes(&attr, k_tight_eval<Layout::SoA>) != cudaSuccess) {
+    if (cudaFuncGetAttributes(&attr, k_selftest_subinterval) != cudaSuccess) {
         cudaGetLastError();
         cudaStreamDestroy(h->stream);
         delete h;
@@ -359,6 +417,20 @@ int cc_set_stage_timing(cc_handle* h, int enable) {
     return CC_OK;
 }
 
+int cc_last_eval_counts(cc_handle* h, unsigned long long* counts) {
+    if (!h || !counts) return ccrt::fail(h, CC_ERR_PARAM, "cc_last_eval_counts: bad argument");
+    if (!h->eval_counts) return ccrt::fail(h, CC_ERR_PARAM, "cc_last_eval_counts: no evaluation recorded");
+    CC_CUDA(h, cudaSetDevice(h->device));
+    CC_CUDA(h, cudaDeviceSynchronize());
+    unsigned long long c[kEvalCounters];
+    CC_CUDA(h, cudaMemcpy(c, h->eval_counts, sizeof(c), cudaMemcpyDeviceToHost));
+    counts[0] = c[3];
+    counts[1] = c[0];
+    counts[2] = c[1];
+    counts[3] = c[2];
+    return CC_OK;
+}
+
 int cc_last_stage_times(cc_handle* h, float* ms, int max_stages, int* n_stages) {
     if (!h || !ms || !n_stages || max_stages < 0) return ccrt::fail(h, CC_ERR_PARAM, "cc_last_stage_times: bad argument");
     *n_stages = 0;
@@ -387,13 +459,15 @@ int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* ma
     return eval_batch<Layout::SoA>(h, soa, n, masks, s);
 }
 
-// ---- autotuner ------------------------------------------------------------------
-// For each of the three evaluation passes, every register budget (MinB 1, 4,
-// 8) and grid size (2, 4, 8, 16 blocks of 128 per SM) is timed with CUDA
-// events on the caller's sample batch (the main pass first; the bisection
-// passes then rerun on the queues it filled: they only OR bits into the
-// masks, so reruns change nothing); the fastest setting of each pass is kept
-// in the handle for later cc_tight_eval_device / cc_tight_eval calls.
+// Autotuner (no reference counterpart).  Each pass, with every register
+// budget (minimum resident blocks 1, 4, 8) and grid size (2, 4, 8, 16 blocks
+// of 128 per SM), is timed with CUDA events on the caller's sample batch, in
+// pass order: the FP32 pass from empty queues; the FP64 pass on the queue the
+// chosen FP32 run filled, its appends undone before every run (the queue
+// counters are restored from a snapshot); the bisection passes on the final
+// queues (they only OR bits into the masks, so reruns change nothing).  The
+// fastest setting of each pass is kept in the handle for later
+// cc_tight_eval_device / cc_tight_eval calls.
 extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint32_t* masks, cc_tune_result* out) {
     if (!h || !soa || !masks || !n) return CC_ERR_PARAM;
     CC_CUDA(h, cudaSetDevice(h->device));
@@ -405,16 +479,16 @@ extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint3
     CC_CUDA(h, cudaEventCreate(&e0));
     CC_CUDA(h, cudaEventCreate(&e1));
     const int minbs[3] = {1, 4, 8}, grids[4] = {2, 4, 8, 16};
+    unsigned long long snap[kEvalCounters] = {};
     cc_tune_result r{};
-    auto time_stage = [&](int stage, int minb, int grid, float* ms) -> int {
+    auto time_pass = [&](int pass, int minb, int grid, float* ms) -> int {
         const int g = h->sm_count * grid;
         float best = 1e30f;
         for (int rep = 0; rep < 2; ++rep) {
-            if (stage == 0) CC_CUDA(h, cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s));
+            if (pass == 0) CC_CUDA(h, cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s));
+            if (pass == 1) CC_CUDA(h, cudaMemcpyAsync(q.counts, snap, sizeof(snap), cudaMemcpyHostToDevice, s));
             CC_CUDA(h, cudaEventRecord(e0, s));
-            if (stage == 0) launch_main<Layout::SoA>(minb, g, s, soa, n, masks, q);
-            else if (stage == 1) launch_cover(minb, g, s, q, masks);
-            else launch_gaps(minb, g, s, q, masks);
+            launch_pass<Layout::SoA>(pass, minb, g, s, soa, n, masks, q);
             CC_LAUNCHED(h);
             CC_CUDA(h, cudaEventRecord(e1, s));
             CC_CUDA(h, cudaEventSynchronize(e1));
@@ -425,24 +499,30 @@ extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint3
         *ms = best;
         return CC_OK;
     };
-    for (int stage = 0; stage < 3; ++stage) {
+    for (int pass = 0; pass < CC_EVAL_STAGES; ++pass) {
         float best = 1e30f;
         int bm = 1, bg = 8;
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 4; ++b) {
                 float t;
-                if ((st = time_stage(stage, minbs[a], grids[b], &t))) return st;
-                if (minbs[a] == 1 && grids[b] == 8) r.ms_default[stage] = t;
+                if ((st = time_pass(pass, minbs[a], grids[b], &t))) return st;
+                if (minbs[a] == 1 && grids[b] == 8) r.ms_default[pass] = t;
                 if (t < best) best = t, bm = minbs[a], bg = grids[b];
             }
-        // leave the queues filled by the chosen main pass for the later stages
-        float rerun;
-        if (stage == 0 && (st = time_stage(0, bm, bg, &rerun))) return st;
-        h->tune_minb[stage] = bm;
-        h->tune_grid[stage] = bg;
-        r.min_blocks[stage] = bm;
-        r.blocks_per_sm[stage] = bg;
-        r.ms[stage] = best;
+        // leave the queues as the chosen setting of a queue-filling pass leaves them
+        if (pass <= 1) {
+            float rerun;
+            if ((st = time_pass(pass, bm, bg, &rerun))) return st;
+            if (pass == 0) {
+                CC_CUDA(h, cudaMemcpyAsync(snap, q.counts, sizeof(snap), cudaMemcpyDeviceToHost, s));
+                CC_CUDA(h, cudaStreamSynchronize(s));
+            }
+        }
+        h->tune_minb[pass] = bm;
+        h->tune_grid[pass] = bg;
+        r.min_blocks[pass] = bm;
+        r.blocks_per_sm[pass] = bg;
+        r.ms[pass] = best;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -465,7 +545,7 @@ extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint3
 static constexpr size_t kStaticMaxBoxes = CC_STATIC_EVAL_MAX_BOXES;
 static constexpr size_t kStaticCountersBytes = 256;
 static constexpr size_t kStaticScratchBytes =
-    kStaticCountersBytes + kStaticMaxBoxes * (sizeof(ct::CoverJob) + sizeof(uint32_t) + sizeof(ct::GapsJob) + sizeof(uint32_t));
+    kStaticCountersBytes + kStaticMaxBoxes * 3 * sizeof(uint32_t);
 static_assert(kStaticScratchBytes <= CC_STATIC_EVAL_SCRATCH_BYTES, "static scratch larger than advertised");
 static __device__ __align__(256) unsigned char cc_static_eval_scratch[CC_STATIC_EVAL_SCRATCH_BYTES];
 
@@ -507,24 +587,20 @@ extern "C" int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t
     EvalQueues q;
     q.counts = (unsigned long long*)base;
     unsigned char* p = base + kStaticCountersBytes;
-    q.cover = (ct::CoverJob*)p;
-    p += kStaticMaxBoxes * sizeof(ct::CoverJob);
-    q.gaps = (ct::GapsJob*)p;
-    p += kStaticMaxBoxes * sizeof(ct::GapsJob);
+    q.full = (uint32_t*)p;
+    p += kStaticMaxBoxes * sizeof(uint32_t);
     q.cover_box = (uint32_t*)p;
     p += kStaticMaxBoxes * sizeof(uint32_t);
     q.gaps_box = (uint32_t*)p;
     q.cap = kStaticMaxBoxes;
     cudaStream_t s = (cudaStream_t)stream;
     // the queue counters are the only state that must start at zero
-    if (cudaMemsetAsync(q.counts, 0, 4 * sizeof(unsigned long long), s) != cudaSuccess) {
+    if (cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s) != cudaSuccess) {
         cudaGetLastError();
         return CC_ERR_CUDA;
     }
     const int g = g_static_sms[dev] * 8;
-    k_eval_main<Layout::SoA, 1><<<g, 128, 0, s>>>(soa, n, masks, q);
-    k_eval_cover<1><<<g, 128, 0, s>>>(q, masks);
-    k_eval_gaps<1><<<g, 128, 0, s>>>(q, masks);
+    for (int pass = 0; pass < CC_EVAL_STAGES; ++pass) launch_pass<Layout::SoA>(pass, 1, g, s, soa, n, masks, q);
     if (cudaGetLastError() != cudaSuccess) return CC_ERR_CUDA;
     return CC_OK;
 }

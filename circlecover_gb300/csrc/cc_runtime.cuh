@@ -33,8 +33,8 @@ struct cc_handle {
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
     // evaluation passes' register budget and grid (blocks per SM), set by cc_autotune_eval
-    int tune_minb[3] = {1, 1, 1};
-    int tune_grid[3] = {8, 8, 8};
+    int tune_minb[CC_EVAL_STAGES] = {1, 1, 1, 1};
+    int tune_grid[CC_EVAL_STAGES] = {8, 8, 8, 8};
     // where the tight proof writes its state after each generation (empty: off)
     std::string checkpoint_path;
     // sample of r3 cells logged by the last tight proof (CC_PROVE_LOG_CELLS)
@@ -47,6 +47,8 @@ struct cc_handle {
     bool timing = false;
     cudaEvent_t stage_ev[CC_EVAL_STAGES + 1] = {};
     int stages_recorded = 0;
+    // queue counters of the last evaluation batch (device memory)
+    unsigned long long* eval_counts = nullptr;
 };
 
 namespace ccrt {

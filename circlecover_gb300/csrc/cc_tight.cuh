@@ -14,14 +14,24 @@
 #include "cc_f32.cuh"
 
 namespace cc {
+#if CC_DEVICE_BUILD
+namespace sb {
+// one out-of-line copy for the FP32 evaluation (the 2x2 criterion calls it six times)
+__device__ __noinline__ inline f32::Fv two_disks_maximize_height(f32::IvF d1, f32::IvF d2, f32::Fv ub_w) {
+    return two_disks_maximize_height_t<f32::IvF>(d1, d2, ub_w);
+}
+}  // namespace sb
+#endif
 namespace tight {
 
 // A box of the tight proof: aspect ratio and the four largest squared radii
 // (reference: tight_rectangle/strategies.cuh:33-50, same 80-byte layout).
-struct Box {
-    Iv la;
-    Iv r[4];
+template <class I>
+struct BoxT {
+    I la;
+    I r[4];
 };
+using Box = BoxT<Iv>;
 
 // Break-even aspect ratio lambda_2 = sqrt(sqrt(7)/2 - 1/4) between the
 // three-disk and the two-disk worst case, as outward-rounded bounds.  The
@@ -37,46 +47,53 @@ CC_FN double break_even_hi_formula() { return sqrt_up(add_up(mul_up(0.5, sqrt_up
 // lambda >= 1 (critical_ratio.cu:58-78):
 //   lambda <= lambda_2:  (3/256)/lambda * (16 lambda^2 + 40 + 9/lambda^2)
 //   lambda >= lambda_2:  lambda/4 + 1/(2 lambda)
-CC_FN Iv ratio_three_disk(Iv la) {
-    Iv la2 = square(la);
+template <class I>
+CC_FN I ratio_three_disk(I la) {
+    I la2 = square(la);
     return ((3.0 / 256.0) / la) * (16.0 * la2 + 40.0 + 9.0 / la2);
 }
-CC_FN Iv ratio_two_disk(Iv la) { return 0.25 * la + 0.5 * reciprocal(la); }
+template <class I>
+CC_FN I ratio_two_disk(I la) { return 0.25 * la + 0.5 * reciprocal(la); }
 
-CC_FN Iv critical_ratio(Iv la) {
+template <class I>
+CC_FN I critical_ratio(I la) {
     if (definitely(la <= kBreakEvenLo)) {
         return ratio_three_disk(la);
     }
     if (definitely(la >= kBreakEvenHi)) {
         return ratio_two_disk(la);
     }
-    Iv a = ratio_three_disk(la);
-    Iv b = ratio_two_disk(la);
-    return Iv{a.lo < b.lo ? a.lo : b.lo, a.hi < b.hi ? b.hi : a.hi};
+    I a = ratio_three_disk(la);
+    I b = ratio_two_disk(la);
+    return I{lesser(a.lo, b.lo), greater(b.hi, a.hi)};
 }
 
 // ratio for a w x h rectangle in either orientation (critical_ratio.cu:32-52)
-CC_FN Iv critical_ratio(Iv w, Iv h) {
+template <class I>
+CC_FN I critical_ratio(I w, I h) {
     if (w.hi <= h.lo) {
         return critical_ratio(h / w);
     }
     if (h.hi <= w.lo) {
         return critical_ratio(w / h);
     }
-    Iv tall = h / w;
+    I tall = h / w;
     tighten_lb(tall, 1.0);
-    Iv wide = w / h;
+    I wide = w / h;
     tighten_lb(wide, 1.0);
-    Iv a = critical_ratio(tall);
-    Iv b = critical_ratio(wide);
-    return Iv{a.lo < b.lo ? a.lo : b.lo, a.hi < b.hi ? b.hi : a.hi};
+    I a = critical_ratio(tall);
+    I b = critical_ratio(wide);
+    return I{lesser(a.lo, b.lo), greater(b.hi, a.hi)};
 }
 
-CC_FN Iv required_weight_for(Iv w, Iv h) { return critical_ratio(w, h) * w * h; }  // critical_ratio.cu:80-82
-CC_FN Iv required_weight_for(Iv la) { return critical_ratio(la) * la; }            // critical_ratio.cu:84-86
+template <class I>
+CC_FN I required_weight_for(I w, I h) { return critical_ratio(w, h) * w * h; }  // critical_ratio.cu:80-82
+template <class I>
+CC_FN I required_weight_for(I la) { return critical_ratio(la) * la; }            // critical_ratio.cu:84-86
 
 // can_apply_size_bounded_covering.cu:49-52
-CC_FN double required_weight_for_bounded_size(double ub_w, double ub_h) {
+template <class S>
+CC_FN S required_weight_for_bounded_size(S ub_w, S ub_h) {
     return mul_up(sb::kCriticalRatio, mul_up(ub_w, ub_h));
 }
 
@@ -84,80 +101,88 @@ CC_FN double required_weight_for_bounded_size(double ub_w, double ub_h) {
 // weight <= ub_largest and total weight >= lb_weight?  Best of the worst-case
 // ratio, the size-bounded corollary and the 9/64 size-bound ratio
 // (can_recurse.cu:32-62).
-CC_FN bool can_recurse(double ub_w, double ub_h, double ub_largest, double lb_weight) {
-    double ub_area = mul_up(ub_w, ub_h);
-    double side_min = ub_w < ub_h ? ub_w : ub_h;
-    double s = rcp_up(side_min);
-    double s_sq = mul_up(s, s);
-    double largest_norm = mul_up(s_sq, ub_largest);
+template <class S>
+CC_FN bool can_recurse_t(S ub_w, S ub_h, S ub_largest, S lb_weight) {
+    S ub_area = mul_up(ub_w, ub_h);
+    S side_min = lesser(ub_w, ub_h);
+    S s = rcp_up(side_min);
+    S s_sq = mul_up(s, s);
+    S largest_norm = mul_up(s_sq, ub_largest);
 
-    double ratio;
+    S ratio;
     if (largest_norm <= sb::kUbDiskWeight) {
         // the size-bound ratio replaces whatever was computed before
         ratio = sb::kCriticalRatio;
     } else {
         ratio = critical_ratio(ivp(ub_w), ivp(ub_h)).hi;
-        double ratio_cor = mul_up(0.5, sqrt_up(add_up(sqrt_up(add_up(mul_up(largest_norm, largest_norm), 1.0)), 1.0)));
-        if (ratio_cor < 195.0 / 256) {
-            ratio_cor = 195.0 / 256;
-        }
-        if (ratio > ratio_cor) {
-            ratio = ratio_cor;
-        }
+        S ratio_cor = mul_up(0.5, sqrt_up(add_up(sqrt_up(add_up(mul_up(largest_norm, largest_norm), 1.0)), 1.0)));
+        ratio_cor = greater(S(195.0 / 256), ratio_cor);  // at least 195/256
+        ratio = lesser(ratio_cor, ratio);                // the better of the two
     }
-    double ub_needed = mul_up(ratio, ub_area);
+    S ub_needed = mul_up(ratio, ub_area);
     return lb_weight >= ub_needed;
 }
+CC_FN bool can_recurse(double ub_w, double ub_h, double ub_largest, double lb_weight) {
+    return can_recurse_t<double>(ub_w, ub_h, ub_largest, lb_weight);
+}
+#if CC_DEVICE_BUILD
+// one out-of-line copy for the FP32 evaluation (it is called from many sites)
+__device__ __noinline__ inline bool can_recurse(f32::Fv ub_w, f32::Fv ub_h, f32::Fv ub_largest, f32::Fv lb_weight) {
+    return can_recurse_t<f32::Fv>(ub_w, ub_h, ub_largest, lb_weight);
+}
+#endif
 
 // ------------------------------------------------------------ one disk
 // Place disk 1 as a full-height strip, in a corner, or as an uneven split;
 // recurse on the rest (r1_strategies.cu:27-87).  `weight` is
 // required_weight_for(la), which the reference recomputes inside every
 // criterion; callers compute it once per box (same bits).
-CC_FN_INL bool r1_strategies(Iv la, Iv weight, Iv r1, double ub_r2) {
-    double square_w = sqrt_dn(mul_dn(2.0, r1.lo));
-    double strip_w = add_dn(mul_dn(4.0, r1.lo), -1.0);
-    const double lb_rem = (weight - r1).lo;
+template <class I>
+CC_FN_INL bool r1_strategies(I la, I weight, I r1, typename I::S ub_r2) {
+    using S = typename I::S;
+    S square_w = sqrt_dn(mul_dn(2.0, r1.lo));
+    S strip_w = add_dn(mul_dn(4.0, r1.lo), -1.0);
+    const S lb_rem = (weight - r1).lo;
 
     if (strip_w > 0.0) {
         strip_w = sqrt_dn(strip_w);
-        Iv w_rest = la - strip_w;
+        I w_rest = la - strip_w;
         if (can_recurse(w_rest.hi, 1.0, ub_r2, lb_rem)) {
             return true;
         }
     }
 
     if (square_w < 1.0) {
-        double w_right = add_up(la.hi, -square_w);
-        double min_right = w_right < 1.0 ? w_right : 1.0;
-        double ub_weight_right;
-        if (sb::disk_satisfies_size_bound(ub_r2, min_right)) {
+        S w_right = add_up(la.hi, -square_w);
+        S min_right = lesser(w_right, S(1.0));
+        S ub_weight_right;
+        if (sb::disk_satisfies_size_bound<S>(ub_r2, min_right)) {
             ub_weight_right = mul_up(w_right, sb::kCriticalRatio);
         } else {
-            ub_weight_right = required_weight_for(ivp(w_right), ivp(1.0)).hi;
+            ub_weight_right = required_weight_for(ivp(w_right), ivp(S(1.0))).hi;
         }
         ub_weight_right = add_up(ub_weight_right, ub_r2);
-        double lb_rem_top = add_dn(lb_rem, -ub_weight_right);
-        if (lb_rem_top > 0) {
-            double h_top = add_up(1.0, -square_w);
+        S lb_rem_top = add_dn(lb_rem, -ub_weight_right);
+        if (lb_rem_top > 0.0) {
+            S h_top = add_up(1.0, -square_w);
             if (can_recurse(square_w, h_top, ub_r2, lb_rem_top)) {
                 return true;
             }
         }
     }
 
-    double lb_S1 = add_dn(mul_dn(4.0, r1.lo), -1.0);
+    S lb_S1 = add_dn(mul_dn(4.0, r1.lo), -1.0);
     if (lb_S1 > 0.0) {
         lb_S1 = sqrt_dn(lb_S1);
-        double t = add_up(la.hi, -mul_dn(0.5, lb_S1));
+        S t = add_up(la.hi, -mul_dn(0.5, lb_S1));
         t = mul_up(t, t);
-        double lb_h1 = add_dn(r1.lo, -t);
+        S lb_h1 = add_dn(r1.lo, -t);
         if (lb_h1 > 0.0) {
             lb_h1 = mul_dn(2.0, sqrt_dn(lb_h1));
-            double ub_pocket_h = mul_up(0.5, add_up(1.0, -lb_h1));
-            double ub_pocket_w = add_up(la.hi, -lb_S1);
-            double lb_rem_half = mul_dn(0.5, add_dn(lb_rem, -ub_r2));
-            if (lb_rem_half > 0 && can_recurse(ub_pocket_w, ub_pocket_h, ub_r2, lb_rem_half)) {
+            S ub_pocket_h = mul_up(0.5, add_up(1.0, -lb_h1));
+            S ub_pocket_w = add_up(la.hi, -lb_S1);
+            S lb_rem_half = mul_dn(0.5, add_dn(lb_rem, -ub_r2));
+            if (lb_rem_half > 0.0 && can_recurse(ub_pocket_w, ub_pocket_h, ub_r2, lb_rem_half)) {
                 return true;
             }
         }
@@ -168,83 +193,88 @@ CC_FN_INL bool r1_strategies(Iv la, Iv weight, Iv r1, double ub_r2) {
 // ----------------------------------------------------------- two disks
 // Region around the two-disk worst case settled by hand in the paper
 // (r1_r2_strategies.cu:29-46).
-CC_FN bool two_pocket_by_hand(Iv la, Iv r1, Iv r2) {
+template <class I>
+CC_FN bool two_pocket_by_hand(I la, I r1, I r2) {
+    using S = typename I::S;
     if (r2.lo < 0.2400000000000000188 || r1.lo < 0.4900000000000000466) {
         return false;
     }
-    Iv la2 = square(la);
-    double r1_need = (0.25 * (la2 + 1.0) - 0.00999999999999999847).hi;
+    I la2 = square(la);
+    S r1_need = (0.25 * (la2 + 1.0) - 0.00999999999999999847).hi;
     if (r1.lo < r1_need) {
         return false;
     }
-    Iv S1 = 2.0 * sqrt(r1 - 0.25);
-    Iv pocket = la - S1;
+    I S1 = 2.0 * sqrt(r1 - 0.25);
+    I pocket = la - S1;
     tighten_lb(pocket, 0.0);
-    double r2_need = (0.25 + square(pocket) - 0.00999999999999999847).hi;
+    S r2_need = (0.25 + square(pocket) - 0.00999999999999999847).hi;
     return r2.lo >= r2_need;
 }
 
 // disks 1 and 2 side by side as a strip (r1_r2_strategies.cu:48-72)
-CC_FN bool r1_r2_side_by_side(Iv la, Iv weight, Iv r1, Iv r2, double ub_r3) {
+template <class I>
+CC_FN bool r1_r2_side_by_side(I la, I weight, I r1, I r2, typename I::S ub_r3) {
+    using S = typename I::S;
     if (two_pocket_by_hand(la, r1, r2)) {
         return true;
     }
-    double lb_width = sb::two_disks_maximize_height(r1, r2, 1.0);
+    S lb_width = sb::two_disks_maximize_height(r1, r2, 1.0);
     if (lb_width <= 0.0) {
         return false;
     }
-    double lb_w2 = add_dn(mul_dn(4.0, r2.lo), -1.0);
+    S lb_w2 = add_dn(mul_dn(4.0, r2.lo), -1.0);
     if (lb_w2 > 0.0) {
         lb_w2 = sqrt_dn(lb_w2);
-        double lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
-        double lb_w = add_dn(lb_w1, lb_w2);
-        if (lb_w > lb_width) {
-            lb_width = lb_w;
-            if (lb_w > la.hi) {
-                return true;
-            }
+        S lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
+        S lb_w = add_dn(lb_w1, lb_w2);
+        // the reference: if (lb_w > lb_width) { lb_width = lb_w; if (lb_w > la.hi) return true; }
+        if (lb_w > la.hi && lb_w > lb_width) {
+            return true;
         }
+        lb_width = greater(lb_w, lb_width);
     }
-    double w_rem = add_dn(la.hi, lb_width);  // sic: '+' (parity)
-    double lb_R3 = (weight - r1 - r2).lo;
+    S w_rem = add_dn(la.hi, lb_width);  // sic: '+' (parity)
+    S lb_R3 = (weight - r1 - r2).lo;
     return can_recurse(w_rem, 1.0, ub_r3, lb_R3);
 }
 
 // disk 1 in a corner square, disk 2 across the top (r1_r2_strategies.cu:74-129)
-CC_FN bool r1_r2_stacked(Iv la, Iv weight, Iv r1, Iv r2, double ub_r3) {
-    double sq_side = sqrt_dn(mul_dn(2.0, r1.lo));
+template <class I>
+CC_FN bool r1_r2_stacked(I la, I weight, I r1, I r2, typename I::S ub_r3) {
+    using S = typename I::S;
+    S sq_side = sqrt_dn(mul_dn(2.0, r1.lo));
     if (sq_side > 1.0) {
         return false;
     }
-    double h_top = add_up(1.0, -sq_side);
-    double lb_w2 = add_dn(mul_dn(4.0, r2.lo), -mul_up(h_top, h_top));
+    S h_top = add_up(1.0, -sq_side);
+    S lb_w2 = add_dn(mul_dn(4.0, r2.lo), -mul_up(h_top, h_top));
     if (lb_w2 < 0.0) {
         return false;
     }
     lb_w2 = sqrt_dn(lb_w2);
 
-    double w_top = add_up(la.hi, -lb_w2);
-    double w_bot = add_up(la.hi, -sq_side);
-    double top_min = w_top < h_top ? w_top : h_top;
-    double bot_min = w_bot < sq_side ? w_bot : sq_side;
-    double lb_R3 = (weight - r1 - r2).lo;
+    S w_top = add_up(la.hi, -lb_w2);
+    S w_bot = add_up(la.hi, -sq_side);
+    S top_min = lesser(w_top, h_top);
+    S bot_min = lesser(w_bot, sq_side);
+    S lb_R3 = (weight - r1 - r2).lo;
 
-    if (sb::disk_satisfies_size_bound(ub_r3, top_min)) {
-        double need_top = add_up(required_weight_for_bounded_size(w_top, h_top), ub_r3);
-        double left = add_dn(lb_R3, -need_top);
+    if (sb::disk_satisfies_size_bound<S>(ub_r3, top_min)) {
+        S need_top = add_up(required_weight_for_bounded_size<S>(w_top, h_top), ub_r3);
+        S left = add_dn(lb_R3, -need_top);
         if (left > 0.0 && can_recurse(w_bot, sq_side, ub_r3, left)) {
             return true;
         }
-    } else if (sb::disk_satisfies_size_bound(ub_r3, bot_min)) {
-        double need_bot = add_up(required_weight_for_bounded_size(w_bot, sq_side), ub_r3);
-        double left = add_dn(lb_R3, -need_bot);
+    } else if (sb::disk_satisfies_size_bound<S>(ub_r3, bot_min)) {
+        S need_bot = add_up(required_weight_for_bounded_size<S>(w_bot, sq_side), ub_r3);
+        S left = add_dn(lb_R3, -need_bot);
         if (left > 0.0 && can_recurse(w_top, h_top, ub_r3, left)) {
             return true;
         }
     } else {
-        double need_top = required_weight_for(ivp(w_top), ivp(h_top)).hi;
+        S need_top = required_weight_for(ivp(w_top), ivp(h_top)).hi;
         need_top = add_up(need_top, ub_r3);
-        double left = add_dn(lb_R3, -need_top);
+        S left = add_dn(lb_R3, -need_top);
         if (left > 0.0) {
             return can_recurse(w_bot, sq_side, ub_r3, left);
         }
@@ -253,23 +283,26 @@ CC_FN bool r1_r2_stacked(Iv la, Iv weight, Iv r1, Iv r2, double ub_r3) {
 }
 
 // r1_r2_strategies.cu:131-133
-CC_FN_INL bool r1_r2_strategies(Iv la, Iv weight, Iv r1, Iv r2, double ub_r3) {
+template <class I>
+CC_FN_INL bool r1_r2_strategies(I la, I weight, I r1, I r2, typename I::S ub_r3) {
     return r1_r2_side_by_side(la, weight, r1, r2, ub_r3) || r1_r2_stacked(la, weight, r1, r2, ub_r3);
 }
 
 // --------------------------------------------------------- three disks
 // three full-height strips (r1_r2_r3_strategies.cu:28-47)
-CC_FN bool r1_r2_r3_three_strips(Iv la, Iv weight, Iv r1, Iv r2, Iv r3, double ub_r4) {
-    double lb_w3 = add_dn(mul_dn(4.0, r3.lo), -1.0);
+template <class I>
+CC_FN bool r1_r2_r3_three_strips(I la, I weight, I r1, I r2, I r3, typename I::S ub_r4) {
+    using S = typename I::S;
+    S lb_w3 = add_dn(mul_dn(4.0, r3.lo), -1.0);
     if (lb_w3 <= 0.0) {
         return false;
     }
     lb_w3 = sqrt_dn(lb_w3);
-    double lb_w2 = sqrt_dn(add_dn(mul_dn(4.0, r2.lo), -1.0));
-    double lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
-    double lb_cov = add_dn(lb_w1, add_dn(lb_w2, lb_w3));
-    double lb_R4 = (weight - r1 - r2 - r3).lo;
-    double ub_rem = add_up(la.hi, -lb_cov);
+    S lb_w2 = sqrt_dn(add_dn(mul_dn(4.0, r2.lo), -1.0));
+    S lb_w1 = sqrt_dn(add_dn(mul_dn(4.0, r1.lo), -1.0));
+    S lb_cov = add_dn(lb_w1, add_dn(lb_w2, lb_w3));
+    S lb_R4 = (weight - r1 - r2 - r3).lo;
+    S ub_rem = add_up(la.hi, -lb_cov);
     if (ub_rem <= 0.0) {
         return true;
     }
@@ -278,16 +311,17 @@ CC_FN bool r1_r2_r3_three_strips(Iv la, Iv weight, Iv r1, Iv r2, Iv r3, double u
 
 // Disk 1 on top of a strip of width w, disks 2 and 3 below it side by side
 // (r1_r2_r3_strategies.cu:49-67).
-CC_FN bool strip_width_realizable(double r1, double r2, double r3, double w) {
-    double h1 = add_dn(mul_dn(4.0, r1), -mul_up(w, w));
+template <class S>
+CC_FN bool strip_width_realizable(S r1, S r2, S r3, S w) {
+    S h1 = add_dn(mul_dn(4.0, r1), -mul_up(w, w));
     if (h1 <= 0.0) {
         return false;
     }
     h1 = sqrt_dn(h1);
-    double h_rem = add_up(1.0, -h1);
-    double h_sq = mul_up(h_rem, h_rem);
-    double w2 = add_dn(mul_dn(4.0, r2), -h_sq);
-    double w3 = add_dn(mul_dn(4.0, r3), -h_sq);
+    S h_rem = add_up(1.0, -h1);
+    S h_sq = mul_up(h_rem, h_rem);
+    S w2 = add_dn(mul_dn(4.0, r2), -h_sq);
+    S w3 = add_dn(mul_dn(4.0, r3), -h_sq);
     if (w3 <= 0.0 || w2 <= 0.0) {
         return false;
     }
@@ -410,8 +444,9 @@ CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
     return lo;
 }
 
-CC_FN bool cover_strip_finish(double la_hi, double width, double ub_r4, double lb_R4) {
-    double ub_rem = add_up(la_hi, -width);
+template <class S>
+CC_FN bool cover_strip_finish(S la_hi, S width, S ub_r4, S lb_R4) {
+    S ub_rem = add_up(la_hi, -width);
     return can_recurse(ub_rem, 1.0, ub_r4, lb_R4);
 }
 
@@ -430,41 +465,43 @@ CC_FN_INL bool r1_r2_r3_strategies(Iv la, Iv weight, Iv r1, Iv r2, Iv r3, double
 
 // Disks 2 and 3 form a strip, disk 1 covers the rest of a column
 // (r1_r2_r3_strategies.cu:101-121).
-CC_FN bool three_disk_big_strip(double ub_la, double r1, double r2, double r3, double ub_r4, double lb_R4) {
-    double S_sq = add_dn(add_dn(mul_dn(2.0, r2), add_dn(mul_dn(2.0, r3), -0.25)),
-                         add_dn(add_dn(-mul_up(4.0, mul_up(r2, r2)), mul_dn(8.0, mul_dn(r2, r3))),
-                                -mul_up(4.0, mul_up(r3, r3))));
+template <class S>
+CC_FN bool three_disk_big_strip(S ub_la, S r1, S r2, S r3, S ub_r4, S lb_R4) {
+    S S_sq = add_dn(add_dn(mul_dn(2.0, r2), add_dn(mul_dn(2.0, r3), -0.25)),
+                    add_dn(add_dn(-mul_up(4.0, mul_up(r2, r2)), mul_dn(8.0, mul_dn(r2, r3))),
+                           -mul_up(4.0, mul_up(r3, r3))));
     if (S_sq <= 0.0) {
         return false;
     }
-    double S = sqrt_dn(S_sq);
-    double la_rem = add_up(ub_la, -S);
-    double h1_sq = add_dn(mul_dn(4.0, r1), -mul_up(la_rem, la_rem));
+    S side = sqrt_dn(S_sq);
+    S la_rem = add_up(ub_la, -side);
+    S h1_sq = add_dn(mul_dn(4.0, r1), -mul_up(la_rem, la_rem));
     if (h1_sq <= 0.0) {
         return false;
     }
     if (h1_sq >= 1.0) {
         return true;
     }
-    double h_rem = add_up(1.0, -sqrt_dn(h1_sq));
+    S h_rem = add_up(1.0, -sqrt_dn(h1_sq));
     return can_recurse(la_rem, h_rem, ub_r4, lb_R4);
 }
 
 // disk 3 in a corner, disks 1 and 2 along its sides (r1_r2_r3_strategies.cu:123-165)
-CC_FN bool three_disk_small_corner(double ub_la, double r1, double r2, double r3, double ub_r4, double lb_R4) {
-    double c3 = sqrt_dn(mul_dn(2.0, r3));
+template <class S>
+CC_FN bool three_disk_small_corner(S ub_la, S r1, S r2, S r3, S ub_r4, S lb_R4) {
+    S c3 = sqrt_dn(mul_dn(2.0, r3));
     if (c3 >= 1.0) {
         return false;
     }
-    double la_left = add_up(ub_la, -c3);
-    double la_half = mul_up(la_left, 0.5);
-    double one_left = add_up(1.0, -c3);
+    S la_left = add_up(ub_la, -c3);
+    S la_half = mul_up(la_left, 0.5);
+    S one_left = add_up(1.0, -c3);
 
     if (la_half <= sqrt_dn(r2)) {
-        double c1 = sqrt_dn(add_dn(mul_dn(4.0, r1), -mul_up(one_left, one_left)));
-        double la_after_1 = add_up(ub_la, -c1);
-        double c2 = sqrt_dn(add_dn(mul_dn(4.0, r2), -mul_up(la_left, la_left)));
-        double one_after_2 = add_up(1.0, -c2);
+        S c1 = sqrt_dn(add_dn(mul_dn(4.0, r1), -mul_up(one_left, one_left)));
+        S la_after_1 = add_up(ub_la, -c1);
+        S c2 = sqrt_dn(add_dn(mul_dn(4.0, r2), -mul_up(la_left, la_left)));
+        S one_after_2 = add_up(1.0, -c2);
         return can_recurse(la_after_1, one_after_2, ub_r4, lb_R4);
     }
     if (la_half >= sqrt_dn(r1)) {
@@ -473,42 +510,44 @@ CC_FN bool three_disk_small_corner(double ub_la, double r1, double r2, double r3
     if (one_left >= mul_dn(2.0, sqrt_dn(r2))) {
         return false;
     }
-    double c2 = sqrt_dn(add_dn(mul_dn(4.0, r2), -mul_up(one_left, one_left)));
-    double la_after_2 = add_up(ub_la, -c2);
-    double c1 = sqrt_dn(add_dn(mul_dn(4.0, r1), -mul_up(la_left, la_left)));
-    double one_after_1 = add_up(1.0, -c1);
+    S c2 = sqrt_dn(add_dn(mul_dn(4.0, r2), -mul_up(one_left, one_left)));
+    S la_after_2 = add_up(ub_la, -c2);
+    S c1 = sqrt_dn(add_dn(mul_dn(4.0, r1), -mul_up(la_left, la_left)));
+    S one_after_1 = add_up(1.0, -c1);
     return can_recurse(la_after_2, one_after_1, ub_r4, lb_R4);
 }
 
 // disks 1 and 3 at the sides, 2 in between, a pocket remains
 // (r1_r2_r3_strategies.cu:167-204)
-CC_FN bool three_disk_r1_r3_pocket(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4, double lb_R4) {
+template <class I>
+CC_FN bool three_disk_r1_r3_pocket(I la, I r1, I r2, I r3, typename I::S ub_r4, typename I::S lb_R4) {
+    using S = typename I::S;
     if (r1.lo <= 0.25) {
         return false;
     }
-    Iv S1 = 2.0 * sqrt(r1 - 0.25);
-    Iv la_m_S1 = la - S1;
-    Iv h2_rest = 0.25 * la_m_S1 * la_m_S1;
+    I S1 = 2.0 * sqrt(r1 - 0.25);
+    I la_m_S1 = la - S1;
+    I h2_rest = 0.25 * la_m_S1 * la_m_S1;
     if (r2.lo <= h2_rest.hi) {
         return false;
     }
-    Iv h2 = 2.0 * sqrt(r2 - h2_rest);
-    Iv one_m_h2 = 1.0 - h2;
-    Iv S3_rest = 0.25 * one_m_h2 * one_m_h2;
+    I h2 = 2.0 * sqrt(r2 - h2_rest);
+    I one_m_h2 = 1.0 - h2;
+    I S3_rest = 0.25 * one_m_h2 * one_m_h2;
     if (r3.lo <= S3_rest.hi) {
         return false;
     }
-    Iv S3 = 2.0 * sqrt(r3 - S3_rest);
-    Iv X = la - S1 - S3;
+    I S3 = 2.0 * sqrt(r3 - S3_rest);
+    I X = la - S1 - S3;
     if (X.hi <= 0.0) {
         return true;
     }
-    Iv t = la - 0.5 * S1 - S3;
-    Iv Y_rest = t * t;
+    I t = la - 0.5 * S1 - S3;
+    I Y_rest = t * t;
     if (r1.lo <= Y_rest.hi) {
         return false;
     }
-    Iv Y = 0.5 - sqrt(r1 - Y_rest);
+    I Y = 0.5 - sqrt(r1 - Y_rest);
     if (Y.hi <= 0.0) {
         return true;
     }
@@ -517,49 +556,52 @@ CC_FN bool three_disk_r1_r3_pocket(Iv la, Iv r1, Iv r2, Iv r3, double ub_r4, dou
 
 // Region around the three-disk worst case settled by hand in the paper
 // (r1_r2_r3_strategies.cu:206-247).
-CC_FN bool three_disk_pocket_by_hand(Iv la, Iv r1, Iv r2, Iv r3) {
+template <class I>
+CC_FN bool three_disk_pocket_by_hand(I la, I r1, I r2, I r3) {
     if (la.hi > 1.0499999999999998) {
         return false;
     }
-    Iv la2 = square(la);
-    Iv rstar = 0.0625 * la2 + 0.15625 + 0.03515625 / la2;
-    Iv d1 = rstar - r1;
+    I la2 = square(la);
+    I rstar = 0.0625 * la2 + 0.15625 + 0.03515625 / la2;
+    I d1 = rstar - r1;
     if (d1.lo < -0.0009999999999999998 || d1.hi > 0.0009999999999999998) {
         return false;
     }
-    Iv d2 = rstar - r2;
+    I d2 = rstar - r2;
     if (d2.lo < -0.0019999999999999996 || d2.hi > 0.0019999999999999996) {
         return false;
     }
-    Iv d3 = rstar - r3;
+    I d3 = rstar - r3;
     if (d3.lo < -0.0029999999999999996 || d3.hi > 0.0029999999999999996) {
         return false;
     }
-    Iv S1 = 2.0 * sqrt(r1 - 0.25);
-    Iv la_m_S1 = la - S1;
-    Iv h2_rest = 0.25 * la_m_S1 * la_m_S1;
+    I S1 = 2.0 * sqrt(r1 - 0.25);
+    I la_m_S1 = la - S1;
+    I h2_rest = 0.25 * la_m_S1 * la_m_S1;
     if (r2.lo <= h2_rest.hi) {
         return false;
     }
-    Iv h2 = 2.0 * sqrt(r2 - h2_rest);
-    Iv one_m_h2 = 1.0 - h2;
-    Iv S3_rest = 0.25 * one_m_h2 * one_m_h2;
+    I h2 = 2.0 * sqrt(r2 - h2_rest);
+    I one_m_h2 = 1.0 - h2;
+    I S3_rest = 0.25 * one_m_h2 * one_m_h2;
     if (r3.lo <= S3_rest.hi) {
         return false;
     }
-    Iv S3 = 2.0 * sqrt(r3 - S3_rest);
-    Iv X = la - S1 - S3;
+    I S3 = 2.0 * sqrt(r3 - S3_rest);
+    I X = la - S1 - S3;
     return !(X.hi > 0.046999999999999993);
 }
 
 // r1_r2_r3_strategies.cu:249-260
-CC_FN_INL bool r1_r2_r3_strategies(const Box& b, Iv R4) {
-    const double ub_la = b.la.hi;
-    const double r1 = b.r[0].lo, r2 = b.r[1].lo, r3 = b.r[2].lo;
-    const double ub_r4 = b.r[3].hi;
-    const double lb_R4 = R4.lo;
-    return three_disk_big_strip(ub_la, r1, r2, r3, ub_r4, lb_R4) ||
-           three_disk_small_corner(ub_la, r1, r2, r3, ub_r4, lb_R4) ||
+template <class I>
+CC_FN_INL bool r1_r2_r3_strategies(const BoxT<I>& b, I R4) {
+    using S = typename I::S;
+    const S ub_la = b.la.hi;
+    const S r1 = b.r[0].lo, r2 = b.r[1].lo, r3 = b.r[2].lo;
+    const S ub_r4 = b.r[3].hi;
+    const S lb_R4 = R4.lo;
+    return three_disk_big_strip<S>(ub_la, r1, r2, r3, ub_r4, lb_R4) ||
+           three_disk_small_corner<S>(ub_la, r1, r2, r3, ub_r4, lb_R4) ||
            three_disk_r1_r3_pocket(b.la, b.r[0], b.r[1], b.r[2], ub_r4, lb_R4) ||
            three_disk_pocket_by_hand(b.la, b.r[0], b.r[1], b.r[2]);
 }
@@ -567,70 +609,77 @@ CC_FN_INL bool r1_r2_r3_strategies(const Box& b, Iv R4) {
 // ------------------------------------------------------------ 2 x 2
 // disk 1 as a full-height strip, disks 2..4 stacked beside it
 // (two_by_two_strategies.cu:29-53)
-CC_FN bool two_by_two_r1_large(const Box& b, Iv R) {
-    double w1 = sqrt_dn(add_dn(mul_dn(4.0, b.r[0].lo), -1.0));
-    double w_rem = add_up(b.la.hi, -w1);
-    double w_rem_sq = mul_up(w_rem, w_rem);
-    double h4 = add_dn(mul_dn(4.0, b.r[3].lo), -w_rem_sq);
+template <class I>
+CC_FN bool two_by_two_r1_large(const BoxT<I>& b, I R) {
+    using S = typename I::S;
+    S w1 = sqrt_dn(add_dn(mul_dn(4.0, b.r[0].lo), -1.0));
+    S w_rem = add_up(b.la.hi, -w1);
+    S w_rem_sq = mul_up(w_rem, w_rem);
+    S h4 = add_dn(mul_dn(4.0, b.r[3].lo), -w_rem_sq);
     if (h4 <= 0.0) {
         return false;
     }
     h4 = sqrt_dn(h4);
-    double h3 = sqrt_dn(add_dn(mul_dn(4.0, b.r[2].lo), -w_rem_sq));
-    double h2 = sqrt_dn(add_dn(mul_dn(4.0, b.r[1].lo), -w_rem_sq));
-    double h_tot = add_dn(h2, add_dn(h3, h4));
+    S h3 = sqrt_dn(add_dn(mul_dn(4.0, b.r[2].lo), -w_rem_sq));
+    S h2 = sqrt_dn(add_dn(mul_dn(4.0, b.r[1].lo), -w_rem_sq));
+    S h_tot = add_dn(h2, add_dn(h3, h4));
     if (h_tot >= 1.0) {
         return true;
     }
-    double h_rem = add_up(1.0, -h_tot);
-    double ub_r5 = b.r[3].hi < R.hi ? b.r[3].hi : R.hi;
+    S h_rem = add_up(1.0, -h_tot);
+    S ub_r5 = lesser(b.r[3].hi, R.hi);
     return can_recurse(w_rem, h_rem, ub_r5, R.lo);
 }
 
 // disk 1 in a corner, 2 beside, 4 above, 3 in the opposite corner
 // (two_by_two_strategies.cu:55-86)
-CC_FN bool two_by_two_lambda_small(const Box& b, Iv R) {
-    double sq_side = sqrt_dn(mul_dn(2.0, b.r[0].lo));
+template <class I>
+CC_FN bool two_by_two_lambda_small(const BoxT<I>& b, I R) {
+    using S = typename I::S;
+    S sq_side = sqrt_dn(mul_dn(2.0, b.r[0].lo));
     if (sq_side >= 1.0) {
         return two_by_two_r1_large(b, R);
     }
-    double w_rem = add_up(b.la.hi, -sq_side);
-    double h_rem = add_up(1.0, -sq_side);
-    double h2 = add_dn(mul_dn(4.0, b.r[1].lo), -mul_up(w_rem, w_rem));
-    double w4 = add_dn(mul_dn(4.0, b.r[3].lo), -mul_up(h_rem, h_rem));
+    S w_rem = add_up(b.la.hi, -sq_side);
+    S h_rem = add_up(1.0, -sq_side);
+    S h2 = add_dn(mul_dn(4.0, b.r[1].lo), -mul_up(w_rem, w_rem));
+    S w4 = add_dn(mul_dn(4.0, b.r[3].lo), -mul_up(h_rem, h_rem));
     if (h2 <= 0.0 || w4 <= 0.0) {
         return false;
     }
     h2 = sqrt_dn(h2);
     w4 = sqrt_dn(w4);
-    if (w4 > sq_side) w4 = sq_side;
-    if (h2 > sq_side) h2 = sq_side;
-    double h = add_up(1.0, -h2);
-    double w = add_up(b.la.hi, -w4);
-    double diag = add_up(mul_up(h, h), mul_up(w, w));
+    w4 = lesser(sq_side, w4);  // the reference: if (w4 > sq_side) w4 = sq_side
+    h2 = lesser(sq_side, h2);
+    S h = add_up(1.0, -h2);
+    S w = add_up(b.la.hi, -w4);
+    S diag = add_up(mul_up(h, h), mul_up(w, w));
     return mul_dn(4.0, b.r[2].lo) >= diag;
 }
 
 // best pairing of the four disks into two full-height pairs
 // (two_by_two_strategies.cu:88-111)
-CC_FN bool two_by_two_lambda_big(const Box& b, Iv R) {
-    double lb_w = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[1], 1.0),
-                         sb::two_disks_maximize_height(b.r[2], b.r[3], 1.0));
-    double w_1423 = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[3], 1.0),
-                           sb::two_disks_maximize_height(b.r[1], b.r[2], 1.0));
-    if (w_1423 > lb_w) lb_w = w_1423;
-    double w_1324 = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[2], 1.0),
-                           sb::two_disks_maximize_height(b.r[1], b.r[3], 1.0));
-    if (w_1324 > lb_w) lb_w = w_1324;
+template <class I>
+CC_FN bool two_by_two_lambda_big(const BoxT<I>& b, I R) {
+    using S = typename I::S;
+    S lb_w = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[1], 1.0),
+                    sb::two_disks_maximize_height(b.r[2], b.r[3], 1.0));
+    S w_1423 = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[3], 1.0),
+                      sb::two_disks_maximize_height(b.r[1], b.r[2], 1.0));
+    lb_w = greater(w_1423, lb_w);  // the reference: if (w_1423 > lb_w) lb_w = w_1423
+    S w_1324 = add_dn(sb::two_disks_maximize_height(b.r[0], b.r[2], 1.0),
+                      sb::two_disks_maximize_height(b.r[1], b.r[3], 1.0));
+    lb_w = greater(w_1324, lb_w);
     if (lb_w <= 0.0) {
         return false;
     }
-    double ub_r5 = R.hi < b.r[3].hi ? R.hi : b.r[3].hi;
+    S ub_r5 = lesser(R.hi, b.r[3].hi);
     return can_recurse(add_up(b.la.hi, -lb_w), 1.0, ub_r5, R.lo);
 }
 
 // two_by_two_strategies.cu:113-115
-CC_FN_INL bool two_by_two_strategies(const Box& b, Iv R) {
+template <class I>
+CC_FN_INL bool two_by_two_strategies(const BoxT<I>& b, I R) {
     return two_by_two_lambda_small(b, R) || two_by_two_lambda_big(b, R);
 }
 
@@ -793,17 +842,18 @@ CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
     return lo;
 }
 
-CC_FN bool gaps_finish(double la_hi, GapsStart g, double gap, double r4_hi, Iv R) {
-    double w_tot = add_dn(g.w1, add_dn(gap, g.w2));
-    double w_rem = add_up(la_hi, -w_tot);
+template <class S>
+CC_FN bool gaps_finish_t(S la_hi, S w1, S w2, S gap, S r4_hi, S R_lo, S R_hi) {
+    S w_tot = add_dn(w1, add_dn(gap, w2));
+    S w_rem = add_up(la_hi, -w_tot);
     if (w_rem <= 0.0) {
         return true;
     }
-    double ub_r5 = R.hi;
-    if (ub_r5 > r4_hi) {
-        ub_r5 = r4_hi;
-    }
-    return can_recurse(w_rem, 1.0, ub_r5, R.lo);
+    S ub_r5 = lesser(r4_hi, R_hi);  // the reference: R.hi, lowered to r4_hi if above it
+    return can_recurse(w_rem, 1.0, ub_r5, R_lo);
+}
+CC_FN bool gaps_finish(double la_hi, GapsStart g, double gap, double r4_hi, Iv R) {
+    return gaps_finish_t<double>(la_hi, g.w1, g.w2, gap, r4_hi, R.lo, R.hi);
 }
 
 CC_FN_INL bool r1_r2_large_r3_r4_gaps_strategy(const Box& b, Iv R) {
@@ -923,6 +973,123 @@ CC_FN_INL uint32_t eval_all(const Box& in) {
     if (need_gaps) m |= gaps_pass(gj);
     return m;
 }
+
+#if CC_DEVICE_BUILD
+// ------------------------------------------------ FP32-first evaluation
+// eval_main on FP32 enclosures of the box (cc_f32.cuh): the same criteria,
+// instantiated with IvF.  A box any of whose comparisons could not be decided
+// goes to eval_main; for the others the bits equal eval_main's, and the FP64
+// evaluation would not have trapped.
+template <class S>
+CC_FN bool gaps_enter_test(S r1, S r2) {
+    S w1 = add_dn(mul_dn(4.0, r1), -1.0);
+    S w2 = add_dn(mul_dn(4.0, r2), -1.0);
+    return !(w1 <= 0.0 || w2 <= 0.0);
+}
+
+CC_FN_INL BoxT<f32::IvF> enclose(const Box& b) {
+    return BoxT<f32::IvF>{f32::of(b.la), {f32::of(b.r[0]), f32::of(b.r[1]), f32::of(b.r[2]), f32::of(b.r[3])}};
+}
+
+// The FP32 evaluation is split into criterion groups, one kernel each: the
+// whole of it does not fit the instruction cache.  eval_group_f32<G> returns
+// the verdict bits of its group, the internal bits kF32Cover / kF32Gaps
+// (the box needs the strip-width / gap-width bisection), or kF32Undecided.
+enum : uint32_t { kF32Gaps = 1u << 28, kF32Cover = 1u << 29, kF32Undecided = 1u << 30 };
+enum F32Group { F32_R1 = 0, F32_R12 = 1, F32_R123 = 2, F32_2X2 = 3, F32_LEAF = 4, F32_GROUPS = 5 };
+
+template <int G>
+CC_FN_INL uint32_t eval_group_f32(const Box& in64) {
+    using f32::IvF;
+    using f32::Fv;
+    trap_clear();
+    const BoxT<IvF> in = enclose(in64);
+    const IvF la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2], r4 = in.r[3];
+    const IvF weight = required_weight_for(la);
+    uint32_t m = 0;
+    if (G == F32_R1) {
+        if (r1_strategies(la, weight, r1, r2.hi)) m |= 1u << 0;
+    } else if (G == F32_R12) {
+        if (r1_r2_strategies(la, weight, r1, r2, r3.hi)) m |= 1u << 1;
+    } else {
+        IvF R4 = weight - r1 - r2 - r3;
+        tighten_lb(R4, 0.0);
+        BoxT<IvF> v = in;
+        tighten_lb(v.r[2], v.r[3].lo);
+        tighten_lb(v.r[1], v.r[2].lo);
+        tighten_lb(v.r[0], v.r[1].lo);
+        IvF R = weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+        tighten_lb(R, 0.0);
+        if (G == F32_R123) {
+            if (r1_r2_r3_three_strips(la, weight, r1, r2, r3, r4.hi)) {
+                m |= 1u << 2;
+            } else if (strip_width_realizable<Fv>(r1.lo, r2.lo, r3.lo, 0.3)) {
+                m |= kF32Cover;
+            }
+            if (gaps_enter_test<Fv>(v.r[0].lo, v.r[1].lo)) m |= kF32Gaps;
+            if (empty(R4) || empty(R)) m |= 1u << 6;
+        } else if (G == F32_2X2) {
+            if (two_by_two_strategies(v, R)) m |= 1u << 3;
+        } else {
+            if (r1_r2_r3_strategies(v, R4)) m |= 1u << 4;
+        }
+    }
+    return trap_status() == TRAP_NONE ? m : kF32Undecided;
+}
+
+// The two bisection criteria of one box, from the box itself (the queues
+// hold box indices): the bisection in FP64 (with its FP32 shortcuts), then
+// the recursion check first on FP32 enclosures and, if that is undecided, in
+// FP64.  Same result and trap bit as cover_pass / gaps_pass on eval_main's
+// jobs.
+CC_FN_INL uint32_t cover_pass_box(const Box& b) {
+    trap_clear();
+    const Iv la = b.la, r1 = b.r[0], r2 = b.r[1], r3 = b.r[2];
+    const double width = cover_strip_width(la.hi, r1.lo, r2.lo, r3.lo);
+    uint32_t trapped = trap_status();
+    trap_clear();
+    const BoxT<f32::IvF> e = enclose(b);
+    const f32::Fv lb_R4 = (required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2]).lo;
+    bool ok = cover_strip_finish<f32::Fv>(la.hi, width, b.r[3].hi, lb_R4);
+    if (trap_status() != TRAP_NONE) {
+        trap_clear();
+        ok = cover_strip_finish<double>(la.hi, width, b.r[3].hi, (required_weight_for(la) - r1 - r2 - r3).lo);
+        trapped |= trap_status();
+    }
+    uint32_t m = ok ? (1u << 2) : 0u;
+    if (trapped != TRAP_NONE) m |= 1u << 31;
+    return m;
+}
+
+CC_FN_INL uint32_t gaps_pass_box(const Box& b) {
+    trap_clear();
+    Box v = b;
+    tighten_lb(v.r[2], v.r[3].lo);
+    tighten_lb(v.r[1], v.r[2].lo);
+    tighten_lb(v.r[0], v.r[1].lo);
+    GapsStart g;
+    if (!gaps_enters(v.r[0].lo, v.r[1].lo, g)) {
+        return 0u;
+    }
+    const double gap = gaps_width(v.r[0].lo, v.r[1].lo, v.r[3].lo, g);
+    uint32_t trapped = trap_status();
+    trap_clear();
+    BoxT<f32::IvF> e = enclose(v);
+    f32::IvF R = required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2] - e.r[3];
+    tighten_lb(R, 0.0);
+    bool ok = gaps_finish_t<f32::Fv>(b.la.hi, g.w1, g.w2, gap, v.r[3].hi, R.lo, R.hi);
+    if (trap_status() != TRAP_NONE) {
+        trap_clear();
+        Iv R64 = required_weight_for(v.la) - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+        tighten_lb(R64, 0.0);
+        ok = gaps_finish(b.la.hi, g, gap, v.r[3].hi, R64);
+        trapped |= trap_status();
+    }
+    uint32_t m = ok ? (1u << 5) : 0u;
+    if (trapped != TRAP_NONE) m |= 1u << 31;
+    return m;
+}
+#endif
 
 // ------------------------------------------------ prepared (hoisted) forms
 // In the proof's nested grid a criterion is evaluated for every cell of the

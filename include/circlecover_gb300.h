@@ -265,7 +265,7 @@ int cc_sb_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* masks
 /* Number of kernels the last call on this handle launched. */
 uint64_t cc_last_launch_count(cc_handle* h);
 
-/* Autotuner (no reference counterpart).  Times each of the three
+/* Autotuner (no reference counterpart).  Times each of the four
  * evaluation passes of cc_tight_eval_device with every register budget
  * (minimum resident blocks 1, 4, 8: at most 255, 128, 64 registers per
  * thread) and grid size (2, 4, 8, 16 blocks of 128 threads per SM) on the
@@ -273,25 +273,35 @@ uint64_t cc_last_launch_count(cc_handle* h);
  * fastest per pass in the handle for later evaluation calls.  The defaults
  * are 1 and 8. */
 typedef struct cc_tune_result {
-    int min_blocks[3];     /* chosen register budget of main, strip-width, gap-width pass */
-    int blocks_per_sm[3];  /* chosen grid */
-    float ms[3];           /* time of each pass with the chosen setting */
-    float ms_default[3];   /* time with the defaults */
+    int min_blocks[4];     /* chosen register budget of the FP32, FP64, strip-width and gap-width pass */
+    int blocks_per_sm[4];  /* chosen grid */
+    float ms[4];           /* time of each pass with the chosen setting */
+    float ms_default[4];   /* time with the defaults */
 } cc_tune_result;
 int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint32_t* masks, cc_tune_result* out);
 
 /* Per-stage device timing (no reference counterpart; a measurement aid).
  * While enabled, cc_tight_eval_device records a CUDA event around each of
- * its three kernels on the stream it launches on:
- *   stage 0 = k_eval_main  (all criteria except the two bisections),
- *   stage 1 = k_eval_cover (strip-width bisection of the compacted queue),
- *   stage 2 = k_eval_gaps  (gap-width bisection of the compacted queue).
+ * its four kernels on the stream it launches on:
+ *   stage 0 = k_eval_f32   (all criteria on FP32 enclosures of the FP64
+ *                           values, one kernel per criterion group, and
+ *                           k_eval_collect, which queues the boxes they could
+ *                           not decide and the bisection jobs),
+ *   stage 1 = k_eval_main  (the FP64 criteria on the queued boxes),
+ *   stage 2 = k_eval_cover (strip-width bisection of the compacted queue),
+ *   stage 3 = k_eval_gaps  (gap-width bisection of the compacted queue).
  * cc_last_stage_times waits for the last recorded event and writes the
  * elapsed milliseconds of each stage of the most recent call (at most
  * max_stages values; *n_stages = how many were written). */
-#define CC_EVAL_STAGES 3
+#define CC_EVAL_STAGES 4
 int cc_set_stage_timing(cc_handle* h, int enable);
 int cc_last_stage_times(cc_handle* h, float* ms, int max_stages, int* n_stages);
+/* Queue sizes of the most recent evaluation batch (waits for the device):
+ * counts[0] boxes the FP32 pass left to the FP64 pass, counts[1] boxes that
+ * needed the strip-width bisection, counts[2] the gap-width bisection,
+ * counts[3] nonzero if a queue overflowed (cannot happen: each queue holds
+ * the whole batch). */
+int cc_last_eval_counts(cc_handle* h, unsigned long long* counts);
 
 /* Run the tight proof from `root` with split counts `grid`.  On success
  * *criticals points to *n_crit boxes (release with cc_free), in the order the

@@ -73,7 +73,7 @@ def test_eval_device_soa(prover, port):
     assert np.array_equal(got, port.tight_eval(boxes, threads=16))
 
 
-def test_stage_timing_times_three_kernels_without_changing_masks(prover, port):
+def test_stage_timing_times_four_kernels_without_changing_masks(prover, port):
     import torch
     boxes = W.tight_microbench(40_000, seed=32)
     soa = torch.from_numpy(W.to_soa(boxes)).cuda()
@@ -85,7 +85,7 @@ def test_stage_timing_times_three_kernels_without_changing_masks(prover, port):
     prover.tight_eval_device(soa.data_ptr(), len(boxes), masks.data_ptr())
     ms = prover.stage_times()
     prover.set_stage_timing(False)
-    assert len(ms) == 3 and all(t > 0 for t in ms)
+    assert len(ms) == 4 and all(t > 0 for t in ms)
     assert np.array_equal(masks.cpu().numpy().view(np.uint32), port.tight_eval(boxes, threads=16))
 
 
@@ -155,7 +155,7 @@ def test_autotuned_passes_give_the_same_masks(prover, port):
     masks = torch.zeros(len(boxes), dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     rep = prover.autotune_eval(soa.data_ptr(), len(boxes), masks.data_ptr())
-    assert set(rep) == {"k_eval_main", "k_eval_cover", "k_eval_gaps"}
+    assert set(rep) == {"k_eval_f32", "k_eval_main", "k_eval_cover", "k_eval_gaps"}
     for r in rep.values():
         assert r["min_blocks"] in (1, 4, 8) and r["blocks_per_sm"] in (2, 4, 8, 16)
         assert r["ms"] <= r["ms_default"] * 1.0001
