@@ -18,10 +18,12 @@
 #define CC_FN __device__ __forceinline__
 #define CC_FN_NOINLINE static __device__ __noinline__
 #define CC_FN_INL __device__ inline
+#define CC_METHOD __device__ __forceinline__
 #else
 #define CC_FN static inline
 #define CC_FN_NOINLINE static
 #define CC_FN_INL static inline
+#define CC_METHOD inline
 #endif
 
 namespace cc {

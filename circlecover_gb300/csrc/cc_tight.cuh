@@ -56,7 +56,7 @@ template <class I>
 CC_FN I ratio_two_disk(I la) { return 0.25 * la + 0.5 * reciprocal(la); }
 
 template <class I>
-CC_FN I critical_ratio(I la) {
+CC_FN I critical_ratio_t(I la) {
     if (definitely(la <= kBreakEvenLo)) {
         return ratio_three_disk(la);
     }
@@ -68,9 +68,16 @@ CC_FN I critical_ratio(I la) {
     return I{lesser(a.lo, b.lo), greater(b.hi, a.hi)};
 }
 
+CC_FN Iv critical_ratio(Iv la) { return critical_ratio_t(la); }
+#if CC_DEVICE_BUILD
+// one out-of-line copy of each FP32 form: the criteria call them from many
+// sites, and the evaluation kernels must stay small for the instruction cache
+__device__ __noinline__ inline f32::IvF critical_ratio(f32::IvF la) { return critical_ratio_t(la); }
+#endif
+
 // ratio for a w x h rectangle in either orientation (critical_ratio.cu:32-52)
 template <class I>
-CC_FN I critical_ratio(I w, I h) {
+CC_FN I critical_ratio_t(I w, I h) {
     if (w.hi <= h.lo) {
         return critical_ratio(h / w);
     }
@@ -85,6 +92,10 @@ CC_FN I critical_ratio(I w, I h) {
     I b = critical_ratio(wide);
     return I{lesser(a.lo, b.lo), greater(b.hi, a.hi)};
 }
+CC_FN Iv critical_ratio(Iv w, Iv h) { return critical_ratio_t(w, h); }
+#if CC_DEVICE_BUILD
+__device__ __noinline__ inline f32::IvF critical_ratio(f32::IvF w, f32::IvF h) { return critical_ratio_t(w, h); }
+#endif
 
 template <class I>
 CC_FN I required_weight_for(I w, I h) { return critical_ratio(w, h) * w * h; }  // critical_ratio.cu:80-82
@@ -402,12 +413,28 @@ CC_FN double bisect_all_true(double lo, double hi) {
 __device__ __forceinline__ bool f32_step_for_all(int d) { return __all_sync(__activemask(), d != f32::UNKNOWN); }
 #endif
 
-CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
+// A criterion that ends with a bisection needs only its final check of the
+// bisection's result, and that result always lies in the current bracket
+// [lo, hi].  So the bisections take `early(lo, hi)`: on the device it is
+// asked before the first step and where the FP32 steps end for the final
+// check's outcome for every result in [lo, hi] (FP32 enclosures: YES, NO or
+// UNKNOWN), and a decided answer ends the bisection (*decided; for finite
+// brackets only, where the bisection cannot reach its cap, so no trap is
+// skipped).  NoEarly never decides.
+struct NoEarly {
+    CC_METHOD int operator()(double, double) const { return -1; }
+};
+
+template <class Early>
+CC_FN double cover_strip_width_early(double la_hi, double r1, double r2, double r3, Early early, int* decided) {
     double lo = 0.3;
     double hi = la_hi;
+    *decided = -1;
 #if CC_DEVICE_BUILD
+    const bool finite = lo < hi && hi <= CC_DBL_MAX;
+    if (finite && (*decided = early(lo, hi)) != f32::UNKNOWN) return lo;
     const StripF32 pf = strip_f32_prepare(r1, r2, r3);
-    if (lo < hi && hi <= CC_DBL_MAX) {
+    if (finite) {
         int whole = strip_width_realizable_f32(pf, f32::Fv{__double2float_rd(lo), __double2float_ru(hi)});
         if (whole == f32::NO) return lo;
         if (whole == f32::YES) return bisect_all_true(lo, hi);
@@ -429,7 +456,10 @@ CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
         if (f32_steps && f32_step_for_all(d)) {
             ok = d == f32::YES;
         } else {
-            f32_steps = false;
+            if (f32_steps) {
+                f32_steps = false;
+                if (finite && (*decided = early(lo, hi)) != f32::UNKNOWN) return lo;
+            }
             ok = strip_width_realizable(r1, r2, r3, mid);
         }
 #else
@@ -442,6 +472,11 @@ CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
         }
     }
     return lo;
+}
+
+CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
+    int decided;
+    return cover_strip_width_early(la_hi, r1, r2, r3, NoEarly{}, &decided);
 }
 
 template <class S>
@@ -799,13 +834,16 @@ CC_FN bool gaps_enters(double r1, double r2, GapsStart& g) {
     return true;
 }
 
-CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
+template <class Early>
+CC_FN double gaps_width_early(double r1, double r2, double r4, GapsStart g, Early early, int* decided) {
     const double w1 = g.w1, w2 = g.w2;
     double lo = 0.0, hi = add_dn(sqrt_dn(r1), sqrt_dn(r2));
+    *decided = -1;
 #if CC_DEVICE_BUILD
-    // FP32 shortcuts: see bisect_all_true
+    // FP32 shortcuts: see bisect_all_true and cover_strip_width_early
+    const bool finite = lo < hi && hi <= CC_DBL_MAX;
     const GapsF32 pf = gaps_f32_prepare(r1, r2, w1, w2, r4);
-    if (lo < hi && hi <= CC_DBL_MAX) {
+    if (finite) {
         int whole = gap_width_realizable_f32(f32::Fv{0.0f, __double2float_ru(hi)}, pf);
         if (whole == f32::NO) return lo;
         if (whole == f32::YES) return bisect_all_true(lo, hi);
@@ -827,7 +865,10 @@ CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
         if (f32_steps && f32_step_for_all(d)) {
             ok = d == f32::YES;
         } else {
-            f32_steps = false;
+            if (f32_steps) {
+                f32_steps = false;
+                if (finite && (*decided = early(lo, hi)) != f32::UNKNOWN) return lo;
+            }
             ok = gap_width_realizable(mid, r1, w1, r2, w2, r4);
         }
 #else
@@ -840,6 +881,11 @@ CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
         }
     }
     return lo;
+}
+
+CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
+    int decided;
+    return gaps_width_early(r1, r2, r4, g, NoEarly{}, &decided);
 }
 
 template <class S>
@@ -1043,15 +1089,28 @@ CC_FN_INL uint32_t eval_group_f32(const Box& in64) {
 // FP64.  Same result and trap bit as cover_pass / gaps_pass on eval_main's
 // jobs.
 CC_FN_INL uint32_t cover_pass_box(const Box& b) {
-    trap_clear();
+    using f32::Fv;
     const Iv la = b.la, r1 = b.r[0], r2 = b.r[1], r3 = b.r[2];
-    const double width = cover_strip_width(la.hi, r1.lo, r2.lo, r3.lo);
-    uint32_t trapped = trap_status();
     trap_clear();
     const BoxT<f32::IvF> e = enclose(b);
-    const f32::Fv lb_R4 = (required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2]).lo;
-    bool ok = cover_strip_finish<f32::Fv>(la.hi, width, b.r[3].hi, lb_R4);
-    if (trap_status() != TRAP_NONE) {
+    const Fv lb_R4 = (required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2]).lo;
+    const bool lb_ok = trap_status() == TRAP_NONE;
+    trap_clear();
+    // cover_strip_finish for every width in [lo, hi]
+    auto finish = [&](double lo, double hi) -> int {
+        if (!lb_ok) return f32::UNKNOWN;
+        bool ok = cover_strip_finish<Fv>(la.hi, Fv{__double2float_rd(lo), __double2float_ru(hi)}, b.r[3].hi, lb_R4);
+        int d = trap_status() == TRAP_NONE ? (ok ? f32::YES : f32::NO) : f32::UNKNOWN;
+        trap_clear();  // no trap can be pending where this is asked
+        return d;
+    };
+    int decided;
+    const double width = cover_strip_width_early(la.hi, r1.lo, r2.lo, r3.lo, finish, &decided);
+    if (decided != f32::UNKNOWN) return decided == f32::YES ? (1u << 2) : 0u;
+    uint32_t trapped = trap_status();
+    trap_clear();
+    bool ok = lb_ok ? cover_strip_finish<Fv>(la.hi, width, b.r[3].hi, lb_R4) : false;
+    if (!lb_ok || trap_status() != TRAP_NONE) {
         trap_clear();
         ok = cover_strip_finish<double>(la.hi, width, b.r[3].hi, (required_weight_for(la) - r1 - r2 - r3).lo);
         trapped |= trap_status();
@@ -1062,6 +1121,7 @@ CC_FN_INL uint32_t cover_pass_box(const Box& b) {
 }
 
 CC_FN_INL uint32_t gaps_pass_box(const Box& b) {
+    using f32::Fv;
     trap_clear();
     Box v = b;
     tighten_lb(v.r[2], v.r[3].lo);
@@ -1071,14 +1131,27 @@ CC_FN_INL uint32_t gaps_pass_box(const Box& b) {
     if (!gaps_enters(v.r[0].lo, v.r[1].lo, g)) {
         return 0u;
     }
-    const double gap = gaps_width(v.r[0].lo, v.r[1].lo, v.r[3].lo, g);
-    uint32_t trapped = trap_status();
-    trap_clear();
     BoxT<f32::IvF> e = enclose(v);
     f32::IvF R = required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2] - e.r[3];
     tighten_lb(R, 0.0);
-    bool ok = gaps_finish_t<f32::Fv>(b.la.hi, g.w1, g.w2, gap, v.r[3].hi, R.lo, R.hi);
-    if (trap_status() != TRAP_NONE) {
+    const bool R_ok = trap_status() == TRAP_NONE;
+    trap_clear();
+    // gaps_finish for every gap width in [lo, hi]
+    auto finish = [&](double lo, double hi) -> int {
+        if (!R_ok) return f32::UNKNOWN;
+        bool ok = gaps_finish_t<Fv>(b.la.hi, g.w1, g.w2, Fv{__double2float_rd(lo), __double2float_ru(hi)}, v.r[3].hi,
+                                    R.lo, R.hi);
+        int d = trap_status() == TRAP_NONE ? (ok ? f32::YES : f32::NO) : f32::UNKNOWN;
+        trap_clear();  // no trap can be pending where this is asked
+        return d;
+    };
+    int decided;
+    const double gap = gaps_width_early(v.r[0].lo, v.r[1].lo, v.r[3].lo, g, finish, &decided);
+    if (decided != f32::UNKNOWN) return decided == f32::YES ? (1u << 5) : 0u;
+    uint32_t trapped = trap_status();
+    trap_clear();
+    bool ok = R_ok ? gaps_finish_t<Fv>(b.la.hi, g.w1, g.w2, gap, v.r[3].hi, R.lo, R.hi) : false;
+    if (!R_ok || trap_status() != TRAP_NONE) {
         trap_clear();
         Iv R64 = required_weight_for(v.la) - v.r[0] - v.r[1] - v.r[2] - v.r[3];
         tighten_lb(R64, 0.0);

@@ -291,3 +291,38 @@ def test_fp32_bisection_decisions_equal_fp64(prover, which):
     got, trapped = prover.selftest_bisection_width(which, args)
     assert not trapped.any()
     assert np.array_equal(got.view(np.uint64), fix.view(np.uint64))
+
+
+def _adversarial_boxes(n, seed):
+    """Boxes with degenerate and extreme bounds: point intervals, empty
+    intervals (lo > hi), zero and negative bounds, widths from 0 to huge,
+    bounds near the float range limits, DBL_MAX, infinities and NaNs."""
+    rng = np.random.default_rng(seed)
+    base = W.tight_microbench(n, seed=seed)
+    b = base.copy()
+    flat = b.view(np.float64).reshape(n, 10)
+    specials = np.array([0.0, -0.0, 1e-45, 1e-39, 1e-30, 1e30, 3.5e38, 1e300, W.DBL_MAX, np.inf, -1e-3, 0.25,
+                         0.5, 1.0, 2.0, np.nan], dtype=np.float64)
+    kind = rng.integers(0, 6, n)
+    for col in range(10):
+        pick = rng.random(n) < 0.15
+        flat[pick, col] = rng.choice(specials, pick.sum())
+    pt = kind == 1  # point intervals
+    flat[pt, 1::2] = flat[pt, 0::2]
+    sw = kind == 2  # empty intervals: bounds swapped
+    flat[sw, 0::2], flat[sw, 1::2] = flat[sw, 1::2].copy(), flat[sw, 0::2].copy()
+    tiny = kind == 3  # widths at the FP64 resolution
+    with np.errstate(over="ignore"):
+        flat[tiny, 1::2] = np.nextafter(flat[tiny, 0::2], np.inf)
+    return b
+
+
+def test_eval_adversarial_boxes_match_port(prover, port):
+    """The FP32-first evaluation on degenerate, empty, huge, tiny, infinite
+    and NaN bounds gives the port's masks bit for bit (trap bits included)."""
+    for seed in (71, 72):
+        boxes = _adversarial_boxes(1 << 16, seed)
+        got = prover.tight_eval(boxes)
+        want = port.tight_eval(boxes, threads=16)
+        bad = np.nonzero(got != want)[0]
+        assert len(bad) == 0, (seed, bad[:8], got[bad[:8]], want[bad[:8]])
