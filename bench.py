@@ -238,12 +238,12 @@ def run_ours(args, ws, rank, local):
     e2e = None
     if not args.no_e2e:
         host_boxes = np.ascontiguousarray(boxes)
-        prover.tight_eval(host_boxes[: 1 << 16])
+        prover.tight_eval(host_boxes)  # warm-up at full size: the entry point's buffers grow once
         barrier()
         t0 = time.perf_counter()
-        for _ in range(max(1, args.steps // 2)):
+        for _ in range(args.steps):
             out = prover.tight_eval(host_boxes)
-        dt = (time.perf_counter() - t0) / max(1, args.steps // 2)
+        dt = (time.perf_counter() - t0) / args.steps
         if ws > 1:
             t = torch.tensor([dt], device="cuda", dtype=torch.float64)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -276,10 +276,14 @@ def run_ours(args, ws, rank, local):
                      "ops_per_box": stage_ops[dom], "stages": stages,
                      "step": {"achieved": step_achieved / 1e12, "frac": step_achieved / peak,
                               "ops_per_box": ops_per_box},
-                     "note": "achieved = the reference's directed-rounding ops per box that this kernel executes "
-                             "(shim-counted) x boxes / the kernel's mean CUDA-event time; peak = FP64 directed "
-                             "add/mul instruction rate measured by this bench on this GPU (MEASURED_PEAKS.json "
-                             "holds no FP64 figure); traffic = ncu DRAM bytes per launch (profiles/)"},
+                     "note": "achieved = the reference's FP64 directed-rounding ops per box that this pass "
+                             "settles (shim-counted on the reference) x boxes / the pass's mean CUDA-event time "
+                             "(FP64-equivalent rate); peak = FP64 directed add/mul instruction rate measured by "
+                             "this bench on this GPU (MEASURED_PEAKS.json holds no FP64 figure).  The FP32 pass "
+                             "settles ~99% of the boxes' criteria with FP32 enclosures of the FP64 values (same "
+                             "decisions), so a frac above 1 is work the FP64 pipe did not have to do, not an "
+                             "error; the pass itself is bound by instruction issue (divergent branchy criteria, "
+                             "instruction-cache misses: profiles/).  traffic = ncu DRAM bytes per full-size pass"},
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": ck,
         "e2e": e2e,

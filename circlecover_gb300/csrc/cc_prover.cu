@@ -380,6 +380,13 @@ int cc_create(cc_handle** out, int device) {
         cudaGetLastError();
         return CC_ERR_NO_DEVICE;
     }
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        cudaGetLastError();
+        pageable = 0;
+    }
+    const char* staging = std::getenv("CC_HOST_STAGING");
+    h->pageable_access = pageable == 1 && !(staging && staging[0] == '1');
     // the kernels must exist for this device (built for sm_103a only)
     cudaFuncAttributes attr;
     if (cudaFuncGetAttributes(&attr, k_selftest_subinterval) != cudaSuccess) {
@@ -403,6 +410,10 @@ int cc_destroy(cc_handle* h) {
     for (auto& e : h->stage_ev)
         if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->stream2) {
+        cudaStreamSynchronize(h->stream2);
+        cudaStreamDestroy(h->stream2);
+    }
     delete h;
     return CC_OK;
 }
@@ -605,60 +616,95 @@ extern "C" int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t
     return CC_OK;
 }
 
-// Host-memory entry point: boxes are staged through pinned memory in chunks,
-// copied, evaluated in AoS form on the device, and the masks copied back; the
-// copy of chunk k+1 overlaps the evaluation of chunk k (two buffers, one
-// stream each direction is not needed: one stream, async copies).
+// AoS boxes (80 bytes each) to the SoA layout of the evaluation passes.
+// Consecutive threads load consecutive 16-byte pairs (a warp reads 512
+// contiguous bytes per load), which matters when `aos` is host memory read
+// over the host link.
+__global__ void __launch_bounds__(256) k_aos_to_soa(const double* __restrict__ aos, size_t n, double* __restrict__ soa) {
+    const double2* __restrict__ src = reinterpret_cast<const double2*>(aos);
+    for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < 5 * n; j += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = src[j];
+        const size_t i = j / 5, c = 2 * (j - 5 * i);
+        soa[c * n + i] = v.x;
+        soa[(c + 1) * n + i] = v.y;
+    }
+}
+
+
+// Host-memory entry point.  The boxes move to the device in chunks of 4M by
+// the copy engine, on a second stream, so that chunk k+1 travels while chunk
+// k is evaluated: straight from the caller's array where the device reaches
+// pageable host memory through the host's page tables (GB300 with its host
+// over NVLink-C2C: ~190 GB/s measured), otherwise through two pinned buffers
+// that host threads fill (one thread copies at a fraction of the host's
+// memory bandwidth).  On the evaluation stream each chunk is transposed to
+// SoA in device memory and evaluated by the same passes as
+// cc_tight_eval_device; the masks of all chunks return in one copy at the end.
 int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* masks) {
     if (!h || (n && (!boxes || !masks))) return CC_ERR_PARAM;
     h->launches = 0;
     if (n == 0) return CC_OK;
     CC_CUDA(h, cudaSetDevice(h->device));
-    const size_t chunk = n < ((size_t)1 << 21) ? n : ((size_t)1 << 21);
+    const bool direct = h->pageable_access;
+    const size_t chunk = n < ((size_t)1 << 22) ? n : ((size_t)1 << 22);
     const size_t in_bytes = chunk * sizeof(cc_tight_box);
-    const size_t out_bytes = chunk * sizeof(uint32_t);
-    void* d_in[2];
-    void* d_out[2];
-    for (int k = 0; k < 2; ++k) {
-        int st = ccrt::ensure(h, 0 + k, in_bytes, &d_in[k]);
-        if (st) return st;
-        st = ccrt::ensure(h, 2 + k, out_bytes, &d_out[k]);
-        if (st) return st;
-    }
-    int st = ccrt::ensure_pinned(h, 2 * (in_bytes + out_bytes));
+    void *d_aos[2], *d_soa, *d_masks;
+    int st = CC_OK;
+    for (int b = 0; b < 2 && !st; ++b) st = ccrt::ensure(h, 0 + b, in_bytes, &d_aos[b]);
+    if (!st) st = ccrt::ensure(h, 4, in_bytes, &d_soa);
+    if (!st) st = ccrt::ensure(h, 2, n * sizeof(uint32_t), &d_masks);
+    if (!st && !direct) st = ccrt::ensure_pinned(h, 2 * in_bytes);
     if (st) return st;
-    char* pin = (char*)h->pinned;
-    char* pin_in[2] = {pin, pin + in_bytes};
-    char* pin_out[2] = {pin + 2 * in_bytes, pin + 2 * in_bytes + out_bytes};
-    cudaEvent_t done[2];
-    CC_CUDA(h, cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming));
-    CC_CUDA(h, cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming));
-    size_t prev_off[2] = {0, 0}, prev_cnt[2] = {0, 0};
-    int k = 0;
-    for (size_t off = 0; off < n; off += chunk, k ^= 1) {
-        size_t cnt = n - off < chunk ? n - off : chunk;
-        // wait until this buffer's previous chunk is done, then hand out its masks
-        if (prev_cnt[k]) {
-            CC_CUDA(h, cudaEventSynchronize(done[k]));
-            std::memcpy(masks + prev_off[k], pin_out[k], prev_cnt[k] * sizeof(uint32_t));
-        }
-        std::memcpy(pin_in[k], boxes + off, cnt * sizeof(cc_tight_box));
-        CC_CUDA(h, cudaMemcpyAsync(d_in[k], pin_in[k], cnt * sizeof(cc_tight_box), cudaMemcpyHostToDevice, h->stream));
-        st = eval_batch<Layout::AoS>(h, (const double*)d_in[k], cnt, (uint32_t*)d_out[k], h->stream);
-        if (st) return st;
-        CC_CUDA(h, cudaMemcpyAsync(pin_out[k], d_out[k], cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-        CC_CUDA(h, cudaEventRecord(done[k], h->stream));
-        prev_off[k] = off;
-        prev_cnt[k] = cnt;
+    char* pin[2] = {(char*)h->pinned, (char*)h->pinned + in_bytes};
+    if (!h->stream2) CC_CUDA(h, cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
+    cudaEvent_t moved[2], used[2];
+    for (int b = 0; b < 2; ++b) {
+        CC_CUDA(h, cudaEventCreateWithFlags(&moved[b], cudaEventDisableTiming));
+        CC_CUDA(h, cudaEventCreateWithFlags(&used[b], cudaEventDisableTiming));
     }
+    auto fail_cuda = [&](cudaError_t e) { return ccrt::fail(h, CC_ERR_CUDA, "cc_tight_eval", e); };
+    cudaError_t e = cudaSuccess;
+    int b = 0;
+    for (size_t off = 0; off < n && e == cudaSuccess && st == CC_OK; off += chunk, b ^= 1) {
+        const size_t cnt = n - off < chunk ? n - off : chunk;
+        const size_t bytes = cnt * sizeof(cc_tight_box);
+        if (off >= 2 * chunk) {
+            // d_aos[b] (and pin[b]) are free once chunk k-2 has been transposed
+            e = cudaStreamWaitEvent(h->stream2, used[b], 0);
+            if (e == cudaSuccess && !direct) e = cudaEventSynchronize(used[b]);
+            if (e != cudaSuccess) break;
+        }
+        if (direct) {
+            e = cudaMemcpyAsync(d_aos[b], boxes + off, bytes, cudaMemcpyHostToDevice, h->stream2);
+        } else {
+            const cc_tight_box* src = boxes + off;
+            char* dst = pin[b];
+            ccrt::parallel_blocks(cnt, [&](size_t lo, size_t hi) {
+                std::memcpy(dst + lo * sizeof(cc_tight_box), src + lo, (hi - lo) * sizeof(cc_tight_box));
+            });
+            e = cudaMemcpyAsync(d_aos[b], dst, bytes, cudaMemcpyHostToDevice, h->stream2);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(moved[b], h->stream2);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, moved[b], 0);
+        if (e != cudaSuccess) break;
+        k_aos_to_soa<<<h->sm_count * 8, 256, 0, h->stream>>>((const double*)d_aos[b], cnt, (double*)d_soa);
+        CC_LAUNCHED(h);
+        e = cudaEventRecord(used[b], h->stream);
+        if (e != cudaSuccess) break;
+        st = eval_batch<Layout::SoA>(h, (const double*)d_soa, cnt, (uint32_t*)d_masks + off, h->stream);
+    }
+    if (e == cudaSuccess && st == CC_OK)
+        e = cudaMemcpyAsync(masks, d_masks, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t e2 = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = e2;
+    e2 = cudaStreamSynchronize(h->stream2);
+    if (e == cudaSuccess) e = e2;
     for (int j = 0; j < 2; ++j) {
-        if (prev_cnt[j]) {
-            CC_CUDA(h, cudaEventSynchronize(done[j]));
-            std::memcpy(masks + prev_off[j], pin_out[j], prev_cnt[j] * sizeof(uint32_t));
-        }
+        cudaEventDestroy(moved[j]);
+        cudaEventDestroy(used[j]);
     }
-    cudaEventDestroy(done[0]);
-    cudaEventDestroy(done[1]);
+    if (st) return st;
+    if (e != cudaSuccess) return fail_cuda(e);
     return CC_OK;
 }
 

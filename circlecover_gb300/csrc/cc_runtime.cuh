@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/circlecover_gb300.h"
@@ -49,6 +50,12 @@ struct cc_handle {
     int stages_recorded = 0;
     // queue counters of the last evaluation batch (device memory)
     unsigned long long* eval_counts = nullptr;
+    // kernels may read and write ordinary (pageable) host memory
+    // (cudaDevAttrPageableMemoryAccess, e.g. over NVLink-C2C with the host's
+    // page tables); CC_HOST_STAGING=1 in the environment turns this off
+    bool pageable_access = false;
+    // second stream for transfers that overlap evaluation (created on first use)
+    cudaStream_t stream2 = nullptr;
 };
 
 namespace ccrt {
@@ -111,6 +118,28 @@ inline int ensure_pinned(cc_handle* h, size_t bytes) {
         h->pinned_bytes = bytes;
     }
     return CC_OK;
+}
+
+// Host-side parallel loop over [0, n) in contiguous blocks, for the staging
+// copies of the host-memory entry points (one thread streams memory at a
+// fraction of what the host's memory system delivers).  Small ranges run on
+// the calling thread.
+template <class F>
+inline void parallel_blocks(size_t n, F f) {
+    unsigned t = std::thread::hardware_concurrency();
+    t = t < 1 ? 1 : (t > 16 ? 16 : t);
+    if (n < ((size_t)1 << 16) || t == 1) {
+        f((size_t)0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    const size_t per = (n + t - 1) / t;
+    for (unsigned k = 1; k < t; ++k) {
+        size_t lo = k * per, hi = lo + per < n ? lo + per : n;
+        if (lo < hi) pool.emplace_back(f, lo, hi);
+    }
+    f((size_t)0, per < n ? per : n);
+    for (auto& th : pool) th.join();
 }
 
 }  // namespace ccrt

@@ -220,7 +220,12 @@ const char* cc_last_error(cc_handle* h);
 
 /* Evaluate the six tight criteria on n boxes given in HOST memory (AoS);
  * verdict masks (CC_TV_*) are written to host memory.  Includes the
- * host<->device copies. */
+ * host<->device transfers: where the device can access pageable host memory
+ * (cudaDevAttrPageableMemoryAccess, e.g. GB300 with its host over
+ * NVLink-C2C) its kernels read the boxes and write the masks in place;
+ * otherwise they are staged through pinned buffers by host threads.  The
+ * environment variable CC_HOST_STAGING=1, read when the handle is created,
+ * forces the staging path. */
 int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* masks);
 
 /* Same on DEVICE memory: `soa` holds 10 arrays of n doubles each, in the order

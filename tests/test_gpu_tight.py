@@ -326,3 +326,28 @@ def test_eval_adversarial_boxes_match_port(prover, port):
         want = port.tight_eval(boxes, threads=16)
         bad = np.nonzero(got != want)[0]
         assert len(bad) == 0, (seed, bad[:8], got[bad[:8]], want[bad[:8]])
+
+
+def test_host_entry_staging_and_direct_paths_agree(port):
+    """cc_tight_eval through pinned staging (CC_HOST_STAGING=1) and, where the
+    device can access pageable host memory, in place, on a batch larger than
+    one chunk of either path, equals the port."""
+    import os
+    boxes = W.tight_microbench((1 << 23) + 12345, seed=81)
+    sample = np.r_[0:4096, (1 << 21) - 2048:(1 << 21) + 2048, len(boxes) - 4096:len(boxes)]
+    want = port.tight_eval(boxes[sample], threads=16)
+    old = os.environ.get("CC_HOST_STAGING")
+    try:
+        for staging in ("1", "0"):
+            os.environ["CC_HOST_STAGING"] = staging
+            p = cg.Prover(0)
+            try:
+                got = p.tight_eval(boxes)
+            finally:
+                p.close()
+            assert np.array_equal(got[sample], want), staging
+    finally:
+        if old is None:
+            os.environ.pop("CC_HOST_STAGING", None)
+        else:
+            os.environ["CC_HOST_STAGING"] = old
