@@ -936,7 +936,7 @@ enum { S_CELL_FEAT = 32, S_CELL_LOGITS, S_CELL_LOG };
 // (without side effects on `out`/`tot`) when a device queue ran full.
 int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, size_t b, int k, const int s[4], Caps caps,
               std::vector<cc_tight_box>& out, GenTotals& tot, unsigned long long task_base, bool hoist, int flags,
-              unsigned long long task_lo, unsigned long long task_hi) {
+              unsigned long long task_lo, unsigned long long task_hi, double* demand = nullptr) {
     const bool learned = hoist && (flags & CC_PROVE_LEARNED);
     const bool log_cells = hoist && (flags & CC_PROVE_LOG_CELLS);
     const size_t np = b - a;
@@ -1006,12 +1006,6 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
             }
             h->cell_log_splits = s[3];
         }
-        k_stage4a<true, true><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf,
-                                                 (Leaf2*)d_leaf2, caps, cnt, task_base);
-        CC_LAUNCHED(h);
-        k_stage4a2<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf2*)d_leaf2, (Leaf*)d_leaf, caps,
-                                      cnt, task_base);
-        CC_LAUNCHED(h);
     } else {
         k_stage1<false><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (int)ntasks, s[0], (Cell2*)d_c2, caps, cnt,
                                            task_base);
@@ -1022,20 +1016,56 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
         k_stage3<false><<<g, 128, 0, sm>>>((const Box*)d_par, (const Task*)d_tasks, (const Cell3*)d_c3, s[2], (Cell4*)d_c4,
                                            caps, cnt, task_base);
         CC_LAUNCHED(h);
-        k_stage4a<false, false><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], (Leaf*)d_leaf,
-                                                   nullptr, caps, cnt, task_base);
+    }
+    // The leaf stages run over slices of the r3 cells small enough that the
+    // leaf queues cannot overflow (each cell has s[3] leaves; the queues are
+    // emptied between slices), so a chunk never has to be redone for them.
+    unsigned long long n_c4 = 0;
+    CC_CUDA(h, cudaMemcpyAsync(&n_c4, &cnt->n_cell4, sizeof(n_c4), cudaMemcpyDeviceToHost, sm));
+    CC_CUDA(h, cudaStreamSynchronize(sm));
+    if (n_c4 > caps.cell4) n_c4 = 0;  // stage 3 overflowed: the chunk is retried smaller
+    unsigned long long room = std::min(caps.leaf, caps.gaps);
+    if (hoist) room = std::min(room, caps.leaf2);
+    const unsigned long long slice = std::max<unsigned long long>(1, room / (unsigned long long)s[3]);
+    for (unsigned long long c0 = 0; c0 < n_c4; c0 += slice) {
+        const unsigned long long c1 = std::min(n_c4, c0 + slice);
+        if (c0) {  // the previous slice's leaf queues are consumed
+            CC_CUDA(h, cudaMemsetAsync(&cnt->n_leaf, 0, 2 * sizeof(unsigned long long), sm));  // n_leaf, n_gaps
+            CC_CUDA(h, cudaMemsetAsync(&cnt->n_leaf2, 0, sizeof(unsigned long long), sm));
+        }
+        if (hoist) {
+            k_stage4a<true, true><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], c0, c1,
+                                                     (Leaf*)d_leaf, (Leaf2*)d_leaf2, caps, cnt, task_base);
+            CC_LAUNCHED(h);
+            k_stage4a2<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf2*)d_leaf2, (Leaf*)d_leaf,
+                                          caps, cnt, task_base);
+            CC_LAUNCHED(h);
+            k_stage4b<true><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3],
+                                               (GapsLeaf*)d_gaps, (Critical*)d_crit, caps, cnt, task_base);
+        } else {
+            k_stage4a<false, false><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], c0, c1,
+                                                       (Leaf*)d_leaf, nullptr, caps, cnt, task_base);
+            CC_LAUNCHED(h);
+            k_stage4b<false><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3],
+                                                (GapsLeaf*)d_gaps, (Critical*)d_crit, caps, cnt, task_base);
+        }
+        CC_LAUNCHED(h);
+        k_stage4c<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const GapsLeaf*)d_gaps, s[3],
+                                     (Critical*)d_crit, caps, cnt, task_base);
         CC_LAUNCHED(h);
     }
-    k_stage4b<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3], (GapsLeaf*)d_gaps,
-                                 (Critical*)d_crit, caps, cnt, task_base);
-    CC_LAUNCHED(h);
-    k_stage4c<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const GapsLeaf*)d_gaps, s[3], (Critical*)d_crit,
-                                 caps, cnt, task_base);
-    CC_LAUNCHED(h);
     Counters hc;
     CC_CUDA(h, cudaMemcpyAsync(&hc, cnt, sizeof(Counters), cudaMemcpyDeviceToHost, sm));
     CC_CUDA(h, cudaStreamSynchronize(sm));
-    if (hc.overflow) return CC_ERR_QUEUE_OVERFLOW;
+    if (hc.overflow) {
+        // the queue counters keep counting past their capacity: the first
+        // queue that overflowed tells how much too large this chunk was
+        auto f = [](unsigned long long n, unsigned long long cap) { return cap ? (double)n / (double)cap : 0.0; };
+        double d = std::max({f(hc.n_cell3, caps.cell3), f(hc.n_cell4, caps.cell4), f(hc.n_leaf, caps.leaf),
+                             f(hc.n_gaps, caps.gaps), f(hc.n_crit, caps.crit), hoist ? f(hc.n_leaf2, caps.leaf2) : 0.0});
+        if (demand) *demand = d;
+        return CC_ERR_QUEUE_OVERFLOW;
+    }
     std::vector<Critical> crit(hc.n_crit);
     if (hc.n_crit) {
         CC_CUDA(h, cudaMemcpyAsync(crit.data(), d_crit, hc.n_crit * sizeof(Critical), cudaMemcpyDeviceToHost, sm));
@@ -1069,26 +1099,34 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
     return CC_OK;
 }
 
-// all tasks of one generation, in parent chunks that fit the device queues
+// All tasks of one generation, in chunks of consecutive tasks that fit the
+// device queues.  A chunk may cover part of a parent's lambda pieces (the
+// initial pass has one parent with hundreds of pieces); its criticals are
+// merged per task, so the chunks' lists concatenate in task order.  After an
+// overflow the chunk is retried with the span shrunk by the overflowing
+// queue's demand (its counter keeps counting past the capacity); a single
+// task that overflows doubles the capacities instead.
 int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k, const int s[4],
                    std::vector<cc_tight_box>& out, GenTotals& tot, Caps& caps, bool hoist, int flags,
                    unsigned long long task_lo = 0, unsigned long long task_hi = ~0ULL) {
-    const size_t max_tasks_chunk = 1 << 16;
-    // parents whose tasks meet [task_lo, task_hi)
-    size_t a = (size_t)std::min<unsigned long long>(task_lo / (unsigned long long)k, parents.size());
-    const size_t a_end = (size_t)std::min<unsigned long long>(
-        task_hi == ~0ULL ? parents.size() : (task_hi + (unsigned long long)k - 1) / (unsigned long long)k, parents.size());
-    size_t chunk = std::max<size_t>(1, max_tasks_chunk / (size_t)k);
-    while (a < a_end) {
-        size_t b = std::min(a_end, a + chunk);
+    const unsigned long long n_tasks = (unsigned long long)parents.size() * (unsigned long long)k;
+    unsigned long long t = std::min(task_lo, n_tasks);
+    const unsigned long long t_end = std::min(task_hi, n_tasks);
+    unsigned long long span = 1ULL << 16;
+    while (t < t_end) {
+        const unsigned long long e = std::min(t_end, t + span);
+        const size_t a = (size_t)(t / (unsigned long long)k), b = (size_t)((e - 1) / (unsigned long long)k + 1);
         Caps cp = caps;
-        cp.cell2 = (unsigned long long)(b - a) * k * s[0];
+        cp.cell2 = (e - t) * (unsigned long long)s[0];
         std::vector<cc_tight_box> part;
-        GenTotals t;
-        int st = run_chunk(h, parents, a, b, k, s, cp, part, t, (unsigned long long)a * k, hoist, flags, task_lo, task_hi);
+        GenTotals g;
+        double demand = 0.0;
+        int st = run_chunk(h, parents, a, b, k, s, cp, part, g, (unsigned long long)a * k, hoist, flags, t, e, &demand);
         if (st == CC_ERR_QUEUE_OVERFLOW) {
-            if (b - a > 1) {
-                chunk = std::max<size_t>(1, (b - a) / 2);
+            if (e - t > 1) {
+                const double shrink = demand > 1.0 ? 1.25 * demand : 2.0;
+                span = std::max<unsigned long long>(1, (unsigned long long)((double)(e - t) / shrink));
+                if (span >= e - t) span = (e - t) / 2;
             } else {
                 caps.cell3 *= 2;
                 caps.cell4 *= 2;
@@ -1103,11 +1141,11 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
         if (st) return st;
         out.insert(out.end(), part.begin(), part.end());
         for (int l = 0; l < 4; ++l)
-            for (int o = 0; o < 8; ++o) tot.counts[l][o] += t.counts[l][o];
-        tot.digest += t.digest;
-        tot.leaf_evals += t.leaf_evals;
-        tot.trapped += t.trapped;
-        a = b;
+            for (int o = 0; o < 8; ++o) tot.counts[l][o] += g.counts[l][o];
+        tot.digest += g.digest;
+        tot.leaf_evals += g.leaf_evals;
+        tot.trapped += g.trapped;
+        t = e;
     }
     return CC_OK;
 }
@@ -1178,7 +1216,7 @@ static int prove_generations(cc_handle* h, const cc_tight_grid* grid, int flags,
     h->interrupt.store(0);
     CC_CUDA(h, cudaSetDevice(h->device));
     auto t0 = std::chrono::steady_clock::now();
-    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 22, 1ULL << 20, 1ULL << 26};
+    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 24, 1ULL << 20, 1ULL << 26};
     std::vector<cc_tight_box> next;
     int gens_run = start_gen > 0 ? start_gen - 1 : 0;
     int status = CC_OK;
@@ -1298,7 +1336,7 @@ extern "C" int cc_tight_generation(cc_handle* h, const cc_tight_box* parents, si
     h->launches = 0;
     CC_CUDA(h, cudaSetDevice(h->device));
     auto t0 = std::chrono::steady_clock::now();
-    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 22, 1ULL << 20, 1ULL << 26};
+    Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 24, 1ULL << 20, 1ULL << 26};
     GenTotals tot;
     std::vector<cc_tight_box> in(parents, parents + n_parents), out;
     int st = run_generation(h, in, la_splits, r_splits, out, tot, caps, !(flags & CC_PROVE_PLAIN), flags, task_lo, task_hi);

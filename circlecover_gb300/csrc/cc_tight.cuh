@@ -1083,6 +1083,32 @@ CC_FN_INL uint32_t eval_group_f32(const Box& in64) {
     return trap_status() == TRAP_NONE ? m : kF32Undecided;
 }
 
+// A whole criterion on FP32 enclosures first, then, if undecided, in FP64:
+// the same outcome and trap status as the FP64 criterion alone (a decided
+// FP32 evaluation stands for an FP64 one that did not trap).  The caller's
+// pending trap status is kept.
+template <class Crit>
+CC_FN_INL bool first_f32(Crit crit, const Box& v, Iv rest) {
+    const uint32_t saved = trap_status();
+    trap_clear();
+    const bool ok32 = crit(enclose(v), f32::of(rest));
+    const bool decided = trap_status() == TRAP_NONE;
+    trap_clear();
+    if (saved != TRAP_NONE) trap(saved);
+    return decided ? ok32 : crit(v, rest);
+}
+struct TwoByTwo {
+    template <class I>
+    CC_METHOD bool operator()(const BoxT<I>& v, I R) const { return two_by_two_strategies(v, R); }
+};
+struct LeafR123 {
+    template <class I>
+    CC_METHOD bool operator()(const BoxT<I>& v, I R4) const { return r1_r2_r3_strategies(v, R4); }
+};
+// two_by_two_strategies(v, R) and r1_r2_r3_strategies(v, R4), FP32 first
+CC_FN_INL bool two_by_two_first_f32(const Box& v, Iv R) { return first_f32(TwoByTwo{}, v, R); }
+CC_FN_INL bool r1_r2_r3_leaf_first_f32(const Box& v, Iv R4) { return first_f32(LeafR123{}, v, R4); }
+
 // The two bisection criteria of one box, from the box itself (the queues
 // hold box indices): the bisection in FP64 (with its FP32 shortcuts), then
 // the recursion check first on FP32 enclosures and, if that is undecided, in

@@ -13,6 +13,11 @@
 //   stage 4a (r3 cell, i4)     leaves:    r1_r2_r3_strategies, R, two_by_two
 //                                         (prepared form: two_by_two in stage
 //                                         4a2 on the compacted leaves that need it)
+//
+// In the prepared form the per-leaf criteria (two_by_two, the leaf form of
+// r1_r2_r3_strategies) are evaluated on FP32 enclosures first and in FP64
+// only where those cannot decide (cc_f32.cuh, tight::first_f32): same
+// outcomes and trap status, so the same trace.
 //   stage 4b (leaf queue)      leaves:    r1_r2_r3_strategies(box, R4), gaps precondition
 //   stage 4c (gaps queue)      leaves:    gaps bisection
 //
@@ -380,14 +385,16 @@ __device__ __forceinline__ Box leaf_box(const Cell4& p, Iv la, Iv r4) {
 // form: the leaves that reach the 2x2 criterion (about half of them; its six
 // bisections are the stage's main cost) are compacted into a queue for
 // stage 4a2 instead of being checked here next to lanes that have finished.
+// stage 4a over the r3 cells [cell_lo, cell_hi) (the host runs the leaf
+// stages in slices of cells that the leaf queues can hold)
 template <bool Hoist, bool Split>
 __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks, const Cell4* __restrict__ in, int s4,
+                                                 unsigned long long cell_lo, unsigned long long cell_hi,
                                                  Leaf* __restrict__ out, Leaf2* __restrict__ out2, Caps caps, Counters* c,
                                                  unsigned long long task_base) {
     __shared__ BlockTrace bt;
     trace_init(bt);
-    const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cell4;
-    const unsigned long long total = (n_in < caps.cell4 ? n_in : caps.cell4) * s4;
+    const unsigned long long total = (cell_hi - cell_lo) * s4;
     unsigned long long evals = 0;
     CC_WARP_LOOP(total) {
         unsigned long long idx = base_ + (threadIdx.x & 31);
@@ -399,7 +406,7 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
         Iv r4{0.0, 0.0};
         if (valid) {
             evals += 1;
-            pidx = (uint32_t)(idx / s4);
+            pidx = (uint32_t)(cell_lo + idx / s4);
             i4 = (int)(idx % s4);
             const Cell4& p = in[pidx];
             task = p.task;
@@ -422,7 +429,7 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
                 } else if (Split) {
                     outcome = -3;  // on to stage 4a2
                     if (p.order) {  // learned order: the cheap leaf criterion first
-                        const bool ok4 = tight::r1_r2_r3_strategies(v, p.R4);
+                        const bool ok4 = tight::r1_r2_r3_leaf_first_f32(v, p.R4);
                         if (ok4 && trap_status() == TRAP_NONE) outcome = CC_T_L4_R123LEAF;
                         else if (!ok4) leaf_tried = true;  // (a trap leaves it to the plain order)
                     }
@@ -479,7 +486,7 @@ __global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks
             Box v = leaf_box(p, tk.la, lf.r4);
             Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
             tighten_lb(R, 0.0);
-            bool ok = tight::two_by_two_strategies(v, R);
+            bool ok = tight::two_by_two_first_f32(v, R);
             trapped = (lf.pad & 1) != 0 || trap_status() != TRAP_NONE;
             outcome = (ok && !trapped) ? CC_T_L4_2X2 : -2;
         }
@@ -499,6 +506,9 @@ __device__ __forceinline__ void push_critical(Critical* crit, unsigned long long
 
 // stage 4b: r1_r2_r3_strategies(box, R4); leaves that reach the gaps strategy
 // go on to its bisection in stage 4c (tight_rectangle.cu:246-255)
+// F32: the leaf criterion on FP32 enclosures first (prepared form); the
+// plain form evaluates it in FP64 only, as the reference does
+template <bool F32>
 __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
                                                  const Leaf* __restrict__ in, int s4, GapsLeaf* __restrict__ gq,
                                                  Critical* __restrict__ crit, Caps caps, Counters* c,
@@ -531,7 +541,8 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
             Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
             tighten_lb(R, 0.0);
             tight::GapsStart g;
-            if (!(lf.trapped & 2) && tight::r1_r2_r3_strategies(v, p.R4)) {
+            if (!(lf.trapped & 2) &&
+                (F32 ? tight::r1_r2_r3_leaf_first_f32(v, p.R4) : tight::r1_r2_r3_strategies(v, p.R4))) {
                 outcome = CC_T_L4_R123LEAF;
             } else if (tight::gaps_enters(v.r[0].lo, v.r[1].lo, g)) {
                 need_gaps = true;
