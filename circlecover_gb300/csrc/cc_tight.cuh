@@ -137,8 +137,40 @@ CC_FN bool can_recurse(double ub_w, double ub_h, double ub_largest, double lb_we
     return can_recurse_t<double>(ub_w, ub_h, ub_largest, lb_weight);
 }
 #if CC_DEVICE_BUILD
-// one out-of-line copy for the FP32 evaluation (it is called from many sites)
+// One out-of-line copy for the FP32 evaluation (it is called from many
+// sites), with a shortcut before its costly part.  Where largest_norm is
+// certainly above 9/64, can_recurse_t takes ratio = lesser(ratio_cor,
+// ratio_wh) with ratio_wh the upper bound of the w x h rectangle's critical
+// ratio (critical_ratio(), several interval divisions).  So ratio <=
+// ratio_cor, and ratio >= min(ratio_cor, sqrt(2)/2): every critical ratio is
+// at least sqrt(2)/2 (the two-disk formula lambda/4 + 1/(2 lambda) has that
+// minimum at lambda = sqrt 2; the three-disk one is decreasing on [1,
+// lambda_2] down to its value there, 0.74), and the FP64 upper bound of an
+// enclosure of it is not below the exact value by more than a few ulps
+// (0.7070 leaves a margin of 1e-4); this needs w, h > 0, so that the ratio's
+// argument is an aspect ratio >= 1.  As mul_up is monotone, lb_weight above
+// the FP32 enclosure of ratio_cor * area (or below that of 0.7070 or
+// ratio_cor times area) decides can_recurse_t without ratio_wh; no trap site
+// is skipped (the critical ratio has none).  Only certain comparisons are
+// used here; anything else falls through to can_recurse_t.
 __device__ __noinline__ inline bool can_recurse(f32::Fv ub_w, f32::Fv ub_h, f32::Fv ub_largest, f32::Fv lb_weight) {
+    using f32::Fv;
+    const Fv ub_area = f32::mul(ub_w, ub_h);
+    const Fv s = f32::rcp_up(f32::lesser(ub_w, ub_h));
+    const Fv largest_norm = f32::mul(f32::mul(s, s), ub_largest);
+    // w and h certainly positive and finite: then the critical ratio's
+    // argument is an aspect ratio >= 1 and everything stays finite
+    const bool sane = ub_w.lo > 0.0f && ub_h.lo > 0.0f && ub_w.hi < 1e30f && ub_h.hi < 1e30f;
+    if (sane && largest_norm.lo > 0.140625f && largest_norm.lo <= largest_norm.hi && lb_weight.lo <= lb_weight.hi) {
+        const Fv t = f32::add(f32::sqrt_nn(f32::add(f32::mul(largest_norm, largest_norm), Fv{1.0f, 1.0f})),
+                              Fv{1.0f, 1.0f});
+        const Fv ratio_cor = f32::greater(Fv{0.76171875f, 0.76171875f}, f32::scale(f32::sqrt_nn(t), 0.5f));
+        const float need_hi = f32::mul(ratio_cor, ub_area).hi;  // >= the FP64 ub_needed
+        if (lb_weight.lo >= need_hi) return true;
+        const float r_lo = fminf(ratio_cor.lo, 0.7070f);
+        const float need_lo = __fmul_rd(r_lo, ub_area.lo);     // <= the FP64 ub_needed
+        if (lb_weight.hi < need_lo) return false;
+    }
     return can_recurse_t<f32::Fv>(ub_w, ub_h, ub_largest, lb_weight);
 }
 #endif
