@@ -87,9 +87,15 @@ enum TrapSite : uint32_t {
 // one status byte per thread, kept in shared memory so that any device
 // function can set it without threading a context argument through every
 // criterion; 1024 threads per block at most.
+// Bit 7 of the byte is a mode bit of the FP32 evaluation (cc_tight.cuh:
+// can_recurse records its arguments instead of evaluating); trap_clear()
+// clears it, trap() keeps it.
 static __shared__ uint8_t cc_trap_words[1024];
-CC_FN void trap(uint32_t site) { cc_trap_words[threadIdx.x] = (uint8_t)site; }
-CC_FN uint32_t trap_status() { return cc_trap_words[threadIdx.x]; }
+static constexpr uint8_t kTrapModeBit = 0x80;
+CC_FN void trap(uint32_t site) {
+    cc_trap_words[threadIdx.x] = (uint8_t)((cc_trap_words[threadIdx.x] & kTrapModeBit) | site);
+}
+CC_FN uint32_t trap_status() { return cc_trap_words[threadIdx.x] & (uint8_t)~kTrapModeBit; }
 CC_FN void trap_clear() { cc_trap_words[threadIdx.x] = TRAP_NONE; }
 #else
 // host build: per-thread status (initial-exec TLS: a plain load per access)

@@ -71,23 +71,92 @@ struct EvalQueues {
     uint32_t* gaps_box;
     unsigned long long* counts;  // [0] cover, [1] gaps, [2] overflow, [3] full
     unsigned long long cap;
+    // recorded calls of the heavy FP32 groups (null: every group in one kernel)
+    ct::CrArgs* args;        // n x kCrRecordSlots
+    uint8_t* states;         // kRecGroups x n
+    uint32_t* q[2];          // pending boxes of a call round
+    unsigned long long* rc;  // the two rounds' queue counters
 };
 static constexpr int kEvalCounters = 4;
+// the groups whose can_recurse calls are recorded, and their verdict bits
+static constexpr int kRecGroups = 4;
+__host__ __device__ constexpr int rec_group(int k) { return k < 2 ? k : k + 1; }  // 0, 1, 3, 4
 
 // MinB: the register budget (__launch_bounds__ minimum resident blocks per
 // SM: 1 = up to 255 registers per thread, 4 = 128, 8 = 64), chosen per
 // pass by the autotuner (cc_autotune_eval) together with the grid size.
 template <Layout L, int G, int MinB = 1>
 __global__ void __launch_bounds__(128, MinB) k_eval_f32(const double* __restrict__ in, size_t n,
-                                                        uint32_t* __restrict__ masks) {
+                                                        uint32_t* __restrict__ masks, int first) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        if (G == 0) {
+        if (first) {
             masks[i] = ct::eval_group_f32<G>(load_box<L>(in, n, i));
         } else {
             const uint32_t prev = masks[i];
             if (prev & ct::kF32Undecided) continue;  // left to the FP64 pass anyway
             masks[i] = prev | ct::eval_group_f32<G>(load_box<L>(in, n, i));
         }
+    }
+}
+
+// A group with recorded calls: the record pass runs the criterion with
+// can_recurse recording instead of evaluating; boxes with calls to make go
+// to the first round's queue.
+template <Layout L, int G, int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_record(const double* __restrict__ in, size_t n,
+                                                           ct::CrArgs* __restrict__ args, uint8_t* __restrict__ state,
+                                                           uint32_t* __restrict__ q, unsigned long long* nq,
+                                                           unsigned long long* overflow) {
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n;
+         base += stride) {
+        unsigned long long i = base + (threadIdx.x & 31);
+        bool pending = false;
+        if (i < n) {
+            const uint8_t st = ct::record_group_f32<G>(load_box<L>(in, n, i), args + i * ct::kCrRecordSlots);
+            state[i] = st;
+            pending = (st & 3) == ct::kRecPending;
+        }
+        __syncwarp();
+        unsigned long long s = cc::prove::warp_append(nq, pending, n, overflow);
+        if (s != ~0ULL) q[s] = (uint32_t)i;
+    }
+}
+
+// Round `round` of the recorded calls: call `round` of every box still
+// pending, on full warps.  A true or undecided answer settles the box (the
+// FP64 criterion returns at its first true call); a false one sends it to the
+// next round, or, after its last call, to the status its criterion ends with.
+__global__ void __launch_bounds__(128) k_eval_calls(const ct::CrArgs* __restrict__ args, uint8_t* __restrict__ state,
+                                                    int round, const uint32_t* __restrict__ q_in,
+                                                    const unsigned long long* n_in, uint32_t* __restrict__ q_out,
+                                                    unsigned long long* n_out, unsigned long long cap,
+                                                    unsigned long long* overflow) {
+    const unsigned long long total = *n_in < cap ? *n_in : cap;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
+         base += stride) {
+        unsigned long long j = base + (threadIdx.x & 31);
+        bool more = false;
+        uint32_t i = 0;
+        if (j < total) {
+            i = q_in[j];
+            const uint8_t st = state[i];
+            const ct::CrArgs a = args[(size_t)i * ct::kCrRecordSlots + round];
+            cc::trap_clear();
+            const bool ok = ct::can_recurse(a.w, a.h, a.largest, a.lb);
+            const bool undecided = cc::trap_status() != cc::TRAP_NONE;
+            cc::trap_clear();
+            uint8_t next;
+            if (undecided) next = ct::kRecUndecided;
+            else if (ok) next = ct::kRecTrue;
+            else if (round + 1 < ((st >> 2) & 7)) more = true, next = st;
+            else next = (uint8_t)((st >> 5) & 3);
+            state[i] = next;
+        }
+        __syncwarp();
+        unsigned long long s = cc::prove::warp_append(n_out, more, cap, overflow);
+        if (s != ~0ULL) q_out[s] = i;
     }
 }
 
@@ -98,10 +167,17 @@ __global__ void __launch_bounds__(128) k_eval_collect(size_t n, uint32_t* __rest
         unsigned long long i = base + (threadIdx.x & 31);
         bool valid = i < n;
         uint32_t m = valid ? masks[i] : 0u;
+        if (valid && q.states) {
+            for (int k = 0; k < kRecGroups; ++k) {
+                const uint8_t st = q.states[(size_t)k * n + i] & 3;
+                if (st == ct::kRecTrue) m |= 1u << rec_group(k);
+                else if (st != ct::kRecFalse) m |= ct::kF32Undecided;
+            }
+        }
         const bool undecided = (m & ct::kF32Undecided) != 0;
         const bool need_cover = !undecided && (m & ct::kF32Cover);
         const bool need_gaps = !undecided && (m & ct::kF32Gaps);
-        if (valid && (m & (ct::kF32Undecided | ct::kF32Cover | ct::kF32Gaps)))
+        if (valid && (q.states || (m & (ct::kF32Undecided | ct::kF32Cover | ct::kF32Gaps))))
             masks[i] = m & ~(ct::kF32Undecided | ct::kF32Cover | ct::kF32Gaps);
         unsigned long long s = cc::prove::warp_append(&q.counts[3], valid && undecided, q.cap, &q.counts[2]);
         if (s != ~0ULL) q.full[s] = (uint32_t)i;
@@ -162,15 +238,22 @@ __global__ void __launch_bounds__(128, MinB) k_eval_gaps(const double* __restric
     }
 }
 
-// queue buffers for up to `cap` boxes in handle slots 16..19
+// queue and record buffers for up to `cap` boxes in handle slots 16..20 and
+// 35..38 (about 150 bytes per box)
 static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
-    void *a, *b, *c, *e;
+    void *a, *b, *c, *e, *args, *states, *q0, *q1, *rc;
     int st;
     if ((st = ccrt::ensure(h, 16, cap * sizeof(uint32_t), &a))) return st;
     if ((st = ccrt::ensure(h, 17, cap * sizeof(uint32_t), &b))) return st;
     if ((st = ccrt::ensure(h, 18, cap * sizeof(uint32_t), &c))) return st;
     if ((st = ccrt::ensure(h, 19, kEvalCounters * sizeof(unsigned long long), &e))) return st;
-    *q = EvalQueues{(uint32_t*)a, (uint32_t*)b, (uint32_t*)c, (unsigned long long*)e, cap};
+    if ((st = ccrt::ensure(h, 20, cap * ct::kCrRecordSlots * sizeof(ct::CrArgs), &args))) return st;
+    if ((st = ccrt::ensure(h, 35, cap * kRecGroups, &states))) return st;
+    if ((st = ccrt::ensure(h, 36, cap * sizeof(uint32_t), &q0))) return st;
+    if ((st = ccrt::ensure(h, 37, cap * sizeof(uint32_t), &q1))) return st;
+    if ((st = ccrt::ensure(h, 38, 2 * sizeof(unsigned long long), &rc))) return st;
+    *q = EvalQueues{(uint32_t*)a, (uint32_t*)b, (uint32_t*)c, (unsigned long long*)e, cap,
+                    (ct::CrArgs*)args, (uint8_t*)states, {(uint32_t*)q0, (uint32_t*)q1}, (unsigned long long*)rc};
     return CC_OK;
 }
 
@@ -190,17 +273,48 @@ static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
             KERNEL<L, 1><<<g, 128, 0, s>>>(__VA_ARGS__);                                              \
         }                                                                                             \
     }
-// pass 0: the FP32 group kernels, then the collection of the queues
+// pass 0: the FP32 group kernels, then the collection of the queues.  With
+// record buffers, the heavy groups (r1, r1_r2, 2x2, leaf) run as a record
+// pass plus call rounds; the three-strip group runs in one kernel either way.
 template <Layout L>
 static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks,
                               EvalQueues q) {
+    if (q.args) {
+#define CC_F32_RECORD(K)                                                                                      \
+    {                                                                                                         \
+        constexpr int G = rec_group(K);                                                                       \
+        uint8_t* st = q.states + (size_t)(K) * n;                                                             \
+        cudaMemsetAsync(q.rc, 0, 2 * sizeof(unsigned long long), s);                                          \
+        if (minb == 4 && L == Layout::SoA)                                                                    \
+            k_eval_record<L, G, 4><<<g, 128, 0, s>>>(in, n, q.args, st, q.q[0], &q.rc[0], &q.counts[2]);      \
+        else if (minb == 8 && L == Layout::SoA)                                                               \
+            k_eval_record<L, G, 8><<<g, 128, 0, s>>>(in, n, q.args, st, q.q[0], &q.rc[0], &q.counts[2]);      \
+        else                                                                                                  \
+            k_eval_record<L, G, 1><<<g, 128, 0, s>>>(in, n, q.args, st, q.q[0], &q.rc[0], &q.counts[2]);      \
+        for (int r = 0; r < ct::kCrRecordSlots; ++r) {                                                        \
+            cudaMemsetAsync(&q.rc[(r + 1) & 1], 0, sizeof(unsigned long long), s);                            \
+            k_eval_calls<<<g, 128, 0, s>>>(q.args, st, r, q.q[r & 1], &q.rc[r & 1], q.q[(r + 1) & 1],          \
+                                          &q.rc[(r + 1) & 1], n, &q.counts[2]);                               \
+        }                                                                                                     \
+    }
+        if (minb == 4 && L == Layout::SoA) k_eval_f32<L, ct::F32_R123, 4><<<g, 128, 0, s>>>(in, n, masks, 1);
+        else if (minb == 8 && L == Layout::SoA) k_eval_f32<L, ct::F32_R123, 8><<<g, 128, 0, s>>>(in, n, masks, 1);
+        else k_eval_f32<L, ct::F32_R123, 1><<<g, 128, 0, s>>>(in, n, masks, 1);
+        CC_F32_RECORD(0)
+        CC_F32_RECORD(1)
+        CC_F32_RECORD(2)
+        CC_F32_RECORD(3)
+#undef CC_F32_RECORD
+        k_eval_collect<<<g, 128, 0, s>>>(n, masks, q);
+        return;
+    }
 #define CC_F32_GROUP(G)                                                                         \
     if constexpr (L == Layout::SoA) {                                                           \
-        if (minb == 4) k_eval_f32<L, G, 4><<<g, 128, 0, s>>>(in, n, masks);                     \
-        else if (minb == 8) k_eval_f32<L, G, 8><<<g, 128, 0, s>>>(in, n, masks);                \
-        else k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks);                               \
+        if (minb == 4) k_eval_f32<L, G, 4><<<g, 128, 0, s>>>(in, n, masks, G == 0);             \
+        else if (minb == 8) k_eval_f32<L, G, 8><<<g, 128, 0, s>>>(in, n, masks, G == 0);        \
+        else k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks, G == 0);                       \
     } else {                                                                                    \
-        k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks);                                    \
+        k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks, G == 0);                            \
     }
     CC_F32_GROUP(0)
     CC_F32_GROUP(1)
@@ -239,7 +353,7 @@ static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks,
         if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[pass], s));
         launch_pass<L>(pass, h->tune_minb[pass], h->sm_count * h->tune_grid[pass], s, in, n, masks, q);
         CC_LAUNCHED(h);
-        if (pass == 0) h->launches += ct::F32_GROUPS;  // the group kernels and the collection
+        if (pass == 0) h->launches += 1 + kRecGroups * (1 + ct::kCrRecordSlots);  // groups, rounds, collection
     }
     if (h->timing) {
         CC_CUDA(h, cudaEventRecord(h->stage_ev[CC_EVAL_STAGES], s));
@@ -604,6 +718,10 @@ extern "C" int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t
     p += kStaticMaxBoxes * sizeof(uint32_t);
     q.gaps_box = (uint32_t*)p;
     q.cap = kStaticMaxBoxes;
+    q.args = nullptr;  // no room for the record buffers: every group in one kernel
+    q.states = nullptr;
+    q.q[0] = q.q[1] = nullptr;
+    q.rc = nullptr;
     cudaStream_t s = (cudaStream_t)stream;
     // the queue counters are the only state that must start at zero
     if (cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s) != cudaSuccess) {

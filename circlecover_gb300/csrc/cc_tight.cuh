@@ -153,8 +153,38 @@ CC_FN bool can_recurse(double ub_w, double ub_h, double ub_largest, double lb_we
 // ratio_cor times area) decides can_recurse_t without ratio_wh; no trap site
 // is skipped (the critical ratio has none).  Only certain comparisons are
 // used here; anything else falls through to can_recurse_t.
+//
+// Record mode (mode bit of the trap word, set by record_group_f32): the call
+// stores its arguments in the thread's next record slot and answers "false",
+// so the criterion goes on exactly as the FP64 one would after a false
+// result; the calls are evaluated afterwards, in rounds over compacted
+// queues (k_eval_calls), and combined in order (a true call settles the
+// criterion, as in the FP64 short circuit).
+struct CrArgs {
+    f32::Fv w, h, largest, lb;
+};
+static constexpr int kCrRecordSlots = 4;
+static __shared__ CrArgs cc_cr_rec[kCrRecordSlots][128];
+// bits 0-2: calls recorded; bit 3 + j: the path to call j was already undecided
+static __shared__ uint8_t cc_cr_info[128];
+
+__device__ __noinline__ inline bool can_recurse_record(f32::Fv ub_w, f32::Fv ub_h, f32::Fv ub_largest,
+                                                       f32::Fv lb_weight) {
+    uint8_t info = cc_cr_info[threadIdx.x];
+    const int j = info & 7;
+    if (j >= kCrRecordSlots) {  // more calls than slots: the criterion stays undecided
+        trap(TRAP_F32_UNDECIDED);
+        return false;
+    }
+    cc_cr_rec[j][threadIdx.x] = CrArgs{ub_w, ub_h, ub_largest, lb_weight};
+    if (trap_status() != TRAP_NONE) info |= (uint8_t)(8u << j);
+    cc_cr_info[threadIdx.x] = (uint8_t)(info + 1);
+    return false;
+}
+
 __device__ __noinline__ inline bool can_recurse(f32::Fv ub_w, f32::Fv ub_h, f32::Fv ub_largest, f32::Fv lb_weight) {
     using f32::Fv;
+    if (cc_trap_words[threadIdx.x] & kTrapModeBit) return can_recurse_record(ub_w, ub_h, ub_largest, lb_weight);
     const Fv ub_area = f32::mul(ub_w, ub_h);
     const Fv s = f32::rcp_up(f32::lesser(ub_w, ub_h));
     const Fv largest_norm = f32::mul(f32::mul(s, s), ub_largest);
@@ -1075,6 +1105,53 @@ CC_FN_INL BoxT<f32::IvF> enclose(const Box& b) {
 // (the box needs the strip-width / gap-width bisection), or kF32Undecided.
 enum : uint32_t { kF32Gaps = 1u << 28, kF32Cover = 1u << 29, kF32Undecided = 1u << 30 };
 enum F32Group { F32_R1 = 0, F32_R12 = 1, F32_R123 = 2, F32_2X2 = 3, F32_LEAF = 4, F32_GROUPS = 5 };
+
+// criterion G of the group kernels on the enclosed box (G != F32_R123)
+template <int G>
+CC_FN_INL bool group_criterion_f32(const BoxT<f32::IvF>& in, const f32::IvF& weight) {
+    using f32::IvF;
+    const IvF la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2];
+    if (G == F32_R1) return r1_strategies(la, weight, r1, r2.hi);
+    if (G == F32_R12) return r1_r2_strategies(la, weight, r1, r2, r3.hi);
+    IvF R4 = weight - r1 - r2 - r3;
+    tighten_lb(R4, 0.0);
+    BoxT<IvF> v = in;
+    tighten_lb(v.r[2], v.r[3].lo);
+    tighten_lb(v.r[1], v.r[2].lo);
+    tighten_lb(v.r[0], v.r[1].lo);
+    IvF R = weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+    tighten_lb(R, 0.0);
+    if (G == F32_2X2) return two_by_two_strategies(v, R);
+    return r1_r2_r3_strategies(v, R4);
+}
+
+// State byte of a criterion evaluated with recorded calls: bits 0-1 the
+// status; while pending, bits 2-4 the number of calls to evaluate and bits
+// 5-6 the status if they all answer false (the criterion's own end).
+enum : uint8_t { kRecPending = 0, kRecFalse = 1, kRecTrue = 2, kRecUndecided = 3 };
+
+// Criterion G in record mode; the calls to evaluate (those before the first
+// one reached on an undecided path) go to args[0..).
+template <int G>
+CC_FN_INL uint8_t record_group_f32(const Box& in64, CrArgs* __restrict__ args) {
+    trap_clear();
+    cc_cr_info[threadIdx.x] = 0;
+    cc_trap_words[threadIdx.x] |= kTrapModeBit;
+    const BoxT<f32::IvF> in = enclose(in64);
+    const bool end_value = group_criterion_f32<G>(in, required_weight_for(in.la));
+    const bool end_undecided = trap_status() != TRAP_NONE;
+    trap_clear();
+    const uint8_t info = cc_cr_info[threadIdx.x];
+    const int m = info & 7;
+    int calls = 0;
+    while (calls < m && !(info & (8u << calls))) {
+        args[calls] = cc_cr_rec[calls][threadIdx.x];
+        ++calls;
+    }
+    const uint8_t end = (calls < m || end_undecided) ? kRecUndecided : (end_value ? kRecTrue : kRecFalse);
+    if (calls == 0) return end;
+    return (uint8_t)(kRecPending | (calls << 2) | (end << 5));
+}
 
 template <int G>
 CC_FN_INL uint32_t eval_group_f32(const Box& in64) {
