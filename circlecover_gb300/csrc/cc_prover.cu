@@ -76,6 +76,7 @@ struct EvalQueues {
     uint8_t* states;         // kRecGroups x n
     uint32_t* q[2];          // pending boxes of a call round
     unsigned long long* rc;  // the two rounds' queue counters
+    ct::EncBox* enc;         // enclosed boxes and weights (n)
 };
 static constexpr int kEvalCounters = 4;
 // the groups whose can_recurse calls are recorded, and their verdict bits
@@ -87,10 +88,11 @@ __host__ __device__ constexpr int rec_group(int k) { return k < 2 ? k : k + 1; }
 // pass by the autotuner (cc_autotune_eval) together with the grid size.
 template <Layout L, int G, int MinB = 1>
 __global__ void __launch_bounds__(128, MinB) k_eval_f32(const double* __restrict__ in, size_t n,
-                                                        uint32_t* __restrict__ masks, int first) {
+                                                        uint32_t* __restrict__ masks, int first,
+                                                        ct::EncBox* __restrict__ enc) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         if (first) {
-            masks[i] = ct::eval_group_f32<G>(load_box<L>(in, n, i));
+            masks[i] = ct::eval_group_f32<G>(load_box<L>(in, n, i), enc ? enc + i : nullptr);
         } else {
             const uint32_t prev = masks[i];
             if (prev & ct::kF32Undecided) continue;  // left to the FP64 pass anyway
@@ -102,8 +104,9 @@ __global__ void __launch_bounds__(128, MinB) k_eval_f32(const double* __restrict
 // A group with recorded calls: the record pass runs the criterion with
 // can_recurse recording instead of evaluating; boxes with calls to make go
 // to the first round's queue.
-template <Layout L, int G, int MinB = 1>
-__global__ void __launch_bounds__(128, MinB) k_eval_record(const double* __restrict__ in, size_t n,
+template <int G, int MinB = 1>
+__global__ void __launch_bounds__(128, MinB) k_eval_record(const ct::EncBox* __restrict__ enc, size_t n,
+                                                           const uint32_t* __restrict__ masks,
                                                            ct::CrArgs* __restrict__ args, uint8_t* __restrict__ state,
                                                            uint32_t* __restrict__ q, unsigned long long* nq,
                                                            unsigned long long* overflow) {
@@ -113,7 +116,8 @@ __global__ void __launch_bounds__(128, MinB) k_eval_record(const double* __restr
         unsigned long long i = base + (threadIdx.x & 31);
         bool pending = false;
         if (i < n) {
-            const uint8_t st = ct::record_group_f32<G>(load_box<L>(in, n, i), args + i * ct::kCrRecordSlots);
+            uint8_t st = ct::kRecUndecided;  // a box the first kernel left undecided goes to the FP64 pass anyway
+            if (!(masks[i] & ct::kF32Undecided)) st = ct::record_group_f32<G>(enc[i], args + i * ct::kCrRecordSlots);
             state[i] = st;
             pending = (st & 3) == ct::kRecPending;
         }
@@ -239,7 +243,7 @@ __global__ void __launch_bounds__(128, MinB) k_eval_gaps(const double* __restric
 }
 
 // queue and record buffers for up to `cap` boxes in handle slots 16..20 and
-// 35..38 (about 150 bytes per box)
+// 35..39 (about 250 bytes per box)
 static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
     void *a, *b, *c, *e, *args, *states, *q0, *q1, *rc;
     int st;
@@ -252,8 +256,11 @@ static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
     if ((st = ccrt::ensure(h, 36, cap * sizeof(uint32_t), &q0))) return st;
     if ((st = ccrt::ensure(h, 37, cap * sizeof(uint32_t), &q1))) return st;
     if ((st = ccrt::ensure(h, 38, 2 * sizeof(unsigned long long), &rc))) return st;
+    void* enc;
+    if ((st = ccrt::ensure(h, 39, cap * sizeof(ct::EncBox), &enc))) return st;
     *q = EvalQueues{(uint32_t*)a, (uint32_t*)b, (uint32_t*)c, (unsigned long long*)e, cap,
-                    (ct::CrArgs*)args, (uint8_t*)states, {(uint32_t*)q0, (uint32_t*)q1}, (unsigned long long*)rc};
+                    (ct::CrArgs*)args, (uint8_t*)states, {(uint32_t*)q0, (uint32_t*)q1}, (unsigned long long*)rc,
+                    (ct::EncBox*)enc};
     return CC_OK;
 }
 
@@ -285,21 +292,21 @@ static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in,
         constexpr int G = rec_group(K);                                                                       \
         uint8_t* st = q.states + (size_t)(K) * n;                                                             \
         cudaMemsetAsync(q.rc, 0, 2 * sizeof(unsigned long long), s);                                          \
-        if (minb == 4 && L == Layout::SoA)                                                                    \
-            k_eval_record<L, G, 4><<<g, 128, 0, s>>>(in, n, q.args, st, q.q[0], &q.rc[0], &q.counts[2]);      \
-        else if (minb == 8 && L == Layout::SoA)                                                               \
-            k_eval_record<L, G, 8><<<g, 128, 0, s>>>(in, n, q.args, st, q.q[0], &q.rc[0], &q.counts[2]);      \
+        if (minb == 4)                                                                                        \
+            k_eval_record<G, 4><<<g, 128, 0, s>>>(q.enc, n, masks, q.args, st, q.q[0], &q.rc[0], &q.counts[2]); \
+        else if (minb == 8)                                                                                   \
+            k_eval_record<G, 8><<<g, 128, 0, s>>>(q.enc, n, masks, q.args, st, q.q[0], &q.rc[0], &q.counts[2]); \
         else                                                                                                  \
-            k_eval_record<L, G, 1><<<g, 128, 0, s>>>(in, n, q.args, st, q.q[0], &q.rc[0], &q.counts[2]);      \
+            k_eval_record<G, 1><<<g, 128, 0, s>>>(q.enc, n, masks, q.args, st, q.q[0], &q.rc[0], &q.counts[2]); \
         for (int r = 0; r < ct::kCrRecordSlots; ++r) {                                                        \
             cudaMemsetAsync(&q.rc[(r + 1) & 1], 0, sizeof(unsigned long long), s);                            \
             k_eval_calls<<<g, 128, 0, s>>>(q.args, st, r, q.q[r & 1], &q.rc[r & 1], q.q[(r + 1) & 1],          \
                                           &q.rc[(r + 1) & 1], n, &q.counts[2]);                               \
         }                                                                                                     \
     }
-        if (minb == 4 && L == Layout::SoA) k_eval_f32<L, ct::F32_R123, 4><<<g, 128, 0, s>>>(in, n, masks, 1);
-        else if (minb == 8 && L == Layout::SoA) k_eval_f32<L, ct::F32_R123, 8><<<g, 128, 0, s>>>(in, n, masks, 1);
-        else k_eval_f32<L, ct::F32_R123, 1><<<g, 128, 0, s>>>(in, n, masks, 1);
+        if (minb == 4 && L == Layout::SoA) k_eval_f32<L, ct::F32_R123, 4><<<g, 128, 0, s>>>(in, n, masks, 1, q.enc);
+        else if (minb == 8 && L == Layout::SoA) k_eval_f32<L, ct::F32_R123, 8><<<g, 128, 0, s>>>(in, n, masks, 1, q.enc);
+        else k_eval_f32<L, ct::F32_R123, 1><<<g, 128, 0, s>>>(in, n, masks, 1, q.enc);
         CC_F32_RECORD(0)
         CC_F32_RECORD(1)
         CC_F32_RECORD(2)
@@ -310,11 +317,11 @@ static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in,
     }
 #define CC_F32_GROUP(G)                                                                         \
     if constexpr (L == Layout::SoA) {                                                           \
-        if (minb == 4) k_eval_f32<L, G, 4><<<g, 128, 0, s>>>(in, n, masks, G == 0);             \
-        else if (minb == 8) k_eval_f32<L, G, 8><<<g, 128, 0, s>>>(in, n, masks, G == 0);        \
-        else k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks, G == 0);                       \
+        if (minb == 4) k_eval_f32<L, G, 4><<<g, 128, 0, s>>>(in, n, masks, G == 0, nullptr);          \
+        else if (minb == 8) k_eval_f32<L, G, 8><<<g, 128, 0, s>>>(in, n, masks, G == 0, nullptr);        \
+        else k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks, G == 0, nullptr);                       \
     } else {                                                                                    \
-        k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks, G == 0);                            \
+        k_eval_f32<L, G, 1><<<g, 128, 0, s>>>(in, n, masks, G == 0, nullptr);                            \
     }
     CC_F32_GROUP(0)
     CC_F32_GROUP(1)
@@ -722,6 +729,7 @@ extern "C" int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t
     q.states = nullptr;
     q.q[0] = q.q[1] = nullptr;
     q.rc = nullptr;
+    q.enc = nullptr;
     cudaStream_t s = (cudaStream_t)stream;
     // the queue counters are the only state that must start at zero
     if (cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s) != cudaSuccess) {

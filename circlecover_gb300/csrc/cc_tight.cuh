@@ -1130,15 +1130,21 @@ CC_FN_INL bool group_criterion_f32(const BoxT<f32::IvF>& in, const f32::IvF& wei
 // 5-6 the status if they all answer false (the criterion's own end).
 enum : uint8_t { kRecPending = 0, kRecFalse = 1, kRecTrue = 2, kRecUndecided = 3 };
 
+// The enclosed box and its required weight, computed once by the first FP32
+// kernel for the record passes (96 bytes per box).
+struct EncBox {
+    BoxT<f32::IvF> b;
+    f32::IvF weight;
+};
+
 // Criterion G in record mode; the calls to evaluate (those before the first
 // one reached on an undecided path) go to args[0..).
 template <int G>
-CC_FN_INL uint8_t record_group_f32(const Box& in64, CrArgs* __restrict__ args) {
+CC_FN_INL uint8_t record_group_f32(const EncBox& in, CrArgs* __restrict__ args) {
     trap_clear();
     cc_cr_info[threadIdx.x] = 0;
     cc_trap_words[threadIdx.x] |= kTrapModeBit;
-    const BoxT<f32::IvF> in = enclose(in64);
-    const bool end_value = group_criterion_f32<G>(in, required_weight_for(in.la));
+    const bool end_value = group_criterion_f32<G>(in.b, in.weight);
     const bool end_undecided = trap_status() != TRAP_NONE;
     trap_clear();
     const uint8_t info = cc_cr_info[threadIdx.x];
@@ -1154,13 +1160,14 @@ CC_FN_INL uint8_t record_group_f32(const Box& in64, CrArgs* __restrict__ args) {
 }
 
 template <int G>
-CC_FN_INL uint32_t eval_group_f32(const Box& in64) {
+CC_FN_INL uint32_t eval_group_f32(const Box& in64, EncBox* keep = nullptr) {
     using f32::IvF;
     using f32::Fv;
     trap_clear();
     const BoxT<IvF> in = enclose(in64);
     const IvF la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2], r4 = in.r[3];
     const IvF weight = required_weight_for(la);
+    if (keep) *keep = EncBox{in, weight};
     uint32_t m = 0;
     if (G == F32_R1) {
         if (r1_strategies(la, weight, r1, r2.hi)) m |= 1u << 0;
