@@ -300,10 +300,13 @@ class Prover:
     def last_launch_count(self):
         return int(self.lib.cc_last_launch_count(self.h))
 
-    def tight_eval(self, boxes):
-        """Verdict masks (TV_* bits) of host boxes (TIGHT_BOX records)."""
+    def tight_eval(self, boxes, out=None):
+        """Verdict masks (TV_* bits) of host boxes (TIGHT_BOX records), into
+        `out` (a uint32 host array, e.g. page-locked) if given."""
         boxes = np.ascontiguousarray(boxes, dtype=TIGHT_BOX)
-        masks = np.zeros(len(boxes), dtype=np.uint32)
+        masks = np.zeros(len(boxes), dtype=np.uint32) if out is None else out
+        if masks.dtype != np.uint32 or len(masks) != len(boxes) or not masks.flags["C_CONTIGUOUS"]:
+            raise ValueError("out: a contiguous uint32 array of len(boxes)")
         self._check(self.lib.cc_tight_eval(self.h, boxes.ctypes.data, len(boxes), masks.ctypes.data), "cc_tight_eval")
         return masks
 

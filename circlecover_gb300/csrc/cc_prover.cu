@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(128, MinB) k_eval_cover(const double* __restri
     for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < nq;
          j += (unsigned long long)gridDim.x * blockDim.x) {
         const uint32_t i = q.cover_box[j];
-        uint32_t m = ct::cover_pass_box(load_box<L>(in, n, i));
+        uint32_t m = ct::cover_pass_box(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr);
         if (m) masks[i] |= m;
     }
 }
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(128, MinB) k_eval_gaps(const double* __restric
     for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < nq;
          j += (unsigned long long)gridDim.x * blockDim.x) {
         const uint32_t i = q.gaps_box[j];
-        uint32_t m = ct::gaps_pass_box(load_box<L>(in, n, i));
+        uint32_t m = ct::gaps_pass_box(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr);
         if (m) masks[i] |= m;
     }
 }
@@ -759,9 +759,10 @@ __global__ void __launch_bounds__(256) k_aos_to_soa(const double* __restrict__ a
 
 // Host-memory entry point.  The boxes move to the device in chunks of 4M by
 // the copy engine, on a second stream, so that chunk k+1 travels while chunk
-// k is evaluated: straight from the caller's array where the device reaches
-// pageable host memory through the host's page tables (GB300 with its host
-// over NVLink-C2C: ~190 GB/s measured), otherwise through two pinned buffers
+// k is evaluated: straight from the caller's array if it is page-locked, or
+// where the device reaches pageable host memory through the host's page
+// tables (GB300 with its host over NVLink-C2C: ~190-210 GB/s measured),
+// otherwise through two pinned buffers
 // that host threads fill (one thread copies at a fraction of the host's
 // memory bandwidth).  On the evaluation stream each chunk is transposed to
 // SoA in device memory and evaluated by the same passes as
@@ -771,7 +772,12 @@ int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* m
     h->launches = 0;
     if (n == 0) return CC_OK;
     CC_CUDA(h, cudaSetDevice(h->device));
-    const bool direct = h->pageable_access;
+    // page-locked input (cudaHostAlloc / cudaHostRegister) is copied as it is
+    cudaPointerAttributes pa;
+    bool pinned_in = false;
+    if (cudaPointerGetAttributes(&pa, boxes) == cudaSuccess) pinned_in = pa.type == cudaMemoryTypeHost;
+    else cudaGetLastError();
+    const bool direct = h->pageable_access || pinned_in;
     const size_t chunk = n < ((size_t)1 << 22) ? n : ((size_t)1 << 22);
     const size_t in_bytes = chunk * sizeof(cc_tight_box);
     void *d_aos[2], *d_soa, *d_masks;

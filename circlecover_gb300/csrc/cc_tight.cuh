@@ -1167,7 +1167,9 @@ CC_FN_INL uint32_t eval_group_f32(const Box& in64, EncBox* keep = nullptr) {
     const BoxT<IvF> in = enclose(in64);
     const IvF la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2], r4 = in.r[3];
     const IvF weight = required_weight_for(la);
-    if (keep) *keep = EncBox{in, weight};
+    // a weight whose computation met an undecided comparison need not enclose
+    // the FP64 one: kept as NaN, so that every decision on it stays undecided
+    if (keep) *keep = EncBox{in, trap_status() == TRAP_NONE ? weight : IvF{f32::nan_fv(), f32::nan_fv()}};
     uint32_t m = 0;
     if (G == F32_R1) {
         if (r1_strategies(la, weight, r1, r2.hi)) m |= 1u << 0;
@@ -1230,12 +1232,15 @@ CC_FN_INL bool r1_r2_r3_leaf_first_f32(const Box& v, Iv R4) { return first_f32(L
 // the recursion check first on FP32 enclosures and, if that is undecided, in
 // FP64.  Same result and trap bit as cover_pass / gaps_pass on eval_main's
 // jobs.
-CC_FN_INL uint32_t cover_pass_box(const Box& b) {
+// (enc: the box's enclosure and weight if the FP32 pass kept them)
+CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr) {
     using f32::Fv;
     const Iv la = b.la, r1 = b.r[0], r2 = b.r[1], r3 = b.r[2];
     trap_clear();
-    const BoxT<f32::IvF> e = enclose(b);
-    const Fv lb_R4 = (required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2]).lo;
+    const Fv lb_R4 = enc ? (enc->weight - enc->b.r[0] - enc->b.r[1] - enc->b.r[2]).lo : [&] {
+        const BoxT<f32::IvF> e = enclose(b);
+        return (required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2]).lo;
+    }();
     const bool lb_ok = trap_status() == TRAP_NONE;
     trap_clear();
     // cover_strip_finish for every width in [lo, hi]
@@ -1262,7 +1267,7 @@ CC_FN_INL uint32_t cover_pass_box(const Box& b) {
     return m;
 }
 
-CC_FN_INL uint32_t gaps_pass_box(const Box& b) {
+CC_FN_INL uint32_t gaps_pass_box(const Box& b, const EncBox* enc = nullptr) {
     using f32::Fv;
     trap_clear();
     Box v = b;
@@ -1273,8 +1278,17 @@ CC_FN_INL uint32_t gaps_pass_box(const Box& b) {
     if (!gaps_enters(v.r[0].lo, v.r[1].lo, g)) {
         return 0u;
     }
-    BoxT<f32::IvF> e = enclose(v);
-    f32::IvF R = required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2] - e.r[3];
+    f32::IvF R;
+    if (enc) {  // the same tightening on the kept enclosure encloses v
+        BoxT<f32::IvF> e = enc->b;
+        tighten_lb(e.r[2], e.r[3].lo);
+        tighten_lb(e.r[1], e.r[2].lo);
+        tighten_lb(e.r[0], e.r[1].lo);
+        R = enc->weight - e.r[0] - e.r[1] - e.r[2] - e.r[3];
+    } else {
+        BoxT<f32::IvF> e = enclose(v);
+        R = required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2] - e.r[3];
+    }
     tighten_lb(R, 0.0);
     const bool R_ok = trap_status() == TRAP_NONE;
     trap_clear();
