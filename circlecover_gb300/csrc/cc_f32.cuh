@@ -323,6 +323,64 @@ __device__ __forceinline__ UbF operator<=(IvF a, IvF b) { return UbF{a.hi, b.lo,
 __device__ __forceinline__ UbF operator>(IvF a, IvF b) { return b < a; }
 __device__ __forceinline__ UbF operator>=(IvF a, IvF b) { return b <= a; }
 
+// FP64 `x <= 0 ? 0 : sqrt_dn(x)` for x in the enclosure a: 0, the root, or
+// either of them when the sign of x is not certain
+__device__ __forceinline__ Fv clipped_root(Fv a) {
+    if (a.hi <= 0.0f) return Fv{0.0f, 0.0f};
+    if (a.lo > 0.0f) return sqrt_nn(a);
+    if (!(a.lo <= a.hi)) return nan_fv();
+    return Fv{0.0f, __fsqrt_ru(a.hi)};
+}
+
+// The reference's bisection to the FP64 fixpoint from 0 <= lo < hi: mid =
+// 0.5 * (lo + hi) while strictly inside the bracket, `pred(mid)` true raises
+// lo, a trap after CC_BISECTION_CAP steps; the result is lo.  Run with the
+// FP32 shortcuts of the tight bisections (cc_tight.cuh, bisect_all_true):
+// `dec(W)` decides the predicate for every point of the enclosure W (YES,
+// NO, UNKNOWN) -- first for the whole bracket (false everywhere: the result
+// is lo, and a finite bracket reaches its fixpoint in fewer than 2,100
+// steps, so the cap cannot trap; true everywhere: the steps are replayed),
+// then for the leading steps while every converged lane of the warp has a
+// decision; from the first step some lane cannot decide, the FP64 predicate.
+template <class Dec, class Pred>
+__device__ __forceinline__ double bisect(double lo, double hi, const Dec& dec, const Pred& pred) {
+    int it = 0;
+    if (lo >= 0.0 && lo < hi && hi <= 1.7976931348623157e308) {
+        const int whole = dec(Fv{__double2float_rd(lo), __double2float_ru(hi)});
+        if (whole == NO) return lo;
+        if (whole == YES) {
+            for (;; ++it) {
+                const double mid = 0.5 * (lo + hi);
+                if (mid <= lo || mid >= hi) return lo;
+                if (it >= CC_BISECTION_CAP) {
+                    trap(TRAP_BISECTION_CAP);
+                    return lo;
+                }
+                lo = mid;
+            }
+        }
+    }
+    bool f32_steps = true;
+    for (;; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) return lo;
+        if (it >= CC_BISECTION_CAP) {
+            trap(TRAP_BISECTION_CAP);
+            return lo;
+        }
+        bool ok;
+        const int d = f32_steps ? dec(of(mid)) : UNKNOWN;
+        if (f32_steps && __all_sync(__activemask(), d != UNKNOWN)) {
+            ok = d == YES;
+        } else {
+            f32_steps = false;
+            ok = pred(mid);
+        }
+        if (ok) lo = mid;
+        else hi = mid;
+    }
+}
+
 __device__ __forceinline__ void tighten_lb(IvF& a, Fv l) { a.lo = greater(l, a.lo); }
 __device__ __forceinline__ void tighten_ub(IvF& a, Fv u) { a.hi = lesser(u, a.hi); }
 __device__ __forceinline__ bool empty(IvF a) { return a.lo > a.hi; }
