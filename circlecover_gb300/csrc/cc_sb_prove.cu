@@ -11,8 +11,10 @@
 //   tasks   one thread per task: its box (running r1 tightening,
 //           from_la_r1_r2), empty check, whole-task shortcuts
 //   cells   one thread per (task, r3 piece): the three r3 shortcuts
-//   leaves  one thread per (cell, r4, r5, r6 piece): leaf box, tighten, R,
-//           empty check, the first criterion of the cascade
+//   leaves  one thread per (cell, r4, r5, r6 piece): an FP32 emptiness
+//           pre-filter; then, on the compacted list of leaves it did not
+//           prove empty, leaf box, tighten, R, empty check and the first
+//           criterion of the cascade
 //   pass K  one thread per leaf still undecided: criterion K (K = 1..12),
 //           survivors compacted into the next pass's queue; the r1-in-corner
 //           criterion (K = 4) runs one thread per (leaf, placement)
@@ -265,7 +267,6 @@ __global__ void __launch_bounds__(kThreads) k_sbp_cells(const SbTask* __restrict
 
 struct LeafGrid {
     int gen, n4, n5, n6;
-    int fp32;                  // run the FP32 pre-filter
     uint32_t rem0;             // l0 % (n4 n5 n6), when that product is below 2^31
     unsigned long long cell0;  // l0 / (n4 n5 n6)
 };
@@ -330,9 +331,73 @@ __device__ __forceinline__ bool f32_leaf_empty(const SbTaskF32& t, float r3_lo, 
     return empty || u < 0.0f;
 }
 
-// Leaves [l0, l1) of the cell grid (rectangle_size_bound.cu:180-205): box,
-// tighten, R and the empty checks, then criterion 0 of the cascade.
-// Undecided leaves go to queue `q`, trapped ones to the criticals.
+// Coordinates of leaf idx in [l0, l1) of the cell grid: r3 cell and r4..r6
+// piece indices
+struct LeafAt {
+    unsigned long long ci;
+    int i4, i5, i6;
+};
+__device__ __forceinline__ LeafAt leaf_at(const LeafGrid& g, unsigned long long l0, unsigned long long l1,
+                                          unsigned long long idx) {
+    const unsigned long long n456 = (unsigned long long)g.n4 * g.n5 * g.n6;
+    LeafAt a;
+    if (n456 < (1ULL << 31) && l1 - l0 < (1ULL << 31)) {
+        // 32-bit index arithmetic: offsets from the slice's first cell
+        const uint32_t off = g.rem0 + (uint32_t)(idx - l0);  // < 2^32
+        const uint32_t q = off / (uint32_t)n456;
+        const uint32_t rem = off - q * (uint32_t)n456;
+        const uint32_t r56 = rem / (uint32_t)g.n6;
+        a.ci = g.cell0 + q;
+        a.i6 = (int)(rem - r56 * (uint32_t)g.n6);
+        a.i4 = (int)(r56 / (uint32_t)g.n5);
+        a.i5 = (int)(r56 - (uint32_t)a.i4 * (uint32_t)g.n5);
+    } else {
+        a.ci = idx / n456;
+        const unsigned long long rem = idx % n456;
+        a.i6 = (int)(rem % g.n6);
+        a.i5 = (int)((rem / g.n6) % g.n5);
+        a.i4 = (int)(rem / ((unsigned long long)g.n6 * g.n5));
+    }
+    return a;
+}
+
+// The FP64 part of a leaf (rectangle_size_bound.cu:180-205): box, tighten,
+// R and the empty checks, then criterion 0 of the cascade.  Returns the leaf
+// outcome (0, EMPTY, TRAPPED, or CRITICAL for undecided); fills leaf.box.
+__device__ __forceinline__ int leaf_fp64(const SbTask& task, const SbCell& cell, const LeafAt& a, const LeafGrid& g,
+                                         SbLeaf& leaf, sb::Vals& v) {
+    leaf.box = sb::leaf_box_steps(task.box, task.step, cell.r3, a.i4, g.n4, a.i5, g.n5, a.i6, g.n6);
+    v.R = sb::remaining_weight(leaf.box);
+    if (sb::box_empty(leaf.box) || cc::empty(v.R)) return CC_SBT_LEAF_EMPTY;
+    cc::trap_clear();
+    const bool ok = sb::sb_criterion(0, leaf.box, v);
+    int outcome;
+    if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
+    else outcome = ok ? 0 : CC_SBT_LEAF_CRITICAL;  // CRITICAL here = undecided
+    cc::trap_clear();
+    return outcome;
+}
+
+// Trace, queue and criticals of a warp's leaves after the leaf stage
+__device__ __forceinline__ void leaf_emit(BlockTrace<CC_SBT_LEAF_OUTCOMES>& bt, bool valid, int outcome, SbLeaf& leaf,
+                                          int gen, SbLeaf* __restrict__ q, unsigned long long* n_q,
+                                          unsigned long long q_cap, SbLeaf* __restrict__ crit,
+                                          unsigned long long crit_cap, SbCounters* c) {
+    const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
+    trace_note(bt, valid && !undecided, valid ? leaf_key(gen, leaf, outcome) : 0, outcome);
+    unsigned long long slot = warp_append(n_q, undecided, q_cap, &c->overflow);
+    if (slot != ~0ULL) q[slot] = leaf;
+    const bool trapped = valid && outcome == CC_SBT_LEAF_TRAPPED;
+    slot = warp_append(&c->n_crit, trapped, crit_cap, &c->overflow);
+    if (slot != ~0ULL) {
+        leaf.idx |= 1ULL << 63;
+        crit[slot] = leaf;
+    }
+}
+
+// Leaves [l0, l1) of the cell grid without the pre-filter: the FP64 leaf
+// stage on every leaf.  Undecided leaves go to queue `q`, trapped ones to the
+// criticals.
 __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restrict__ tasks,
                                                           const SbCell* __restrict__ cells, unsigned long long l0,
                                                           unsigned long long l1, LeafGrid g, SbLeaf* __restrict__ q,
@@ -340,99 +405,127 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
                                                           SbLeaf* __restrict__ crit, unsigned long long crit_cap,
                                                           SbCounters* c) {
     __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
-    __shared__ unsigned long long fp32_empty_b, widen_n_b, widen_max_b;
-    __shared__ double widen_sum_b;
-    if (threadIdx.x == 0) fp32_empty_b = 0, widen_n_b = 0, widen_sum_b = 0.0, widen_max_b = 0;
-    // per-thread pre-filter statistics, reduced once per block
-    unsigned int fp32_empty = 0, widen_n = 0;
-    double widen_sum = 0.0, widen_max = 0.0;
     trace_init(bt);
-    const unsigned long long n456 = (unsigned long long)g.n4 * g.n5 * g.n6;
     SB_WARP_LOOP(l1 - l0) {
         const unsigned long long idx = l0 + base_ + (threadIdx.x & 31);
         const bool valid = idx < l1;
         int outcome = CC_SBT_LEAF_EMPTY;
         SbLeaf leaf;
         if (valid) {
-            unsigned long long ci;
-            int i4, i5, i6;
-            if (n456 < (1ULL << 31) && l1 - l0 < (1ULL << 31)) {
-                // 32-bit index arithmetic: offsets from the slice's first cell
-                const uint32_t off = g.rem0 + (uint32_t)(idx - l0);  // < 2^32
-                const uint32_t q = off / (uint32_t)n456;
-                const uint32_t rem = off - q * (uint32_t)n456;
-                const uint32_t r56 = rem / (uint32_t)g.n6;
-                ci = g.cell0 + q;
-                i6 = (int)(rem - r56 * (uint32_t)g.n6);
-                i4 = (int)(r56 / (uint32_t)g.n5);
-                i5 = (int)(r56 - (uint32_t)i4 * (uint32_t)g.n5);
-            } else {
-                ci = idx / n456;
-                const unsigned long long rem = idx % n456;
-                i6 = (int)(rem % g.n6);
-                i5 = (int)((rem / g.n6) % g.n5);
-                i4 = (int)(rem / ((unsigned long long)g.n6 * g.n5));
-            }
-            const SbCell cell = cells[ci];
+            const LeafAt a = leaf_at(g, l0, l1, idx);
+            const SbCell cell = cells[a.ci];
             const SbTask& task = tasks[cell.task];
             leaf.id = task.id;
-            leaf.idx = pack_idx((int)cell.i3, i4, i5, i6);
-            float lb_R = 0.0f, ub_R = 0.0f;
-            const int pidx[3] = {i4, i5, i6}, pn[3] = {g.n4, g.n5, g.n6};
-            if (g.fp32 && f32_leaf_empty(task.f, cell.r3_lo_dn, cell.r3_hi_up, pidx, pn, lb_R, ub_R)) {
-                outcome = CC_SBT_LEAF_EMPTY;
-                ++fp32_empty;
-                goto decided;
-            }
-            leaf.box = sb::leaf_box_steps(task.box, task.step, cell.r3, i4, g.n4, i5, g.n5, i6, g.n6);
-            {
+            leaf.idx = pack_idx((int)cell.i3, a.i4, a.i5, a.i6);
             sb::Vals v;
-            v.R = sb::remaining_weight(leaf.box);
-            if (g.fp32 && v.R.hi > v.R.lo) {  // widening of the FP32 bounds of R over FP64 R
+            outcome = leaf_fp64(task, cell, a, g, leaf, v);
+        }
+        const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
+        if ((threadIdx.x & 31) == 0) atomicAdd(&bt.extra, (unsigned long long)nv);
+        leaf_emit(bt, valid, outcome, leaf, g.gen, q, n_q, q_cap, crit, crit_cap, c);
+    }
+    trace_flush(bt, c->leaf_counts, c, &c->leaf_evals);
+}
+
+// Leaves [l0, l1) through the FP32 pre-filter: a leaf it proves empty is
+// decided (outcome EMPTY); the offsets (idx - l0) of the others go to the
+// candidate list for k_sbp_leaf_check, so that the FP64 leaf stage runs on
+// full warps of leaves that need it (most warps hold only empty leaves).
+__global__ void __launch_bounds__(kThreads) k_sbp_leaf_filter(const SbTask* __restrict__ tasks,
+                                                               const SbCell* __restrict__ cells, unsigned long long l0,
+                                                               unsigned long long l1, LeafGrid g,
+                                                               uint32_t* __restrict__ cand, unsigned long long* n_cand,
+                                                               unsigned long long cand_cap, SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    unsigned int fp32_empty = 0;
+    SB_WARP_LOOP(l1 - l0) {
+        const unsigned long long idx = l0 + base_ + (threadIdx.x & 31);
+        const bool valid = idx < l1;
+        bool empty = false;
+        SbLeaf leaf;
+        if (valid) {
+            const LeafAt a = leaf_at(g, l0, l1, idx);
+            const SbCell cell = cells[a.ci];
+            const SbTask& task = tasks[cell.task];
+            leaf.id = task.id;
+            leaf.idx = pack_idx((int)cell.i3, a.i4, a.i5, a.i6);
+            float lb_R, ub_R;
+            const int pidx[3] = {a.i4, a.i5, a.i6}, pn[3] = {g.n4, g.n5, g.n6};
+            empty = f32_leaf_empty(task.f, cell.r3_lo_dn, cell.r3_hi_up, pidx, pn, lb_R, ub_R);
+            fp32_empty += empty;
+        }
+        trace_note(bt, valid && empty, valid && empty ? leaf_key(g.gen, leaf, CC_SBT_LEAF_EMPTY) : 0,
+                   CC_SBT_LEAF_EMPTY);
+        const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
+        if ((threadIdx.x & 31) == 0) atomicAdd(&bt.extra, (unsigned long long)nv);
+        const unsigned long long slot = warp_append(n_cand, valid && !empty, cand_cap, &c->overflow);
+        if (slot != ~0ULL) cand[slot] = (uint32_t)(idx - l0);
+    }
+    // one atomic per warp for the pre-filter count
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) fp32_empty += __shfl_xor_sync(0xffffffffu, fp32_empty, o);
+    if ((threadIdx.x & 31) == 0 && fp32_empty) atomicAdd(&c->fp32_empty, (unsigned long long)fp32_empty);
+    trace_flush(bt, c->leaf_counts, c, &c->leaf_evals);
+}
+
+// The FP64 leaf stage on the pre-filter's candidates (offsets into the
+// slice [l0, l1)); also the statistics of the pre-filter's widening of R.
+__global__ void __launch_bounds__(kThreads) k_sbp_leaf_check(const SbTask* __restrict__ tasks,
+                                                              const SbCell* __restrict__ cells, unsigned long long l0,
+                                                              unsigned long long l1, LeafGrid g,
+                                                              const uint32_t* __restrict__ cand,
+                                                              const unsigned long long* n_cand,
+                                                              unsigned long long cand_cap, SbLeaf* __restrict__ q,
+                                                              unsigned long long* n_q, unsigned long long q_cap,
+                                                              SbLeaf* __restrict__ crit, unsigned long long crit_cap,
+                                                              SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    __shared__ unsigned long long widen_n_b, widen_max_b;
+    __shared__ double widen_sum_b;
+    if (threadIdx.x == 0) widen_n_b = 0, widen_sum_b = 0.0, widen_max_b = 0;
+    // per-thread statistics, reduced once per block
+    unsigned int widen_n = 0;
+    double widen_sum = 0.0, widen_max = 0.0;
+    trace_init(bt);
+    // an overflowed list (the slice is redone) is read no further than its capacity
+    const unsigned long long total = *n_cand < cand_cap ? *n_cand : cand_cap;
+    SB_WARP_LOOP(total) {
+        const unsigned long long k = base_ + (threadIdx.x & 31);
+        const bool valid = k < total;
+        int outcome = CC_SBT_LEAF_EMPTY;
+        SbLeaf leaf;
+        if (valid) {
+            const unsigned long long idx = l0 + cand[k];
+            const LeafAt a = leaf_at(g, l0, l1, idx);
+            const SbCell cell = cells[a.ci];
+            const SbTask& task = tasks[cell.task];
+            leaf.id = task.id;
+            leaf.idx = pack_idx((int)cell.i3, a.i4, a.i5, a.i6);
+            float lb_R, ub_R;
+            const int pidx[3] = {a.i4, a.i5, a.i6}, pn[3] = {g.n4, g.n5, g.n6};
+            f32_leaf_empty(task.f, cell.r3_lo_dn, cell.r3_hi_up, pidx, pn, lb_R, ub_R);
+            sb::Vals v;
+            outcome = leaf_fp64(task, cell, a, g, leaf, v);
+            if (v.R.hi > v.R.lo) {  // widening of the FP32 bounds of R over FP64 R
                 const double w = ((double)ub_R - (double)(lb_R > 0.0f ? lb_R : 0.0f)) / (v.R.hi - v.R.lo);
                 ++widen_n;
                 widen_sum += w;
                 widen_max = w > widen_max ? w : widen_max;
             }
-            if (sb::box_empty(leaf.box) || cc::empty(v.R)) {
-                outcome = CC_SBT_LEAF_EMPTY;
-            } else {
-                cc::trap_clear();
-                const bool ok = sb::sb_criterion(0, leaf.box, v);
-                if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
-                else outcome = ok ? 0 : CC_SBT_LEAF_CRITICAL;  // CRITICAL here = undecided
-                cc::trap_clear();
-            }
-            }
         }
-    decided:
-        const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
-        trace_note(bt, valid && !undecided, valid ? leaf_key(g.gen, leaf, outcome) : 0, outcome);
-        const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
-        if ((threadIdx.x & 31) == 0) atomicAdd(&bt.extra, (unsigned long long)nv);
-        unsigned long long slot = warp_append(n_q, undecided, q_cap, &c->overflow);
-        if (slot != ~0ULL) q[slot] = leaf;
-        const bool trapped = valid && outcome == CC_SBT_LEAF_TRAPPED;
-        slot = warp_append(&c->n_crit, trapped, crit_cap, &c->overflow);
-        if (slot != ~0ULL) {
-            leaf.idx |= 1ULL << 63;
-            crit[slot] = leaf;
-        }
+        leaf_emit(bt, valid, outcome, leaf, g.gen, q, n_q, q_cap, crit, crit_cap, c);
     }
-    if (fp32_empty) atomicAdd(&fp32_empty_b, (unsigned long long)fp32_empty);
     if (widen_n) {
         atomicAdd(&widen_n_b, (unsigned long long)widen_n);
         atomicAdd(&widen_sum_b, widen_sum);
         atomicMax(&widen_max_b, (unsigned long long)__double_as_longlong(widen_max));
     }
-    trace_flush(bt, c->leaf_counts, c, &c->leaf_evals);
-    if (threadIdx.x == 0) {
-        if (fp32_empty_b) atomicAdd(&c->fp32_empty, fp32_empty_b);
-        if (widen_n_b) {
-            atomicAdd(&c->widen_count, widen_n_b);
-            atomicAdd(&c->widen_sum, widen_sum_b);
-            atomicMax(&c->widen_max_bits, widen_max_b);
-        }
+    trace_flush(bt, c->leaf_counts, c, nullptr);
+    if (threadIdx.x == 0 && widen_n_b) {
+        atomicAdd(&c->widen_count, widen_n_b);
+        atomicAdd(&c->widen_sum, widen_sum_b);
+        atomicMax(&c->widen_max_bits, widen_max_b);
     }
 }
 
@@ -848,7 +941,7 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
     if (chunk > e.task_chunk) chunk = e.task_chunk;
     if (chunk < 1) chunk = 1;
     TaskGrid tg{gen, nla, rn[0], rn[1], rn[3], rn[4], rn[5], per_parent};
-    LeafGrid lg{gen, rn[3], rn[4], rn[5], e.fp32 ? 1 : 0, 0u, 0ULL};
+    LeafGrid lg{gen, rn[3], rn[4], rn[5], 0u, 0ULL};
     for (unsigned long long t0 = 0; t0 < ntasks; t0 += chunk) {
         if (gen > 0 && e.h->interrupt.load()) return CC_ERR_INTERRUPTED;
         const unsigned long long t1 = t0 + chunk < ntasks ? t0 + chunk : ntasks;
@@ -867,12 +960,24 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
             if (e.hc->n_crit > e.crit_cap - e.slice && (st = drain_criticals(e))) return st;
             const unsigned long long l1 = n_leaves - l0 > e.range ? l0 + e.range : n_leaves;
             CC_CUDA(e.h, cudaMemcpyAsync(e.backup, e.dc, sizeof(SbCounters), cudaMemcpyDeviceToDevice, e.s));
-            CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[0], 0, sizeof(unsigned long long), e.s));
+            CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[0], 0, 2 * sizeof(unsigned long long), e.s));
             int lgrid = (int)std::min<unsigned long long>((l1 - l0 + kThreads - 1) / kThreads, (unsigned long long)e.grid);
             lg.cell0 = l0 / n456;
             lg.rem0 = (uint32_t)(l0 % n456);
             if (e.plain) {
                 k_sbp_leaves_plain<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, e.crit, e.crit_cap, e.dc);
+            } else if (e.fp32) {
+                // the candidate list lives in the second pass queue's memory
+                // (free until pass 1) and is counted by its counter
+                uint32_t* cand = reinterpret_cast<uint32_t*>(e.q[1]);
+                const unsigned long long cand_cap = e.slice * (sizeof(SbLeaf) / sizeof(uint32_t));
+                k_sbp_leaf_filter<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, cand, &e.dc->n_q[1],
+                                                               cand_cap, e.dc);
+                CC_LAUNCHED(e.h);
+                e.launches++;
+                k_sbp_leaf_check<<<e.grid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, cand, &e.dc->n_q[1],
+                                                               cand_cap, e.q[0], &e.dc->n_q[0], e.slice, e.crit,
+                                                               e.crit_cap, e.dc);
             } else {
                 k_sbp_leaves<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, e.q[0], &e.dc->n_q[0],
                                                           e.slice, e.crit, e.crit_cap, e.dc);
