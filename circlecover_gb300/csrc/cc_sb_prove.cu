@@ -94,6 +94,7 @@ struct SbCounters {
     unsigned long long widen_count;     // leaves with an FP64 R of nonzero width
     double widen_sum;                   // sum of FP32 / FP64 width of R over them
     unsigned long long widen_max_bits;  // bits of the largest ratio (positive doubles order as integers)
+    unsigned long long n_strip;         // FP64 jobs of the multi-disk strip criterion
 };
 
 struct SevenJob {  // a leaf whose seven-disk prefix left r7 pieces to check
@@ -613,6 +614,95 @@ __global__ void __launch_bounds__(kThreads) k_sbp_pass(const SbLeaf* __restrict_
     trace_flush(bt, c->leaf_counts, c, nullptr);
 }
 
+// The multi-disk strip criterion (K = 2) FP32-first.  Its placements 0..6
+// run on FP32 enclosures of the leaf box in order: the first that works
+// decided, or every one decided not to work, is the FP64 outcome up to there
+// (cc_f32.cuh).  A leaf whose placements all failed, or whose evaluation met
+// an undecided comparison at placement k, becomes a job (its queue index,
+// and k or 7 in bits 28..30) for k_sbp_strip_fp64, which resumes the FP64
+// criterion at that placement.
+constexpr uint32_t kStripJobIndexBits = 28;
+static_assert(kStripJobIndexBits <= 28 && (1u << kStripJobIndexBits) >= (1u << 26), "queue index of a strip job");
+
+__global__ void __launch_bounds__(kThreads) k_sbp_strip_f32(const SbLeaf* __restrict__ qin,
+                                                             const unsigned long long* n_in, uint32_t* __restrict__ jobs,
+                                                             unsigned long long* n_jobs, unsigned long long job_cap,
+                                                             int gen, SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    const unsigned long long total = *n_in;
+    SB_WARP_LOOP(total) {
+        const unsigned long long idx = base_ + (threadIdx.x & 31);
+        const bool valid = idx < total;
+        bool works = false;
+        int from = sb::kStripPlacements - 1;
+        SbLeaf leaf;
+        if (valid) {
+            leaf = qin[idx];
+            const sb::Box6T<cc::f32::IvF> e = sb::enclose6(leaf.box);
+            for (int k = 0; k < sb::kStripPlacements - 1; ++k) {
+                cc::trap_clear();
+                const bool ok = sb::strip_placement(e, k);
+                if (cc::trap_status() != cc::TRAP_NONE) {
+                    from = k;
+                    break;
+                }
+                if (ok) {
+                    works = true;
+                    break;
+                }
+            }
+            cc::trap_clear();
+        }
+        trace_note(bt, valid && works, valid && works ? leaf_key(gen, leaf, sb::SB_MULTI_DISK_STRIP) : 0,
+                   sb::SB_MULTI_DISK_STRIP);
+        const unsigned long long slot = warp_append(n_jobs, valid && !works, job_cap, &c->overflow);
+        if (slot != ~0ULL) jobs[slot] = (uint32_t)idx | ((uint32_t)from << kStripJobIndexBits);
+    }
+    trace_flush(bt, c->leaf_counts, c, nullptr);
+}
+
+__global__ void __launch_bounds__(kThreads) k_sbp_strip_fp64(const SbLeaf* __restrict__ qin,
+                                                              const uint32_t* __restrict__ jobs,
+                                                              const unsigned long long* n_jobs,
+                                                              unsigned long long job_cap, SbLeaf* __restrict__ qout,
+                                                              unsigned long long* n_out, unsigned long long q_cap,
+                                                              SbLeaf* __restrict__ crit, unsigned long long crit_cap,
+                                                              int gen, SbCounters* c) {
+    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
+    trace_init(bt);
+    const unsigned long long total = *n_jobs < job_cap ? *n_jobs : job_cap;
+    SB_WARP_LOOP(total) {
+        const unsigned long long k = base_ + (threadIdx.x & 31);
+        const bool valid = k < total;
+        int outcome = CC_SBT_LEAF_CRITICAL;
+        SbLeaf leaf;
+        if (valid) {
+            const uint32_t job = jobs[k];
+            leaf = qin[job & ((1u << kStripJobIndexBits) - 1)];
+            sb::Vals v;
+            v.R = sb::remaining_weight(leaf.box);
+            cc::trap_clear();
+            const bool ok = sb::multi_disk_strip_from(leaf.box, v, (int)(job >> kStripJobIndexBits));
+            if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
+            else if (ok) outcome = sb::SB_MULTI_DISK_STRIP;
+            cc::trap_clear();
+        }
+        const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
+        const bool decided = valid && !undecided;
+        trace_note(bt, decided, decided ? leaf_key(gen, leaf, outcome) : 0, outcome);
+        unsigned long long slot = warp_append(n_out, undecided, q_cap, &c->overflow);
+        if (slot != ~0ULL) qout[slot] = leaf;
+        const bool to_crit = valid && outcome == CC_SBT_LEAF_TRAPPED;
+        slot = warp_append(&c->n_crit, to_crit, crit_cap, &c->overflow);
+        if (slot != ~0ULL) {
+            leaf.idx |= 1ULL << 63;
+            crit[slot] = leaf;
+        }
+    }
+    trace_flush(bt, c->leaf_counts, c, nullptr);
+}
+
 // A criterion made of independent placements tried in order until one
 // works (r1 in a corner: nine placements) runs one placement per thread; the
 // resolve kernel then combines them as the sequential loop would: the first
@@ -882,6 +972,21 @@ int launch_passes(Engine& e, int gen, int src) {
         return launch_passes<K + 1>(e, gen, dst);
     } else if constexpr (K < sb::SB_SEVEN_DISK) {
         const int dst = src ^ 1;
+        if (K == sb::SB_MULTI_DISK_STRIP && e.fp32) {
+            // the jobs live in the seven-disk job buffer (free until then)
+            uint32_t* jobs = reinterpret_cast<uint32_t*>(e.jobs);
+            const unsigned long long job_cap = e.slice * (sizeof(SevenJob) / sizeof(uint32_t));
+            CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
+            CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_strip, 0, sizeof(unsigned long long), e.s));
+            k_sbp_strip_f32<<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], jobs, &e.dc->n_strip, job_cap,
+                                                           gen, e.dc);
+            CC_LAUNCHED(e.h);
+            k_sbp_strip_fp64<<<e.grid, kThreads, 0, e.s>>>(e.q[src], jobs, &e.dc->n_strip, job_cap, e.q[dst],
+                                                            &e.dc->n_q[dst], e.slice, e.crit, e.crit_cap, gen, e.dc);
+            CC_LAUNCHED(e.h);
+            e.launches += 2;
+            return launch_passes<K + 1>(e, gen, dst);
+        }
         CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
         k_sbp_pass<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], e.q[dst], &e.dc->n_q[dst], e.slice,
                                                      e.crit, e.crit_cap, gen, e.dc);
