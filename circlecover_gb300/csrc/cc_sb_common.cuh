@@ -25,7 +25,10 @@ CC_FN bool disk_satisfies_size_bound(S r_sq_ub, S height_lb) {
 }
 
 // (disk_satisfies_size_bound.cu:30-32)
-CC_FN double bound_required_height(double r_sq_ub) { return div_up(sqrt_up(r_sq_ub), kUbDiskRadius); }
+template <class S>
+CC_FN S bound_required_height(S r_sq_ub) {
+    return div_up(sqrt_up(r_sq_ub), kUbDiskRadius);
+}
 
 // (disk_satisfies_size_bound.cu:34-37)
 CC_FN double bound_allowed_weight(double lb_height) {

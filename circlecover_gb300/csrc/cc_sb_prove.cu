@@ -94,7 +94,7 @@ struct SbCounters {
     unsigned long long widen_count;     // leaves with an FP64 R of nonzero width
     double widen_sum;                   // sum of FP32 / FP64 width of R over them
     unsigned long long widen_max_bits;  // bits of the largest ratio (positive doubles order as integers)
-    unsigned long long n_strip;         // FP64 jobs of the multi-disk strip criterion
+    unsigned long long n_f32_jobs;      // FP64 jobs of an FP32-first pass
 };
 
 struct SevenJob {  // a leaf whose seven-disk prefix left r7 pieces to check
@@ -614,37 +614,68 @@ __global__ void __launch_bounds__(kThreads) k_sbp_pass(const SbLeaf* __restrict_
     trace_flush(bt, c->leaf_counts, c, nullptr);
 }
 
-// The multi-disk strip criterion (K = 2) FP32-first.  Its placements 0..6
-// run on FP32 enclosures of the leaf box in order: the first that works
-// decided, or every one decided not to work, is the FP64 outcome up to there
-// (cc_f32.cuh).  A leaf whose placements all failed, or whose evaluation met
-// an undecided comparison at placement k, becomes a job (its queue index,
-// and k or 7 in bits 28..30) for k_sbp_strip_fp64, which resumes the FP64
-// criterion at that placement.
-constexpr uint32_t kStripJobIndexBits = 28;
-static_assert(kStripJobIndexBits <= 28 && (1u << kStripJobIndexBits) >= (1u << 26), "queue index of a strip job");
+// FP32-first passes.  A criterion with an FP32 form is a sequence of
+// placements tried in order until one works; placements 0..kPlacements-1
+// are templates over the interval type and run first on FP32 enclosures of
+// the leaf box: the first that works decided, or every one decided not to
+// work, is the FP64 outcome up to there (cc_f32.cuh).  A leaf whose
+// evaluation met an undecided comparison at placement k, or whose FP32
+// placements all failed when FP64-only placements follow (kTail), becomes a
+// job -- its queue index, and k (or kPlacements) in bits 28..30 -- for
+// k_sbp_fp64<K>, which resumes the FP64 criterion at that placement.
+template <int K>
+struct F32Pass;
+template <>
+struct F32Pass<sb::SB_UNEVEN_SPLIT> {  // one placement, the whole criterion
+    static constexpr int kPlacements = 1;
+    static constexpr bool kTail = false;
+    template <class I>
+    __device__ static bool placement(const sb::Box6T<I>& b, int) {
+        return sb::uneven_split_t(b);
+    }
+    __device__ static bool fp64_from(const Box6& b, const sb::Vals& v, int) { return sb::uneven_split_recursion(b, v); }
+};
+template <>
+struct F32Pass<sb::SB_MULTI_DISK_STRIP> {  // placements 0..6; three rows in FP64 only
+    static constexpr int kPlacements = sb::kStripPlacements - 1;
+    static constexpr bool kTail = true;
+    template <class I>
+    __device__ static bool placement(const sb::Box6T<I>& b, int k) {
+        return sb::strip_placement(b, k);
+    }
+    __device__ static bool fp64_from(const Box6& b, const sb::Vals& v, int from) {
+        return sb::multi_disk_strip_from(b, v, from);
+    }
+};
 
-__global__ void __launch_bounds__(kThreads) k_sbp_strip_f32(const SbLeaf* __restrict__ qin,
-                                                             const unsigned long long* n_in, uint32_t* __restrict__ jobs,
-                                                             unsigned long long* n_jobs, unsigned long long job_cap,
-                                                             int gen, SbCounters* c) {
+constexpr uint32_t kF32JobIndexBits = 28;  // queue indices are below 2^26 (the largest slice)
+static_assert(F32Pass<sb::SB_MULTI_DISK_STRIP>::kPlacements < 8, "placement index in bits 28..30");
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_sbp_f32(const SbLeaf* __restrict__ qin, const unsigned long long* n_in,
+                                                       uint32_t* __restrict__ jobs, unsigned long long* n_jobs,
+                                                       unsigned long long job_cap, SbLeaf* __restrict__ qout,
+                                                       unsigned long long* n_out, unsigned long long q_cap, int gen,
+                                                       SbCounters* c) {
+    using P = F32Pass<K>;
     __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
     trace_init(bt);
     const unsigned long long total = *n_in;
     SB_WARP_LOOP(total) {
         const unsigned long long idx = base_ + (threadIdx.x & 31);
         const bool valid = idx < total;
-        bool works = false;
-        int from = sb::kStripPlacements - 1;
+        bool works = false, undecided = false;
+        int from = P::kPlacements;
         SbLeaf leaf;
         if (valid) {
             leaf = qin[idx];
             const sb::Box6T<cc::f32::IvF> e = sb::enclose6(leaf.box);
-            for (int k = 0; k < sb::kStripPlacements - 1; ++k) {
+            for (int k = 0; k < P::kPlacements; ++k) {
                 cc::trap_clear();
-                const bool ok = sb::strip_placement(e, k);
+                const bool ok = P::placement(e, k);
                 if (cc::trap_status() != cc::TRAP_NONE) {
                     from = k;
+                    undecided = true;
                     break;
                 }
                 if (ok) {
@@ -654,21 +685,24 @@ __global__ void __launch_bounds__(kThreads) k_sbp_strip_f32(const SbLeaf* __rest
             }
             cc::trap_clear();
         }
-        trace_note(bt, valid && works, valid && works ? leaf_key(gen, leaf, sb::SB_MULTI_DISK_STRIP) : 0,
-                   sb::SB_MULTI_DISK_STRIP);
-        const unsigned long long slot = warp_append(n_jobs, valid && !works, job_cap, &c->overflow);
-        if (slot != ~0ULL) jobs[slot] = (uint32_t)idx | ((uint32_t)from << kStripJobIndexBits);
+        trace_note(bt, valid && works, valid && works ? leaf_key(gen, leaf, K) : 0, K);
+        const bool job = valid && !works && (undecided || P::kTail);
+        unsigned long long slot = warp_append(n_jobs, job, job_cap, &c->overflow);
+        if (slot != ~0ULL) jobs[slot] = (uint32_t)idx | ((uint32_t)from << kF32JobIndexBits);
+        // decided not to work, nothing after the FP32 placements: next pass
+        slot = warp_append(n_out, valid && !works && !job, q_cap, &c->overflow);
+        if (slot != ~0ULL) qout[slot] = leaf;
     }
     trace_flush(bt, c->leaf_counts, c, nullptr);
 }
 
-__global__ void __launch_bounds__(kThreads) k_sbp_strip_fp64(const SbLeaf* __restrict__ qin,
-                                                              const uint32_t* __restrict__ jobs,
-                                                              const unsigned long long* n_jobs,
-                                                              unsigned long long job_cap, SbLeaf* __restrict__ qout,
-                                                              unsigned long long* n_out, unsigned long long q_cap,
-                                                              SbLeaf* __restrict__ crit, unsigned long long crit_cap,
-                                                              int gen, SbCounters* c) {
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_sbp_fp64(const SbLeaf* __restrict__ qin,
+                                                        const uint32_t* __restrict__ jobs,
+                                                        const unsigned long long* n_jobs, unsigned long long job_cap,
+                                                        SbLeaf* __restrict__ qout, unsigned long long* n_out,
+                                                        unsigned long long q_cap, SbLeaf* __restrict__ crit,
+                                                        unsigned long long crit_cap, int gen, SbCounters* c) {
     __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
     trace_init(bt);
     const unsigned long long total = *n_jobs < job_cap ? *n_jobs : job_cap;
@@ -679,13 +713,13 @@ __global__ void __launch_bounds__(kThreads) k_sbp_strip_fp64(const SbLeaf* __res
         SbLeaf leaf;
         if (valid) {
             const uint32_t job = jobs[k];
-            leaf = qin[job & ((1u << kStripJobIndexBits) - 1)];
+            leaf = qin[job & ((1u << kF32JobIndexBits) - 1)];
             sb::Vals v;
             v.R = sb::remaining_weight(leaf.box);
             cc::trap_clear();
-            const bool ok = sb::multi_disk_strip_from(leaf.box, v, (int)(job >> kStripJobIndexBits));
+            const bool ok = F32Pass<K>::fp64_from(leaf.box, v, (int)(job >> kF32JobIndexBits));
             if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
-            else if (ok) outcome = sb::SB_MULTI_DISK_STRIP;
+            else if (ok) outcome = K;
             cc::trap_clear();
         }
         const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
@@ -972,20 +1006,22 @@ int launch_passes(Engine& e, int gen, int src) {
         return launch_passes<K + 1>(e, gen, dst);
     } else if constexpr (K < sb::SB_SEVEN_DISK) {
         const int dst = src ^ 1;
-        if (K == sb::SB_MULTI_DISK_STRIP && e.fp32) {
-            // the jobs live in the seven-disk job buffer (free until then)
-            uint32_t* jobs = reinterpret_cast<uint32_t*>(e.jobs);
-            const unsigned long long job_cap = e.slice * (sizeof(SevenJob) / sizeof(uint32_t));
-            CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
-            CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_strip, 0, sizeof(unsigned long long), e.s));
-            k_sbp_strip_f32<<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], jobs, &e.dc->n_strip, job_cap,
-                                                           gen, e.dc);
-            CC_LAUNCHED(e.h);
-            k_sbp_strip_fp64<<<e.grid, kThreads, 0, e.s>>>(e.q[src], jobs, &e.dc->n_strip, job_cap, e.q[dst],
-                                                            &e.dc->n_q[dst], e.slice, e.crit, e.crit_cap, gen, e.dc);
-            CC_LAUNCHED(e.h);
-            e.launches += 2;
-            return launch_passes<K + 1>(e, gen, dst);
+        if constexpr (K == sb::SB_UNEVEN_SPLIT || K == sb::SB_MULTI_DISK_STRIP) {
+            if (e.fp32) {
+                // the jobs live in the seven-disk job buffer (free until then)
+                uint32_t* jobs = reinterpret_cast<uint32_t*>(e.jobs);
+                const unsigned long long job_cap = e.slice * (sizeof(SevenJob) / sizeof(uint32_t));
+                CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
+                CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_f32_jobs, 0, sizeof(unsigned long long), e.s));
+                k_sbp_f32<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], jobs, &e.dc->n_f32_jobs, job_cap,
+                                                            e.q[dst], &e.dc->n_q[dst], e.slice, gen, e.dc);
+                CC_LAUNCHED(e.h);
+                k_sbp_fp64<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], jobs, &e.dc->n_f32_jobs, job_cap, e.q[dst],
+                                                             &e.dc->n_q[dst], e.slice, e.crit, e.crit_cap, gen, e.dc);
+                CC_LAUNCHED(e.h);
+                e.launches += 2;
+                return launch_passes<K + 1>(e, gen, dst);
+            }
         }
         CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
         k_sbp_pass<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], e.q[dst], &e.dc->n_q[dst], e.slice,
