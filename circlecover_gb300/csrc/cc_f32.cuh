@@ -381,6 +381,41 @@ __device__ __forceinline__ double bisect(double lo, double hi, const Dec& dec, c
     }
 }
 
+// The same bisection on FP32 decisions alone, for callers that can go on
+// with an enclosure of its result: the steps run while every one is decided
+// (they are then the FP64 steps); the exact result if the fixpoint is
+// reached that way, else the FP32 enclosure of the bracket at the first
+// undecided step, which holds the FP64 result.  For 0 <= lo and a finite hi
+// the FP64 bisection ends in fewer than 2,100 steps, so its cap cannot trap;
+// other brackets mark the evaluation undecided.
+template <class Dec>
+__device__ __forceinline__ Fv bisect_enclosure(double lo, double hi, const Dec& dec) {
+    if (!(lo >= 0.0 && hi <= 1.7976931348623157e308)) {
+        undecided();
+        return nan_fv();
+    }
+    if (!(lo < hi)) return of(lo);  // the first midpoint is not above lo
+    const int whole = dec(Fv{__double2float_rd(lo), __double2float_ru(hi)});
+    if (whole == NO) return of(lo);
+    for (int it = 0; it < CC_BISECTION_CAP; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) return of(lo);
+        const int d = whole == YES ? YES : dec(of(mid));
+        if (d == UNKNOWN) return Fv{__double2float_rd(lo), __double2float_ru(hi)};
+        if (d == YES) lo = mid;
+        else hi = mid;
+    }
+    undecided();
+    return nan_fv();
+}
+
+// FP64 `a == b`: decided when both are the same point or the enclosures are
+// disjoint
+__device__ __forceinline__ bool operator==(Fv a, Fv b) {
+    const bool ok = a.lo <= a.hi && b.lo <= b.hi;
+    return decide(ok && a.lo == a.hi && b.lo == b.hi && a.lo == b.lo, ok && (a.hi < b.lo || b.hi < a.lo));
+}
+
 __device__ __forceinline__ void tighten_lb(IvF& a, Fv l) { a.lo = greater(l, a.lo); }
 __device__ __forceinline__ void tighten_ub(IvF& a, Fv u) { a.hi = lesser(u, a.hi); }
 __device__ __forceinline__ bool empty(IvF a) { return a.lo > a.hi; }

@@ -795,11 +795,53 @@ __global__ void __launch_bounds__(kThreads) k_sbp_r1c_start(const SbLeaf* __rest
 }
 
 // r1 in a corner, second half: the backtracking of the jobs (the start is
-// recomputed; same operations, same values)
+// recomputed; same operations, same values).  Run FP32-first: the
+// backtracking on FP32 enclosures of the group heights
+// (corner_groups_reach_t<Fv>, its bisections on FP32 decisions alone); a job
+// whose evaluation it leaves undecided, or whose start reached a trap site,
+// goes to `jobs64` for k_sbp_r1c_reach64.
 __global__ void __launch_bounds__(kThreads) k_sbp_r1c_reach(const SbLeaf* __restrict__ qin,
                                                              const unsigned long long* __restrict__ jobs,
-                                                             const unsigned long long* n_jobs, uint32_t* masks) {
-    const unsigned long long total = *n_jobs;
+                                                             const unsigned long long* n_jobs,
+                                                             unsigned long long job_cap, uint32_t* masks,
+                                                             unsigned long long* __restrict__ jobs64,
+                                                             unsigned long long* n64, SbCounters* c) {
+    const unsigned long long total = *n_jobs < job_cap ? *n_jobs : job_cap;
+    SB_WARP_LOOP(total) {
+        const unsigned long long k = base_ + (threadIdx.x & 31);
+        const bool valid = k < total;
+        bool need64 = false;
+        unsigned long long job = 0;
+        if (valid) {
+            job = jobs[k];
+            const unsigned long long leaf = job >> 4;
+            const int i = (int)(job & 15);
+            const Box6 box = qin[leaf].box;
+            sb::Vals v;
+            v.R = sb::remaining_weight(box);
+            cc::trap_clear();
+            sb::CornerStart st;
+            const bool started = sb::r1_corner_start(box, v, i, st);
+            if (cc::trap_status() != cc::TRAP_NONE || !started) {
+                need64 = true;
+            } else {
+                const bool ok = sb::corner_groups_reach_t<cc::f32::Fv>(box, 2 + i / 2, st.cross, st.first, st.limit);
+                if (cc::trap_status() != cc::TRAP_NONE) need64 = true;
+                else if (ok) atomicOr(&masks[2 * leaf], 1u << i);
+            }
+            cc::trap_clear();
+        }
+        const unsigned long long slot = warp_append(n64, need64, job_cap, &c->overflow);
+        if (slot != ~0ULL) jobs64[slot] = job;
+    }
+}
+
+// the FP64 backtracking of the jobs
+__global__ void __launch_bounds__(kThreads) k_sbp_r1c_reach64(const SbLeaf* __restrict__ qin,
+                                                               const unsigned long long* __restrict__ jobs,
+                                                               const unsigned long long* n_jobs,
+                                                               unsigned long long job_cap, uint32_t* masks) {
+    const unsigned long long total = *n_jobs < job_cap ? *n_jobs : job_cap;
     for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
          idx += (unsigned long long)gridDim.x * blockDim.x) {
         const unsigned long long job = jobs[idx];
@@ -990,14 +1032,26 @@ int launch_passes(Engine& e, int gen, int src) {
         // the jobs live in the output queue's memory until the resolve kernel
         // writes the queue; n_q[dst] counts them until then
         unsigned long long* r1c_jobs = reinterpret_cast<unsigned long long*>(e.q[dst]);
-        static_assert(sizeof(SbLeaf) >= 8 * sizeof(unsigned long long), "8 jobs per queue record");
+        static_assert(sizeof(SbLeaf) >= 16 * sizeof(unsigned long long), "16 jobs per queue record");
         CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
         CC_CUDA(e.h, cudaMemsetAsync(masks, 0, e.slice * 2 * sizeof(uint32_t), e.s));
         k_sbp_r1c_start<<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], masks, r1c_jobs, &e.dc->n_q[dst],
                                                        e.slice * 8, e.dc);
         CC_LAUNCHED(e.h);
-        k_sbp_r1c_reach<<<e.grid, kThreads, 0, e.s>>>(e.q[src], r1c_jobs, &e.dc->n_q[dst], masks);
-        CC_LAUNCHED(e.h);
+        const unsigned long long job_cap = e.slice * 8;
+        if (e.fp32) {  // FP32-first; the FP64 jobs in the queue memory's second half
+            unsigned long long* jobs64 = r1c_jobs + job_cap;
+            CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_f32_jobs, 0, sizeof(unsigned long long), e.s));
+            k_sbp_r1c_reach<<<e.grid, kThreads, 0, e.s>>>(e.q[src], r1c_jobs, &e.dc->n_q[dst], job_cap, masks, jobs64,
+                                                           &e.dc->n_f32_jobs, e.dc);
+            CC_LAUNCHED(e.h);
+            k_sbp_r1c_reach64<<<e.grid, kThreads, 0, e.s>>>(e.q[src], jobs64, &e.dc->n_f32_jobs, job_cap, masks);
+            CC_LAUNCHED(e.h);
+            e.launches++;
+        } else {
+            k_sbp_r1c_reach64<<<e.grid, kThreads, 0, e.s>>>(e.q[src], r1c_jobs, &e.dc->n_q[dst], job_cap, masks);
+            CC_LAUNCHED(e.h);
+        }
         CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
         k_sbp_split_resolve<K><<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], masks, e.q[dst],
                                                               &e.dc->n_q[dst], e.slice, e.crit, e.crit_cap, gen, e.dc);
