@@ -139,10 +139,16 @@ CC_FN uint64_t sb_mix64(uint64_t x) {
     x ^= x >> 31;
     return x;
 }
-CC_FN uint64_t sb_trace_key(int gen, uint64_t task, int level, int i3, int i4, int i5, int i6, int outcome) {
+// the key in two parts: the task's share (computed once per task) and the rest
+CC_FN uint64_t sb_trace_task_mix(uint64_t task) { return sb_mix64(task + 0x9e3779b97f4a7c15ULL); }
+CC_FN uint64_t sb_trace_key_mixed(int gen, uint64_t task_mix, int level, int i3, int i4, int i5, int i6,
+                                  int outcome) {
     uint64_t packed = (uint64_t)outcome | ((uint64_t)i6 << 5) | ((uint64_t)i5 << 16) | ((uint64_t)i4 << 27) |
                       ((uint64_t)i3 << 38) | ((uint64_t)level << 49) | ((uint64_t)gen << 51);
-    return sb_mix64(packed ^ sb_mix64(task + 0x9e3779b97f4a7c15ULL));
+    return sb_mix64(packed ^ task_mix);
+}
+CC_FN uint64_t sb_trace_key(int gen, uint64_t task, int level, int i3, int i4, int i5, int i6, int outcome) {
+    return sb_trace_key_mixed(gen, sb_trace_task_mix(task), level, i3, i4, i5, i6, outcome);
 }
 
 }  // namespace sb

@@ -66,6 +66,7 @@ struct SbTaskF32 {
 struct SbTask {  // a task that passed the whole-task shortcuts
     Box6 box;
     uint64_t id;
+    uint64_t id_mix;  // sb_trace_task_mix(id)
     double step[3];  // steps of its r4, r5, r6 splits
     SbTaskF32 f;
 };
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(kThreads) k_sbp_tasks(const Box6* __restrict__
         if (slot != ~0ULL) {
             out[slot].box = tb;
             out[slot].id = idx;
+            out[slot].id_mix = sb::sb_trace_task_mix(idx);
             out[slot].step[0] = cc::subinterval_step(tb.r[3], g.n4);
             out[slot].step[1] = cc::subinterval_step(tb.r[4], g.n5);
             out[slot].step[2] = cc::subinterval_step(tb.r[5], g.n6);
@@ -437,37 +439,44 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaf_filter(const SbTask* __re
                                                                unsigned long long l1, LeafGrid g,
                                                                uint32_t* __restrict__ cand, unsigned long long* n_cand,
                                                                unsigned long long cand_cap, SbCounters* c) {
-    __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
-    trace_init(bt);
-    unsigned int fp32_empty = 0;
+    // the trace of the empty leaves, summed per thread and flushed once
+    unsigned long long digest = 0;
+    unsigned int n_empty = 0, n_valid = 0;
     SB_WARP_LOOP(l1 - l0) {
         const unsigned long long idx = l0 + base_ + (threadIdx.x & 31);
         const bool valid = idx < l1;
         bool empty = false;
-        SbLeaf leaf;
         if (valid) {
             const LeafAt a = leaf_at(g, l0, l1, idx);
             const SbCell cell = cells[a.ci];
             const SbTask& task = tasks[cell.task];
-            leaf.id = task.id;
-            leaf.idx = pack_idx((int)cell.i3, a.i4, a.i5, a.i6);
             float lb_R, ub_R;
             const int pidx[3] = {a.i4, a.i5, a.i6}, pn[3] = {g.n4, g.n5, g.n6};
             empty = f32_leaf_empty(task.f, cell.r3_lo_dn, cell.r3_hi_up, pidx, pn, lb_R, ub_R);
-            fp32_empty += empty;
+            if (empty) {
+                digest += sb::sb_trace_key_mixed(g.gen, task.id_mix, 2, (int)cell.i3, a.i4, a.i5, a.i6,
+                                                 CC_SBT_LEAF_EMPTY);
+                ++n_empty;
+            }
+            ++n_valid;
         }
-        trace_note(bt, valid && empty, valid && empty ? leaf_key(g.gen, leaf, CC_SBT_LEAF_EMPTY) : 0,
-                   CC_SBT_LEAF_EMPTY);
-        const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
-        if ((threadIdx.x & 31) == 0) atomicAdd(&bt.extra, (unsigned long long)nv);
         const unsigned long long slot = warp_append(n_cand, valid && !empty, cand_cap, &c->overflow);
         if (slot != ~0ULL) cand[slot] = (uint32_t)(idx - l0);
     }
-    // one atomic per warp for the pre-filter count
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) fp32_empty += __shfl_xor_sync(0xffffffffu, fp32_empty, o);
-    if ((threadIdx.x & 31) == 0 && fp32_empty) atomicAdd(&c->fp32_empty, (unsigned long long)fp32_empty);
-    trace_flush(bt, c->leaf_counts, c, &c->leaf_evals);
+    for (int o = 16; o > 0; o >>= 1) {
+        digest += __shfl_xor_sync(0xffffffffu, digest, o);
+        n_empty += __shfl_xor_sync(0xffffffffu, n_empty, o);
+        n_valid += __shfl_xor_sync(0xffffffffu, n_valid, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (digest) atomicAdd(&c->digest, digest);
+        if (n_empty) {
+            atomicAdd(&c->leaf_counts[CC_SBT_LEAF_EMPTY], (unsigned long long)n_empty);
+            atomicAdd(&c->fp32_empty, (unsigned long long)n_empty);
+        }
+        if (n_valid) atomicAdd(&c->leaf_evals, (unsigned long long)n_valid);
+    }
 }
 
 // The FP64 leaf stage on the pre-filter's candidates (offsets into the
