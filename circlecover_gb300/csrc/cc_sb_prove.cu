@@ -365,14 +365,23 @@ __device__ __forceinline__ LeafAt leaf_at(const LeafGrid& g, unsigned long long 
 }
 
 // The FP64 part of a leaf (rectangle_size_bound.cu:180-205): box, tighten,
-// R and the empty checks, then criterion 0 of the cascade.  Returns the leaf
-// outcome (0, EMPTY, TRAPPED, or CRITICAL for undecided); fills leaf.box.
+// R and the empty checks, then criterion 0 of the cascade (with F32, first
+// on FP32 enclosures of the box and R, in FP64 where they leave it
+// undecided).  Returns the leaf outcome (0, EMPTY, TRAPPED, or CRITICAL for
+// undecided); fills leaf.box.
+template <bool F32>
 __device__ __forceinline__ int leaf_fp64(const SbTask& task, const SbCell& cell, const LeafAt& a, const LeafGrid& g,
                                          SbLeaf& leaf, sb::Vals& v) {
     leaf.box = sb::leaf_box_steps(task.box, task.step, cell.r3, a.i4, g.n4, a.i5, g.n5, a.i6, g.n6);
     v.R = sb::remaining_weight(leaf.box);
     if (sb::box_empty(leaf.box) || cc::empty(v.R)) return CC_SBT_LEAF_EMPTY;
     cc::trap_clear();
+    if (F32) {
+        static_assert(sb::SB_EVEN_SPLIT == 0, "criterion 0");
+        const bool ok32 = sb::even_split_t(sb::enclose6(leaf.box), cc::f32::of(v.R));
+        if (cc::trap_status() == cc::TRAP_NONE) return ok32 ? 0 : CC_SBT_LEAF_CRITICAL;
+        cc::trap_clear();
+    }
     const bool ok = sb::sb_criterion(0, leaf.box, v);
     int outcome;
     if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
@@ -421,7 +430,7 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
             leaf.id = task.id;
             leaf.idx = pack_idx((int)cell.i3, a.i4, a.i5, a.i6);
             sb::Vals v;
-            outcome = leaf_fp64(task, cell, a, g, leaf, v);
+            outcome = leaf_fp64<false>(task, cell, a, g, leaf, v);
         }
         const unsigned nv = __popc(__ballot_sync(0xffffffffu, valid));
         if ((threadIdx.x & 31) == 0) atomicAdd(&bt.extra, (unsigned long long)nv);
@@ -516,7 +525,7 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaf_check(const SbTask* __res
             const int pidx[3] = {a.i4, a.i5, a.i6}, pn[3] = {g.n4, g.n5, g.n6};
             f32_leaf_empty(task.f, cell.r3_lo_dn, cell.r3_hi_up, pidx, pn, lb_R, ub_R);
             sb::Vals v;
-            outcome = leaf_fp64(task, cell, a, g, leaf, v);
+            outcome = leaf_fp64<true>(task, cell, a, g, leaf, v);
             if (v.R.hi > v.R.lo) {  // widening of the FP32 bounds of R over FP64 R
                 const double w = ((double)ub_R - (double)(lb_R > 0.0f ? lb_R : 0.0f)) / (v.R.hi - v.R.lo);
                 ++widen_n;
