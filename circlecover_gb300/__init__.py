@@ -192,7 +192,8 @@ EXPORTS = [
     "cc_sb_eval", "cc_sb_eval_device", "cc_set_stage_timing", "cc_last_stage_times", "cc_sb_prove", "cc_sb_prove_ex",
     "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
-    "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume", "cc_last_eval_counts",
+    "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume", "cc_last_eval_counts", "cc_set_eval_graph",
+    "cc_eval_graph_stats",
 ]
 
 MLP_PARAMS = 5319
@@ -250,6 +251,8 @@ def load_library(path=LIB_PATH):
     lib.cc_sb_prove_ex.argtypes = [vp, vp, ctypes.POINTER(CcSbGrid), ctypes.c_int, ctypes.POINTER(vp),
                                    ctypes.POINTER(sz), ctypes.POINTER(vp), ctypes.POINTER(CcSbProveStats)]
     lib.cc_set_stage_timing.argtypes = [vp, ctypes.c_int]
+    lib.cc_set_eval_graph.argtypes = [vp, ctypes.c_int]
+    lib.cc_eval_graph_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]
     lib.cc_last_stage_times.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     lib.cc_free.argtypes = [vp]
     if hasattr(lib, "cc_selftest_round"):
@@ -325,6 +328,17 @@ class Prover:
                                               ctypes.byref(r)), "cc_autotune_eval")
         return {k: {"min_blocks": r.min_blocks[i], "blocks_per_sm": r.blocks_per_sm[i],
                     "ms": float(r.ms[i]), "ms_default": float(r.ms_default[i])} for i, k in enumerate(EVAL_PASSES)}
+
+    def set_eval_graph(self, enable=True):
+        """Replay the evaluation's launch sequence as a CUDA graph while its
+        arguments repeat (cc_set_eval_graph; on by default)."""
+        self._check(self.lib.cc_set_eval_graph(self.h, int(bool(enable))), "cc_set_eval_graph")
+
+    def eval_graph_stats(self):
+        """(captures, replays) of the evaluation graph on this handle."""
+        c, r = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        self._check(self.lib.cc_eval_graph_stats(self.h, ctypes.byref(c), ctypes.byref(r)), "cc_eval_graph_stats")
+        return int(c.value), int(r.value)
 
     def set_stage_timing(self, enable=True):
         """Record a CUDA event around each evaluation kernel (see stage_times)."""

@@ -347,26 +347,100 @@ static void launch_pass(int pass, int minb, int g, cudaStream_t s, const double*
     }
 }
 
-// the four passes on one batch already on the device
+// the launch sequence of the four passes
 template <Layout L>
-static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks, cudaStream_t s) {
-    EvalQueues q;
-    int st = eval_queues(h, n, &q);
-    if (st) return st;
+static int eval_launches(cc_handle* h, const double* in, size_t n, uint32_t* masks, cudaStream_t s,
+                         const EvalQueues& q) {
     CC_CUDA(h, cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s));
-    h->stages_recorded = 0;
-    h->eval_counts = q.counts;
+    // a small batch takes no more blocks than it has boxes to spread over
+    const size_t need = (n + 127) / 128;
     for (int pass = 0; pass < CC_EVAL_STAGES; ++pass) {
         if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[pass], s));
-        launch_pass<L>(pass, h->tune_minb[pass], h->sm_count * h->tune_grid[pass], s, in, n, masks, q);
+        int g = h->sm_count * h->tune_grid[pass];
+        if ((size_t)g > need) g = (int)need;
+        launch_pass<L>(pass, h->tune_minb[pass], g, s, in, n, masks, q);
         CC_LAUNCHED(h);
         if (pass == 0) h->launches += 1 + kRecGroups * (1 + ct::kCrRecordSlots);  // groups, rounds, collection
     }
-    if (h->timing) {
-        CC_CUDA(h, cudaEventRecord(h->stage_ev[CC_EVAL_STAGES], s));
-        h->stages_recorded = CC_EVAL_STAGES;
-    }
+    if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[CC_EVAL_STAGES], s));
     return CC_OK;
+}
+
+// The four passes on one batch already on the device.  With the handle's
+// evaluation graph on (the default) and graph_ok, the launch sequence is captured once
+// into a CUDA graph and replayed by one cudaGraphLaunch while the same
+// arguments repeat (a batch loop over fixed buffers); a call with other
+// arguments re-captures it and updates the executable graph in place.  Not
+// while stage timing is on, and not on a stream the caller is capturing
+// (the launches then join the caller's graph).
+template <Layout L>
+static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks, cudaStream_t s,
+                      bool graph_ok = true) {
+    EvalQueues q;
+    int st = eval_queues(h, n, &q);
+    if (st) return st;
+    h->stages_recorded = 0;
+    h->eval_counts = q.counts;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    bool graph = graph_ok && h->eval_graph && !h->timing && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
+                 cap == cudaStreamCaptureStatusNone;
+    if (!graph) cudaGetLastError();
+    if (graph) {
+        const uintptr_t key_items[] = {(uintptr_t)L, (uintptr_t)in, (uintptr_t)n, (uintptr_t)masks, (uintptr_t)s,
+                                       (uintptr_t)q.full, (uintptr_t)q.cover_box, (uintptr_t)q.gaps_box,
+                                       (uintptr_t)q.counts, (uintptr_t)q.args, (uintptr_t)q.states,
+                                       (uintptr_t)q.q[0], (uintptr_t)q.q[1], (uintptr_t)q.rc, (uintptr_t)q.enc,
+                                       (uintptr_t)h->sm_count, (uintptr_t)h->tune_minb[0], (uintptr_t)h->tune_minb[1],
+                                       (uintptr_t)h->tune_minb[2], (uintptr_t)h->tune_minb[3],
+                                       (uintptr_t)h->tune_grid[0], (uintptr_t)h->tune_grid[1],
+                                       (uintptr_t)h->tune_grid[2], (uintptr_t)h->tune_grid[3]};
+        std::vector<uintptr_t> key(std::begin(key_items), std::end(key_items));
+        if (!h->graph_exec || key != h->graph_key) {
+            const uint64_t before = h->launches;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                cudaGetLastError();  // a stream that cannot be captured (the legacy default stream)
+                goto direct;
+            }
+            st = eval_launches<L>(h, in, n, masks, s, q);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(s, &g);
+            if (st) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (ce != cudaSuccess) return ccrt::fail(h, CC_ERR_CUDA, "cudaStreamEndCapture", ce);
+            bool updated = false;
+            if (h->graph_exec) {
+                cudaGraphExecUpdateResultInfo info;
+                updated = cudaGraphExecUpdate(h->graph_exec, g, &info) == cudaSuccess;
+                if (!updated) {
+                    cudaGetLastError();
+                    cudaGraphExecDestroy(h->graph_exec);
+                    h->graph_exec = nullptr;
+                }
+            }
+            cudaError_t ie = cudaSuccess;
+            if (!updated) ie = cudaGraphInstantiate(&h->graph_exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) {
+                h->graph_exec = nullptr;
+                h->graph_key.clear();
+                return ccrt::fail(h, CC_ERR_CUDA, "cudaGraphInstantiate", ie);
+            }
+            h->graph_key = key;
+            h->graph_launches = h->launches - before;
+            h->graph_captures++;
+            h->launches = before;
+        }
+        CC_CUDA(h, cudaGraphLaunch(h->graph_exec, s));
+        h->launches += h->graph_launches;
+        h->graph_replays++;
+        return CC_OK;
+    }
+direct:
+    st = eval_launches<L>(h, in, n, masks, s, q);
+    if (!st && h->timing) h->stages_recorded = CC_EVAL_STAGES;
+    return st;
 }
 
 static int eval_grid(cc_handle* h, size_t n) {
@@ -535,7 +609,21 @@ int cc_destroy(cc_handle* h) {
         cudaStreamSynchronize(h->stream2);
         cudaStreamDestroy(h->stream2);
     }
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     delete h;
+    return CC_OK;
+}
+
+int cc_set_eval_graph(cc_handle* h, int enable) {
+    if (!h) return CC_ERR_PARAM;
+    h->eval_graph = enable != 0;
+    return CC_OK;
+}
+
+int cc_eval_graph_stats(cc_handle* h, unsigned long long* captures, unsigned long long* replays) {
+    if (!h || !captures || !replays) return CC_ERR_PARAM;
+    *captures = h->graph_captures;
+    *replays = h->graph_replays;
     return CC_OK;
 }
 
@@ -778,7 +866,14 @@ int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* m
     if (cudaPointerGetAttributes(&pa, boxes) == cudaSuccess) pinned_in = pa.type == cudaMemoryTypeHost;
     else cudaGetLastError();
     const bool direct = h->pageable_access || pinned_in;
-    const size_t chunk = n < ((size_t)1 << 22) ? n : ((size_t)1 << 22);
+    // boxes per chunk (CC_EVAL_CHUNK_LOG2 in the environment, 16..26, changes
+    // only how the same work is cut)
+    static const int chunk_log2 = [] {
+        const char* v = std::getenv("CC_EVAL_CHUNK_LOG2");
+        const int x = v ? std::atoi(v) : 22;
+        return x < 16 ? 16 : (x > 26 ? 26 : x);
+    }();
+    const size_t chunk = n < ((size_t)1 << chunk_log2) ? n : ((size_t)1 << chunk_log2);
     const size_t in_bytes = chunk * sizeof(cc_tight_box);
     void *d_aos[2], *d_soa, *d_masks;
     int st = CC_OK;
@@ -823,7 +918,9 @@ int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* m
         CC_LAUNCHED(h);
         e = cudaEventRecord(used[b], h->stream);
         if (e != cudaSuccess) break;
-        st = eval_batch<Layout::SoA>(h, (const double*)d_soa, cnt, (uint32_t*)d_masks + off, h->stream);
+        // direct launches: the chunks' arguments differ (a graph would be
+        // re-captured for every chunk)
+        st = eval_batch<Layout::SoA>(h, (const double*)d_soa, cnt, (uint32_t*)d_masks + off, h->stream, false);
     }
     if (e == cudaSuccess && st == CC_OK)
         e = cudaMemcpyAsync(masks, d_masks, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream);

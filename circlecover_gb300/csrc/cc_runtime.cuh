@@ -56,6 +56,14 @@ struct cc_handle {
     bool pageable_access = false;
     // second stream for transfers that overlap evaluation (created on first use)
     cudaStream_t stream2 = nullptr;
+    // CUDA graph of the evaluation's launch sequence (cc_set_eval_graph):
+    // replayed while its key (every pointer, size and setting the launches
+    // take) repeats, re-captured into the same executable graph otherwise
+    bool eval_graph = true;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<uintptr_t> graph_key;
+    uint64_t graph_launches = 0;  // kernels in the captured sequence
+    uint64_t graph_captures = 0, graph_replays = 0;
 };
 
 namespace ccrt {

@@ -300,6 +300,16 @@ int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint32_t* masks,
  * max_stages values; *n_stages = how many were written). */
 #define CC_EVAL_STAGES 4
 int cc_set_stage_timing(cc_handle* h, int enable);
+/* CUDA graph of the evaluation's launch sequence (on by default; no
+ * reference counterpart): cc_tight_eval_device captures its launches once
+ * into a CUDA graph and replays it with one cudaGraphLaunch while the same
+ * arguments (input, count, masks, stream, tuning) repeat, and re-captures it
+ * into the same executable graph when they change.  Off while stage timing
+ * is on, and on a stream the caller is capturing (the launches then join
+ * the caller's graph); cc_tight_eval launches its chunks directly.
+ * cc_eval_graph_stats: how many captures and replays this handle made. */
+int cc_set_eval_graph(cc_handle* h, int enable);
+int cc_eval_graph_stats(cc_handle* h, unsigned long long* captures, unsigned long long* replays);
 int cc_last_stage_times(cc_handle* h, float* ms, int max_stages, int* n_stages);
 /* Queue sizes of the most recent evaluation batch (waits for the device):
  * counts[0] boxes the FP32 pass left to the FP64 pass, counts[1] boxes that

@@ -351,3 +351,40 @@ def test_host_entry_staging_and_direct_paths_agree(port):
             os.environ.pop("CC_HOST_STAGING", None)
         else:
             os.environ["CC_HOST_STAGING"] = old
+
+
+def test_eval_graph_replay_matches_direct_launches(port):
+    """The evaluation's CUDA graph (cc_set_eval_graph): replays give the masks
+    of direct launches, a call with other arguments re-captures, and small
+    batches (grids cut to the batch) and the chunked host entry equal the
+    port."""
+    import torch
+    p = cg.Prover(0)
+    try:
+        masks = {}
+        for n, seed in ((70_000, 91), (50_000, 92)):
+            boxes = W.tight_microbench(n, seed=seed)
+            soa = torch.from_numpy(W.to_soa(boxes)).to("cuda")
+            out = torch.zeros(n, dtype=torch.int32, device="cuda")
+            p.set_eval_graph(False)
+            p.tight_eval_device(soa.data_ptr(), n, out.data_ptr())
+            torch.cuda.synchronize()
+            direct = out.cpu().numpy().view(np.uint32).copy()
+            p.set_eval_graph(True)
+            for _ in range(3):
+                out.zero_()
+                p.tight_eval_device(soa.data_ptr(), n, out.data_ptr())
+                torch.cuda.synchronize()
+                assert np.array_equal(out.cpu().numpy().view(np.uint32), direct), n
+            masks[n] = (boxes, direct)
+        captures, replays = p.eval_graph_stats()
+        assert captures == 2 and replays == 6, (captures, replays)
+        boxes, direct = masks[50_000]
+        sample = np.r_[0:2000, 48_000:50_000]
+        assert np.array_equal(direct[sample], port.tight_eval(boxes[sample], threads=16))
+        big = W.tight_microbench((1 << 22) + 777, seed=93)
+        got = p.tight_eval(big)
+        sample = np.r_[0:3000, len(big) - 3000:len(big)]
+        assert np.array_equal(got[sample], port.tight_eval(big[sample], threads=16))
+    finally:
+        p.close()
