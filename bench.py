@@ -457,7 +457,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-proof", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", default="tight_eval", choices=["tight_eval", "sb_proof", "tight_proof"])
+    ap.add_argument("--workload", default="tight_eval", choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof"])
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.workload == "tight_proof":  # the tight proof forms alone (for profiling)
@@ -468,6 +468,16 @@ def main():
             r = proof_comparison(prover)
             if rank == 0:
                 print(json.dumps(r), flush=True)
+        return
+    if args.workload == "sb_forms":  # the smaller size-bound workload in its three forms (for profiling)
+        import __graft_entry__
+        __graft_entry__.build()
+        import circlecover_gb300 as cg
+        with cg.Prover(local) as prover:
+            for i in range(args.warmup + args.steps):
+                r = sb_forms(prover)
+                if i >= args.warmup and rank == 0:
+                    print(json.dumps(r), flush=True)
         return
     if args.workload == "sb_proof":  # the size-bound proof slice alone (for profiling)
         import __graft_entry__

@@ -257,6 +257,7 @@ def load_library(path=LIB_PATH):
     lib.cc_free.argtypes = [vp]
     if hasattr(lib, "cc_selftest_round"):
         lib.cc_selftest_round.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, sz]
+        lib.cc_selftest_round_to_floats.argtypes = [vp, vp, sz, vp]
         lib.cc_selftest_subinterval.argtypes = [vp, vp, vp, vp, vp, sz, vp, vp]
         lib.cc_selftest_bisection_f32.argtypes = [vp, ctypes.c_int, vp, sz, vp, vp]
         lib.cc_selftest_bisection_width.argtypes = [vp, ctypes.c_int, vp, sz, vp, vp]
@@ -534,6 +535,15 @@ class Prover:
         self._check(self.lib.cc_selftest_round(self.h, op, 1 if up else 0, a.ctypes.data,
                                                bb.ctypes.data if bb is not None else None, out.ctypes.data, len(a)),
                     "cc_selftest_round")
+        return out
+
+    def selftest_round_to_floats(self, x):
+        """(n, 4) floats per double: the FP32 enclosures' rounding down and up,
+        then __double2float_rd / __double2float_ru."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.empty((len(x), 4), dtype=np.float32)
+        self._check(self.lib.cc_selftest_round_to_floats(self.h, x.ctypes.data, len(x), out.ctypes.data),
+                    "cc_selftest_round_to_floats")
         return out
 
     def selftest_subinterval(self, lo, hi, idx, cnt):

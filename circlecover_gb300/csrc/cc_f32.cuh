@@ -23,7 +23,8 @@
 //
 // The intrinsics are IEEE correctly rounded in the direction named
 // (__fadd_rd, __fmul_ru, __fdiv_rd, __fsqrt_ru, __double2float_rd, ...),
-// denormals included (the library is built without -ftz).
+// denormals included (the library is built without -ftz); doubles are
+// rounded to floats by round_to_floats below.
 #pragma once
 
 #include "cc_iv.cuh"
@@ -36,20 +37,50 @@ struct Fv {
     float lo, hi;
     Fv() = default;
     __device__ __forceinline__ Fv(float l, float h) : lo(l), hi(h) {}
-    // enclosure of a double; a constant that is a float folds to {x, x}
-    __device__ __forceinline__ Fv(double x) {
-        float f = (float)x;
-        if ((double)f == x) {
-            lo = hi = f;
-        } else {
-            lo = __double2float_rd(x);
-            hi = __double2float_ru(x);
-        }
-    }
+    // enclosure of a double (a double that is a float gives {x, x})
+    __device__ __forceinline__ Fv(double x);
 };
 
+// The double rounded down and up to floats, by integer operations on its
+// bits: GB300 runs the conversion instructions on its FP64 unit, at the
+// FP64 rate.  For 2^-126 <= |x| < 2^128 (biased exponent 897..1150) the
+// float with x's sign, exponent (rebased from 1023 to 127) and leading 23
+// mantissa bits is x rounded toward zero, and the next float bit pattern
+// away from zero is x rounded away from zero when a discarded mantissa bit
+// is set (a mantissa carry moves into the exponent, past the largest float
+// to infinity, as rounding does).  Other values (zero, results below the
+// normal floats, infinities, NaN) take the directed conversions.
+__device__ __forceinline__ void round_to_floats(double x, float& dn, float& up) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    if (e - 897u <= 253u) {
+        const unsigned mag = __funnelshift_l(lo, (hi & 0x7fffffffu) - (896u << 20), 3);
+        const unsigned away = mag + ((lo & 0x1fffffffu) != 0u ? 1u : 0u);
+        const unsigned s = hi & 0x80000000u;
+        dn = __uint_as_float(s | (s ? away : mag));
+        up = __uint_as_float(s | (s ? mag : away));
+        return;
+    }
+    dn = __double2float_rd(x);
+    up = __double2float_ru(x);
+}
+__device__ __forceinline__ float round_dn(double x) {
+    float d, u;
+    round_to_floats(x, d, u);
+    return d;
+}
+__device__ __forceinline__ float round_up(double x) {
+    float d, u;
+    round_to_floats(x, d, u);
+    return u;
+}
+
+__device__ __forceinline__ Fv::Fv(double x) { round_to_floats(x, lo, hi); }
+
 // enclosure of a double
-__device__ __forceinline__ Fv of(double x) { return Fv{__double2float_rd(x), __double2float_ru(x)}; }
+__device__ __forceinline__ Fv of(double x) { return Fv(x); }
+// enclosure of the doubles between lo and hi
+__device__ __forceinline__ Fv hull(double lo, double hi) { return Fv{round_dn(lo), round_up(hi)}; }
 __device__ __forceinline__ Fv point(float x) { return Fv{x, x}; }
 __device__ __forceinline__ float qnan() { return __int_as_float(0x7fffffff); }
 __device__ __forceinline__ Fv nan_fv() { return Fv{qnan(), qnan()}; }
@@ -346,7 +377,7 @@ template <class Dec, class Pred>
 __device__ __forceinline__ double bisect(double lo, double hi, const Dec& dec, const Pred& pred) {
     int it = 0;
     if (lo >= 0.0 && lo < hi && hi <= 1.7976931348623157e308) {
-        const int whole = dec(Fv{__double2float_rd(lo), __double2float_ru(hi)});
+        const int whole = dec(hull(lo, hi));
         if (whole == NO) return lo;
         if (whole == YES) {
             for (;; ++it) {
@@ -395,13 +426,13 @@ __device__ __forceinline__ Fv bisect_enclosure(double lo, double hi, const Dec& 
         return nan_fv();
     }
     if (!(lo < hi)) return of(lo);  // the first midpoint is not above lo
-    const int whole = dec(Fv{__double2float_rd(lo), __double2float_ru(hi)});
+    const int whole = dec(hull(lo, hi));
     if (whole == NO) return of(lo);
     for (int it = 0; it < CC_BISECTION_CAP; ++it) {
         const double mid = 0.5 * (lo + hi);
         if (mid <= lo || mid >= hi) return of(lo);
         const int d = whole == YES ? YES : dec(of(mid));
-        if (d == UNKNOWN) return Fv{__double2float_rd(lo), __double2float_ru(hi)};
+        if (d == UNKNOWN) return hull(lo, hi);
         if (d == YES) lo = mid;
         else hi = mid;
     }

@@ -990,6 +990,35 @@ int cc_selftest_round(cc_handle* h, int op, int up, const double* a, const doubl
     return CC_OK;
 }
 
+__global__ void k_selftest_round_to_floats(const double* x, size_t n, float* out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float d, u;
+    cc::f32::round_to_floats(x[i], d, u);
+    out[4 * i] = d;
+    out[4 * i + 1] = u;
+    out[4 * i + 2] = __double2float_rd(x[i]);
+    out[4 * i + 3] = __double2float_ru(x[i]);
+}
+
+// Diagnostic: f32::round_to_floats next to the directed conversions
+int cc_selftest_round_to_floats(cc_handle* h, const double* x, size_t n, float* out) {
+    if (!h || !x || !out) return CC_ERR_PARAM;
+    h->launches = 0;
+    if (n == 0) return CC_OK;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    void *dx, *dout;
+    int st = ccrt::ensure(h, 0, n * 8, &dx);
+    if (!st) st = ccrt::ensure(h, 1, n * 16, &dout);
+    if (st) return st;
+    CC_CUDA(h, cudaMemcpyAsync(dx, x, n * 8, cudaMemcpyHostToDevice, h->stream));
+    k_selftest_round_to_floats<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>((const double*)dx, n, (float*)dout);
+    CC_LAUNCHED(h);
+    CC_CUDA(h, cudaMemcpyAsync(out, dout, n * 16, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CC_OK;
+}
+
 // Diagnostic: subinterval splits computed (a) with the explicit FMA the
 // prover uses and (b) by the plain expression `lb + diff*i` compiled with
 // nvcc's default contraction (cc_selftest_fmad.cu); out_a/out_b get 2n doubles.

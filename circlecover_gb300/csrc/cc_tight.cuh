@@ -497,7 +497,7 @@ CC_FN double cover_strip_width_early(double la_hi, double r1, double r2, double 
     if (finite && (*decided = early(lo, hi)) != f32::UNKNOWN) return lo;
     const StripF32 pf = strip_f32_prepare(r1, r2, r3);
     if (finite) {
-        int whole = strip_width_realizable_f32(pf, f32::Fv{__double2float_rd(lo), __double2float_ru(hi)});
+        int whole = strip_width_realizable_f32(pf, f32::hull(lo, hi));
         if (whole == f32::NO) return lo;
         if (whole == f32::YES) return bisect_all_true(lo, hi);
     }
@@ -906,7 +906,7 @@ CC_FN double gaps_width_early(double r1, double r2, double r4, GapsStart g, Earl
     const bool finite = lo < hi && hi <= CC_DBL_MAX;
     const GapsF32 pf = gaps_f32_prepare(r1, r2, w1, w2, r4);
     if (finite) {
-        int whole = gap_width_realizable_f32(f32::Fv{0.0f, __double2float_ru(hi)}, pf);
+        int whole = gap_width_realizable_f32(f32::Fv{0.0f, f32::round_up(hi)}, pf);
         if (whole == f32::NO) return lo;
         if (whole == f32::YES) return bisect_all_true(lo, hi);
     }
@@ -1246,7 +1246,7 @@ CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr) {
     // cover_strip_finish for every width in [lo, hi]
     auto finish = [&](double lo, double hi) -> int {
         if (!lb_ok) return f32::UNKNOWN;
-        bool ok = cover_strip_finish<Fv>(la.hi, Fv{__double2float_rd(lo), __double2float_ru(hi)}, b.r[3].hi, lb_R4);
+        bool ok = cover_strip_finish<Fv>(la.hi, f32::hull(lo, hi), b.r[3].hi, lb_R4);
         int d = trap_status() == TRAP_NONE ? (ok ? f32::YES : f32::NO) : f32::UNKNOWN;
         trap_clear();  // no trap can be pending where this is asked
         return d;
@@ -1295,7 +1295,7 @@ CC_FN_INL uint32_t gaps_pass_box(const Box& b, const EncBox* enc = nullptr) {
     // gaps_finish for every gap width in [lo, hi]
     auto finish = [&](double lo, double hi) -> int {
         if (!R_ok) return f32::UNKNOWN;
-        bool ok = gaps_finish_t<Fv>(b.la.hi, g.w1, g.w2, Fv{__double2float_rd(lo), __double2float_ru(hi)}, v.r[3].hi,
+        bool ok = gaps_finish_t<Fv>(b.la.hi, g.w1, g.w2, f32::hull(lo, hi), v.r[3].hi,
                                     R.lo, R.hi);
         int d = trap_status() == TRAP_NONE ? (ok ? f32::YES : f32::NO) : f32::UNKNOWN;
         trap_clear();  // no trap can be pending where this is asked

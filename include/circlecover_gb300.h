@@ -451,6 +451,10 @@ void cc_free(void* p);
  * 3 sqrt, 4 reciprocal; up: round toward +inf, else toward -inf; b unused for
  * ops 3 and 4). */
 int cc_selftest_round(cc_handle* h, int op, int up, const double* a, const double* b, double* out, size_t n);
+/* The FP32 enclosures' rounding of doubles to floats (integer operations on
+ * the bits) next to the directed conversion instructions: out gets 4 floats
+ * per value (rounded down, rounded up, __double2float_rd, __double2float_ru). */
+int cc_selftest_round_to_floats(cc_handle* h, const double* x, size_t n, float* out);
 /* Equal splits computed with the prover's explicit FMA (out_a) and with the
  * reference's plain expression under nvcc's default contraction (out_b),
  * 2n doubles each (reference: subintervals.hpp:33-43). */

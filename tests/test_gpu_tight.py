@@ -388,3 +388,31 @@ def test_eval_graph_replay_matches_direct_launches(port):
         assert np.array_equal(got[sample], port.tight_eval(big[sample], threads=16))
     finally:
         p.close()
+
+
+def test_round_to_floats_equals_directed_conversions(prover):
+    """The FP32 enclosures round doubles to floats by integer operations on
+    the bits; they equal __double2float_rd / __double2float_ru bit for bit
+    (random bit patterns, the normal float range, exact floats and their
+    neighbours, the range boundaries, zeros, infinities, NaN)."""
+    rng = np.random.default_rng(77)
+    bits = rng.integers(0, 2**63, 400_000, dtype=np.int64).astype(np.uint64)
+    bits[::2] |= np.uint64(1 << 63)
+    pat = bits.view(np.float64)
+    logu = np.exp2(rng.uniform(-135, 135, 400_000)) * rng.choice([-1.0, 1.0], 400_000)
+    f = (rng.standard_normal(200_000) * np.exp2(rng.integers(-126, 127, 200_000))).astype(np.float32)
+    fd = f.astype(np.float64)
+    near = np.r_[fd, np.nextafter(fd, np.inf), np.nextafter(fd, -np.inf)]
+    fmax = float(np.finfo(np.float32).max)
+    edges = []
+    for v in (fmax, 2.0**128, 2.0**-126, 2.0**-149, 2.0**127, 1.0, 0.61):
+        for w in (v, np.nextafter(v, np.inf), np.nextafter(v, 0.0)):
+            edges += [w, -w]
+    edges += [0.0, -0.0, np.inf, -np.inf, np.nan, 1e300, -1e300, 1e-300, -1e-300]
+    x = np.r_[pat, logu, near, np.array(edges)]
+    out = prover.selftest_round_to_floats(x)
+    ours, ref = out[:, :2], out[:, 2:]
+    both_nan = np.isnan(ours) & np.isnan(ref)
+    same = (ours.view(np.uint32) == ref.view(np.uint32)) | both_nan
+    bad = np.nonzero(~same.all(axis=1))[0]
+    assert len(bad) == 0, (x[bad[:5]], ours[bad[:5]], ref[bad[:5]])
