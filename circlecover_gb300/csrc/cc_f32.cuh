@@ -48,15 +48,22 @@ struct Fv {
 // mantissa bits is x rounded toward zero, and the next float bit pattern
 // away from zero is x rounded away from zero when a discarded mantissa bit
 // is set (a mantissa carry moves into the exponent, past the largest float
-// to infinity, as rounding does).  Other values (zero, results below the
-// normal floats, infinities, NaN) take the directed conversions.
+// to infinity, as rounding does).  Zeros keep their sign.  Other values
+// (results below the normal floats, infinities, NaN) take the directed
+// conversions.  Plain shifts and bit casts only, so that the compiler folds
+// the conversion of a constant.
 __device__ __forceinline__ void round_to_floats(double x, float& dn, float& up) {
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)bits;
+    const unsigned s = hi & 0x80000000u;
+    if ((bits << 1) == 0ull) {
+        dn = up = __uint_as_float(s);
+        return;
+    }
     const unsigned e = (hi >> 20) & 0x7ffu;
     if (e - 897u <= 253u) {
-        const unsigned mag = __funnelshift_l(lo, (hi & 0x7fffffffu) - (896u << 20), 3);
+        const unsigned mag = (((hi & 0x7fffffffu) - (896u << 20)) << 3) | (lo >> 29);
         const unsigned away = mag + ((lo & 0x1fffffffu) != 0u ? 1u : 0u);
-        const unsigned s = hi & 0x80000000u;
         dn = __uint_as_float(s | (s ? away : mag));
         up = __uint_as_float(s | (s ? mag : away));
         return;
