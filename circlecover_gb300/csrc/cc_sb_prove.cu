@@ -775,10 +775,12 @@ struct SplitCriterion<sb::SB_R1_CORNER_EXPLICIT> {
 // a job for the backtracking kernel, so that the backtracking (93 % of the
 // criterion's operations, reached by about a fifth of the placements) runs
 // on full warps.  A job is (leaf << 4) | placement.
+// With f32, a placement's start is decided on FP32 enclosures first (the
+// FP64 start where they leave it undecided).
 __global__ void __launch_bounds__(kThreads) k_sbp_r1c_start(const SbLeaf* __restrict__ qin,
                                                              const unsigned long long* n_in, uint32_t* masks,
                                                              unsigned long long* jobs, unsigned long long* n_jobs,
-                                                             unsigned long long job_cap, SbCounters* c) {
+                                                             unsigned long long job_cap, SbCounters* c, int f32) {
     constexpr int I = sb::kR1CornerItems;
     const unsigned long long nl = *n_in, total = nl * (unsigned long long)I;
     SB_WARP_LOOP(total) {
@@ -791,16 +793,24 @@ __global__ void __launch_bounds__(kThreads) k_sbp_r1c_start(const SbLeaf* __rest
             i = (int)(idx / nl);
             leaf = idx - (unsigned long long)i * nl;
             const Box6 box = qin[leaf].box;
-            sb::Vals v;
-            v.R = sb::remaining_weight(box);
             cc::trap_clear();
-            bool ok;
+            bool ok = false;
             if (i == 8) {
                 ok = sb::r1_corner_r34_and_r2(box);
             } else {
-                sb::CornerStart st;
-                job = sb::r1_corner_start(box, v, i, st);
-                ok = false;
+                bool decided = false;
+                if (f32) {
+                    const sb::Box6T<cc::f32::IvF> e = sb::enclose6(box);
+                    job = sb::r1_corner_starts_f32(e, sb::remaining_weight(e), i);
+                    decided = cc::trap_status() == cc::TRAP_NONE;
+                    cc::trap_clear();
+                }
+                if (!decided) {
+                    sb::Vals v;
+                    v.R = sb::remaining_weight(box);
+                    sb::CornerStart st;
+                    job = sb::r1_corner_start(box, v, i, st);
+                }
             }
             const bool trapped = cc::trap_status() != cc::TRAP_NONE;
             cc::trap_clear();
@@ -1054,7 +1064,7 @@ int launch_passes(Engine& e, int gen, int src) {
         CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_q[dst], 0, sizeof(unsigned long long), e.s));
         CC_CUDA(e.h, cudaMemsetAsync(masks, 0, e.slice * 2 * sizeof(uint32_t), e.s));
         k_sbp_r1c_start<<<e.grid, kThreads, 0, e.s>>>(e.q[src], &e.dc->n_q[src], masks, r1c_jobs, &e.dc->n_q[dst],
-                                                       e.slice * 8, e.dc);
+                                                       e.slice * 8, e.dc, e.fp32 ? 1 : 0);
         CC_LAUNCHED(e.h);
         const unsigned long long job_cap = e.slice * 8;
         if (e.fp32) {  // FP32-first; the FP64 jobs in the queue memory's second half
