@@ -220,12 +220,17 @@ const char* cc_last_error(cc_handle* h);
 
 /* Evaluate the six tight criteria on n boxes given in HOST memory (AoS);
  * verdict masks (CC_TV_*) are written to host memory.  Includes the
- * host<->device transfers: where the device can access pageable host memory
+ * host<->device transfers: the boxes move in chunks (4M boxes; above 2^20
+ * boxes the first chunk is a quarter of that) by the copy engine on a
+ * second stream, which also transposes each chunk to SoA, while the
+ * previous chunk is evaluated; straight from the caller's array when it is
+ * page-locked or the device can access pageable host memory
  * (cudaDevAttrPageableMemoryAccess, e.g. GB300 with its host over
- * NVLink-C2C) its kernels read the boxes and write the masks in place;
- * otherwise they are staged through pinned buffers by host threads.  The
- * environment variable CC_HOST_STAGING=1, read when the handle is created,
- * forces the staging path. */
+ * NVLink-C2C), otherwise through pinned buffers that host threads fill.  The
+ * masks return in one copy at the end.  Environment: CC_HOST_STAGING=1,
+ * read when the handle is created, forces the staging path;
+ * CC_EVAL_CHUNK_LOG2 (16..26, read once) sets the chunk size (same
+ * results). */
 int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* masks);
 
 /* Same on DEVICE memory: `soa` holds 10 arrays of n doubles each, in the order
