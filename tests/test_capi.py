@@ -58,3 +58,8 @@ def test_null_arguments_are_rejected(lib_path):
     assert lib.cc_create(None, 0) == 2
     assert lib.cc_tight_eval(None, None, 0, None) == 2
     assert lib.cc_tight_prove(None, None, None, None, None, None) == 2
+    assert lib.cc_set_eval_graph(None, 1) == 2
+    assert lib.cc_eval_graph_stats(None, None, None) == 2
+    assert lib.cc_selftest_round_to_floats(None, None, ctypes.c_size_t(0), None) == 2
+    assert lib.cc_sb_prove(None, None, None, None, None, None, None) == 2
+    assert lib.cc_autotune_eval(None, None, ctypes.c_size_t(0), None, None) == 2
