@@ -11,11 +11,18 @@ between steps.
 
 One JSON line on rank 0.  `value` = boxes/s with the inputs resident in HBM
 (device entry point cc_tight_eval_device, CUDA events on the launching
-stream); `e2e` = the same through the host entry point cc_tight_eval with host
-buffers (host->device copy of the boxes and device->host copy of the masks in
-the timed region).  --impl reference times the CPU implementation of the
-criteria on the host cores (the reference's own code where it was built here,
-otherwise the oracle's port of it) on the same workload.
+stream), in the certified form: every verdict the FP32 pre-filter decides
+"true" is checked again in FP64 (`certification` reports the uncertified
+FP32 form and the cost); `e2e` = the same through the host entry point
+cc_tight_eval with host buffers (host->device copy of the boxes and
+device->host copy of the masks in the timed region); `roofline` per pass
+against the instruction rates the library's probe measures on this GPU;
+`proof` = the full tight_rectangle proof (the reference's root and schedule)
+in its plain, batched and learned forms.  --impl reference times the CPU
+implementation of the criteria on the host cores (the reference's own code
+where it was built here, otherwise the oracle's port of it) on the same
+workload.  --workload config1 runs the small plain-method proof in the three
+forms instead.
 """
 import argparse
 import json
@@ -85,34 +92,78 @@ class ClockSampler:
 def algorithmic_ops_per_box():
     """Mean number of FP64 directed-rounding operations the REFERENCE's code
     executes per box of this workload (shim counters on the reference built
-    for the host; first 2**16 boxes of the 2**24-box set), split by the kernel
-    that executes them: the strip-width and gap-width bisection loops (counted
-    on the port, whose loops execute the reference's operations one for one)
-    and the main pass (the rest of the reference's count)."""
+    for the host; first 2**16 boxes of the 2**24-box set), and the golden
+    masks of those boxes."""
     z = np.load(os.path.join(ROOT, "tests", "golden", "tight_bench_ops.npz"))
-    total = float(z["ops"].astype(np.float64).mean())
-    cover = float(z["cover_ops"].astype(np.float64).mean())
-    gaps = float(z["gaps_ops"].astype(np.float64).mean())
-    # the main criteria's operations are decided by the FP32 pass, or by the
-    # FP64 pass for the boxes the FP32 pass leaves to it: counted at the FP32 pass
-    return total, {"k_eval_f32": total - cover - gaps, "k_eval_main": 0.0, "k_eval_cover": cover,
-                   "k_eval_gaps": gaps}, z["masks"]
+    return float(z["ops"].astype(np.float64).mean()), z["masks"]
 
 
-def ncu_traffic(kernel):
-    """DRAM bytes (read + write) per full-size launch of `kernel` from the
-    committed ncu summary (a line `traffic_bytes_per_launch[<kernel>]: B`)."""
-    p = os.path.join(ROOT, "profiles", "tight_eval_microbench_2e24.md")
-    if not os.path.exists(p):
-        return None
-    key = "traffic_bytes_per_launch[%s]:" % kernel
-    for line in open(p):
-        if line.startswith(key):
-            try:
-                return float(line.split(":", 1)[1])
-            except ValueError:
-                return None
-    return None
+PROFILE = os.path.join(ROOT, "profiles", "tight_eval_microbench_2e24.md")
+
+
+def profile_per_box():
+    """Per-box counts of each evaluation pass from the committed ncu summary
+    (lines `per_box[<pass>].<metric>: value`, measured on a 2^21-box sample of
+    this workload): warp instructions, thread instructions, FP64 and FP32
+    thread instructions, DRAM bytes.  Counts grow with the number of boxes."""
+    out = {}
+    if not os.path.exists(PROFILE):
+        return out
+    for line in open(PROFILE):
+        if not line.startswith("per_box["):
+            continue
+        key, val = line.split(":", 1)
+        name, metric = key[len("per_box["):].split("].", 1)
+        try:
+            out.setdefault(name, {})[metric.strip()] = float(val)
+        except ValueError:
+            pass
+    return out
+
+
+def peaks(prover):
+    """Instruction-throughput ceilings measured on this GPU by the library's
+    probe (cc_selftest_peak): FP64 directed add/mul, FP32 directed add/mul and
+    FP32 FMA thread instructions per second; the FP32 FMA rate / 32 is the
+    warp-instruction issue rate (one FMA warp instruction per cycle per SM
+    sub-partition)."""
+    import ctypes
+    lib = prover.lib
+    lib.cc_selftest_peak.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    out = {}
+    for name, kind in (("fp64", 0), ("fp64_fma", 1), ("fp32", 2), ("fp32_fma", 3)):
+        v = ctypes.c_double()
+        rc = lib.cc_selftest_peak(prover.h, kind, ctypes.byref(v))
+        out[name] = v.value if rc == 0 else float("nan")
+    out["issue"] = out["fp32_fma"] / 32.0
+    return out
+
+
+FP64_PASSES = ("k_eval_main", "k_eval_cover", "k_eval_gaps", "k_eval_cert", "k_eval_repair")
+
+
+def pass_rooflines(stage_ms, n, pk, per_box):
+    """Per-pass roofline from the live pass times: the FP32 pass against the
+    warp-instruction issue rate, the FP64 passes against the FP64 pipe in
+    useful (active-lane) operations; DRAM traffic per launch alongside."""
+    import circlecover_gb300 as cg
+    res = {}
+    for i, name in enumerate(cg.EVAL_PASSES):
+        ms = float(stage_ms[i])
+        d = per_box.get(name, {})
+        r = {"ms": ms}
+        if d and ms > 0:
+            sec = ms * 1e-3
+            warp = d.get("warp_inst", 0.0) * n
+            thr = d.get("thread_inst", 0.0) * n
+            f64 = d.get("fp64_inst", 0.0) * n
+            r.update({"warp_inst_per_s": warp / sec, "issue_frac": warp / sec / pk["issue"],
+                      "lanes_per_inst": thr / warp if warp else None,
+                      "fp64_ops_per_s": f64 / sec, "fp64_useful_frac": f64 / sec / pk["fp64"],
+                      "traffic_bytes": d.get("dram_bytes", 0.0) * n})
+            r["bound"] = "fp64" if name in FP64_PASSES else "issue"
+        res[name] = r
+    return res
 
 
 _CPU_BOXES = {}
@@ -192,6 +243,23 @@ def run_ours(args, ws, rank, local):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    def timed(steps):
+        """mean ms per step over `steps` steps (CUDA events on the stream),
+        max over ranks"""
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if ws > 1:
+            t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
     barrier()  # inputs were copied on the default stream
     tune = None
     if not args.no_autotune:  # register budget and grid of each pass, on a 2^22-box sample
@@ -203,36 +271,38 @@ def run_ours(args, ws, rank, local):
         torch.cuda.synchronize()
         tune = prover.autotune_eval(sample.data_ptr(), m, smask.data_ptr())
         del sample, smask
+    # the uncertified FP32 form (opt-in, measurement only), timed first
+    prover.set_eval_certify(False)
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    ms_fp32_only = timed(args.steps)
+    prover.set_eval_certify(True)
+    # the product: every FP32-decided "true" verdict certified in FP64
     for _ in range(args.warmup):
         step()
     barrier()
     launches_per_step = prover.last_launch_count
-    # per-kernel CUDA events (recorded by the library on the same stream)
-    prover.set_stage_timing(True)
-    stage_ms = np.zeros(len(cg.EVAL_PASSES))
+    cert = prover.eval_cert_counts()
+    queues = prover.eval_counts()
     clocks = ClockSampler(local)
     clocks.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    ms = timed(args.steps)
+    ck = clocks.stop()
+    value = ws * n / (ms * 1e-3)
+    # per-pass CUDA events (recorded by the library on the same stream), in
+    # separate steps so that the headline steps run as one graph launch each
+    prover.set_stage_timing(True)
+    stage_ms = np.zeros(len(cg.EVAL_PASSES))
     for _ in range(args.steps):
         step()
         stage_ms += np.array(prover.stage_times())
-    e1.record(stream)
-    barrier()
-    ck = clocks.stop()
     prover.set_stage_timing(False)
-    ms = e0.elapsed_time(e1) / args.steps
     stage_ms /= args.steps
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * n / (ms * 1e-3)
 
     # correctness of the timed output: the sampled boxes' masks equal the
     # reference's (golden) masks
-    ops_per_box, stage_ops, ref_masks = algorithmic_ops_per_box()
+    ops_per_box, ref_masks = algorithmic_ops_per_box()
     got = masks[: len(ref_masks)].cpu().numpy().view(np.uint32)
     verified = bool(rank != 0 or np.array_equal(got, ref_masks))
 
@@ -260,14 +330,36 @@ def run_ours(args, ws, rank, local):
     if rank != 0:
         prover.close()
         return
-    peak = ctypes_peak(prover)
-    names = list(cg.EVAL_PASSES)
-    stages = {k: {"ms": float(stage_ms[i]), "ops_per_box": stage_ops[k],
-                  "achieved": stage_ops[k] * n / (stage_ms[i] * 1e-3) / 1e12,
-                  "frac": stage_ops[k] * n / (stage_ms[i] * 1e-3) / peak} for i, k in enumerate(names)}
-    dom = names[int(np.argmax(stage_ms))]
-    achieved = stage_ops[dom] * n / (stage_ms[names.index(dom)] * 1e-3)
-    step_achieved = ops_per_box * n / (ms * 1e-3)
+    pk = peaks(prover)
+    per_box = profile_per_box()
+    passes = pass_rooflines(stage_ms, n, pk, per_box)
+    dom = cg.EVAL_PASSES[int(np.argmax(stage_ms))]
+    dp = passes[dom]
+    if dp.get("bound") == "fp64":
+        roof = {"bound": "fp64", "achieved": dp["fp64_ops_per_s"] / 1e12, "peak": pk["fp64"] / 1e12,
+                "unit": "T FP64 thread-ops/s (active lanes only)", "frac": dp["fp64_useful_frac"],
+                "probe": "cc_selftest_peak kind 0 (FP64 directed add/mul chains)"}
+    elif dp.get("bound") == "issue":
+        roof = {"bound": "issue", "achieved": dp["warp_inst_per_s"] / 1e9, "peak": pk["issue"] / 1e9,
+                "unit": "G warp-instructions/s", "frac": dp["issue_frac"],
+                "probe": "cc_selftest_peak kind 3 (FP32 FMA chains) / 32"}
+    else:
+        roof = {"bound": None, "achieved": None, "peak": None, "unit": None, "frac": None,
+                "probe": "no ncu per-box counts committed for this pass"}
+    step_ref_ops = ops_per_box * n / (ms * 1e-3)
+    roof.update({
+        "kernel": dom, "traffic": dp.get("traffic_bytes"), "algorithmic_bytes": 84 * n,
+        "lanes_per_inst": dp.get("lanes_per_inst"), "passes": passes,
+        "peaks": {k: v / 1e12 for k, v in pk.items()}, "peaks_unit": "T thread-instructions/s (issue: T warp-inst/s)",
+        "fp64_equivalent": {"ref_fp64_ops_per_box": ops_per_box, "rate": step_ref_ops / 1e12,
+                            "unit": "T reference-FP64-ops/s", "vs_fp64_peak": step_ref_ops / pk["fp64"],
+                            "note": "the reference's FP64 directed-rounding operations per box (shim-counted) "
+                                    "x boxes / step time: FP64 work the reference does per box, most of "
+                                    "which this build decides on FP32 enclosures; not a pipe utilisation"},
+        "note": "achieved = executed instructions per box (ncu, profiles/tight_eval_microbench_2e24.md, "
+                "2^21-box sample) x boxes / the pass's live CUDA-event time; peak = this GPU's "
+                "instruction rate measured by the library's probe at bench time; traffic = ncu DRAM "
+                "bytes per box x boxes; algorithmic_bytes = 80 B in + 4 B out per box"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -275,21 +367,13 @@ def run_ours(args, ws, rank, local):
         "config": {"workload": "tight criteria microbench: 2^24 boxes per GPU, lambda~U[1,4], log-uniform widths "
                                "2^-20..2^-4, total weight critical*(1+eps), eps log-uniform 1e-6..1e-1",
                    "boxes_per_gpu": n, "l2_flush": "not needed: inputs (%.2f GB) exceed L2" % (n * 80 / 1e9),
-                   "layout": "SoA, 10 x n float64", "autotune": tune},
+                   "layout": "SoA, 10 x n float64", "autotune": tune,
+                   "form": "certified: every FP32-decided true verdict re-checked in FP64"},
         "verified_vs_reference_masks": verified,
-        "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved / 1e12, "peak": peak / 1e12,
-                     "unit": "Top/s (FP64 ops)", "frac": achieved / peak, "traffic": ncu_traffic(dom),
-                     "ops_per_box": stage_ops[dom], "stages": stages,
-                     "step": {"achieved": step_achieved / 1e12, "frac": step_achieved / peak,
-                              "ops_per_box": ops_per_box},
-                     "note": "achieved = the reference's FP64 directed-rounding ops per box that this pass "
-                             "settles (shim-counted on the reference) x boxes / the pass's mean CUDA-event time "
-                             "(FP64-equivalent rate); peak = FP64 directed add/mul instruction rate measured by "
-                             "this bench on this GPU (MEASURED_PEAKS.json holds no FP64 figure).  The FP32 pass "
-                             "settles ~99% of the boxes' criteria with FP32 enclosures of the FP64 values (same "
-                             "decisions), so a frac above 1 is work the FP64 pipe did not have to do, not an "
-                             "error; the pass itself is bound by instruction issue (divergent branchy criteria, "
-                             "instruction-cache misses: profiles/).  traffic = ncu DRAM bytes per full-size pass"},
+        "certification": {"counts": cert, "queues": queues,
+                          "fp32_uncertified": {"ms_per_step": ms_fp32_only, "value": ws * n / (ms_fp32_only * 1e-3)},
+                          "cost": ms / ms_fp32_only},
+        "roofline": roof,
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": ck,
         "e2e": e2e,
@@ -305,26 +389,43 @@ def run_ours(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def proof_comparison(prover):
-    """Wall time of the tight proof's initial pass on the small plain-method
-    workload (lambda in [1, 1.1] in 256 pieces, r1 in 64, r2..r4 in 128
-    each) in three forms, all with identical criticals:
+# the reference's schedule (tight_rectangle.cu:44-58): initial splits, then
+# eleven refinement generations with these lambda splits and r splits
+TIGHT_GENS = (1, 2, 2, 2, 2, 1, 2, 1, 2, 1, 2)
+TIGHT_R_GEN = (128, 128, 128, 64)
+PROOFS = {
+    # the full tight_rectangle proof: lambda in [1, 2.0898841580413818342]
+    # (tight_rectangle.cu:461-464), 256 x 128^4 initial splits
+    "full": ("tight proof, full (reference schedule): lambda [1, 2.0899] x 256, r1..r4 x 128, 11 generations "
+             "(lambda x 1 or 2, r 128^3 x 64)", (1.0, None), (256, (128, 128, 128, 128))),
+    # the plain-method workload: lambda in [1, 1.1], r1 in 64 pieces
+    "config1": ("tight proof, small plain-method workload: lambda [1, 1.1] x 256, r1 x 64, r2..r4 x 128, "
+                "refinement schedule of the reference", (1.0, 1.1), (256, (64, 128, 128, 128))),
+}
+
+
+def proof_comparison(prover, which="full"):
+    """Wall time of a whole tight proof in three forms, all with identical
+    criticals, generation sizes and leaf counts:
       plain    -- every criterion re-evaluated in every cell, the reference's
-                  leaf order;
-      batched  -- criteria prepared once per parent cell, compacted stages;
+                  leaf order, FP64 only;
+      batched  -- criteria prepared once per parent cell, compacted stages,
+                  leaf criteria FP32-first with every FP32 "true" certified
+                  in FP64;
       learned  -- batched, with the leaf criteria ordered per r3 cell by the
                   network, trained first (by the library's kernels) on
-                  records from this workload's own plain-order cells."""
+                  records of the initial pass's plain-order cells."""
     import circlecover_gb300 as cg
     from circlecover_gb300 import learn
     from circlecover_gb300 import workloads as W
-    root = W.tight_root(1.0, 1.1)
-    grid = cg.make_grid(256, (64, 128, 128, 128))
-    out = {"workload": "tight proof, initial pass: lambda [1,1.1] x 256, r1 x 64, r2..r4 x 128"}
+    desc, (la_lo, la_hi), (la0, r0) = PROOFS[which]
+    root = W.tight_root(la_lo, la_hi if la_hi is not None else W.TIGHT_LAMBDA_MAX)
+    grid = cg.make_grid(la0, r0, TIGHT_GENS, TIGHT_R_GEN)
+    out = {"workload": desc}
     prover.tight_find_critical_intervals(W.tight_root(1.0, 1.0001), cg.make_grid(2, (8, 8, 8, 8)))  # buffers
     t0 = time.perf_counter()
     prover.mlp_init(3)
-    rec, ncells = learn.proof_records(prover, root, grid, per_cell=16)
+    rec, ncells = learn.proof_records(prover, root, cg.make_grid(la0, r0), per_cell=16)
     hist = learn.train(prover, rec, epochs=4, batch=8192)
     train_s = time.perf_counter() - t0
     rep = learn.prediction_report(learn.predict(prover, rec), rec.labels_np)
@@ -339,11 +440,16 @@ def proof_comparison(prover):
                for r in res.values())
     out.update({"plain_s": res["plain"][0], "batched_s": bt, "learned_s": res["learned"][0],
                 "speedup_batched": res["plain"][0] / bt, "speedup_learned": res["plain"][0] / res["learned"][0],
-                "leaves": bs["leaf_evals"], "criticals": len(bc), "identical_criticals": bool(same),
+                "leaves": bs["leaf_evals"], "criticals": len(bc), "gen_sizes": bs["gen_sizes"],
+                "identical_criticals": bool(same),
                 "identical_trace_plain_batched": bool(res["plain"][2]["digest"] == bs["digest"]),
+                "digest": bs["digest"],
                 "training": {"cells_logged": ncells, "records": rec.n, "seconds": train_s, "loss": hist,
                              "error_rate_per_output": rep["error_rate_per_output"]},
-                "leaf_outcomes": {k: res[k][2]["counts"][3][:7] for k in res}})
+                "leaf_outcomes": {k: res[k][2]["counts"][3][:7] for k in res},
+                "fp32_first": {k: res[k][2]["fp32_first"] for k in res},
+                "cert_failures": {k: res[k][2]["cert_failures"] for k in res},
+                "kernel_launches": {k: res[k][2]["kernel_launches"] for k in res}})
     return out
 
 
@@ -436,17 +542,6 @@ def sb_forms(prover):
             "plain_s": res["plain"][0], "speedup_vs_plain": res["plain"][0] / b[0], "identical": bool(same)}
 
 
-def ctypes_peak(prover):
-    import ctypes
-    lib = prover.lib
-    lib.cc_selftest_fp64_peak.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
-    v = ctypes.c_double()
-    rc = lib.cc_selftest_fp64_peak(prover.h, 0, ctypes.byref(v))
-    if rc != 0:
-        return float("nan")
-    return v.value
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -459,15 +554,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-proof", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", default="tight_eval", choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof"])
+    ap.add_argument("--workload", default="tight_eval",
+                    choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof", "config1"])
     args = ap.parse_args()
     ws, rank, local = dist_env()
-    if args.workload == "tight_proof":  # the tight proof forms alone (for profiling)
+    if args.workload in ("tight_proof", "config1"):  # the tight proof forms alone
         import __graft_entry__
         __graft_entry__.build()
         import circlecover_gb300 as cg
         with cg.Prover(local) as prover:
-            r = proof_comparison(prover)
+            r = proof_comparison(prover, "full" if args.workload == "tight_proof" else "config1")
             if rank == 0:
                 print(json.dumps(r), flush=True)
         return

@@ -72,6 +72,8 @@ class CcProveStats(ctypes.Structure):
         ("reserved", ctypes.c_int32),
         ("seconds", ctypes.c_double),
         ("kernel_launches", ctypes.c_uint64),
+        ("fp32_first", ctypes.c_uint64 * 4),
+        ("cert_failures", ctypes.c_uint64),
     ]
 
 
@@ -97,7 +99,10 @@ class CcTuneResult(ctypes.Structure):
                 ("ms_default", ctypes.c_float * 4)]
 
 
-EVAL_PASSES = ("k_eval_f32", "k_eval_main", "k_eval_cover", "k_eval_gaps")
+# the evaluation's passes (cc_last_stage_times order); the first four are
+# the ones the autotuner tunes
+EVAL_PASSES = ("k_eval_f32", "k_eval_main", "k_eval_cover", "k_eval_gaps", "k_eval_cert", "k_eval_repair")
+TUNED_PASSES = EVAL_PASSES[:4]
 
 
 class CcSbGrid(ctypes.Structure):
@@ -181,6 +186,8 @@ def stats_to_dict(s):
         "generations_run": int(s.generations_run),
         "seconds": float(s.seconds),
         "kernel_launches": int(s.kernel_launches),
+        "fp32_first": [int(x) for x in s.fp32_first],
+        "cert_failures": int(s.cert_failures),
     }
 
 
@@ -193,7 +200,7 @@ EXPORTS = [
     "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
     "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume", "cc_last_eval_counts", "cc_set_eval_graph",
-    "cc_eval_graph_stats",
+    "cc_eval_graph_stats", "cc_set_eval_certify", "cc_last_eval_cert",
 ]
 
 MLP_PARAMS = 5319
@@ -252,6 +259,8 @@ def load_library(path=LIB_PATH):
                                    ctypes.POINTER(sz), ctypes.POINTER(vp), ctypes.POINTER(CcSbProveStats)]
     lib.cc_set_stage_timing.argtypes = [vp, ctypes.c_int]
     lib.cc_set_eval_graph.argtypes = [vp, ctypes.c_int]
+    lib.cc_set_eval_certify.argtypes = [vp, ctypes.c_int]
+    lib.cc_last_eval_cert.argtypes = [vp, vp]
     lib.cc_eval_graph_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]
     lib.cc_last_stage_times.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     lib.cc_free.argtypes = [vp]
@@ -328,7 +337,7 @@ class Prover:
         self._check(self.lib.cc_autotune_eval(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
                                               ctypes.byref(r)), "cc_autotune_eval")
         return {k: {"min_blocks": r.min_blocks[i], "blocks_per_sm": r.blocks_per_sm[i],
-                    "ms": float(r.ms[i]), "ms_default": float(r.ms_default[i])} for i, k in enumerate(EVAL_PASSES)}
+                    "ms": float(r.ms[i]), "ms_default": float(r.ms_default[i])} for i, k in enumerate(TUNED_PASSES)}
 
     def set_eval_graph(self, enable=True):
         """Replay the evaluation's launch sequence as a CUDA graph while its
@@ -353,6 +362,21 @@ class Prover:
         self._check(self.lib.cc_last_stage_times(self.h, ms.ctypes.data, len(ms), ctypes.byref(n)),
                     "cc_last_stage_times")
         return [float(x) for x in ms[: n.value]]
+
+    def set_eval_certify(self, enable=True):
+        """FP64 certification of the evaluation's FP32 "true" verdicts (on by
+        default); off is the uncertified FP32 form, for measurement only."""
+        self._check(self.lib.cc_set_eval_certify(self.h, 1 if enable else 0), "cc_set_eval_certify")
+
+    def eval_cert_counts(self):
+        """Certification counts of the last evaluation batch: FP32 "true"
+        verdicts certified per criterion group (r1, r1_r2, 2x2, leaf, three
+        strips or emptiness), boxes whose certification failed (evaluated
+        again in FP64), strip-width and gap-width results certified."""
+        c = (ctypes.c_ulonglong * 8)()
+        self._check(self.lib.cc_last_eval_cert(self.h, c), "cc_last_eval_cert")
+        keys = ("r1", "r1_r2", "two_by_two", "leaf", "three_strips_or_empty", "failed", "cover", "gaps")
+        return {k: int(v) for k, v in zip(keys, c)}
 
     def eval_counts(self):
         """Queue sizes of the last evaluation batch (cc_last_eval_counts):
@@ -536,6 +560,20 @@ class Prover:
                                                bb.ctypes.data if bb is not None else None, out.ctypes.data, len(a)),
                     "cc_selftest_round")
         return out
+
+    def selftest_certify(self, group, boxes, call):
+        """FP64 certification runs of criterion group `group` (0 r1, 1 r1_r2,
+        2 2x2, 3 leaf r1_r2_r3) with call number call[i] per box (1-based;
+        0 none; -1 all): bool array, the criterion held."""
+        boxes = np.ascontiguousarray(boxes, dtype=TIGHT_BOX)
+        call = np.ascontiguousarray(call, dtype=np.int32)
+        out = np.zeros(len(boxes), dtype=np.uint8)
+        f = self.lib.cc_selftest_certify
+        f.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                      ctypes.c_void_p]
+        self._check(f(self.h, group, boxes.ctypes.data, call.ctypes.data, len(boxes), out.ctypes.data),
+                    "cc_selftest_certify")
+        return out.astype(bool)
 
     def selftest_round_to_floats(self, x):
         """(n, 4) floats per double: the FP32 enclosures' rounding down and up,

@@ -87,16 +87,24 @@ enum TrapSite : uint32_t {
 // one status byte per thread, kept in shared memory so that any device
 // function can set it without threading a context argument through every
 // criterion; 1024 threads per block at most.
-// Bit 7 of the byte is a mode bit of the FP32 evaluation (cc_tight.cuh:
-// can_recurse records its arguments instead of evaluating); trap_clear()
-// clears it, trap() keeps it.
+// Bits 6 and 7 of the byte are mode bits (cc_tight.cuh): bit 7 makes the
+// FP32 can_recurse record its arguments instead of evaluating, bit 6 makes
+// the FP64 can_recurse evaluate only one chosen call of a certification run
+// (cc_cert_state) and answer "false" to the others.  trap_clear() clears
+// both, trap() keeps them.
 static __shared__ uint8_t cc_trap_words[1024];
 static constexpr uint8_t kTrapModeBit = 0x80;
+static constexpr uint8_t kCertModeBit = 0x40;
+static constexpr uint8_t kTrapModeBits = kTrapModeBit | kCertModeBit;
 CC_FN void trap(uint32_t site) {
-    cc_trap_words[threadIdx.x] = (uint8_t)((cc_trap_words[threadIdx.x] & kTrapModeBit) | site);
+    cc_trap_words[threadIdx.x] = (uint8_t)((cc_trap_words[threadIdx.x] & kTrapModeBits) | site);
 }
-CC_FN uint32_t trap_status() { return cc_trap_words[threadIdx.x] & (uint8_t)~kTrapModeBit; }
+CC_FN uint32_t trap_status() { return cc_trap_words[threadIdx.x] & (uint8_t)~kTrapModeBits; }
 CC_FN void trap_clear() { cc_trap_words[threadIdx.x] = TRAP_NONE; }
+// Per-thread call bookkeeping of the certification runs: the low byte counts
+// can_recurse calls, the high byte is the number (1-based) of the one call a
+// certification run evaluates (0: none).
+static __shared__ uint16_t cc_cert_state[1024];
 #else
 // host build: per-thread status (initial-exec TLS: a plain load per access)
 #ifndef CC_HOST_TLS

@@ -63,13 +63,18 @@ __device__ __forceinline__ ct::Box load_box(const double* __restrict__ in, size_
 //   pass 1  k_eval_main on the `full` queue: the FP64 criteria (ct::eval_main);
 //   pass 2  k_eval_cover: boxes that need the strip-width bisection (~19% of
 //           the microbench: ~700 operations each), on full warps;
-//   pass 3  k_eval_gaps: boxes that need the gap-width bisection (~30%).
+//   pass 3  k_eval_gaps: boxes that need the gap-width bisection (~30%);
+//   pass 4  k_eval_cert: FP64 certification of every verdict bit pass 0
+//           decided "true", one kernel per criterion group on its queue
+//           (passes 2 and 3 certify their own true results);
+//   pass 5  k_eval_repair: the boxes whose certification failed, evaluated
+//           again in FP64 alone.
 // The queues hold box indices; each pass reads the box itself.
 struct EvalQueues {
     uint32_t* full;
     uint32_t* cover_box;
     uint32_t* gaps_box;
-    unsigned long long* counts;  // [0] cover, [1] gaps, [2] overflow, [3] full
+    unsigned long long* counts;  // kCnt* below
     unsigned long long cap;
     // recorded calls of the heavy FP32 groups (null: every group in one kernel)
     ct::CrArgs* args;        // n x kCrRecordSlots
@@ -77,8 +82,20 @@ struct EvalQueues {
     uint32_t* q[2];          // pending boxes of a call round
     unsigned long long* rc;  // the two rounds' queue counters
     ct::EncBox* enc;         // enclosed boxes and weights (n)
+    // FP64 certification (cert[0] null: off)
+    uint32_t* cert[5];  // FP32 "true" verdicts to certify: record groups r1, r1_r2, 2x2, leaf; three-strip group
+    uint8_t* cflags;    // per box: the three-strip group's bits to certify (1: bit 2, 2: bit 6)
+    uint32_t* repair;   // boxes whose certification failed
 };
-static constexpr int kEvalCounters = 4;
+enum : int {
+    kCntCover = 0, kCntGaps = 1, kCntOverflow = 2, kCntFull = 3,
+    kCntCert = 4,          // 4..8: the certification queues
+    kCntRepair = 9,        // boxes to evaluate again in FP64 alone
+    kCntCoverCert = 10,    // true strip-width results certified
+    kCntGapsCert = 11,     // true gap-width results certified
+};
+static constexpr int kEvalCounters = 12;
+static constexpr int kCertQueues = 5;
 // the groups whose can_recurse calls are recorded, and their verdict bits
 static constexpr int kRecGroups = 4;
 __host__ __device__ constexpr int rec_group(int k) { return k < 2 ? k : k + 1; }  // 0, 1, 3, 4
@@ -153,7 +170,7 @@ __global__ void __launch_bounds__(128) k_eval_calls(const ct::CrArgs* __restrict
             cc::trap_clear();
             uint8_t next;
             if (undecided) next = ct::kRecUndecided;
-            else if (ok) next = ct::kRecTrue;
+            else if (ok) next = (uint8_t)(ct::kRecTrue | ((round + 1) << 2));  // the call that settled it
             else if (round + 1 < ((st >> 2) & 7)) more = true, next = st;
             else next = (uint8_t)((st >> 5) & 3);
             state[i] = next;
@@ -189,7 +206,83 @@ __global__ void __launch_bounds__(128) k_eval_collect(size_t n, uint32_t* __rest
         if (s != ~0ULL) q.cover_box[s] = (uint32_t)i;
         s = cc::prove::warp_append(&q.counts[1], valid && need_gaps, q.cap, &q.counts[2]);
         if (s != ~0ULL) q.gaps_box[s] = (uint32_t)i;
+        if (q.cert[0]) {  // the FP32 pass's "true" bits, to certify in FP64
+            const bool fp32 = valid && !undecided;
+            for (int k = 0; k < kRecGroups; ++k) {
+                s = cc::prove::warp_append(&q.counts[kCntCert + k], fp32 && ((m >> rec_group(k)) & 1u), q.cap,
+                                           &q.counts[kCntOverflow]);
+                if (s != ~0ULL) q.cert[k][s] = (uint32_t)i;
+            }
+            const uint8_t cf = (uint8_t)(((m >> 2) & 1u) | (((m >> 6) & 1u) << 1));
+            s = cc::prove::warp_append(&q.counts[kCntCert + 4], fp32 && cf, q.cap, &q.counts[kCntOverflow]);
+            if (s != ~0ULL) {
+                q.cert[4][s] = (uint32_t)i;
+                q.cflags[i] = cf;
+            }
+        }
     }
+}
+
+// pass 4: FP64 certification of the FP32 pass's "true" verdicts of group K
+// (0..3: the record groups r1, r1_r2, 2x2, leaf; 4: the three-strip group).
+// A record group's state byte names the call that settled the criterion
+// (bits 2-4, 1-based; 0: none); without record buffers every call is
+// evaluated.  Failures go to the repair queue.
+template <Layout L, int K>
+__global__ void __launch_bounds__(128) k_eval_cert(const double* __restrict__ in, size_t n, EvalQueues q) {
+    const unsigned long long c = q.counts[kCntCert + K];
+    const unsigned long long nq = c < q.cap ? c : q.cap;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nq;
+         base += stride) {
+        const unsigned long long j = base + (threadIdx.x & 31);
+        const bool valid = j < nq;
+        bool fail = false;
+        uint32_t i = 0;
+        if (valid) {
+            i = q.cert[K][j];
+            const ct::Box b = load_box<L>(in, n, i);
+            if (K < kRecGroups) {
+                const int call = q.states ? (int)((q.states[(size_t)K * n + i] >> 2) & 7) : -1;
+                fail = !ct::certify_group<rec_group(K)>(b, call);
+            } else {
+                const uint8_t f = q.cflags[i];
+                fail = !ct::certify_r123(b, ((f & 1) ? (1u << 2) : 0u) | ((f & 2) ? (1u << 6) : 0u));
+            }
+        }
+        __syncwarp();
+        const unsigned long long s = cc::prove::warp_append(&q.counts[kCntRepair], valid && fail, q.cap,
+                                                            &q.counts[kCntOverflow]);
+        if (s != ~0ULL) q.repair[s] = i;
+    }
+}
+
+// pass 5: boxes whose certification failed, evaluated again in FP64 alone
+// (every criterion and both bisections as the reference computes them)
+template <Layout L>
+__global__ void __launch_bounds__(128) k_eval_repair(const double* __restrict__ in, size_t n, EvalQueues q,
+                                                     uint32_t* __restrict__ masks) {
+    const unsigned long long c = q.counts[kCntRepair];
+    const unsigned long long nq = c < q.cap ? c : q.cap;
+    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < nq;
+         j += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t i = q.repair[j];
+        masks[i] = ct::eval_all_fp64(load_box<L>(in, n, i));
+    }
+}
+
+// a failed certificate of a bisection pass: the box to the repair queue
+__device__ __forceinline__ void eval_repair_push(const EvalQueues& q, uint32_t i) {
+    const unsigned long long s = atomicAdd(&q.counts[kCntRepair], 1ULL);
+    if (s < q.cap) q.repair[s] = i;
+    else atomicExch(&q.counts[kCntOverflow], 1ULL);
+}
+// per-thread tally summed over the warp, one atomic per warp (every lane
+// of the block reaches the end of the kernel's loop)
+__device__ __forceinline__ void warp_tally(unsigned long long* counter, unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(counter, v);
 }
 
 template <Layout L, int MinB = 1>
@@ -222,24 +315,36 @@ template <Layout L, int MinB = 1>
 __global__ void __launch_bounds__(128, MinB) k_eval_cover(const double* __restrict__ in, size_t n, EvalQueues q,
                                                           uint32_t* __restrict__ masks) {
     const unsigned long long nq = q.counts[0] < q.cap ? q.counts[0] : q.cap;
+    const bool certify = q.cert[0] != nullptr;
+    unsigned long long certified = 0;
     for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < nq;
          j += (unsigned long long)gridDim.x * blockDim.x) {
         const uint32_t i = q.cover_box[j];
-        uint32_t m = ct::cover_pass_box(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr);
+        bool repair = false;
+        uint32_t m = ct::cover_pass_box(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr, certify, &repair);
         if (m) masks[i] |= m;
+        if (repair) eval_repair_push(q, i);
+        else if (certify && (m & (1u << 2)) && !(m >> 31)) ++certified;
     }
+    if (certify) warp_tally(&q.counts[kCntCoverCert], certified);
 }
 
 template <Layout L, int MinB = 1>
 __global__ void __launch_bounds__(128, MinB) k_eval_gaps(const double* __restrict__ in, size_t n, EvalQueues q,
                                                          uint32_t* __restrict__ masks) {
     const unsigned long long nq = q.counts[1] < q.cap ? q.counts[1] : q.cap;
+    const bool certify = q.cert[0] != nullptr;
+    unsigned long long certified = 0;
     for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < nq;
          j += (unsigned long long)gridDim.x * blockDim.x) {
         const uint32_t i = q.gaps_box[j];
-        uint32_t m = ct::gaps_pass_box(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr);
+        bool repair = false;
+        uint32_t m = ct::gaps_pass_box(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr, certify, &repair);
         if (m) masks[i] |= m;
+        if (repair) eval_repair_push(q, i);
+        else if (certify && (m & (1u << 5)) && !(m >> 31)) ++certified;
     }
+    if (certify) warp_tally(&q.counts[kCntGapsCert], certified);
 }
 
 // queue and record buffers for up to `cap` boxes in handle slots 16..20 and
@@ -260,7 +365,16 @@ static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
     if ((st = ccrt::ensure(h, 39, cap * sizeof(ct::EncBox), &enc))) return st;
     *q = EvalQueues{(uint32_t*)a, (uint32_t*)b, (uint32_t*)c, (unsigned long long*)e, cap,
                     (ct::CrArgs*)args, (uint8_t*)states, {(uint32_t*)q0, (uint32_t*)q1}, (unsigned long long*)rc,
-                    (ct::EncBox*)enc};
+                    (ct::EncBox*)enc, {}, nullptr, nullptr};
+    if (h->eval_certify) {  // certification queues in slots 24..26 (25 bytes per box)
+        void *cq, *cf, *rq;
+        if ((st = ccrt::ensure(h, 24, cap * kCertQueues * sizeof(uint32_t), &cq))) return st;
+        if ((st = ccrt::ensure(h, 25, cap, &cf))) return st;
+        if ((st = ccrt::ensure(h, 26, cap * sizeof(uint32_t), &rq))) return st;
+        for (int k = 0; k < kCertQueues; ++k) q->cert[k] = (uint32_t*)cq + (size_t)k * cap;
+        q->cflags = (uint8_t*)cf;
+        q->repair = (uint32_t*)rq;
+    }
     return CC_OK;
 }
 
@@ -336,6 +450,16 @@ CC_EVAL_LAUNCH(k_eval_cover, in, n, q, masks)
 CC_EVAL_LAUNCH(k_eval_gaps, in, n, q, masks)
 #undef CC_EVAL_LAUNCH
 
+// kernels launched by pass k beyond one (the FP32 pass's groups, rounds and
+// collection; the certification pass's five group kernels) and whether a
+// pass launches at all
+static int pass_kernels(int pass, const EvalQueues& q) {
+    if (pass == 0) return q.args ? 1 + kRecGroups * (1 + ct::kCrRecordSlots) + 1 : ct::F32_GROUPS + 1;
+    if (pass == 4) return q.cert[0] ? kCertQueues : 0;
+    if (pass == 5) return q.cert[0] ? 1 : 0;
+    return 1;
+}
+
 template <Layout L>
 static void launch_pass(int pass, int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks,
                         EvalQueues q) {
@@ -343,7 +467,18 @@ static void launch_pass(int pass, int minb, int g, cudaStream_t s, const double*
         case 0: launch_k_eval_f32<L>(minb, g, s, in, n, masks, q); break;
         case 1: launch_k_eval_main<L>(minb, g, s, in, n, masks, q); break;
         case 2: launch_k_eval_cover<L>(minb, g, s, in, n, masks, q); break;
-        default: launch_k_eval_gaps<L>(minb, g, s, in, n, masks, q); break;
+        case 3: launch_k_eval_gaps<L>(minb, g, s, in, n, masks, q); break;
+        case 4:
+            if (!q.cert[0]) break;
+            k_eval_cert<L, 0><<<g, 128, 0, s>>>(in, n, q);
+            k_eval_cert<L, 1><<<g, 128, 0, s>>>(in, n, q);
+            k_eval_cert<L, 2><<<g, 128, 0, s>>>(in, n, q);
+            k_eval_cert<L, 3><<<g, 128, 0, s>>>(in, n, q);
+            k_eval_cert<L, 4><<<g, 128, 0, s>>>(in, n, q);
+            break;
+        default:
+            if (q.cert[0]) k_eval_repair<L><<<g, 128, 0, s>>>(in, n, q, masks);
+            break;
     }
 }
 
@@ -360,7 +495,7 @@ static int eval_launches(cc_handle* h, const double* in, size_t n, uint32_t* mas
         if ((size_t)g > need) g = (int)need;
         launch_pass<L>(pass, h->tune_minb[pass], g, s, in, n, masks, q);
         CC_LAUNCHED(h);
-        if (pass == 0) h->launches += 1 + kRecGroups * (1 + ct::kCrRecordSlots);  // groups, rounds, collection
+        h->launches += pass_kernels(pass, q) - 1;
     }
     if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[CC_EVAL_STAGES], s));
     return CC_OK;
@@ -393,7 +528,8 @@ static int eval_batch(cc_handle* h, const double* in, size_t n, uint32_t* masks,
                                        (uintptr_t)h->sm_count, (uintptr_t)h->tune_minb[0], (uintptr_t)h->tune_minb[1],
                                        (uintptr_t)h->tune_minb[2], (uintptr_t)h->tune_minb[3],
                                        (uintptr_t)h->tune_grid[0], (uintptr_t)h->tune_grid[1],
-                                       (uintptr_t)h->tune_grid[2], (uintptr_t)h->tune_grid[3]};
+                                       (uintptr_t)h->tune_grid[2], (uintptr_t)h->tune_grid[3],
+                                       (uintptr_t)q.cert[0], (uintptr_t)q.cflags, (uintptr_t)q.repair};
         std::vector<uintptr_t> key(std::begin(key_items), std::end(key_items));
         if (!h->graph_exec || key != h->graph_key) {
             const uint64_t before = h->launches;
@@ -495,6 +631,34 @@ __global__ void __launch_bounds__(256) k_fp64_peak(double* out, int iters, int u
     if (s == 12345.678) out[0] = s;  // keeps the chains alive
 }
 
+// FP32 counterpart: chains of directed-rounding adds and multiplies (the
+// FP32 enclosures' instructions) or of FMAs.  An FP32 FMA warp instruction
+// issues every cycle on each SM sub-partition, so the FMA rate / 32 is also
+// the device's warp-instruction issue rate.
+__global__ void __launch_bounds__(256) k_fp32_peak(float* out, int iters, int use_fma) {
+    float a[8], b = 1.0000001f, c = 1e-7f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = threadIdx.x * 1e-4f + k;
+    if (use_fma) {
+        for (int i = 0; i < iters; ++i) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], b, c);
+        }
+    } else {
+        for (int i = 0; i < iters; ++i) {
+#pragma unroll
+            for (int k = 0; k < 8; k += 2) {
+                a[k] = __fadd_rd(a[k], c);
+                a[k + 1] = __fmul_ru(a[k + 1], b);
+            }
+        }
+    }
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    if (s == 12345.678f) out[0] = s;  // keeps the chains alive
+}
+
 extern "C" int cc_selftest_subinterval_contracted(const double* lo, const double* hi, const int* idx, const int* cnt,
                                                   double* out, size_t n, void* stream);
 
@@ -525,6 +689,16 @@ __global__ void k_selftest_bisection_f32(int which, const double* __restrict__ a
         f64_out[i] = ct::gap_width_realizable(a[6], a[0], a[2], a[1], a[3], a[4]) ? 1 : 0;
     }
     if (cc::trap_status() != cc::TRAP_NONE) f64_out[i] |= 2;
+}
+
+// the FP64 certification run of record group K on each box, with the call
+// number given per box (1-based; 0 none; -1 every call evaluated)
+template <int K>
+__global__ void k_selftest_certify(const double* __restrict__ aos, size_t n, const int* __restrict__ call,
+                                   uint8_t* __restrict__ out) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = ct::certify_group<rec_group(K)>(load_box<Layout::AoS>(aos, n, i), call[i]) ? 1 : 0;
 }
 
 // the whole bisection (with the FP32 shortcuts) of each row
@@ -651,6 +825,26 @@ int cc_last_eval_counts(cc_handle* h, unsigned long long* counts) {
     return CC_OK;
 }
 
+int cc_set_eval_certify(cc_handle* h, int enable) {
+    if (!h) return CC_ERR_PARAM;
+    h->eval_certify = enable != 0;
+    return CC_OK;
+}
+
+int cc_last_eval_cert(cc_handle* h, unsigned long long* counts) {
+    if (!h || !counts) return ccrt::fail(h, CC_ERR_PARAM, "cc_last_eval_cert: bad argument");
+    if (!h->eval_counts) return ccrt::fail(h, CC_ERR_PARAM, "cc_last_eval_cert: no evaluation recorded");
+    CC_CUDA(h, cudaSetDevice(h->device));
+    CC_CUDA(h, cudaDeviceSynchronize());
+    unsigned long long c[kEvalCounters];
+    CC_CUDA(h, cudaMemcpy(c, h->eval_counts, sizeof(c), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < kCertQueues; ++k) counts[k] = c[kCntCert + k];
+    counts[5] = c[kCntRepair];
+    counts[6] = c[kCntCoverCert];
+    counts[7] = c[kCntGapsCert];
+    return CC_OK;
+}
+
 int cc_last_stage_times(cc_handle* h, float* ms, int max_stages, int* n_stages) {
     if (!h || !ms || !n_stages || max_stages < 0) return ccrt::fail(h, CC_ERR_PARAM, "cc_last_stage_times: bad argument");
     *n_stages = 0;
@@ -695,9 +889,10 @@ extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint3
     int st = eval_queues(h, n, &q);
     if (st) return st;
     cudaStream_t s = h->stream;
-    cudaEvent_t e0, e1;
-    CC_CUDA(h, cudaEventCreate(&e0));
-    CC_CUDA(h, cudaEventCreate(&e1));
+    ccrt::EventPair ev;
+    CC_CUDA(h, cudaEventCreate(&ev.e0));
+    CC_CUDA(h, cudaEventCreate(&ev.e1));
+    const cudaEvent_t e0 = ev.e0, e1 = ev.e1;
     const int minbs[3] = {1, 4, 8}, grids[4] = {2, 4, 8, 16};
     unsigned long long snap[kEvalCounters] = {};
     cc_tune_result r{};
@@ -719,7 +914,7 @@ extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint3
         *ms = best;
         return CC_OK;
     };
-    for (int pass = 0; pass < CC_EVAL_STAGES; ++pass) {
+    for (int pass = 0; pass < CC_EVAL_TUNED_STAGES; ++pass) {
         float best = 1e30f;
         int bm = 1, bg = 8;
         for (int a = 0; a < 3; ++a)
@@ -744,8 +939,6 @@ extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint3
         r.blocks_per_sm[pass] = bg;
         r.ms[pass] = best;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (out) *out = r;
     return CC_OK;
 }
@@ -757,16 +950,21 @@ extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint3
 // cudaMalloc would block on device-wide synchronisation, and processes that
 // run close to the memory limit and pre-reserve everything at start-up.
 // cc_tight_eval_device_static evaluates a batch already in device memory
-// with the same three passes as cc_tight_eval_device, but keeps its
-// bisection queues in the fixed array below instead of handle-owned buffers,
-// and needs no handle.  The array is part of the library image: every GPU
-// that loads the library holds CC_STATIC_EVAL_SCRATCH_BYTES for it until
-// the process exits.
+// with the same passes as cc_tight_eval_device (FP64 certification
+// included), but keeps its queues in the fixed array below instead of
+// handle-owned buffers, and needs no handle.  Without room for the record
+// buffers its FP32 pass runs every criterion group in one kernel, and the
+// certification evaluates every call of a criterion.  The array is part of
+// the library image: every GPU that loads the library holds
+// CC_STATIC_EVAL_SCRATCH_BYTES for it until the process exits.
 static constexpr size_t kStaticMaxBoxes = CC_STATIC_EVAL_MAX_BOXES;
 static constexpr size_t kStaticCountersBytes = 256;
-static constexpr size_t kStaticScratchBytes =
-    kStaticCountersBytes + kStaticMaxBoxes * 3 * sizeof(uint32_t);
-static_assert(kStaticScratchBytes <= CC_STATIC_EVAL_SCRATCH_BYTES, "static scratch larger than advertised");
+// per box: the full, strip-width and gap-width queues, the five
+// certification queues and the repair queue (4 bytes each), one flag byte
+static constexpr size_t kStaticBytesPerBox = (3 + kCertQueues + 1) * sizeof(uint32_t) + 1;
+static constexpr size_t kStaticScratchBytes = kStaticCountersBytes + kStaticMaxBoxes * kStaticBytesPerBox;
+static_assert(kEvalCounters * sizeof(unsigned long long) <= kStaticCountersBytes, "counters do not fit");
+static_assert(kStaticScratchBytes == CC_STATIC_EVAL_SCRATCH_BYTES, "static scratch size differs from the header");
 static __device__ __align__(256) unsigned char cc_static_eval_scratch[CC_STATIC_EVAL_SCRATCH_BYTES];
 
 namespace {
@@ -818,15 +1016,32 @@ extern "C" int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t
     q.q[0] = q.q[1] = nullptr;
     q.rc = nullptr;
     q.enc = nullptr;
+    p += kStaticMaxBoxes * sizeof(uint32_t);
+    for (int k = 0; k < kCertQueues; ++k) {
+        q.cert[k] = (uint32_t*)p;
+        p += kStaticMaxBoxes * sizeof(uint32_t);
+    }
+    q.repair = (uint32_t*)p;
+    p += kStaticMaxBoxes * sizeof(uint32_t);
+    q.cflags = p;
     cudaStream_t s = (cudaStream_t)stream;
+    // an error the caller left pending is not ours to report or to clear
+    if (cudaPeekAtLastError() != cudaSuccess) return CC_ERR_CUDA;
     // the queue counters are the only state that must start at zero
-    if (cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s) != cudaSuccess) {
-        cudaGetLastError();
+    const cudaError_t me = cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s);
+    if (me != cudaSuccess) {
+        cudaGetLastError();  // the memset's own error
         return CC_ERR_CUDA;
     }
-    const int g = g_static_sms[dev] * 8;
+    // a small batch takes no more blocks than it has boxes to spread over
+    const size_t need = (n + 127) / 128;
+    int g = g_static_sms[dev] * 8;
+    if ((size_t)g > need) g = (int)need;
     for (int pass = 0; pass < CC_EVAL_STAGES; ++pass) launch_pass<Layout::SoA>(pass, 1, g, s, soa, n, masks, q);
-    if (cudaGetLastError() != cudaSuccess) return CC_ERR_CUDA;
+    if (cudaPeekAtLastError() != cudaSuccess) {
+        cudaGetLastError();  // a launch of this call failed
+        return CC_ERR_CUDA;
+    }
     return CC_OK;
 }
 
@@ -947,35 +1162,73 @@ int cc_tight_eval(cc_handle* h, const cc_tight_box* boxes, size_t n, uint32_t* m
     return CC_OK;
 }
 
-// Diagnostic: measured FP64 instruction throughput of this device in
-// operations per second (one op = one FP64 instruction; an FMA counts 1).
-int cc_selftest_fp64_peak(cc_handle* h, int use_fma, double* ops_per_s) {
-    if (!h || !ops_per_s) return CC_ERR_PARAM;
+// Diagnostic: the FP64 certification run of a record group (0 r1, 1 r1_r2,
+// 2 2x2, 3 leaf r1_r2_r3) on host boxes, one call number per box.
+int cc_selftest_certify(cc_handle* h, int group, const cc_tight_box* boxes, const int* call, size_t n,
+                        uint8_t* out) {
+    if (!h || !boxes || !call || !out || group < 0 || group >= kRecGroups) return CC_ERR_PARAM;
+    h->launches = 0;
+    if (n == 0) return CC_OK;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    void *d_b, *d_c, *d_o;
+    int st;
+    if ((st = ccrt::ensure(h, 0, n * sizeof(cc_tight_box), &d_b))) return st;
+    if ((st = ccrt::ensure(h, 1, n * sizeof(int), &d_c))) return st;
+    if ((st = ccrt::ensure(h, 2, n, &d_o))) return st;
+    CC_CUDA(h, cudaMemcpyAsync(d_b, boxes, n * sizeof(cc_tight_box), cudaMemcpyHostToDevice, h->stream));
+    CC_CUDA(h, cudaMemcpyAsync(d_c, call, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    const int g = (int)((n + 127) / 128);
+    const double* b = (const double*)d_b;
+    switch (group) {
+        case 0: k_selftest_certify<0><<<g, 128, 0, h->stream>>>(b, n, (const int*)d_c, (uint8_t*)d_o); break;
+        case 1: k_selftest_certify<1><<<g, 128, 0, h->stream>>>(b, n, (const int*)d_c, (uint8_t*)d_o); break;
+        case 2: k_selftest_certify<2><<<g, 128, 0, h->stream>>>(b, n, (const int*)d_c, (uint8_t*)d_o); break;
+        default: k_selftest_certify<3><<<g, 128, 0, h->stream>>>(b, n, (const int*)d_c, (uint8_t*)d_o); break;
+    }
+    CC_LAUNCHED(h);
+    CC_CUDA(h, cudaMemcpyAsync(out, d_o, n, cudaMemcpyDeviceToHost, h->stream));
+    CC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CC_OK;
+}
+
+// Diagnostic: measured instruction throughput of this device in operations
+// per second (one op = one thread instruction; an FMA counts 1): kind 0 FP64
+// directed add/mul, 1 FP64 FMA, 2 FP32 directed add/mul, 3 FP32 FMA.  Best
+// of three timed launches (CUDA events) after a warm-up launch.
+int cc_selftest_peak(cc_handle* h, int kind, double* ops_per_s) {
+    if (!h || !ops_per_s || kind < 0 || kind > 3) return CC_ERR_PARAM;
     CC_CUDA(h, cudaSetDevice(h->device));
     void* d;
     int st = ccrt::ensure(h, 0, 64, &d);
     if (st) return st;
-    const int blocks = h->sm_count * 8, threads = 256, iters = 4096;
-    cudaEvent_t e0, e1;
-    CC_CUDA(h, cudaEventCreate(&e0));
-    CC_CUDA(h, cudaEventCreate(&e1));
-    k_fp64_peak<<<blocks, threads, 0, h->stream>>>((double*)d, 64, use_fma);  // warm-up
+    const int blocks = h->sm_count * 8, threads = 256, iters = kind >= 2 ? 16384 : 4096;
+    ccrt::EventPair ev;
+    CC_CUDA(h, cudaEventCreate(&ev.e0));
+    CC_CUDA(h, cudaEventCreate(&ev.e1));
+    auto launch = [&](int it) {
+        if (kind < 2) k_fp64_peak<<<blocks, threads, 0, h->stream>>>((double*)d, it, kind & 1);
+        else k_fp32_peak<<<blocks, threads, 0, h->stream>>>((float*)d, it, kind & 1);
+    };
+    launch(64);  // warm-up
     CC_LAUNCHED(h);
     float best = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
-        CC_CUDA(h, cudaEventRecord(e0, h->stream));
-        k_fp64_peak<<<blocks, threads, 0, h->stream>>>((double*)d, iters, use_fma);
+        CC_CUDA(h, cudaEventRecord(ev.e0, h->stream));
+        launch(iters);
         CC_LAUNCHED(h);
-        CC_CUDA(h, cudaEventRecord(e1, h->stream));
-        CC_CUDA(h, cudaEventSynchronize(e1));
+        CC_CUDA(h, cudaEventRecord(ev.e1, h->stream));
+        CC_CUDA(h, cudaEventSynchronize(ev.e1));
         float ms = 0;
-        CC_CUDA(h, cudaEventElapsedTime(&ms, e0, e1));
+        CC_CUDA(h, cudaEventElapsedTime(&ms, ev.e0, ev.e1));
         if (ms < best) best = ms;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     *ops_per_s = (double)blocks * threads * iters * 8 / (best * 1e-3);
     return CC_OK;
+}
+
+// Diagnostic: FP64 instruction throughput (kind 0 or 1 of cc_selftest_peak).
+int cc_selftest_fp64_peak(cc_handle* h, int use_fma, double* ops_per_s) {
+    return cc_selftest_peak(h, use_fma ? 1 : 0, ops_per_s);
 }
 
 // Diagnostic: the device's directed-rounding primitives on host arrays
@@ -1119,7 +1372,27 @@ static_assert(S_LEAF2 < 16, "proof buffers overlap the evaluation queues");
 struct GenTotals {
     unsigned long long counts[4][8] = {};
     unsigned long long digest = 0, leaf_evals = 0, trapped = 0;
+    unsigned long long fp32[4] = {};  // first_f32 outcomes (Counters::fp32)
+    void add(const GenTotals& g) {
+        for (int l = 0; l < 4; ++l)
+            for (int o = 0; o < 8; ++o) counts[l][o] += g.counts[l][o];
+        digest += g.digest;
+        leaf_evals += g.leaf_evals;
+        trapped += g.trapped;
+        for (int k = 0; k < 4; ++k) fp32[k] += g.fp32[k];
+    }
 };
+
+// FP64 certification failures of this translation unit's kernels so far
+// (cc_cert_fail_count; expected to stay 0)
+static unsigned long long cert_failures_so_far() {
+    unsigned long long v = 0;
+    if (cudaMemcpyFromSymbol(&v, cc::tight::cc_cert_fail_count, sizeof(v)) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return v;
+}
 
 int stage_grid(cc_handle* h) { return h->sm_count * 6; }
 
@@ -1364,6 +1637,7 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
     tot.digest += hc.digest;
     tot.leaf_evals += hc.leaf_evals;
     tot.trapped += trapped;
+    for (int k = 0; k < 4; ++k) tot.fp32[k] += hc.fp32[k];
     return CC_OK;
 }
 
@@ -1408,11 +1682,7 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
         }
         if (st) return st;
         out.insert(out.end(), part.begin(), part.end());
-        for (int l = 0; l < 4; ++l)
-            for (int o = 0; o < 8; ++o) tot.counts[l][o] += g.counts[l][o];
-        tot.digest += g.digest;
-        tot.leaf_evals += g.leaf_evals;
-        tot.trapped += g.trapped;
+        tot.add(g);
         t = e;
     }
     return CC_OK;
@@ -1484,6 +1754,7 @@ static int prove_generations(cc_handle* h, const cc_tight_grid* grid, int flags,
     h->interrupt.store(0);
     CC_CUDA(h, cudaSetDevice(h->device));
     auto t0 = std::chrono::steady_clock::now();
+    const unsigned long long fails0 = cert_failures_so_far();
     Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 24, 1ULL << 20, 1ULL << 26};
     std::vector<cc_tight_box> next;
     int gens_run = start_gen > 0 ? start_gen - 1 : 0;
@@ -1519,6 +1790,8 @@ static int prove_generations(cc_handle* h, const cc_tight_grid* grid, int flags,
         stats->generations_run = gens_run;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         stats->kernel_launches = h->launches;
+        std::memcpy(stats->fp32_first, tot.fp32, sizeof(stats->fp32_first));
+        stats->cert_failures = cert_failures_so_far() - fails0;
     }
     return status;
 }
@@ -1606,6 +1879,7 @@ extern "C" int cc_tight_generation(cc_handle* h, const cc_tight_box* parents, si
     auto t0 = std::chrono::steady_clock::now();
     Caps caps{0, 1ULL << 22, 1ULL << 23, 1ULL << 24, 1ULL << 24, 1ULL << 20, 1ULL << 26};
     GenTotals tot;
+    const unsigned long long fails0 = cert_failures_so_far();
     std::vector<cc_tight_box> in(parents, parents + n_parents), out;
     int st = run_generation(h, in, la_splits, r_splits, out, tot, caps, !(flags & CC_PROVE_PLAIN), flags, task_lo, task_hi);
     if (st) return st;
@@ -1622,6 +1896,8 @@ extern "C" int cc_tight_generation(cc_handle* h, const cc_tight_box* parents, si
         stats->gen_sizes[0] = out.size();
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         stats->kernel_launches = h->launches;
+        std::memcpy(stats->fp32_first, tot.fp32, sizeof(stats->fp32_first));
+        stats->cert_failures = cert_failures_so_far() - fails0;
     }
     return CC_OK;
 }

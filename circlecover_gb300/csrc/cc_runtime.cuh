@@ -34,8 +34,11 @@ struct cc_handle {
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
     // evaluation passes' register budget and grid (blocks per SM), set by cc_autotune_eval
-    int tune_minb[CC_EVAL_STAGES] = {1, 1, 1, 1};
-    int tune_grid[CC_EVAL_STAGES] = {8, 8, 8, 8};
+    // (the certification and repair passes, 4 and 5, keep the defaults)
+    int tune_minb[CC_EVAL_STAGES] = {1, 1, 1, 1, 1, 1};
+    int tune_grid[CC_EVAL_STAGES] = {8, 8, 8, 8, 8, 8};
+    // FP64 certification of the evaluation's FP32 decisions (cc_set_eval_certify)
+    bool eval_certify = true;
     // where the tight proof writes its state after each generation (empty: off)
     std::string checkpoint_path;
     // sample of r3 cells logged by the last tight proof (CC_PROVE_LOG_CELLS)
@@ -91,6 +94,18 @@ inline int fail(cc_handle* h, int status, const char* what, cudaError_t e = cuda
         if (cc_e_ != cudaSuccess) return ccrt::fail((h), CC_ERR_CUDA, "launch", cc_e_); \
         (h)->launches += 1;                                                             \
     } while (0)
+
+// two CUDA events, destroyed on every return path
+struct EventPair {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    EventPair() = default;
+    EventPair(const EventPair&) = delete;
+    EventPair& operator=(const EventPair&) = delete;
+    ~EventPair() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    }
+};
 
 // grow-only device buffer; contents are not preserved
 inline int ensure(cc_handle* h, int slot, size_t bytes, void** out) {

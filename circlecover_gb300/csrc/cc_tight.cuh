@@ -133,10 +133,41 @@ CC_FN bool can_recurse_t(S ub_w, S ub_h, S ub_largest, S lb_weight) {
     S ub_needed = mul_up(ratio, ub_area);
     return lb_weight >= ub_needed;
 }
+// Certification runs (device only): an FP32 evaluation decided that a
+// criterion holds and which of its can_recurse calls settled it; the FP64
+// criterion then runs with only that call evaluated and every other call
+// answering "false".  Every call site of the criteria is of the form
+// "if (... && can_recurse(...)) return true" or "return can_recurse(...)"
+// inside placements joined by ||, so a call forced to "false" can only make
+// the criterion false: an FP64 run that returns true is an FP64 proof that
+// the criterion holds, whatever the FP32 evaluation did.
 CC_FN bool can_recurse(double ub_w, double ub_h, double ub_largest, double lb_weight) {
+#if CC_DEVICE_BUILD
+    if (cc_trap_words[threadIdx.x] & kCertModeBit) {
+        const uint16_t s = cc_cert_state[threadIdx.x];
+        cc_cert_state[threadIdx.x] = (uint16_t)(s + 1);
+        if ((s & 0xff) + 1 != (s >> 8)) return false;
+    }
+#endif
     return can_recurse_t<double>(ub_w, ub_h, ub_largest, lb_weight);
 }
 #if CC_DEVICE_BUILD
+// start / end of a certification run that evaluates call number `call`
+// (1-based; 0 = no call) of the FP64 criterion; the trap status is cleared
+CC_FN void cert_begin(int call) {
+    cc_cert_state[threadIdx.x] = (uint16_t)(call << 8);
+    cc_trap_words[threadIdx.x] = kCertModeBit;
+}
+CC_FN void cert_end() { cc_trap_words[threadIdx.x] &= (uint8_t)~kCertModeBit; }
+// the FP32 can_recurse counts its calls (low byte of cc_cert_state)
+CC_FN void cert_count_reset() { cc_cert_state[threadIdx.x] = 0; }
+CC_FN int cert_count() { return cc_cert_state[threadIdx.x] & 0xff; }
+// FP64 certifications that failed in this translation unit's kernels since
+// the library was loaded: an FP32 decision the FP64 check did not confirm
+// (the FP64 result is used instead).  Expected to stay 0; the host reads it
+// with cudaMemcpyFromSymbol.
+static __device__ unsigned long long cc_cert_fail_count;
+CC_FN void cert_failed() { atomicAdd(&cc_cert_fail_count, 1ULL); }
 // One out-of-line copy for the FP32 evaluation (it is called from many
 // sites), with a shortcut before its costly part.  Where largest_norm is
 // certainly above 9/64, can_recurse_t takes ratio = lesser(ratio_cor,
@@ -185,6 +216,7 @@ __device__ __noinline__ inline bool can_recurse_record(f32::Fv ub_w, f32::Fv ub_
 __device__ __noinline__ inline bool can_recurse(f32::Fv ub_w, f32::Fv ub_h, f32::Fv ub_largest, f32::Fv lb_weight) {
     using f32::Fv;
     if (cc_trap_words[threadIdx.x] & kTrapModeBit) return can_recurse_record(ub_w, ub_h, ub_largest, lb_weight);
+    cc_cert_state[threadIdx.x]++;  // call count for a later certification run (cert_count)
     const Fv ub_area = f32::mul(ub_w, ub_h);
     const Fv s = f32::rcp_up(f32::lesser(ub_w, ub_h));
     const Fv largest_norm = f32::mul(f32::mul(s, s), ub_largest);
@@ -536,9 +568,41 @@ CC_FN double cover_strip_width_early(double la_hi, double r1, double r2, double 
     return lo;
 }
 
+CC_FN double cover_strip_width_fp64(double la_hi, double r1, double r2, double r3);
+
+// The widest realizable strip.  On the device the bisection's FP32 steps are
+// followed by an FP64 certificate: the width it returns must pass the FP64
+// predicate (the reference's bisection keeps lo realizable by construction,
+// r1_r2_r3_strategies.cu:90: "a strip width we can definitely achieve").  If
+// it does not, the bisection is redone in FP64 alone (cert_failed).
 CC_FN double cover_strip_width(double la_hi, double r1, double r2, double r3) {
     int decided;
-    return cover_strip_width_early(la_hi, r1, r2, r3, NoEarly{}, &decided);
+    const double w = cover_strip_width_early(la_hi, r1, r2, r3, NoEarly{}, &decided);
+#if CC_DEVICE_BUILD
+    if (!strip_width_realizable(r1, r2, r3, w)) {
+        cert_failed();
+        return cover_strip_width_fp64(la_hi, r1, r2, r3);
+    }
+#endif
+    return w;
+}
+
+// The bisection exactly as the reference runs it (r1_r2_r3_strategies.cu:
+// 77-88): FP64 steps only, no FP32 shortcut.  Used to repair a box whose
+// FP64 certification failed.
+CC_FN double cover_strip_width_fp64(double la_hi, double r1, double r2, double r3) {
+    double lo = 0.3, hi = la_hi;
+    for (int it = 0;; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (it >= CC_BISECTION_CAP) {
+            trap(TRAP_BISECTION_CAP);
+            break;
+        }
+        if (strip_width_realizable(r1, r2, r3, mid)) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
 template <class S>
@@ -945,9 +1009,39 @@ CC_FN double gaps_width_early(double r1, double r2, double r4, GapsStart g, Earl
     return lo;
 }
 
+CC_FN double gaps_width_fp64(double r1, double r2, double r4, GapsStart g);
+
+// The widest gap disk 4 can close.  On the device the result of the
+// bisection with FP32 steps gets an FP64 certificate: 0 (no gap, nothing to
+// close) or a width that passes the FP64 predicate, as every lower end of
+// the reference's bracket does; otherwise the bisection is redone in FP64.
 CC_FN double gaps_width(double r1, double r2, double r4, GapsStart g) {
     int decided;
-    return gaps_width_early(r1, r2, r4, g, NoEarly{}, &decided);
+    const double gap = gaps_width_early(r1, r2, r4, g, NoEarly{}, &decided);
+#if CC_DEVICE_BUILD
+    if (gap != 0.0 && !gap_width_realizable(gap, r1, g.w1, r2, g.w2, r4)) {
+        cert_failed();
+        return gaps_width_fp64(r1, r2, r4, g);
+    }
+#endif
+    return gap;
+}
+
+// The gap-width bisection exactly as the reference runs it
+// (r1_r2_large_r3_r4_gaps_strategy.cu:73-86): FP64 steps only.
+CC_FN double gaps_width_fp64(double r1, double r2, double r4, GapsStart g) {
+    double lo = 0.0, hi = add_dn(sqrt_dn(r1), sqrt_dn(r2));
+    for (int it = 0;; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (it >= CC_BISECTION_CAP) {
+            trap(TRAP_BISECTION_CAP);
+            break;
+        }
+        if (gap_width_realizable(mid, r1, g.w1, r2, g.w2, r4)) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
 template <class S>
@@ -1082,6 +1176,30 @@ CC_FN_INL uint32_t eval_all(const Box& in) {
     return m;
 }
 
+// The verdict mask of one box in FP64 alone, both bisections as the
+// reference runs them (no FP32 step): the repair of a box one of whose
+// FP64 certifications failed.
+CC_FN_INL uint32_t eval_all_fp64(const Box& in) {
+    bool need_cover, need_gaps;
+    CoverJob cj;
+    GapsJob gj;
+    uint32_t m = eval_main(in, need_cover, cj, need_gaps, gj);
+    if (need_cover) {
+        trap_clear();
+        const double width = cover_strip_width_fp64(cj.la_hi, cj.r1, cj.r2, cj.r3);
+        if (cover_strip_finish(cj.la_hi, width, cj.ub_r4, cj.lb_R4)) m |= 1u << 2;
+        if (trap_status() != TRAP_NONE) m |= 1u << 31;
+    }
+    if (need_gaps) {
+        trap_clear();
+        const GapsStart g{gj.w1, gj.w2};
+        const double gap = gaps_width_fp64(gj.r1, gj.r2, gj.r4, g);
+        if (gaps_finish(gj.la_hi, g, gap, gj.r4_hi, Iv{gj.R_lo, gj.R_hi})) m |= 1u << 5;
+        if (trap_status() != TRAP_NONE) m |= 1u << 31;
+    }
+    return m;
+}
+
 #if CC_DEVICE_BUILD
 // ------------------------------------------------ FP32-first evaluation
 // eval_main on FP32 enclosures of the box (cc_f32.cuh): the same criteria,
@@ -1201,19 +1319,106 @@ CC_FN_INL uint32_t eval_group_f32(const Box& in64, EncBox* keep = nullptr) {
     return trap_status() == TRAP_NONE ? m : kF32Undecided;
 }
 
-// A whole criterion on FP32 enclosures first, then, if undecided, in FP64:
-// the same outcome and trap status as the FP64 criterion alone (a decided
-// FP32 evaluation stands for an FP64 one that did not trap).  The caller's
-// pending trap status is kept.
+// FP64 certification of a "true" that the FP32 pass decided for criterion
+// group G (F32_R1, F32_R12, F32_2X2, F32_LEAF) at eval_main's arguments: the
+// FP64 criterion with only call number `call` evaluated (1-based, the call
+// whose FP32 answer settled the criterion; 0: none, the criterion held
+// without one), or with all its calls for call < 0.  True if it holds
+// without reaching a trap site.
+template <int G>
+CC_FN_INL bool certify_group(const Box& in, int call) {
+    const Iv la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2];
+    const Iv weight = required_weight_for(la);
+    if (call >= 0) cert_begin(call);
+    else trap_clear();
+    bool ok;
+    if (G == F32_R1) {
+        ok = r1_strategies(la, weight, r1, r2.hi);
+    } else if (G == F32_R12) {
+        ok = r1_r2_strategies(la, weight, r1, r2, r3.hi);
+    } else {
+        Iv R4 = weight - r1 - r2 - r3;
+        tighten_lb(R4, 0.0);
+        Box v = in;
+        tighten_lb(v.r[2], v.r[3].lo);
+        tighten_lb(v.r[1], v.r[2].lo);
+        tighten_lb(v.r[0], v.r[1].lo);
+        Iv R = weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+        tighten_lb(R, 0.0);
+        ok = G == F32_2X2 ? two_by_two_strategies(v, R) : r1_r2_r3_strategies(v, R4);
+    }
+    const bool clean = trap_status() == TRAP_NONE;
+    cert_end();
+    trap_clear();
+    return ok && clean;
+}
+
+// FP64 certification of the bits the FP32 three-strip group decided "true":
+// bit 2 by the three-strips placement (one call at most, evaluated in full),
+// bit 6 (R or R4 empty).
+CC_FN_INL bool certify_r123(const Box& in, uint32_t bits) {
+    trap_clear();
+    const Iv la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2], r4 = in.r[3];
+    const Iv weight = required_weight_for(la);
+    bool ok = true;
+    if (bits & (1u << 2)) ok = r1_r2_r3_three_strips(la, weight, r1, r2, r3, r4.hi);
+    if (ok && (bits & (1u << 6))) {
+        Iv R4 = weight - r1 - r2 - r3;
+        tighten_lb(R4, 0.0);
+        Box v = in;
+        tighten_lb(v.r[2], v.r[3].lo);
+        tighten_lb(v.r[1], v.r[2].lo);
+        tighten_lb(v.r[0], v.r[1].lo);
+        Iv R = weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+        tighten_lb(R, 0.0);
+        ok = empty(R4) || empty(R);
+    }
+    ok = ok && trap_status() == TRAP_NONE;
+    trap_clear();
+    return ok;
+}
+
+// A whole criterion on FP32 enclosures first: the same outcome and trap
+// status as the FP64 criterion alone (a decided FP32 evaluation stands for an
+// FP64 one that did not trap).  A decided "false" stands (the leaf goes on
+// to the next criterion, as after an FP64 "false"); a decided "true" is
+// certified by the FP64 criterion with only the call that settled the FP32
+// run evaluated (cert_begin: the last call it made, or none); an undecided
+// run, or a certification that fails (cert_failed), takes the FP64
+// criterion's own result.  The caller's pending trap status is kept.
+// *how (optional): 0 FP64 evaluation, 1 FP32 "false", 2 FP32 "true" certified
+// in FP64, 3 certification failed.
 template <class Crit>
-CC_FN_INL bool first_f32(Crit crit, const Box& v, Iv rest) {
+CC_FN_INL bool first_f32(Crit crit, const Box& v, Iv rest, int* how = nullptr) {
     const uint32_t saved = trap_status();
     trap_clear();
+    cert_count_reset();
     const bool ok32 = crit(enclose(v), f32::of(rest));
     const bool decided = trap_status() == TRAP_NONE;
+    const int calls = cert_count();
     trap_clear();
+    if (decided && ok32) {
+        cert_begin(calls);
+        const bool ok64 = crit(v, rest);
+        const bool clean = trap_status() == TRAP_NONE;
+        cert_end();
+        trap_clear();
+        if (saved != TRAP_NONE) trap(saved);
+        if (ok64 && clean) {
+            if (how) *how = 2;
+            return true;
+        }
+        cert_failed();
+        if (how) *how = 3;
+        return crit(v, rest);
+    }
     if (saved != TRAP_NONE) trap(saved);
-    return decided ? ok32 : crit(v, rest);
+    if (decided) {
+        if (how) *how = 1;
+        return false;
+    }
+    if (how) *how = 0;
+    return crit(v, rest);
 }
 struct TwoByTwo {
     template <class I>
@@ -1224,16 +1429,56 @@ struct LeafR123 {
     CC_METHOD bool operator()(const BoxT<I>& v, I R4) const { return r1_r2_r3_strategies(v, R4); }
 };
 // two_by_two_strategies(v, R) and r1_r2_r3_strategies(v, R4), FP32 first
-CC_FN_INL bool two_by_two_first_f32(const Box& v, Iv R) { return first_f32(TwoByTwo{}, v, R); }
-CC_FN_INL bool r1_r2_r3_leaf_first_f32(const Box& v, Iv R4) { return first_f32(LeafR123{}, v, R4); }
+CC_FN_INL bool two_by_two_first_f32(const Box& v, Iv R, int* how = nullptr) {
+    return first_f32(TwoByTwo{}, v, R, how);
+}
+CC_FN_INL bool r1_r2_r3_leaf_first_f32(const Box& v, Iv R4, int* how = nullptr) {
+    return first_f32(LeafR123{}, v, R4, how);
+}
 
 // The two bisection criteria of one box, from the box itself (the queues
 // hold box indices): the bisection in FP64 (with its FP32 shortcuts), then
 // the recursion check first on FP32 enclosures and, if that is undecided, in
 // FP64.  Same result and trap bit as cover_pass / gaps_pass on eval_main's
 // jobs.
+// A true result gets an FP64 certificate, the argument the reference's
+// criterion makes with the width its bisection reaches: the strip of the
+// width used is realizable and the rest of the rectangle can be covered
+// recursively (r1_r2_r3_strategies.cu:77-93), resp. the gap of the width used
+// is 0 or can be closed by disk 4 and the rest covered
+// (r1_r2_large_r3_r4_gaps_strategy.cu:73-97) -- both in FP64.  If it fails
+// (*repair), the caller recomputes the box in FP64 alone (eval_all_fp64).
 // (enc: the box's enclosure and weight if the FP32 pass kept them)
-CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr) {
+CC_FN_INL bool cover_certificate(const Box& b, double width) {
+    trap_clear();
+    const Iv la = b.la, r1 = b.r[0], r2 = b.r[1], r3 = b.r[2];
+    bool ok = strip_width_realizable(r1.lo, r2.lo, r3.lo, width) &&
+              cover_strip_finish<double>(la.hi, width, b.r[3].hi, (required_weight_for(la) - r1 - r2 - r3).lo);
+    ok = ok && trap_status() == TRAP_NONE;
+    trap_clear();
+    return ok;
+}
+CC_FN_INL bool gaps_certificate(const Box& b, double gap) {
+    trap_clear();
+    Box v = b;
+    tighten_lb(v.r[2], v.r[3].lo);
+    tighten_lb(v.r[1], v.r[2].lo);
+    tighten_lb(v.r[0], v.r[1].lo);
+    GapsStart g;
+    bool ok = gaps_enters(v.r[0].lo, v.r[1].lo, g);
+    if (ok && gap != 0.0) ok = gap_width_realizable(gap, v.r[0].lo, g.w1, v.r[1].lo, g.w2, v.r[3].lo);
+    if (ok) {
+        Iv R = required_weight_for(v.la) - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+        tighten_lb(R, 0.0);
+        ok = gaps_finish(b.la.hi, g, gap, v.r[3].hi, R);
+    }
+    ok = ok && trap_status() == TRAP_NONE;
+    trap_clear();
+    return ok;
+}
+
+CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr, bool certify = false,
+                                  bool* repair = nullptr) {
     using f32::Fv;
     const Iv la = b.la, r1 = b.r[0], r2 = b.r[1], r3 = b.r[2];
     trap_clear();
@@ -1253,7 +1498,11 @@ CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr) {
     };
     int decided;
     const double width = cover_strip_width_early(la.hi, r1.lo, r2.lo, r3.lo, finish, &decided);
-    if (decided != f32::UNKNOWN) return decided == f32::YES ? (1u << 2) : 0u;
+    if (decided != f32::UNKNOWN) {
+        if (decided != f32::YES) return 0u;
+        if (certify && !cover_certificate(b, width)) *repair = true;
+        return 1u << 2;
+    }
     uint32_t trapped = trap_status();
     trap_clear();
     bool ok = lb_ok ? cover_strip_finish<Fv>(la.hi, width, b.r[3].hi, lb_R4) : false;
@@ -1264,10 +1513,12 @@ CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr) {
     }
     uint32_t m = ok ? (1u << 2) : 0u;
     if (trapped != TRAP_NONE) m |= 1u << 31;
+    else if (ok && certify && !cover_certificate(b, width)) *repair = true;
     return m;
 }
 
-CC_FN_INL uint32_t gaps_pass_box(const Box& b, const EncBox* enc = nullptr) {
+CC_FN_INL uint32_t gaps_pass_box(const Box& b, const EncBox* enc = nullptr, bool certify = false,
+                                 bool* repair = nullptr) {
     using f32::Fv;
     trap_clear();
     Box v = b;
@@ -1303,7 +1554,11 @@ CC_FN_INL uint32_t gaps_pass_box(const Box& b, const EncBox* enc = nullptr) {
     };
     int decided;
     const double gap = gaps_width_early(v.r[0].lo, v.r[1].lo, v.r[3].lo, g, finish, &decided);
-    if (decided != f32::UNKNOWN) return decided == f32::YES ? (1u << 5) : 0u;
+    if (decided != f32::UNKNOWN) {
+        if (decided != f32::YES) return 0u;
+        if (certify && !gaps_certificate(b, gap)) *repair = true;
+        return 1u << 5;
+    }
     uint32_t trapped = trap_status();
     trap_clear();
     bool ok = R_ok ? gaps_finish_t<Fv>(b.la.hi, g.w1, g.w2, gap, v.r[3].hi, R.lo, R.hi) : false;
@@ -1316,6 +1571,7 @@ CC_FN_INL uint32_t gaps_pass_box(const Box& b, const EncBox* enc = nullptr) {
     }
     uint32_t m = ok ? (1u << 5) : 0u;
     if (trapped != TRAP_NONE) m |= 1u << 31;
+    else if (ok && certify && !gaps_certificate(b, gap)) *repair = true;
     return m;
 }
 #endif

@@ -99,6 +99,10 @@ struct Counters {
     unsigned long long digest;
     unsigned long long counts[4][8];
     unsigned long long n_leaf2;  // leaves waiting for the 2x2 criterion (split stage 4a)
+    // leaf criteria evaluated FP32-first (tight::first_f32), by outcome:
+    // FP64 evaluation, FP32 "false", FP32 "true" certified in FP64,
+    // certification failed
+    unsigned long long fp32[4];
 };
 
 struct Leaf2 {  // a leaf that needs the 2x2 criterion
@@ -180,6 +184,25 @@ __device__ __forceinline__ unsigned long long warp_append(unsigned long long* co
     }
     return slot;
 }
+
+// per-thread tally of first_f32 outcomes, summed over the warp and added to
+// the counters once per warp at the end of a stage kernel (every lane of the
+// block reaches it)
+struct F32Tally {
+    unsigned n[4] = {0, 0, 0, 0};
+    __device__ __forceinline__ void note(int how) {
+        if (how >= 0) n[how] += 1;
+    }
+    __device__ __forceinline__ void flush(Counters* c) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            unsigned v = n[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31) == 0 && v) atomicAdd(&c->fp32[k], (unsigned long long)v);
+        }
+    }
+};
 
 // warp-uniform grid-stride loop over [0, total): all 32 lanes enter every
 // iteration (lanes past the end with valid = false), so warp collectives are safe
@@ -396,6 +419,7 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
     trace_init(bt);
     const unsigned long long total = (cell_hi - cell_lo) * s4;
     unsigned long long evals = 0;
+    F32Tally tally;
     CC_WARP_LOOP(total) {
         unsigned long long idx = base_ + (threadIdx.x & 31);
         bool valid = idx < total;
@@ -429,7 +453,9 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
                 } else if (Split) {
                     outcome = -3;  // on to stage 4a2
                     if (p.order) {  // learned order: the cheap leaf criterion first
-                        const bool ok4 = tight::r1_r2_r3_leaf_first_f32(v, p.R4);
+                        int how = -1;
+                        const bool ok4 = tight::r1_r2_r3_leaf_first_f32(v, p.R4, &how);
+                        tally.note(how);
                         if (ok4 && trap_status() == TRAP_NONE) outcome = CC_T_L4_R123LEAF;
                         else if (!ok4) leaf_tried = true;  // (a trap leaves it to the plain order)
                     }
@@ -455,6 +481,7 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
     }
     for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
     if ((threadIdx.x & 31) == 0 && evals) atomicAdd(&c->leaf_evals, evals);
+    if (Split) tally.flush(c);
     trace_flush(bt, c, 3);
 }
 
@@ -467,6 +494,7 @@ __global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks
     trace_init(bt);
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_leaf2;
     const unsigned long long total = n_in < caps.leaf2 ? n_in : caps.leaf2;
+    F32Tally tally;
     CC_WARP_LOOP(total) {
         unsigned long long idx = base_ + (threadIdx.x & 31);
         bool valid = idx < total;
@@ -486,7 +514,9 @@ __global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks
             Box v = leaf_box(p, tk.la, lf.r4);
             Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
             tighten_lb(R, 0.0);
-            bool ok = tight::two_by_two_first_f32(v, R);
+            int how = -1;
+            bool ok = tight::two_by_two_first_f32(v, R, &how);
+            tally.note(how);
             trapped = (lf.pad & 1) != 0 || trap_status() != TRAP_NONE;
             outcome = (ok && !trapped) ? CC_T_L4_2X2 : -2;
         }
@@ -497,6 +527,7 @@ __global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks
         unsigned long long slot = warp_append(&c->n_leaf, valid && outcome == -2, caps.leaf, &c->overflow);
         if (slot != ~0ULL) out[slot] = Leaf{lf.cell4, lf.i4, (uint16_t)((trapped ? 1 : 0) | (lf.pad & 2))};
     }
+    tally.flush(c);
     trace_flush(bt, c, 3);
 }
 
@@ -517,6 +548,7 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
     trace_init(bt);
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_leaf;
     const unsigned long long total = n_in < caps.leaf ? n_in : caps.leaf;
+    F32Tally tally;
     CC_WARP_LOOP(total) {
         unsigned long long idx = base_ + (threadIdx.x & 31);
         bool valid = idx < total;
@@ -541,8 +573,9 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
             Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
             tighten_lb(R, 0.0);
             tight::GapsStart g;
+            int how = -1;
             if (!(lf.trapped & 2) &&
-                (F32 ? tight::r1_r2_r3_leaf_first_f32(v, p.R4) : tight::r1_r2_r3_strategies(v, p.R4))) {
+                (F32 ? tight::r1_r2_r3_leaf_first_f32(v, p.R4, &how) : tight::r1_r2_r3_strategies(v, p.R4))) {
                 outcome = CC_T_L4_R123LEAF;
             } else if (tight::gaps_enters(v.r[0].lo, v.r[1].lo, g)) {
                 need_gaps = true;
@@ -552,6 +585,7 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
             } else {
                 outcome = CC_T_L4_CRITICAL;
             }
+            tally.note(how);
             trapped = trap_status() != TRAP_NONE;
             gl.trapped = trapped ? 1 : 0;
             if (trapped && !need_gaps) outcome = CC_T_L4_TRAPPED;
@@ -565,6 +599,7 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
         bool keep = decided && (outcome == CC_T_L4_CRITICAL || outcome == CC_T_L4_TRAPPED);
         push_critical(crit, warp_append(&c->n_crit, keep, caps.crit, &c->overflow), v, task, trapped);
     }
+    if (F32) tally.flush(c);
     trace_flush(bt, c, 3);
 }
 

@@ -139,6 +139,18 @@ typedef struct cc_prove_stats {
     int32_t reserved;
     double seconds;            /* wall time of the call */
     uint64_t kernel_launches;  /* kernels launched by the call */
+    /* Leaf criteria evaluated FP32-first (the prepared form's 2x2 and leaf
+     * r1_r2_r3 criteria), by outcome: [0] FP32 undecided, evaluated in FP64;
+     * [1] FP32 "false"; [2] FP32 "true", certified in FP64 (the criterion's
+     * FP64 code with only the settling can_recurse call evaluated); [3]
+     * certification failed, the FP64 result used.  Generations run by this
+     * call only (a resumed proof counts from the checkpoint on). */
+    uint64_t fp32_first[4];
+    /* FP64 certifications that failed during the call (leaf criteria and the
+     * bisections' results; expected 0): the FP64 result was used instead.
+     * Counted per device for the library's tight kernels, so calls running
+     * at the same time on other handles of the device add theirs. */
+    uint64_t cert_failures;
 } cc_prove_stats;
 
 /* ---- size-bound proof ------------------------------------------------------
@@ -246,21 +258,30 @@ int cc_tight_eval_device(cc_handle* h, const double* soa, size_t n, uint32_t* ma
  * latency-critical loop in which cudaMalloc's implicit synchronisation is not
  * acceptable, a process that reserves all memory at start-up -- and so cannot
  * create a handle either.  Same inputs, outputs and results as
- * cc_tight_eval_device; it works on the calling thread's current device and
- * launches on `stream` (a cudaStream_t; NULL = the legacy default stream)
- * without synchronising.
+ * cc_tight_eval_device (FP64 certification included); it works on the
+ * calling thread's current device and launches on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream) without synchronising.
  *   - Its scratch is a fixed array inside the library image,
- *     CC_STATIC_EVAL_SCRATCH_BYTES per GPU, held until the process exits;
+ *     CC_STATIC_EVAL_SCRATCH_BYTES per GPU (about 2.3 MiB: the queues of the
+ *     evaluation passes, 37 bytes per box), held until the process exits;
  *     batches of more than CC_STATIC_EVAL_MAX_BOXES boxes are rejected with
  *     CC_ERR_TOO_LARGE (split larger batches into several calls).
- *   - The first call on a device looks up that array's device address; make
- *     that first call before any stream capture.
- *   - All calls on a device share the array: calls that can overlap on the
- *     GPU (different streams, or other threads) race and give wrong masks;
- *     serialise them (one stream, or events).
- *   - It calls no cudaMalloc, cudaFree or allocating library routine. */
+ *   - Set-up: the first call on a device looks up that array's device
+ *     address, and the first launch of each of its kernels may make the CUDA
+ *     driver load the library's module (lazy module loading), which can
+ *     allocate and synchronise.  Make one warm-up call (n = 1 will do) on
+ *     each device at start-up, before any stream capture and before the part
+ *     of the program that must not allocate; later calls then allocate
+ *     nothing.
+ *   - All calls on a device share the array, which keeps the last call's
+ *     queues (each call clears the counters it needs): calls that can
+ *     overlap on the GPU (different streams, or other threads) race and give
+ *     wrong masks; serialise them (one stream, or events).
+ *   - It calls no cudaMalloc, cudaFree or allocating library routine.
+ *   - A CUDA error already pending when it is called is left as it is and
+ *     reported as CC_ERR_CUDA without launching anything. */
 #define CC_STATIC_EVAL_MAX_BOXES 65536
-#define CC_STATIC_EVAL_SCRATCH_BYTES (256 + 65536 * 128) /* 8 MiB + 256 bytes */
+#define CC_STATIC_EVAL_SCRATCH_BYTES (256 + 65536 * 37) /* 2,425,088 bytes */
 int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t* masks, void* stream);
 
 /* Evaluate the size-bound criteria on n boxes in HOST memory (AoS, 112-byte
@@ -292,18 +313,28 @@ int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint32_t* masks,
 
 /* Per-stage device timing (no reference counterpart; a measurement aid).
  * While enabled, cc_tight_eval_device records a CUDA event around each of
- * its four kernels on the stream it launches on:
+ * its six passes on the stream it launches on:
  *   stage 0 = k_eval_f32   (all criteria on FP32 enclosures of the FP64
  *                           values, one kernel per criterion group, and
  *                           k_eval_collect, which queues the boxes they could
- *                           not decide and the bisection jobs),
+ *                           not decide, the bisection jobs and the FP32
+ *                           verdicts to certify),
  *   stage 1 = k_eval_main  (the FP64 criteria on the queued boxes),
- *   stage 2 = k_eval_cover (strip-width bisection of the compacted queue),
- *   stage 3 = k_eval_gaps  (gap-width bisection of the compacted queue).
+ *   stage 2 = k_eval_cover (strip-width bisection of the compacted queue,
+ *                           with the FP64 certificate of a true result),
+ *   stage 3 = k_eval_gaps  (gap-width bisection of the compacted queue,
+ *                           with the FP64 certificate of a true result),
+ *   stage 4 = k_eval_cert  (FP64 certification of every verdict bit the FP32
+ *                           pass decided "true", one kernel per criterion
+ *                           group on its compacted queue),
+ *   stage 5 = k_eval_repair (the boxes whose certification failed, evaluated
+ *                           again in FP64 alone; expected to be none).
  * cc_last_stage_times waits for the last recorded event and writes the
  * elapsed milliseconds of each stage of the most recent call (at most
  * max_stages values; *n_stages = how many were written). */
-#define CC_EVAL_STAGES 4
+#define CC_EVAL_STAGES 6
+/* the first four stages are the ones cc_autotune_eval tunes */
+#define CC_EVAL_TUNED_STAGES 4
 int cc_set_stage_timing(cc_handle* h, int enable);
 /* CUDA graph of the evaluation's launch sequence (on by default; no
  * reference counterpart): cc_tight_eval_device captures its launches once
@@ -322,6 +353,31 @@ int cc_last_stage_times(cc_handle* h, float* ms, int max_stages, int* n_stages);
  * counts[3] nonzero if a queue overflowed (cannot happen: each queue holds
  * the whole batch). */
 int cc_last_eval_counts(cc_handle* h, unsigned long long* counts);
+
+/* FP64 certification of the evaluation (no reference counterpart).  The FP32
+ * pass decides most verdict bits on outward-rounded FP32 enclosures of the
+ * FP64 values.  With certification on (the default), every bit it decides
+ * "true" -- a criterion certifies the box, or R / R4 is empty -- is checked
+ * again in FP64 directed rounding before it is reported: the criterion's
+ * FP64 code runs with only the can_recurse call that settled the FP32 run
+ * evaluated (every other call answers "false", which can only make the
+ * criterion false), the three-strips placement and the emptiness test run
+ * in full, and a bisection's result is checked as the reference's own
+ * argument (the width used is realizable in FP64 and the rest of the
+ * rectangle recursively coverable in FP64).  A bit whose certification fails
+ * sends its box through the FP64 evaluation alone, whose mask is reported.
+ * Bits decided "false" are not re-checked: a false bit can only keep a box,
+ * never discard one.  cc_set_eval_certify(h, 0) is the uncertified FP32
+ * form (opt-in, for measurement). */
+int cc_set_eval_certify(cc_handle* h, int enable);
+/* Certification counts of the most recent evaluation batch (waits for the
+ * device), CC_EVAL_CERT_COUNTS values: [0..4] FP32 "true" verdicts certified
+ * per criterion group (r1 bit 0, r1_r2 bit 1, 2x2 bit 3, leaf r1_r2_r3 bit 4,
+ * and boxes with the three-strips bit 2 or the emptiness bit 6), [5] boxes
+ * whose certification failed and were evaluated in FP64 alone, [6] true
+ * strip-width results certified, [7] true gap-width results certified. */
+#define CC_EVAL_CERT_COUNTS 8
+int cc_last_eval_cert(cc_handle* h, unsigned long long* counts);
 
 /* Run the tight proof from `root` with split counts `grid`.  On success
  * *criticals points to *n_crit boxes (release with cc_free), in the order the
@@ -485,9 +541,25 @@ int cc_selftest_bisection_f32(cc_handle* h, int which, const double* args, size_
  * where the bisection reached its iteration cap. */
 int cc_selftest_bisection_width(cc_handle* h, int which, const double* args, size_t n, double* out,
                                 int8_t* trapped);
+/* The FP64 certification run of a tight criterion group (0 r1_strategies,
+ * 1 r1_r2_strategies, 2 two_by_two_strategies, 3 the leaf form of
+ * r1_r2_r3_strategies) on n boxes in host memory, at the arguments of
+ * cc_tight_eval, each with its own call number call[i]: 1-based number of
+ * the one can_recurse call evaluated (every other call answers "false"), 0
+ * for none, -1 for all (the plain FP64 criterion).  out[i] = 1 if the
+ * criterion holds without reaching a trap site. */
+int cc_selftest_certify(cc_handle* h, int group, const cc_tight_box* boxes, const int* call, size_t n,
+                        uint8_t* out);
 /* Measured FP64 instruction throughput of the device (ops/s; one FP64
  * instruction = one op): chains of directed-rounding add/mul, or of FMA. */
 int cc_selftest_fp64_peak(cc_handle* h, int use_fma, double* ops_per_s);
+/* Measured instruction throughput of the device in thread instructions per
+ * second, the roofline denominators of the evaluation's passes: kind 0 FP64
+ * directed add/mul, 1 FP64 FMA, 2 FP32 directed add/mul, 3 FP32 FMA (an FP32
+ * FMA warp instruction issues every cycle on each SM sub-partition, so kind
+ * 3 / 32 is the warp-instruction issue rate).  Independent chains, 8 per
+ * thread, 8 blocks of 256 threads per SM; best of three timed launches. */
+int cc_selftest_peak(cc_handle* h, int kind, double* ops_per_s);
 
 #ifdef __cplusplus
 }

@@ -9,7 +9,11 @@ Builds the CPU oracle libraries:
   for the host (``oracle/ref/Makefile``); built only where the reference
   sources are present.
 
-Run ``python oracle/build.py [--ref PATH]``.
+Run ``python oracle/build.py [--ref PATH]``.  The reference's ``Prover/``
+directory is taken from ``--ref``, else from the environment variable
+``CC_REFERENCE_PROVER``, else from a checkout of the reference beside this
+repository (``<repo>/../reference/Prover``); without one, only the port is
+built.
 """
 import argparse
 import os
@@ -20,7 +24,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference/Prover"
 
 PORT_FLAGS = [
     "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread",
@@ -65,11 +68,18 @@ def build_port(force=False):
     return outs
 
 
+def reference_dir():
+    """The reference's Prover/ directory when the reference is checked out
+    beside this repository, else None."""
+    d = os.path.normpath(os.path.join(ROOT, os.pardir, "reference", "Prover"))
+    return d if os.path.isdir(d) else None
+
+
 def build_ref(ref=None, force=False):
     """Build the reference criteria library; returns its path or None if the
     reference sources are not available here."""
-    ref = ref or os.environ.get("CC_REFERENCE_PROVER", DEFAULT_REF)
-    if not os.path.isdir(ref):
+    ref = ref or os.environ.get("CC_REFERENCE_PROVER") or reference_dir()
+    if not ref or not os.path.isdir(ref):
         return None
     cmd = ["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + ref, "-j%d" % (os.cpu_count() or 4)]
     if force:

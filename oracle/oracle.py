@@ -55,6 +55,8 @@ class CcProveStats(ctypes.Structure):
         ("reserved", ctypes.c_int32),
         ("seconds", ctypes.c_double),
         ("kernel_launches", ctypes.c_uint64),
+        ("fp32_first", ctypes.c_uint64 * 4),
+        ("cert_failures", ctypes.c_uint64),
     ]
 
 
@@ -165,7 +167,29 @@ class _Lib:
         return arr, fl, sb_stats_to_dict(st)
 
 
-class Ref(_Lib):
+class _Generation:
+    def tight_generation(self, parents, la_splits, r_splits, lo=0, hi=(1 << 64) - 1, threads=4):
+        """One generation over the tasks [lo, hi) on the CPU: (criticals in
+        task order, stats)."""
+        parents = np.ascontiguousarray(parents, dtype=TIGHT_BOX)
+        rs = (ctypes.c_int * 4)(*r_splits)
+        out = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcProveStats()
+        f = getattr(self.lib, self.prefix + "_tight_generation")
+        f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                      ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t),
+                      ctypes.POINTER(CcProveStats)]
+        f(parents.ctypes.data if len(parents) else None, len(parents), la_splits, rs, lo, hi, threads,
+          ctypes.byref(out), ctypes.byref(n), ctypes.byref(st))
+        arr = np.zeros(n.value, dtype=TIGHT_BOX)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)
+        getattr(self.lib, self.prefix + "_free")(out)
+        return arr, stats_to_dict(st)
+
+
+class Ref(_Generation, _Lib):
     """The reference's own criteria code, built for the host."""
     prefix = "ccref"
 
@@ -175,7 +199,7 @@ class Ref(_Lib):
         self.lib.ccref_tight_critical_ratio.restype = ctypes.c_double
 
 
-class Port(_Lib):
+class Port(_Generation, _Lib):
     """The prover's criteria compiled for the host (restatement)."""
     prefix = "ccport"
 
@@ -186,25 +210,6 @@ class Port(_Lib):
                                           ctypes.c_void_p, ctypes.c_size_t]
         self.lib.ccport_subinterval.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_double)]
-
-    def tight_generation(self, parents, la_splits, r_splits, lo=0, hi=(1 << 64) - 1, threads=4):
-        """One generation over the tasks [lo, hi) on the CPU (sharding tests)."""
-        parents = np.ascontiguousarray(parents, dtype=TIGHT_BOX)
-        rs = (ctypes.c_int * 4)(*r_splits)
-        out = ctypes.c_void_p()
-        n = ctypes.c_size_t()
-        st = CcProveStats()
-        f = self.lib.ccport_tight_generation
-        f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
-                      ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t),
-                      ctypes.POINTER(CcProveStats)]
-        f(parents.ctypes.data if len(parents) else None, len(parents), la_splits, rs, lo, hi, threads,
-          ctypes.byref(out), ctypes.byref(n), ctypes.byref(st))
-        arr = np.zeros(n.value, dtype=TIGHT_BOX)
-        if n.value:
-            ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)
-        self.lib.ccport_free(out)
-        return arr, stats_to_dict(st)
 
     def tight_eval_passes(self, boxes):
         """Per-box operation counts of the three evaluation passes (main,

@@ -228,6 +228,38 @@ int ccref_tight_prove(const cc_tight_box* root, const cc_tight_grid* grid, int t
     return 0;
 }
 
+/* One generation of the restated driver over the tasks [lo, hi) (task =
+ * parent index * la_splits + lambda piece), on the reference's own criteria:
+ * the task-range oracle of the full proof's generations.  Criticals in task
+ * order, merged per task; stats as ccref_tight_prove (gen_sizes[0] = count). */
+int ccref_tight_generation(const cc_tight_box* parents, size_t n, int la_splits, const int* splits, uint64_t lo,
+                           uint64_t hi, int threads, cc_tight_box** out, size_t* n_out, cc_prove_stats* stats) {
+    std::vector<Driver::Box> in(n);
+    for (size_t i = 0; i < n; ++i)
+        in[i] = Driver::Box{to_iv(parents[i].la), {to_iv(parents[i].r[0]), to_iv(parents[i].r[1]),
+                                                   to_iv(parents[i].r[2]), to_iv(parents[i].r[3])}};
+    std::vector<Driver::Box> res;
+    cc_oracle::Trace tr;
+    tr.clear();
+    uint64_t trapped = 0;
+    Driver::generation(in, la_splits, splits, threads, res, tr, trapped, lo, hi);
+    *n_out = res.size();
+    *out = (cc_tight_box*)std::malloc(sizeof(cc_tight_box) * (res.size() + 1));
+    for (size_t i = 0; i < res.size(); ++i) {
+        (*out)[i].la = from_iv(res[i].la);
+        for (int k = 0; k < 4; ++k) (*out)[i].r[k] = from_iv(res[i].r[k]);
+    }
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        std::memcpy(stats->counts, tr.counts, sizeof(stats->counts));
+        stats->digest = tr.digest;
+        stats->leaf_evals = tr.leaf_evals;
+        stats->trapped_leaves = trapped;
+        stats->gen_sizes[0] = res.size();
+    }
+    return 0;
+}
+
 void ccref_free(void* p) { std::free(p); }
 
 /* single criteria, for targeted tests */

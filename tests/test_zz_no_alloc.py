@@ -1,14 +1,18 @@
 """GPU test of cc_tight_eval_device_static, the allocation-free entry point.
 
-It serves callers that cannot allocate device memory while they run (a host
-framework that owns all device memory, latency-critical loops, processes that
-reserve everything at start-up): instead of handle-owned queues it works in a
-fixed array compiled into the library.  The test calls it through the C ABI
-twice in a row on different batches -- the second call reuses the array the
-first one filled -- and checks both outputs bit for bit against
-cc_tight_eval_device, the entry point with handle-owned buffers.  The device
-buffers below are the caller's (made with torch); the entry point itself
-allocates nothing.
+It serves callers that cannot allocate device memory while they run: a host
+framework that owns all device memory and hands out its own buffers, a
+latency-critical loop in which cudaMalloc's implicit synchronisation would
+stall the device, a process that reserves everything at start-up.  Instead of
+handle-owned queues it works in a fixed array compiled into the library.
+
+The test calls it through the C ABI twice in a row on different batches --
+the second call reuses the array the first one filled -- and checks both
+outputs bit for bit against cc_tight_eval_device (the entry point with
+handle-owned buffers) and against the CPU oracle's masks.  After a warm-up
+call it checks that a call leaves the device's free memory unchanged, and it
+runs one call on a non-default stream.  The device buffers below are the
+caller's (made with torch); the entry point itself allocates nothing.
 
 Kept in a file of its own that pytest collects last.
 """
@@ -40,7 +44,7 @@ def _device_batch(boxes):
     return soa, masks
 
 
-def _reference_masks(boxes):
+def _device_entry_masks(boxes):
     """Masks from the existing device entry point (handle-owned scratch)."""
     import torch
     import circlecover_gb300 as cg
@@ -50,6 +54,12 @@ def _reference_masks(boxes):
         p.tight_eval_device(soa.data_ptr(), len(boxes), masks.data_ptr())
         torch.cuda.synchronize()
         return masks.cpu().numpy().view(np.uint32)
+
+
+def _oracle_masks(boxes):
+    from oracle import oracle as O
+    O.ensure_built()
+    return O.Port().tight_eval(boxes, threads=16)
 
 
 def test_static_entry_point_matches_device_entry_point_twice():
@@ -67,8 +77,33 @@ def test_static_entry_point_matches_device_entry_point_twice():
         torch.cuda.synchronize()
         outs.append(masks.cpu().numpy().view(np.uint32).copy())
     for boxes, got in zip(batches, outs):
-        want = _reference_masks(boxes)
-        assert np.array_equal(got, want)
+        assert np.array_equal(got, _device_entry_masks(boxes))
+        assert np.array_equal(got, _oracle_masks(boxes))
+
+
+def test_static_entry_point_allocates_nothing_and_runs_on_a_stream():
+    import torch
+    lib = _lib()
+    boxes = W.tight_microbench(30000, seed=74)
+    soa, masks = _device_batch(boxes)
+    warm_soa, warm_masks = _device_batch(boxes[:1])
+    # the caller's stream, made (like every buffer above) before the part of
+    # the program that must not allocate
+    stream = torch.cuda.Stream()
+    assert stream.cuda_stream != 0
+    torch.cuda.synchronize()
+    # warm-up on that stream: the one-time set-up and the loading of the kernels
+    assert lib.cc_tight_eval_device_static(warm_soa.data_ptr(), 1, warm_masks.data_ptr(),
+                                           ctypes.c_void_p(stream.cuda_stream)) == 0
+    stream.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    rc = lib.cc_tight_eval_device_static(soa.data_ptr(), len(boxes), masks.data_ptr(),
+                                         ctypes.c_void_p(stream.cuda_stream))
+    assert rc == 0
+    stream.synchronize()
+    free_after = torch.cuda.mem_get_info()[0]
+    assert free_after == free_before, (free_before, free_after)
+    assert np.array_equal(masks.cpu().numpy().view(np.uint32), _oracle_masks(boxes))
 
 
 def test_static_entry_point_rejects_oversized_batch():
