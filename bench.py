@@ -189,8 +189,63 @@ def cpu_baseline(n_sample, seed=1):
     t0 = time.perf_counter()
     impl.tight_eval(boxes, threads=cores)
     dt = time.perf_counter() - t0
+    # one core on a sixteenth of the sample
+    n1 = max(4096, n_sample // 16)
+    t0 = time.perf_counter()
+    impl.tight_eval(boxes[:n1], threads=1)
+    dt1 = time.perf_counter() - t0
     return {"value": n_sample / dt, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": "first %d boxes of the 2^24-box microbench (seed 1), %d threads, %.2f s" % (n_sample, cores, dt)}
+            "sample": "first %d boxes of the 2^24-box microbench (seed 1), %d threads, %.2f s" % (n_sample, cores, dt),
+            "single_core": {"value": n1 / dt1, "unit": UNIT, "cores": 1,
+                            "sample": "first %d boxes, 1 thread, %.2f s" % (n1, dt1)}}
+
+
+def cpu_variants(n_sample=1 << 16, seed=1):
+    """The CPU implementations side by side on the first n_sample boxes of the
+    microbench: the reference's own criteria built for the host with the
+    error-free-transform rounding layer and with fesetround (where the
+    reference sources are present), and the oracle's port of them, each on
+    one thread and on all host threads (boxes/s; masks checked equal)."""
+    import ctypes
+    from circlecover_gb300 import workloads as W
+    from oracle import oracle as O
+    from oracle import build as OB
+    O.ensure_built()
+    cores = os.cpu_count() or 1
+    boxes = W.tight_microbench(n_sample, seed=seed)
+    impls = [("port", O.Port())]
+    if O.ref_available():
+        impls.insert(0, ("reference_eft", O.Ref()))
+        fe = OB.build_ref_fenv()
+        if fe:
+            impls.insert(1, ("reference_fesetround", O.Ref(fe)))
+    out = {"boxes": n_sample, "cores": cores, "cpu": _cpu_model(), "results": {}}
+    want = None
+    for name, impl in impls:
+        row = {}
+        for threads in (1, cores):
+            sample = boxes if threads > 1 else boxes[: max(1024, n_sample // 8)]
+            impl.tight_eval(sample[:1024], threads=threads)
+            t0 = time.perf_counter()
+            m = impl.tight_eval(sample, threads=threads)
+            dt = time.perf_counter() - t0
+            row["threads_%d" % threads] = len(sample) / dt
+            if threads > 1:
+                if want is None:
+                    want = m
+                row["masks_equal"] = bool(np.array_equal(m, want))
+        out["results"][name] = row
+    return out
+
+
+def _cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
 
 
 def run_reference(args, ws, rank):
@@ -515,7 +570,10 @@ def sb_proof_run(prover, warm=True):
             "fp32_prefilter": {"decided_empty": st["fp32_decided"],
                                "decided_share": st["fp32_decided"] / max(1, st["leaf_evals"]),
                                "widening_R_mean": st["widening_mean"], "widening_R_max": st["widening_max"],
-                               "widening_samples": st["widening_samples"]}}
+                               "widening_samples": st["widening_samples"]},
+            "certification": {"fp32_true_certified": st["fp32_certified"],
+                              "empty_anchors_certified": st["empty_anchors"],
+                              "failures": st["cert_failures"]}}
 
 
 def sb_forms(prover):
@@ -555,9 +613,12 @@ def main():
     ap.add_argument("--no-proof", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="tight_eval",
-                    choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof", "config1"])
+                    choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof", "config1", "cpu_variants"])
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "cpu_variants":  # the CPU implementations side by side (no GPU)
+        print(json.dumps(cpu_variants(args.cpu_sample)), flush=True)
+        return
     if args.workload in ("tight_proof", "config1"):  # the tight proof forms alone
         import __graft_entry__
         __graft_entry__.build()

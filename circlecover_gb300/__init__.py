@@ -94,6 +94,17 @@ class CcTightSummary(ctypes.Structure):
     ]
 
 
+REFINE_MAX_DEPTH = 48
+
+
+class CcRefineStats(ctypes.Structure):
+    _fields_ = [("live", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("decided", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("ms", ctypes.c_float * (REFINE_MAX_DEPTH + 1)),
+                ("depths_run", ctypes.c_int32), ("stopped_at_cap", ctypes.c_int32),
+                ("seconds", ctypes.c_double), ("kernel_launches", ctypes.c_uint64)]
+
+
 class CcTuneResult(ctypes.Structure):
     _fields_ = [("min_blocks", ctypes.c_int * 4), ("blocks_per_sm", ctypes.c_int * 4), ("ms", ctypes.c_float * 4),
                 ("ms_default", ctypes.c_float * 4)]
@@ -133,6 +144,9 @@ class CcSbProveStats(ctypes.Structure):
         ("widening_samples", ctypes.c_uint64),
         ("widening_mean", ctypes.c_double),
         ("widening_max", ctypes.c_double),
+        ("fp32_certified", ctypes.c_uint64),
+        ("empty_anchors", ctypes.c_uint64),
+        ("cert_failures", ctypes.c_uint64),
     ]
 
 
@@ -200,7 +214,7 @@ EXPORTS = [
     "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
     "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume", "cc_last_eval_counts", "cc_set_eval_graph",
-    "cc_eval_graph_stats", "cc_set_eval_certify", "cc_last_eval_cert",
+    "cc_eval_graph_stats", "cc_set_eval_certify", "cc_last_eval_cert", "cc_tight_refine",
 ]
 
 MLP_PARAMS = 5319
@@ -495,6 +509,9 @@ class Prover:
         d["widening_samples"] = int(st.widening_samples)
         d["widening_mean"] = float(st.widening_mean)
         d["widening_max"] = float(st.widening_max)
+        d["fp32_certified"] = int(st.fp32_certified)
+        d["empty_anchors"] = int(st.empty_anchors)
+        d["cert_failures"] = int(st.cert_failures)
         return arr, fl, d
 
     # ---- learned strategy ordering (device pointers are raw ints, e.g.
@@ -538,6 +555,33 @@ class Prover:
         self._check(self.lib.cc_tight_first(self.h, ctypes.c_void_p(soa_ptr), n, 1 if learned else 0,
                                             ctypes.c_void_p(outcome_ptr),
                                             ctypes.c_void_p(evals_ptr) if evals_ptr else None), "cc_tight_first")
+
+    def tight_refine(self, boxes, max_depth, max_live=0):
+        """Adaptive refinement of host boxes (cc_tight_refine): (criticals,
+        flags, stats dict with per-depth live / decided counts and ms)."""
+        boxes = np.ascontiguousarray(boxes, dtype=TIGHT_BOX)
+        out = ctypes.c_void_p()
+        fl = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcRefineStats()
+        f = self.lib.cc_tight_refine
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t,
+                      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t),
+                      ctypes.POINTER(CcRefineStats)]
+        self._check(f(self.h, boxes.ctypes.data if len(boxes) else None, len(boxes), max_depth, max_live,
+                      ctypes.byref(out), ctypes.byref(fl), ctypes.byref(n), ctypes.byref(st)), "cc_tight_refine")
+        arr = np.zeros(n.value, dtype=TIGHT_BOX)
+        flags = np.zeros(n.value, dtype=np.uint32)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * TIGHT_BOX.itemsize)
+            ctypes.memmove(flags.ctypes.data, fl.value, n.value * 4)
+        self.lib.cc_free(out)
+        self.lib.cc_free(fl)
+        d = int(st.depths_run)
+        return arr, flags, {"live": [int(x) for x in st.live[:d]], "decided": [int(x) for x in st.decided[:d]],
+                            "ms": [float(x) for x in st.ms[:d]], "depths_run": d,
+                            "stopped_at_cap": bool(st.stopped_at_cap), "seconds": float(st.seconds),
+                            "kernel_launches": int(st.kernel_launches)}
 
     def tight_summary(self, criticals):
         """Max_distances of a critical set (cc_tight_summary), as the raw

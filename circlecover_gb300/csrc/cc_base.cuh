@@ -13,6 +13,8 @@
 #include <stdint.h>
 #include <math.h>
 
+#include <atomic>
+
 #if defined(__CUDACC__) && !defined(CC_HOST_PORT)
 #define CC_DEVICE_BUILD 1
 #define CC_FN __device__ __forceinline__
@@ -105,6 +107,14 @@ CC_FN void trap_clear() { cc_trap_words[threadIdx.x] = TRAP_NONE; }
 // can_recurse calls, the high byte is the number (1-based) of the one call a
 // certification run evaluates (0: none).
 static __shared__ uint16_t cc_cert_state[1024];
+// FP64 certifications that failed in this translation unit's kernels since
+// the library was loaded: an FP32 decision the FP64 check did not confirm
+// (the FP64 result is used instead).  Expected to stay 0; the host reads it
+// with cudaMemcpyFromSymbol.
+static __device__ unsigned long long cc_cert_fail_count;
+CC_FN void cert_failed() { atomicAdd(&cc_cert_fail_count, 1ULL); }
+// failures the host learnt of from a certification pass's counters
+static std::atomic<unsigned long long> cert_failures_host{0};
 #else
 // host build: per-thread status (initial-exec TLS: a plain load per access)
 #ifndef CC_HOST_TLS

@@ -380,9 +380,29 @@ __device__ __forceinline__ Fv clipped_root(Fv a) {
 // steps, so the cap cannot trap; true everywhere: the steps are replayed),
 // then for the leading steps while every converged lane of the warp has a
 // decision; from the first step some lane cannot decide, the FP64 predicate.
+// The result gets an FP64 certificate: a lower end that an FP32 decision
+// raised must pass the FP64 predicate, as every lower end of the
+// reference's bracket does (the initial one, or a midpoint the predicate
+// accepted).  If it does not, the bisection is redone on the FP64 predicate
+// alone (cert_failed).
+template <class Pred>
+__device__ __forceinline__ double bisect_fp64(double lo, double hi, const Pred& pred) {
+    for (int it = 0;; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) return lo;
+        if (it >= CC_BISECTION_CAP) {
+            trap(TRAP_BISECTION_CAP);
+            return lo;
+        }
+        if (pred(mid)) lo = mid;
+        else hi = mid;
+    }
+}
 template <class Dec, class Pred>
-__device__ __forceinline__ double bisect(double lo, double hi, const Dec& dec, const Pred& pred) {
+__device__ __forceinline__ double bisect_steps(double lo, double hi, const Dec& dec, const Pred& pred,
+                                               bool& lo_by_f32) {
     int it = 0;
+    lo_by_f32 = false;
     if (lo >= 0.0 && lo < hi && hi <= 1.7976931348623157e308) {
         const int whole = dec(hull(lo, hi));
         if (whole == NO) return lo;
@@ -395,6 +415,7 @@ __device__ __forceinline__ double bisect(double lo, double hi, const Dec& dec, c
                     return lo;
                 }
                 lo = mid;
+                lo_by_f32 = true;
             }
         }
     }
@@ -406,17 +427,38 @@ __device__ __forceinline__ double bisect(double lo, double hi, const Dec& dec, c
             trap(TRAP_BISECTION_CAP);
             return lo;
         }
-        bool ok;
+        bool ok, by_f32;
         const int d = f32_steps ? dec(of(mid)) : UNKNOWN;
         if (f32_steps && __all_sync(__activemask(), d != UNKNOWN)) {
             ok = d == YES;
+            by_f32 = true;
         } else {
             f32_steps = false;
             ok = pred(mid);
+            by_f32 = false;
         }
-        if (ok) lo = mid;
-        else hi = mid;
+        if (ok) {
+            lo = mid;
+            lo_by_f32 = by_f32;
+        } else {
+            hi = mid;
+        }
     }
+}
+template <class Dec, class Pred>
+__device__ __forceinline__ double bisect(double lo, double hi, const Dec& dec, const Pred& pred) {
+    const double lo0 = lo, hi0 = hi;
+    bool by_f32;
+    const double r = bisect_steps(lo, hi, dec, pred, by_f32);
+    if (!by_f32) return r;
+    const uint32_t saved = trap_status();
+    trap_clear();
+    const bool ok = pred(r) && trap_status() == TRAP_NONE;
+    trap_clear();
+    if (saved != TRAP_NONE) trap(saved);
+    if (ok) return r;
+    cert_failed();
+    return bisect_fp64(lo0, hi0, pred);
 }
 
 // The same bisection on FP32 decisions alone, for callers that can go on

@@ -228,32 +228,54 @@ __global__ void __launch_bounds__(128) k_eval_collect(size_t n, uint32_t* __rest
 // A record group's state byte names the call that settled the criterion
 // (bits 2-4, 1-based; 0: none); without record buffers every call is
 // evaluated.  Failures go to the repair queue.
+// Each block takes 128 consecutive jobs at a time and sorts them by the
+// call that settled the FP32 run (the three-strip group: by its bits) in
+// shared memory, so that a warp's lanes mostly certify the same call and
+// take the same path through the FP64 criterion.
 template <Layout L, int K>
 __global__ void __launch_bounds__(128) k_eval_cert(const double* __restrict__ in, size_t n, EvalQueues q) {
+    __shared__ uint32_t s_box[128];
+    __shared__ uint8_t s_key[128];
+    __shared__ int s_cnt[8];
     const unsigned long long c = q.counts[kCntCert + K];
     const unsigned long long nq = c < q.cap ? c : q.cap;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nq;
-         base += stride) {
-        const unsigned long long j = base + (threadIdx.x & 31);
-        const bool valid = j < nq;
-        bool fail = false;
+    // block-uniform loop: every thread of the block runs every iteration
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < nq; base += stride) {
+        if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
+        __syncthreads();
+        const unsigned long long j = base + threadIdx.x;
         uint32_t i = 0;
-        if (valid) {
+        int key = 7;  // past the end: sorted last
+        if (j < nq) {
             i = q.cert[K][j];
-            const ct::Box b = load_box<L>(in, n, i);
+            if (K < kRecGroups) key = q.states ? (int)((q.states[(size_t)K * n + i] >> 2) & 7) : 6;
+            else key = q.cflags[i] & 3;
+        }
+        const int rank = atomicAdd(&s_cnt[key], 1);
+        __syncthreads();
+        int off = rank;
+        for (int k = 0; k < key; ++k) off += s_cnt[k];
+        s_box[off] = i;
+        s_key[off] = (uint8_t)key;
+        __syncthreads();
+        const uint32_t b_i = s_box[threadIdx.x];
+        const int b_key = s_key[threadIdx.x];
+        const bool valid = b_key != 7;
+        bool fail = false;
+        if (valid) {
+            const ct::Box b = load_box<L>(in, n, b_i);
             if (K < kRecGroups) {
-                const int call = q.states ? (int)((q.states[(size_t)K * n + i] >> 2) & 7) : -1;
-                fail = !ct::certify_group<rec_group(K)>(b, call);
+                fail = !ct::certify_group<rec_group(K)>(b, q.states ? b_key : -1);
             } else {
-                const uint8_t f = q.cflags[i];
-                fail = !ct::certify_r123(b, ((f & 1) ? (1u << 2) : 0u) | ((f & 2) ? (1u << 6) : 0u));
+                fail = !ct::certify_r123(b, ((b_key & 1) ? (1u << 2) : 0u) | ((b_key & 2) ? (1u << 6) : 0u));
             }
         }
         __syncwarp();
         const unsigned long long s = cc::prove::warp_append(&q.counts[kCntRepair], valid && fail, q.cap,
                                                             &q.counts[kCntOverflow]);
-        if (s != ~0ULL) q.repair[s] = i;
+        if (s != ~0ULL) q.repair[s] = b_i;
+        __syncthreads();  // s_cnt and the sorted arrays are rewritten next iteration
     }
 }
 
@@ -1387,11 +1409,11 @@ struct GenTotals {
 // (cc_cert_fail_count; expected to stay 0)
 static unsigned long long cert_failures_so_far() {
     unsigned long long v = 0;
-    if (cudaMemcpyFromSymbol(&v, cc::tight::cc_cert_fail_count, sizeof(v)) != cudaSuccess) {
+    if (cudaMemcpyFromSymbol(&v, cc::cc_cert_fail_count, sizeof(v)) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
-    return v;
+    return v + cc::cert_failures_host.load();
 }
 
 int stage_grid(cc_handle* h) { return h->sm_count * 6; }
@@ -1472,6 +1494,10 @@ __global__ void k_cell_log(const Task* __restrict__ tasks, const Cell4* __restri
 }
 
 enum { S_CELL_FEAT = 32, S_CELL_LOGITS, S_CELL_LOG };
+constexpr int S_CERT = 27;  // FP32 "true" leaf verdicts awaiting their FP64 certification
+// run_chunk's answer when an FP64 certification failed: redo the chunk in the
+// plain form (FP64 criteria only)
+constexpr int kRedoPlain = 1000;
 
 // One chunk of parents [a, b) of a generation; returns CC_QUEUE_OVERFLOW
 // (without side effects on `out`/`tot`) when a device queue ran full.
@@ -1482,9 +1508,10 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
     const bool log_cells = hoist && (flags & CC_PROVE_LOG_CELLS);
     const size_t np = b - a;
     const size_t ntasks = np * (size_t)k;
-    void *d_par, *d_tasks, *d_c2, *d_c3, *d_c4, *d_leaf, *d_gaps, *d_crit, *d_cnt, *d_leaf2 = nullptr;
+    void *d_par, *d_tasks, *d_c2, *d_c3, *d_c4, *d_leaf, *d_gaps, *d_crit, *d_cnt, *d_leaf2 = nullptr, *d_cert = nullptr;
     int st;
     if (hoist && (st = ccrt::ensure(h, S_LEAF2, caps.leaf2 * sizeof(Leaf2), &d_leaf2))) return st;
+    if (hoist && (st = ccrt::ensure(h, S_CERT, caps.leaf * sizeof(CertLeaf), &d_cert))) return st;
     if ((st = ccrt::ensure(h, S_GAPS, caps.gaps * sizeof(GapsLeaf), &d_gaps))) return st;
     if ((st = ccrt::ensure(h, S_PARENTS, np * sizeof(cc_tight_box), &d_par))) return st;
     if ((st = ccrt::ensure(h, S_TASKS, ntasks * sizeof(Task), &d_tasks))) return st;
@@ -1573,27 +1600,35 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
         if (c0) {  // the previous slice's leaf queues are consumed
             CC_CUDA(h, cudaMemsetAsync(&cnt->n_leaf, 0, 2 * sizeof(unsigned long long), sm));  // n_leaf, n_gaps
             CC_CUDA(h, cudaMemsetAsync(&cnt->n_leaf2, 0, sizeof(unsigned long long), sm));
+            CC_CUDA(h, cudaMemsetAsync(&cnt->n_cert, 0, sizeof(unsigned long long), sm));
         }
         if (hoist) {
             k_stage4a<true, true><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], c0, c1,
-                                                     (Leaf*)d_leaf, (Leaf2*)d_leaf2, caps, cnt, task_base);
+                                                     (Leaf*)d_leaf, (Leaf2*)d_leaf2, caps, cnt, task_base,
+                                                     (CertLeaf*)d_cert);
             CC_LAUNCHED(h);
             k_stage4a2<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf2*)d_leaf2, (Leaf*)d_leaf,
-                                          caps, cnt, task_base);
+                                          caps, cnt, task_base, (CertLeaf*)d_cert);
             CC_LAUNCHED(h);
             k_stage4b<true><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3],
-                                               (GapsLeaf*)d_gaps, (Critical*)d_crit, caps, cnt, task_base);
+                                               (GapsLeaf*)d_gaps, (Critical*)d_crit, caps, cnt, task_base,
+                                               (CertLeaf*)d_cert);
         } else {
             k_stage4a<false, false><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, s[3], c0, c1,
-                                                       (Leaf*)d_leaf, nullptr, caps, cnt, task_base);
+                                                       (Leaf*)d_leaf, nullptr, caps, cnt, task_base, nullptr);
             CC_LAUNCHED(h);
             k_stage4b<false><<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const Leaf*)d_leaf, s[3],
-                                                (GapsLeaf*)d_gaps, (Critical*)d_crit, caps, cnt, task_base);
+                                                (GapsLeaf*)d_gaps, (Critical*)d_crit, caps, cnt, task_base, nullptr);
         }
         CC_LAUNCHED(h);
         k_stage4c<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const GapsLeaf*)d_gaps, s[3],
                                      (Critical*)d_crit, caps, cnt, task_base);
         CC_LAUNCHED(h);
+        if (hoist) {  // FP64 certification of the slice's FP32 "true" leaf verdicts
+            k_stage_cert<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const CertLeaf*)d_cert, s[3],
+                                            caps, cnt);
+            CC_LAUNCHED(h);
+        }
     }
     Counters hc;
     CC_CUDA(h, cudaMemcpyAsync(&hc, cnt, sizeof(Counters), cudaMemcpyDeviceToHost, sm));
@@ -1606,6 +1641,10 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
                              f(hc.n_gaps, caps.gaps), f(hc.n_crit, caps.crit), hoist ? f(hc.n_leaf2, caps.leaf2) : 0.0});
         if (demand) *demand = d;
         return CC_ERR_QUEUE_OVERFLOW;
+    }
+    if (hc.fp32[3]) {  // an FP32 "true" leaf verdict failed its FP64 certification
+        cc::cert_failures_host += hc.fp32[3];
+        return kRedoPlain;
     }
     std::vector<Critical> crit(hc.n_crit);
     if (hc.n_crit) {
@@ -1664,6 +1703,11 @@ int run_generation(cc_handle* h, const std::vector<cc_tight_box>& parents, int k
         GenTotals g;
         double demand = 0.0;
         int st = run_chunk(h, parents, a, b, k, s, cp, part, g, (unsigned long long)a * k, hoist, flags, t, e, &demand);
+        if (st == kRedoPlain) {  // the chunk again, FP64 criteria only: the reference's verdicts
+            part.clear();
+            g = GenTotals();
+            st = run_chunk(h, parents, a, b, k, s, cp, part, g, (unsigned long long)a * k, false, flags, t, e, &demand);
+        }
         if (st == CC_ERR_QUEUE_OVERFLOW) {
             if (e - t > 1) {
                 const double shrink = demand > 1.0 ? 1.25 * demand : 2.0;
@@ -1933,5 +1977,160 @@ extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, siz
     CC_LAUNCHED(h);
     CC_CUDA(h, cudaMemcpyAsync(out, d_out, sizeof(cc_tight_summary_t), cudaMemcpyDeviceToHost, h->stream));
     CC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CC_OK;
+}
+
+// ============================================================ refinement
+// Adaptive refinement of a set of tight boxes to a depth cap (no reference
+// counterpart; the near-critical stress workload).  Every level runs the
+// certified evaluation (the six criteria and the emptiness bits, passes 0-5)
+// on its boxes; k_refine_split then sorts them: certified or empty boxes are
+// done, trapped ones are kept as criticals, the others are bisected into the
+// next level -- or kept as criticals at the last level.  The boxes of a level
+// are independent and of uneven cost (the criteria's branches and
+// bisections), so each level is one batch of the evaluation passes over
+// compacted queues.
+namespace {
+
+enum { S_REF_A = 28, S_REF_B = 29, S_REF_MASKS = 30, S_REF_CRIT = 31 };
+
+struct RefineCounters {
+    unsigned long long n_next, n_crit, n_decided, overflow;
+};
+
+__device__ __forceinline__ void bisect_dim(const cc_tight_box& b, int dim, cc_tight_box& lo_half, cc_tight_box& hi_half) {
+    lo_half = b;
+    hi_half = b;
+    const cc_iv& v = dim == 0 ? b.la : b.r[dim - 1];
+    // 0.5 lo + 0.5 hi: no overflow; the halves' union is the interval
+    const double mid = 0.5 * v.lb + 0.5 * v.ub;
+    cc_iv& l = dim == 0 ? lo_half.la : lo_half.r[dim - 1];
+    cc_iv& u = dim == 0 ? hi_half.la : hi_half.r[dim - 1];
+    l.ub = mid;
+    u.lb = mid;
+}
+
+__global__ void __launch_bounds__(128) k_refine_split(const cc_tight_box* __restrict__ in, size_t n,
+                                                      const uint32_t* __restrict__ masks, int depth, int last,
+                                                      cc_tight_box* __restrict__ out, unsigned long long out_pairs,
+                                                      cc_tight_box* __restrict__ crit, uint32_t* __restrict__ crit_flags,
+                                                      unsigned long long crit_cap, RefineCounters* c) {
+    unsigned decided_n = 0;
+    const int dim = depth % 5;
+    CC_WARP_LOOP(n) {
+        const unsigned long long i = base_ + (threadIdx.x & 31);
+        const bool valid = i < n;
+        bool split = false, keep = false;
+        uint32_t flag = 0;
+        cc_tight_box b{};
+        if (valid) {
+            const uint32_t m = masks[i];
+            const bool trapped = (m >> 31) != 0;
+            const bool decided = !trapped && (m & 0x7Fu) != 0;
+            decided_n += decided ? 1u : 0u;
+            b = in[i];
+            split = !trapped && !decided && !last;
+            keep = trapped || (!decided && last);
+            flag = trapped ? 1u : 2u;
+        }
+        unsigned long long s = cc::prove::warp_append(&c->n_next, split, out_pairs, &c->overflow);
+        if (s != ~0ULL) bisect_dim(b, dim, out[2 * s], out[2 * s + 1]);
+        s = cc::prove::warp_append(&c->n_crit, keep, crit_cap, &c->overflow);
+        if (s != ~0ULL) {
+            crit[s] = b;
+            crit_flags[s] = flag;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) decided_n += __shfl_xor_sync(0xffffffffu, decided_n, o);
+    if ((threadIdx.x & 31) == 0 && decided_n) atomicAdd(&c->n_decided, (unsigned long long)decided_n);
+}
+
+}  // namespace
+
+extern "C" int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n, int max_depth, size_t max_live,
+                               cc_tight_box** criticals, uint32_t** flags, size_t* n_crit, cc_refine_stats* stats) {
+    if (!h || (n && !boxes) || !criticals || !n_crit || max_depth < 0 || max_depth > CC_REFINE_MAX_DEPTH)
+        return CC_ERR_PARAM;
+    *criticals = nullptr;
+    if (flags) *flags = nullptr;
+    *n_crit = 0;
+    CC_CUDA(h, cudaSetDevice(h->device));
+    h->launches = 0;
+    h->interrupt.store(0);
+    const auto t0 = std::chrono::steady_clock::now();
+    if (max_live < 2) max_live = (size_t)1 << 26;
+    cc_refine_stats st{};
+    cudaStream_t s = h->stream;
+    void *a, *cnt_p;
+    int rc;
+    if ((rc = ccrt::ensure(h, S_REF_A, std::max<size_t>(n, 1) * sizeof(cc_tight_box), &a))) return rc;
+    if (n) CC_CUDA(h, cudaMemcpyAsync(a, boxes, n * sizeof(cc_tight_box), cudaMemcpyHostToDevice, s));
+    if ((rc = ccrt::ensure(h, 4, sizeof(RefineCounters), &cnt_p))) return rc;
+    RefineCounters* dc = (RefineCounters*)cnt_p;
+    ccrt::EventPair ev;
+    CC_CUDA(h, cudaEventCreate(&ev.e0));
+    CC_CUDA(h, cudaEventCreate(&ev.e1));
+    std::vector<cc_tight_box> out;
+    std::vector<uint32_t> out_flags;
+    int cur_slot = S_REF_A, next_slot = S_REF_B;
+    size_t cur_n = n;
+    const size_t chunk = (size_t)1 << 24;  // evaluation batches: bounded scratch
+    for (int d = 0; d <= max_depth && cur_n; ++d) {
+        const bool last = d == max_depth || 2 * cur_n > max_live;
+        if (last && d < max_depth) st.stopped_at_cap = 1;
+        void *cur, *next, *masks, *crit;
+        if ((rc = ccrt::ensure(h, cur_slot, cur_n * sizeof(cc_tight_box), &cur))) return rc;
+        if ((rc = ccrt::ensure(h, next_slot, (last ? 1 : 2 * cur_n) * sizeof(cc_tight_box), &next))) return rc;
+        if ((rc = ccrt::ensure(h, S_REF_MASKS, cur_n * sizeof(uint32_t), &masks))) return rc;
+        if ((rc = ccrt::ensure(h, S_REF_CRIT, cur_n * (sizeof(cc_tight_box) + sizeof(uint32_t)), &crit))) return rc;
+        CC_CUDA(h, cudaMemsetAsync(dc, 0, sizeof(RefineCounters), s));
+        CC_CUDA(h, cudaEventRecord(ev.e0, s));
+        for (size_t off = 0; off < cur_n; off += chunk) {
+            const size_t m = std::min(chunk, cur_n - off);
+            rc = eval_batch<Layout::AoS>(h, (const double*)((cc_tight_box*)cur + off), m, (uint32_t*)masks + off, s,
+                                         false);
+            if (rc) return rc;
+        }
+        k_refine_split<<<eval_grid(h, cur_n), 128, 0, s>>>(
+            (const cc_tight_box*)cur, cur_n, (const uint32_t*)masks, d, last ? 1 : 0, (cc_tight_box*)next,
+            last ? 0 : cur_n, (cc_tight_box*)crit, (uint32_t*)((cc_tight_box*)crit + cur_n), cur_n, dc);
+        CC_LAUNCHED(h);
+        CC_CUDA(h, cudaEventRecord(ev.e1, s));
+        RefineCounters hc;
+        CC_CUDA(h, cudaMemcpyAsync(&hc, dc, sizeof(hc), cudaMemcpyDeviceToHost, s));
+        CC_CUDA(h, cudaStreamSynchronize(s));
+        if (hc.overflow) return ccrt::fail(h, CC_ERR_QUEUE_OVERFLOW, "cc_tight_refine: queue overflow");
+        float ms = 0.0f;
+        CC_CUDA(h, cudaEventElapsedTime(&ms, ev.e0, ev.e1));
+        st.live[d] = cur_n;
+        st.decided[d] = hc.n_decided;
+        st.ms[d] = ms;
+        st.depths_run = d + 1;
+        if (hc.n_crit) {
+            const size_t old = out.size();
+            out.resize(old + hc.n_crit);
+            out_flags.resize(old + hc.n_crit);
+            CC_CUDA(h, cudaMemcpyAsync(out.data() + old, crit, hc.n_crit * sizeof(cc_tight_box), cudaMemcpyDeviceToHost, s));
+            CC_CUDA(h, cudaMemcpyAsync(out_flags.data() + old, (cc_tight_box*)crit + cur_n, hc.n_crit * sizeof(uint32_t),
+                                       cudaMemcpyDeviceToHost, s));
+            CC_CUDA(h, cudaStreamSynchronize(s));
+        }
+        cur_n = 2 * hc.n_next;
+        std::swap(cur_slot, next_slot);
+        if (h->interrupt.load()) break;
+    }
+    *n_crit = out.size();
+    *criticals = (cc_tight_box*)std::malloc(sizeof(cc_tight_box) * (out.size() + 1));
+    if (!*criticals) return ccrt::fail(h, CC_ERR_OOM, "malloc criticals");
+    if (!out.empty()) std::memcpy(*criticals, out.data(), sizeof(cc_tight_box) * out.size());
+    if (flags) {
+        *flags = (uint32_t*)std::malloc(sizeof(uint32_t) * (out.size() + 1));
+        if (!*flags) return ccrt::fail(h, CC_ERR_OOM, "malloc flags");
+        if (!out.empty()) std::memcpy(*flags, out_flags.data(), sizeof(uint32_t) * out.size());
+    }
+    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    st.kernel_launches = h->launches;
+    if (stats) *stats = st;
     return CC_OK;
 }

@@ -96,6 +96,12 @@ struct SbCounters {
     double widen_sum;                   // sum of FP32 / FP64 width of R over them
     unsigned long long widen_max_bits;  // bits of the largest ratio (positive doubles order as integers)
     unsigned long long n_f32_jobs;      // FP64 jobs of an FP32-first pass
+    // FP64 certification of the FP32-decided "true" verdicts of the leaf
+    // criteria: certified, and not confirmed (the FP64 verdict was used)
+    unsigned long long cert_ok, cert_fail;
+    // FP64 certification of the pre-filter's empty leaves (k_sbp_empty_cert):
+    // anchors queued, anchors certified, anchors not confirmed (this slice)
+    unsigned long long n_anchor, empty_cert_ok, empty_cert_fail;
 };
 
 struct SevenJob {  // a leaf whose seven-disk prefix left r7 pieces to check
@@ -379,8 +385,11 @@ __device__ __forceinline__ int leaf_fp64(const SbTask& task, const SbCell& cell,
     if (F32) {
         static_assert(sb::SB_EVEN_SPLIT == 0, "criterion 0");
         const bool ok32 = sb::even_split_t(sb::enclose6(leaf.box), cc::f32::of(v.R));
-        if (cc::trap_status() == cc::TRAP_NONE) return ok32 ? 0 : CC_SBT_LEAF_CRITICAL;
+        const bool decided = cc::trap_status() == cc::TRAP_NONE;
         cc::trap_clear();
+        if (decided && !ok32) return CC_SBT_LEAF_CRITICAL;
+        // an FP32 "true" is certified by the FP64 criterion below: its
+        // verdict (the reference's) is the one used
     }
     const bool ok = sb::sb_criterion(0, leaf.box, v);
     int outcome;
@@ -443,11 +452,26 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaves(const SbTask* __restric
 // decided (outcome EMPTY); the offsets (idx - l0) of the others go to the
 // candidate list for k_sbp_leaf_check, so that the FP64 leaf stage runs on
 // full warps of leaves that need it (most warps hold only empty leaves).
+//
+// Every leaf the pre-filter finds empty is certified in FP64.  For a fixed
+// (cell, r4 piece, r5 piece) -- a row -- the FP64 test "la empty, or a
+// tightened lower bound of r1..r5 at least its upper bound, or R.hi < 0" is
+// monotone in the r6 piece index: the r6 lower bound fma(step, i6, lo) grows
+// with i6 (the rounding is monotone), the tightened lower bounds are running
+// maxima of it, the upper bounds of r1..r5 do not depend on it, and R.hi is a
+// chain of round-up subtractions of those lower bounds.  So in each warp the
+// first leaf of every run of FP32-empty leaves of a row (an anchor) goes to
+// k_sbp_empty_cert, which runs that test in FP64: passing it there certifies
+// the leaf and every later leaf of its row as empty in FP64 (the test is
+// part of the reference's own emptiness test; the r6 piece's own width is
+// left out, as the only term that is not monotone).
 __global__ void __launch_bounds__(kThreads) k_sbp_leaf_filter(const SbTask* __restrict__ tasks,
                                                                const SbCell* __restrict__ cells, unsigned long long l0,
                                                                unsigned long long l1, LeafGrid g,
                                                                uint32_t* __restrict__ cand, unsigned long long* n_cand,
-                                                               unsigned long long cand_cap, SbCounters* c) {
+                                                               unsigned long long cand_cap,
+                                                               uint32_t* __restrict__ anchors,
+                                                               unsigned long long anchor_cap, SbCounters* c) {
     // the trace of the empty leaves, summed per thread and flushed once
     unsigned long long digest = 0;
     unsigned int n_empty = 0, n_valid = 0;
@@ -455,6 +479,7 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaf_filter(const SbTask* __re
         const unsigned long long idx = l0 + base_ + (threadIdx.x & 31);
         const bool valid = idx < l1;
         bool empty = false;
+        unsigned long long row = ~0ULL;
         if (valid) {
             const LeafAt a = leaf_at(g, l0, l1, idx);
             const SbCell cell = cells[a.ci];
@@ -468,9 +493,16 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaf_filter(const SbTask* __re
                 ++n_empty;
             }
             ++n_valid;
+            row = (a.ci * (unsigned long long)g.n4 + (unsigned long long)a.i4) * (unsigned long long)g.n5 +
+                  (unsigned long long)a.i5;
         }
-        const unsigned long long slot = warp_append(n_cand, valid && !empty, cand_cap, &c->overflow);
+        const unsigned long long prev_row = __shfl_up_sync(0xffffffffu, row, 1);
+        const int prev_empty = __shfl_up_sync(0xffffffffu, empty ? 1 : 0, 1);
+        const bool anchor = valid && empty && ((threadIdx.x & 31) == 0 || prev_row != row || !prev_empty);
+        unsigned long long slot = warp_append(n_cand, valid && !empty, cand_cap, &c->overflow);
         if (slot != ~0ULL) cand[slot] = (uint32_t)(idx - l0);
+        slot = warp_append(&c->n_anchor, anchor, anchor_cap, &c->overflow);
+        if (slot != ~0ULL) anchors[slot] = (uint32_t)(idx - l0);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -485,6 +517,41 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaf_filter(const SbTask* __re
             atomicAdd(&c->fp32_empty, (unsigned long long)n_empty);
         }
         if (n_valid) atomicAdd(&c->leaf_evals, (unsigned long long)n_valid);
+    }
+}
+
+// The FP64 certificate of the pre-filter's anchors (see k_sbp_leaf_filter).
+__global__ void __launch_bounds__(kThreads) k_sbp_empty_cert(const SbTask* __restrict__ tasks,
+                                                              const SbCell* __restrict__ cells, unsigned long long l0,
+                                                              unsigned long long l1, LeafGrid g,
+                                                              const uint32_t* __restrict__ anchors,
+                                                              unsigned long long anchor_cap, SbCounters* c) {
+    const unsigned long long n = c->n_anchor < anchor_cap ? c->n_anchor : anchor_cap;
+    unsigned ok_n = 0, fail_n = 0;
+    SB_WARP_LOOP(n) {
+        const unsigned long long k = base_ + (threadIdx.x & 31);
+        if (k < n) {
+            const unsigned long long idx = l0 + anchors[k];
+            const LeafAt a = leaf_at(g, l0, l1, idx);
+            const SbCell cell = cells[a.ci];
+            const SbTask& task = tasks[cell.task];
+            const Box6 b = sb::leaf_box_steps(task.box, task.step, cell.r3, a.i4, g.n4, a.i5, g.n5, a.i6, g.n6);
+            bool empty = cc::empty(b.la);
+#pragma unroll
+            for (int r = 0; r < 5; ++r) empty = empty || b.r[r].lo >= b.r[r].hi;
+            empty = empty || sb::remaining_weight(b).hi < 0.0;
+            if (empty) ++ok_n;
+            else ++fail_n;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ok_n += __shfl_xor_sync(0xffffffffu, ok_n, o);
+        fail_n += __shfl_xor_sync(0xffffffffu, fail_n, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (ok_n) atomicAdd(&c->empty_cert_ok, (unsigned long long)ok_n);
+        if (fail_n) atomicAdd(&c->empty_cert_fail, (unsigned long long)fail_n);
     }
 }
 
@@ -698,15 +765,19 @@ __global__ void __launch_bounds__(kThreads) k_sbp_f32(const SbLeaf* __restrict__
                 }
                 if (ok) {
                     works = true;
+                    from = k;
                     break;
                 }
             }
             cc::trap_clear();
         }
-        trace_note(bt, valid && works, valid && works ? leaf_key(gen, leaf, K) : 0, K);
-        const bool job = valid && !works && (undecided || P::kTail);
+        // a placement that works on the enclosures becomes an FP64
+        // certification job at that placement (bit 31): k_sbp_fp64 decides
+        // and traces the leaf with the FP64 criterion from there
+        const bool job = valid && (works || undecided || P::kTail);
         unsigned long long slot = warp_append(n_jobs, job, job_cap, &c->overflow);
-        if (slot != ~0ULL) jobs[slot] = (uint32_t)idx | ((uint32_t)from << kF32JobIndexBits);
+        if (slot != ~0ULL)
+            jobs[slot] = (uint32_t)idx | ((uint32_t)from << kF32JobIndexBits) | (works ? (1u << 31) : 0u);
         // decided not to work, nothing after the FP32 placements: next pass
         slot = warp_append(n_out, valid && !works && !job, q_cap, &c->overflow);
         if (slot != ~0ULL) qout[slot] = leaf;
@@ -724,6 +795,7 @@ __global__ void __launch_bounds__(kThreads) k_sbp_fp64(const SbLeaf* __restrict_
     __shared__ BlockTrace<CC_SBT_LEAF_OUTCOMES> bt;
     trace_init(bt);
     const unsigned long long total = *n_jobs < job_cap ? *n_jobs : job_cap;
+    unsigned cert_ok = 0, cert_fail = 0;
     SB_WARP_LOOP(total) {
         const unsigned long long k = base_ + (threadIdx.x & 31);
         const bool valid = k < total;
@@ -735,10 +807,14 @@ __global__ void __launch_bounds__(kThreads) k_sbp_fp64(const SbLeaf* __restrict_
             sb::Vals v;
             v.R = sb::remaining_weight(leaf.box);
             cc::trap_clear();
-            const bool ok = F32Pass<K>::fp64_from(leaf.box, v, (int)(job >> kF32JobIndexBits));
+            const bool ok = F32Pass<K>::fp64_from(leaf.box, v, (int)((job >> kF32JobIndexBits) & 7));
             if (cc::trap_status() != cc::TRAP_NONE) outcome = CC_SBT_LEAF_TRAPPED;
             else if (ok) outcome = K;
             cc::trap_clear();
+            if (job >> 31) {  // a certification: the FP32 placement worked
+                if (outcome == K) ++cert_ok;
+                else ++cert_fail;
+            }
         }
         const bool undecided = valid && outcome == CC_SBT_LEAF_CRITICAL;
         const bool decided = valid && !undecided;
@@ -751,6 +827,15 @@ __global__ void __launch_bounds__(kThreads) k_sbp_fp64(const SbLeaf* __restrict_
             leaf.idx |= 1ULL << 63;
             crit[slot] = leaf;
         }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cert_ok += __shfl_xor_sync(0xffffffffu, cert_ok, o);
+        cert_fail += __shfl_xor_sync(0xffffffffu, cert_fail, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (cert_ok) atomicAdd(&c->cert_ok, (unsigned long long)cert_ok);
+        if (cert_fail) atomicAdd(&c->cert_fail, (unsigned long long)cert_fail);
     }
     trace_flush(bt, c->leaf_counts, c, nullptr);
 }
@@ -854,8 +939,9 @@ __global__ void __launch_bounds__(kThreads) k_sbp_r1c_reach(const SbLeaf* __rest
                 need64 = true;
             } else {
                 const bool ok = sb::corner_groups_reach_t<cc::f32::Fv>(box, 2 + i / 2, st.cross, st.first, st.limit);
-                if (cc::trap_status() != cc::TRAP_NONE) need64 = true;
-                else if (ok) atomicOr(&masks[2 * leaf], 1u << i);
+                // undecided, or "works" on the enclosures: the FP64
+                // backtracking decides (and so certifies a "works")
+                if (cc::trap_status() != cc::TRAP_NONE || ok) need64 = true;
             }
             cc::trap_clear();
         }
@@ -1048,6 +1134,7 @@ struct Engine {
     SbCounters* hc = nullptr;      // pinned
     std::vector<SbLeaf> found;
     uint64_t launches = 0;
+    uint64_t empty_anchors = 0;  // anchors of empty leaves certified in FP64
 };
 
 // criteria K..12 as passes over the compacted queue, then the seven-disk
@@ -1178,6 +1265,7 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
         if ((st = sync_counters(e))) return st;
         const unsigned long long n_leaves = e.hc->n_cell * n456;
         unsigned long long l0 = 0;
+        bool redo_without_filter = false;
         while (l0 < n_leaves) {
             // room for the criticals of a full pass queue
             if (e.hc->n_crit > e.crit_cap - e.slice && (st = drain_criticals(e))) return st;
@@ -1189,15 +1277,20 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
             lg.rem0 = (uint32_t)(l0 % n456);
             if (e.plain) {
                 k_sbp_leaves_plain<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, e.crit, e.crit_cap, e.dc);
-            } else if (e.fp32) {
+            } else if (e.fp32 && !redo_without_filter) {
                 // the candidate list lives in the second pass queue's memory
-                // (free until pass 1) and is counted by its counter
+                // (free until pass 1) and is counted by its counter; the
+                // anchors of the empty leaves in its upper half
                 uint32_t* cand = reinterpret_cast<uint32_t*>(e.q[1]);
-                const unsigned long long cand_cap = e.slice * (sizeof(SbLeaf) / sizeof(uint32_t));
+                const unsigned long long cand_cap = e.slice * (sizeof(SbLeaf) / sizeof(uint32_t)) / 2;
+                uint32_t* anchors = cand + cand_cap;
+                CC_CUDA(e.h, cudaMemsetAsync(&e.dc->n_anchor, 0, 3 * sizeof(unsigned long long), e.s));
                 k_sbp_leaf_filter<<<lgrid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, cand, &e.dc->n_q[1],
-                                                               cand_cap, e.dc);
+                                                               cand_cap, anchors, cand_cap, e.dc);
                 CC_LAUNCHED(e.h);
-                e.launches++;
+                k_sbp_empty_cert<<<e.grid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, anchors, cand_cap, e.dc);
+                CC_LAUNCHED(e.h);
+                e.launches += 2;
                 k_sbp_leaf_check<<<e.grid, kThreads, 0, e.s>>>(e.tasks, e.cells, l0, l1, lg, cand, &e.dc->n_q[1],
                                                                cand_cap, e.q[0], &e.dc->n_q[0], e.slice, e.crit,
                                                                e.crit_cap, e.dc);
@@ -1216,6 +1309,17 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
                 e.range /= 2;
                 continue;
             }
+            if (e.fp32 && !redo_without_filter && e.hc->empty_cert_fail) {
+                // an empty leaf of the pre-filter failed its FP64 certificate:
+                // undo the slice and redo it with FP64 emptiness tests only
+                cc::cert_failures_host += e.hc->empty_cert_fail;
+                CC_CUDA(e.h, cudaMemcpyAsync(e.dc, e.backup, sizeof(SbCounters), cudaMemcpyDeviceToDevice, e.s));
+                if ((st = sync_counters(e))) return st;
+                redo_without_filter = true;
+                continue;
+            }
+            redo_without_filter = false;
+            e.empty_anchors += e.hc->empty_cert_ok;
             if (e.plain) {  // every leaf was decided in place; at most `slice` criticals per slice
                 e.range = e.slice;
                 l0 = l1;
@@ -1293,11 +1397,22 @@ extern "C" int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid
     return cc_sb_prove_ex(h, root, grid, 0, criticals, n_crit, flags, stats);
 }
 
+// FP64 certification failures of the size-bound kernels so far (expected 0)
+static unsigned long long sb_cert_failures_so_far() {
+    unsigned long long v = 0;
+    if (cudaMemcpyFromSymbol(&v, cc::cc_cert_fail_count, sizeof(v)) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return v + cc::cert_failures_host.load();
+}
+
 extern "C" int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, int options,
                               cc_sb_box** criticals, size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats) {
     if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
     if (!grid_ok(grid)) return ccrt::fail(h, CC_ERR_PARAM, "cc_sb_prove: split counts must be in [1, 2047]");
     const auto t_start = std::chrono::steady_clock::now();
+    const unsigned long long fails0 = sb_cert_failures_so_far();
     h->launches = 0;
     h->interrupt.store(0);
     CC_CUDA(h, cudaSetDevice(h->device));
@@ -1408,6 +1523,9 @@ extern "C" int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_g
         stats->widening_max = wmax;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
         stats->kernel_launches = h->launches;
+        stats->fp32_certified = e.hc->cert_ok;
+        stats->empty_anchors = e.empty_anchors;
+        stats->cert_failures = sb_cert_failures_so_far() - fails0;
     }
     return status;
 }

@@ -162,12 +162,7 @@ CC_FN void cert_end() { cc_trap_words[threadIdx.x] &= (uint8_t)~kCertModeBit; }
 // the FP32 can_recurse counts its calls (low byte of cc_cert_state)
 CC_FN void cert_count_reset() { cc_cert_state[threadIdx.x] = 0; }
 CC_FN int cert_count() { return cc_cert_state[threadIdx.x] & 0xff; }
-// FP64 certifications that failed in this translation unit's kernels since
-// the library was loaded: an FP32 decision the FP64 check did not confirm
-// (the FP64 result is used instead).  Expected to stay 0; the host reads it
-// with cudaMemcpyFromSymbol.
-static __device__ unsigned long long cc_cert_fail_count;
-CC_FN void cert_failed() { atomicAdd(&cc_cert_fail_count, 1ULL); }
+
 // One out-of-line copy for the FP32 evaluation (it is called from many
 // sites), with a shortcut before its costly part.  Where largest_norm is
 // certainly above 9/64, can_recurse_t takes ratio = lesser(ratio_cor,
@@ -1419,6 +1414,38 @@ CC_FN_INL bool first_f32(Crit crit, const Box& v, Iv rest, int* how = nullptr) {
     }
     if (how) *how = 0;
     return crit(v, rest);
+}
+// first_f32 with the certification of a decided "true" left to the caller
+// (the proof queues it for a certification pass): *how as first_f32 (2:
+// FP32 "true", not yet certified), *calls = the number of the call that
+// settled the FP32 run (its last call; 0 if none), for certify_leaf.
+template <class Crit>
+CC_FN_INL bool first_f32_deferred(Crit crit, const Box& v, Iv rest, int* how, int* calls) {
+    const uint32_t saved = trap_status();
+    trap_clear();
+    cert_count_reset();
+    const bool ok32 = crit(enclose(v), f32::of(rest));
+    const bool decided = trap_status() == TRAP_NONE;
+    *calls = cert_count();
+    trap_clear();
+    if (saved != TRAP_NONE) trap(saved);
+    if (decided) {
+        *how = ok32 ? 2 : 1;
+        return ok32;
+    }
+    *how = 0;
+    return crit(v, rest);
+}
+// The FP64 certification of a deferred "true": the criterion with only call
+// number `call` evaluated; true if it holds without reaching a trap site.
+template <class Crit>
+CC_FN_INL bool certify_leaf(Crit crit, const Box& v, Iv rest, int call) {
+    cert_begin(call);
+    const bool ok = crit(v, rest);
+    const bool clean = trap_status() == TRAP_NONE;
+    cert_end();
+    trap_clear();
+    return ok && clean;
 }
 struct TwoByTwo {
     template <class I>

@@ -92,6 +92,17 @@ struct Critical {
     uint32_t flags;
 };
 
+// A leaf verdict that the FP32 enclosures decided "true", queued for its
+// FP64 certification (k_stage_cert): the leaf, its criterion (0: two_by_two,
+// 1: the leaf form of r1_r2_r3_strategies) and the number of the call that
+// settled the FP32 run (0: none).
+struct CertLeaf {
+    uint32_t cell4;
+    uint16_t i4;
+    uint8_t crit;
+    uint8_t call;
+};
+
 struct Counters {
     unsigned long long n_cell2, n_cell3, n_cell4, n_leaf, n_gaps, n_crit;
     unsigned long long overflow;
@@ -99,10 +110,11 @@ struct Counters {
     unsigned long long digest;
     unsigned long long counts[4][8];
     unsigned long long n_leaf2;  // leaves waiting for the 2x2 criterion (split stage 4a)
-    // leaf criteria evaluated FP32-first (tight::first_f32), by outcome:
-    // FP64 evaluation, FP32 "false", FP32 "true" certified in FP64,
-    // certification failed
+    // leaf criteria evaluated FP32-first (tight::first_f32_deferred), by
+    // outcome: FP64 evaluation, FP32 "false", FP32 "true" certified in FP64
+    // (k_stage_cert), certification failed
     unsigned long long fp32[4];
+    unsigned long long n_cert;  // FP32 "true" leaf verdicts queued for certification
 };
 
 struct Leaf2 {  // a leaf that needs the 2x2 criterion
@@ -192,6 +204,10 @@ struct F32Tally {
     unsigned n[4] = {0, 0, 0, 0};
     __device__ __forceinline__ void note(int how) {
         if (how >= 0) n[how] += 1;
+    }
+    // a stage's outcomes: the FP32 "true" ones are counted by k_stage_cert
+    __device__ __forceinline__ void note_stage(int how) {
+        if (how == 0 || how == 1) n[how] += 1;
     }
     __device__ __forceinline__ void flush(Counters* c) {
 #pragma unroll
@@ -414,7 +430,7 @@ template <bool Hoist, bool Split>
 __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks, const Cell4* __restrict__ in, int s4,
                                                  unsigned long long cell_lo, unsigned long long cell_hi,
                                                  Leaf* __restrict__ out, Leaf2* __restrict__ out2, Caps caps, Counters* c,
-                                                 unsigned long long task_base) {
+                                                 unsigned long long task_base, CertLeaf* __restrict__ cq) {
     __shared__ BlockTrace bt;
     trace_init(bt);
     const unsigned long long total = (cell_hi - cell_lo) * s4;
@@ -426,7 +442,8 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
         int outcome = -1;
         uint32_t pidx = 0;
         int i4 = 0, task = 0, i1 = 0, i2 = 0, i3 = 0;
-        bool trapped = false, leaf_tried = false;
+        bool trapped = false, leaf_tried = false, queue_cert = false;
+        int calls = 0;
         Iv r4{0.0, 0.0};
         if (valid) {
             evals += 1;
@@ -454,10 +471,14 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
                     outcome = -3;  // on to stage 4a2
                     if (p.order) {  // learned order: the cheap leaf criterion first
                         int how = -1;
-                        const bool ok4 = tight::r1_r2_r3_leaf_first_f32(v, p.R4, &how);
-                        tally.note(how);
-                        if (ok4 && trap_status() == TRAP_NONE) outcome = CC_T_L4_R123LEAF;
-                        else if (!ok4) leaf_tried = true;  // (a trap leaves it to the plain order)
+                        const bool ok4 = tight::first_f32_deferred(tight::LeafR123{}, v, p.R4, &how, &calls);
+                        tally.note_stage(how);
+                        if (ok4 && trap_status() == TRAP_NONE) {
+                            outcome = CC_T_L4_R123LEAF;
+                            queue_cert = how == 2;
+                        } else if (!ok4) {
+                            leaf_tried = true;  // (a trap leaves it to the plain order)
+                        }
                     }
                 } else {
                     bool ok = tight::two_by_two_strategies(v, R);
@@ -474,6 +495,8 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
             unsigned long long slot = warp_append(&c->n_leaf2, valid && outcome == -3, caps.leaf2, &c->overflow);
             if (slot != ~0ULL)
                 out2[slot] = Leaf2{r4, pidx, (uint16_t)i4, (uint16_t)((trapped ? 1 : 0) | (leaf_tried ? 2 : 0))};
+            slot = warp_append(&c->n_cert, valid && queue_cert, caps.leaf, &c->overflow);
+            if (slot != ~0ULL) cq[slot] = CertLeaf{pidx, (uint16_t)i4, 1, (uint8_t)calls};
         } else {
             unsigned long long slot = warp_append(&c->n_leaf, valid && outcome == -2, caps.leaf, &c->overflow);
             if (slot != ~0ULL) out[slot] = Leaf{pidx, (uint16_t)i4, (uint16_t)(trapped ? 1 : 0)};
@@ -489,7 +512,7 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
 // (tight_rectangle.cu:246); failures go on to stage 4b
 __global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
                                                   const Leaf2* __restrict__ in, Leaf* __restrict__ out, Caps caps,
-                                                  Counters* c, unsigned long long task_base) {
+                                                  Counters* c, unsigned long long task_base, CertLeaf* __restrict__ cq) {
     __shared__ BlockTrace bt;
     trace_init(bt);
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_leaf2;
@@ -501,7 +524,8 @@ __global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks
         int outcome = -1;
         Leaf2 lf{Iv{0.0, 0.0}, 0, 0, 0};
         int task = 0, i1 = 0, i2 = 0, i3 = 0;
-        bool trapped = false;
+        bool trapped = false, queue_cert = false;
+        int calls = 0;
         if (valid) {
             lf = in[idx];
             const Cell4& p = cells[lf.cell4];
@@ -515,10 +539,11 @@ __global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks
             Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
             tighten_lb(R, 0.0);
             int how = -1;
-            bool ok = tight::two_by_two_first_f32(v, R, &how);
-            tally.note(how);
+            bool ok = tight::first_f32_deferred(tight::TwoByTwo{}, v, R, &how, &calls);
+            tally.note_stage(how);
             trapped = (lf.pad & 1) != 0 || trap_status() != TRAP_NONE;
             outcome = (ok && !trapped) ? CC_T_L4_2X2 : -2;
+            queue_cert = outcome == CC_T_L4_2X2 && how == 2;
         }
         __syncwarp();
         bool decided = valid && outcome >= 0;
@@ -526,6 +551,8 @@ __global__ void __launch_bounds__(128) k_stage4a2(const Task* __restrict__ tasks
                    decided ? outcome : 0);
         unsigned long long slot = warp_append(&c->n_leaf, valid && outcome == -2, caps.leaf, &c->overflow);
         if (slot != ~0ULL) out[slot] = Leaf{lf.cell4, lf.i4, (uint16_t)((trapped ? 1 : 0) | (lf.pad & 2))};
+        slot = warp_append(&c->n_cert, valid && queue_cert, caps.leaf, &c->overflow);
+        if (slot != ~0ULL) cq[slot] = CertLeaf{lf.cell4, lf.i4, 0, (uint8_t)calls};
     }
     tally.flush(c);
     trace_flush(bt, c, 3);
@@ -543,7 +570,7 @@ template <bool F32>
 __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
                                                  const Leaf* __restrict__ in, int s4, GapsLeaf* __restrict__ gq,
                                                  Critical* __restrict__ crit, Caps caps, Counters* c,
-                                                 unsigned long long task_base) {
+                                                 unsigned long long task_base, CertLeaf* __restrict__ cq) {
     __shared__ BlockTrace bt;
     trace_init(bt);
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_leaf;
@@ -556,7 +583,8 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
         Leaf lf{0, 0, 0};
         Box v;
         int task = 0, i1 = 0, i2 = 0, i3 = 0;
-        bool trapped = false, need_gaps = false;
+        bool trapped = false, need_gaps = false, queue_cert = false;
+        int calls = 0;
         GapsLeaf gl;
         if (valid) {
             lf = in[idx];
@@ -575,7 +603,8 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
             tight::GapsStart g;
             int how = -1;
             if (!(lf.trapped & 2) &&
-                (F32 ? tight::r1_r2_r3_leaf_first_f32(v, p.R4, &how) : tight::r1_r2_r3_strategies(v, p.R4))) {
+                (F32 ? tight::first_f32_deferred(tight::LeafR123{}, v, p.R4, &how, &calls)
+                     : tight::r1_r2_r3_strategies(v, p.R4))) {
                 outcome = CC_T_L4_R123LEAF;
             } else if (tight::gaps_enters(v.r[0].lo, v.r[1].lo, g)) {
                 need_gaps = true;
@@ -585,10 +614,11 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
             } else {
                 outcome = CC_T_L4_CRITICAL;
             }
-            tally.note(how);
+            tally.note_stage(how);
             trapped = trap_status() != TRAP_NONE;
             gl.trapped = trapped ? 1 : 0;
             if (trapped && !need_gaps) outcome = CC_T_L4_TRAPPED;
+            queue_cert = F32 && outcome == CC_T_L4_R123LEAF && how == 2;
         }
         __syncwarp();
         bool decided = valid && !need_gaps;
@@ -598,9 +628,75 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
         if (slot != ~0ULL) gq[slot] = gl;
         bool keep = decided && (outcome == CC_T_L4_CRITICAL || outcome == CC_T_L4_TRAPPED);
         push_critical(crit, warp_append(&c->n_crit, keep, caps.crit, &c->overflow), v, task, trapped);
+        if (F32) {
+            const unsigned long long cs = warp_append(&c->n_cert, valid && queue_cert, caps.leaf, &c->overflow);
+            if (cs != ~0ULL) cq[cs] = CertLeaf{lf.cell4, lf.i4, 1, (uint8_t)calls};
+        }
     }
     if (F32) tally.flush(c);
     trace_flush(bt, c, 3);
+}
+
+// FP64 certification of the leaf verdicts the FP32 enclosures decided "true"
+// in stages 4a, 4a2 and 4b of the current slice: each block sorts its 128
+// jobs by (criterion, settling call) in shared memory, so that a warp's
+// lanes mostly run the same path, and runs the FP64 criterion with only that
+// call evaluated (tight::certify_leaf).  A failure is counted in fp32[3];
+// the host then redoes the chunk in the plain FP64 form.
+__global__ void __launch_bounds__(128) k_stage_cert(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
+                                                    const CertLeaf* __restrict__ cq, int s4, Caps caps, Counters* c) {
+    __shared__ CertLeaf s_job[128];
+    __shared__ int s_cnt[32];
+    const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cert;
+    const unsigned long long total = n_in < caps.leaf ? n_in : caps.leaf;
+    unsigned ok_n = 0, fail_n = 0;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < total;
+         base += (unsigned long long)gridDim.x * blockDim.x) {
+        if (threadIdx.x < 32) s_cnt[threadIdx.x] = 0;
+        __syncthreads();
+        const unsigned long long j = base + threadIdx.x;
+        CertLeaf job{0, 0, 0, 0};
+        int key = 31;  // past the end: sorted last
+        if (j < total) {
+            job = cq[j];
+            key = (job.crit << 4) | (job.call < 15 ? job.call : 15);
+        }
+        const int rank = atomicAdd(&s_cnt[key], 1);
+        __syncthreads();
+        int off = rank;
+        for (int k = 0; k < key; ++k) off += s_cnt[k];
+        s_job[off] = job;
+        __syncthreads();
+        const bool valid = (int)threadIdx.x < (int)(total - base < 128 ? total - base : 128);
+        if (valid) {
+            const CertLeaf m = s_job[threadIdx.x];
+            const Cell4& p = cells[m.cell4];
+            const Task tk = tasks[p.task];
+            trap_clear();
+            const Box v = leaf_box(p, tk.la, subinterval(p.r4r, m.i4, s4));
+            bool ok;
+            if (m.crit == 0) {
+                Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+                tighten_lb(R, 0.0);
+                ok = tight::certify_leaf(tight::TwoByTwo{}, v, R, m.call);
+            } else {
+                ok = tight::certify_leaf(tight::LeafR123{}, v, p.R4, m.call);
+            }
+            if (ok) ++ok_n;
+            else ++fail_n;
+        }
+        __syncthreads();  // s_cnt and s_job are rewritten next iteration
+    }
+    unsigned v0 = ok_n, v1 = fail_n;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+        v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (v0) atomicAdd(&c->fp32[2], (unsigned long long)v0);
+        if (v1) atomicAdd(&c->fp32[3], (unsigned long long)v1);
+    }
 }
 
 // stage 4c: the gaps bisection on full warps of leaves that need it

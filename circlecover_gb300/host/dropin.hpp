@@ -10,6 +10,7 @@
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "circlecover_gb300.h"
 
@@ -49,6 +50,34 @@ extern "C" inline void on_sigint(int) {
     if (g_interrupts.fetch_add(1) > 0) std::_Exit(SIGINT);
     cc_handle* h = g_active.load();
     if (h) cc_interrupt(h);
+}
+
+// Comma-separated integers of one field of a split-count override
+// ("a,b,c"); returns how many were read (at most `cap`).
+inline int parse_ints(const std::string& field, int* out, int cap) {
+    int n = 0;
+    std::size_t pos = 0;
+    while (pos < field.size() && n < cap) {
+        std::size_t end = field.find(',', pos);
+        if (end == std::string::npos) end = field.size();
+        out[n++] = std::atoi(field.substr(pos, end - pos).c_str());
+        pos = end + 1;
+    }
+    return n;
+}
+
+// Colon-separated fields of an override string.
+inline std::vector<std::string> split_fields(const char* text) {
+    std::vector<std::string> f;
+    std::string s(text);
+    std::size_t pos = 0;
+    for (;;) {
+        std::size_t end = s.find(':', pos);
+        f.push_back(s.substr(pos, end == std::string::npos ? std::string::npos : end - pos));
+        if (end == std::string::npos) break;
+        pos = end + 1;
+    }
+    return f;
 }
 
 inline void check(cc_handle* h, int status, const char* what) {

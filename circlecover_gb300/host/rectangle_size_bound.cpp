@@ -9,7 +9,8 @@
 // final order, Variables' text format with 19-digit intervals), same Ctrl-C
 // behaviour (the refinement stops and the previous generation's result is
 // printed).  The environment variable CC_SB_LAMBDA_MAX narrows the lambda
-// range for short runs.  Leaves that reached a trap site (where the
+// range for short runs, and CC_SB_GRID="la:r1,...,r6:la_gen:s1,...,s6:gens"
+// replaces the split counts.  Leaves that reached a trap site (where the
 // reference would have aborted the run) are printed with a "Trapped: "
 // prefix instead.
 #include <vector>
@@ -41,6 +42,15 @@ cc_sb_grid reference_sb_grid() {
         g.r_splits_gen[k] = subdiv[k];
     }
     g.num_generations = 1;
+    if (const char* e = std::getenv("CC_SB_GRID")) {
+        const std::vector<std::string> f = split_fields(e);
+        if (f.size() != 5) throw std::runtime_error("CC_SB_GRID: la:r1,...,r6:la_gen:s1,...,s6:gens");
+        parse_ints(f[0], &g.la_splits_init, 1);
+        parse_ints(f[1], g.r_splits_init, 6);
+        parse_ints(f[2], &g.la_splits_gen, 1);
+        parse_ints(f[3], g.r_splits_gen, 6);
+        parse_ints(f[4], &g.num_generations, 1);
+    }
     return g;
 }
 

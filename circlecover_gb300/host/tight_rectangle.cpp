@@ -62,7 +62,10 @@ void print_summary(const cc_tight_summary_t& r) {
 }
 
 // The reference's split counts (tight_rectangle.cu:44-58); the environment
-// variable CC_TIGHT_LAMBDA_MAX narrows the lambda range for short runs.
+// variable CC_TIGHT_LAMBDA_MAX narrows the lambda range for short runs, and
+// CC_TIGHT_GRID="la:r1,r2,r3,r4:g1,...,gk:s1,s2,s3,s4" replaces the split
+// counts (initial lambda and radius splits, the lambda splits of the k
+// refinement generations, their radius splits).
 cc_tight_grid reference_grid() {
     cc_tight_grid g{};
     g.la_splits_init = 256;
@@ -74,6 +77,14 @@ cc_tight_grid reference_grid() {
     g.r_splits_gen[1] = 128;
     g.r_splits_gen[2] = 128;
     g.r_splits_gen[3] = 64;
+    if (const char* e = std::getenv("CC_TIGHT_GRID")) {
+        const std::vector<std::string> f = split_fields(e);
+        if (f.size() != 4) throw std::runtime_error("CC_TIGHT_GRID: la:r1,r2,r3,r4:g1,...:s1,s2,s3,s4");
+        parse_ints(f[0], &g.la_splits_init, 1);
+        parse_ints(f[1], g.r_splits_init, 4);
+        g.num_generations = f[2].empty() ? 0 : parse_ints(f[2], g.la_splits_gen, CC_MAX_GENERATIONS);
+        parse_ints(f[3], g.r_splits_gen, 4);
+    }
     return g;
 }
 

@@ -196,6 +196,19 @@ typedef struct cc_sb_prove_stats {
     uint64_t widening_samples;
     double widening_mean;
     double widening_max;
+    /* FP64 certification of the FP32 decisions: leaf verdicts the FP32-first
+     * passes (uneven split, multi-disk strip) decided "true", certified by
+     * the FP64 criterion from that placement on; anchors of the pre-filter's
+     * empty leaves certified by the FP64 emptiness test (one anchor certifies
+     * the run of empty leaves after it in its (r3, r4, r5) row: the test is
+     * monotone in the r6 piece); certifications that failed during the call
+     * (the FP64 verdict was used, a slice with a failed anchor was redone
+     * without the pre-filter; expected 0, counted per device).  The FP32
+     * "true" of the even split and of the r1-in-corner backtracking are
+     * decided by their FP64 form, whose verdict is the one used. */
+    uint64_t fp32_certified;
+    uint64_t empty_anchors;
+    uint64_t cert_failures;
 } cc_sb_prove_stats;
 
 /* summary of the final criticals vs the theoretical worst cases;
@@ -495,6 +508,32 @@ int cc_mlp_infer(cc_handle* h, const float* feat, size_t n, float* logits);
  * outcome[i] = deciding step (0..5 criterion, 6 R empty, 7 none: critical)
  * | 0x80 if a trap site was reached; evals[i] (may be NULL) = steps run. */
 int cc_tight_first(cc_handle* h, const double* soa, size_t n, int learned, uint8_t* outcome, uint8_t* evals);
+
+/* ---- adaptive refinement (no reference counterpart) ----------------------
+ * The near-critical stress workload: n tight boxes (host memory) refined by
+ * bisection up to max_depth levels.  Each level runs the certified
+ * evaluation of cc_tight_eval on all its boxes (device batches of up to 2^24
+ * boxes); a box that a criterion certifies, or whose R or R4 is empty, is
+ * done; a box that reached a trap site is kept as critical (flag 1); any
+ * other box is bisected at mid = 0.5 lo + 0.5 hi (rounded to nearest; the
+ * halves' union is the box) along lambda, r1, r2, r3, r4 in turn by depth
+ * (depth mod 5), and both halves go to the next level.  Boxes still
+ * undecided at the last level are kept as criticals (flag 2); the last level
+ * comes early when the next one would hold more than max_live boxes (0: 2^26),
+ * which stats->stopped_at_cap reports.  *criticals / *flags (cc_free) in
+ * level order.  cc_interrupt stops after the current level. */
+#define CC_REFINE_MAX_DEPTH 48
+typedef struct cc_refine_stats {
+    uint64_t live[CC_REFINE_MAX_DEPTH + 1];    /* boxes evaluated at each depth */
+    uint64_t decided[CC_REFINE_MAX_DEPTH + 1]; /* of which certified or empty */
+    float ms[CC_REFINE_MAX_DEPTH + 1];         /* device time of each depth (CUDA events) */
+    int32_t depths_run;
+    int32_t stopped_at_cap;
+    double seconds;                            /* wall time of the call */
+    uint64_t kernel_launches;
+} cc_refine_stats;
+int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n, int max_depth, size_t max_live,
+                    cc_tight_box** criticals, uint32_t** flags, size_t* n_crit, cc_refine_stats* stats);
 
 /* Ask a running proof on this handle to stop (the reference's Ctrl-C
  * behaviour, interrupt.cpp:30-46).  cc_tight_prove stops after the current

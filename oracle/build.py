@@ -88,6 +88,17 @@ def build_ref(ref=None, force=False):
     return os.path.join(REF_OUT, "libccref.so")
 
 
+def build_ref_fenv(ref=None):
+    """The fesetround variant of the reference criteria library
+    (oracle/_ref/libccref_fe.so), for the CPU baseline's timing; None where
+    the reference sources are not available."""
+    ref = ref or os.environ.get("CC_REFERENCE_PROVER") or reference_dir()
+    if not ref or not os.path.isdir(ref):
+        return None
+    _run(["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + ref, "-j%d" % (os.cpu_count() or 4), "fenv"])
+    return os.path.join(REF_OUT, "libccref_fe.so")
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=None)

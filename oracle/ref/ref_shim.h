@@ -44,16 +44,26 @@ inline void exit() noexcept {}
 extern "C" int cc_ref_printf(const char* fmt, ...);
 #define printf cc_ref_printf
 
-static inline double __dadd_rd(double a, double b) { CC_SHIM_TICK(); return cc_sw_add_rd(a, b); }
-static inline double __dadd_ru(double a, double b) { CC_SHIM_TICK(); return cc_sw_add_ru(a, b); }
-static inline double __dmul_rd(double a, double b) { CC_SHIM_TICK(); return cc_sw_mul_rd(a, b); }
-static inline double __dmul_ru(double a, double b) { CC_SHIM_TICK(); return cc_sw_mul_ru(a, b); }
-static inline double __ddiv_rd(double a, double b) { CC_SHIM_TICK(); return cc_sw_div_rd(a, b); }
-static inline double __ddiv_ru(double a, double b) { CC_SHIM_TICK(); return cc_sw_div_ru(a, b); }
-static inline double __dsqrt_rd(double a) { CC_SHIM_TICK(); return cc_sw_sqrt_rd(a); }
-static inline double __dsqrt_ru(double a) { CC_SHIM_TICK(); return cc_sw_sqrt_ru(a); }
-static inline double __drcp_rd(double a) { CC_SHIM_TICK(); return cc_sw_rcp_rd(a); }
-static inline double __drcp_ru(double a) { CC_SHIM_TICK(); return cc_sw_rcp_ru(a); }
+/* CC_REF_FENV selects the fesetround implementation of every operation (the
+ * slow exact form; libccref_fe.so, for timing only); the default is the
+ * error-free-transform form */
+#ifdef CC_REF_FENV
+#define CC_REF_ROUND(op) cc_fe_##op
+static inline double cc_fe_rcp_rd(double a) { return cc_fe_div_rd(1.0, a); }
+static inline double cc_fe_rcp_ru(double a) { return cc_fe_div_ru(1.0, a); }
+#else
+#define CC_REF_ROUND(op) cc_sw_##op
+#endif
+static inline double __dadd_rd(double a, double b) { CC_SHIM_TICK(); return CC_REF_ROUND(add_rd)(a, b); }
+static inline double __dadd_ru(double a, double b) { CC_SHIM_TICK(); return CC_REF_ROUND(add_ru)(a, b); }
+static inline double __dmul_rd(double a, double b) { CC_SHIM_TICK(); return CC_REF_ROUND(mul_rd)(a, b); }
+static inline double __dmul_ru(double a, double b) { CC_SHIM_TICK(); return CC_REF_ROUND(mul_ru)(a, b); }
+static inline double __ddiv_rd(double a, double b) { CC_SHIM_TICK(); return CC_REF_ROUND(div_rd)(a, b); }
+static inline double __ddiv_ru(double a, double b) { CC_SHIM_TICK(); return CC_REF_ROUND(div_ru)(a, b); }
+static inline double __dsqrt_rd(double a) { CC_SHIM_TICK(); return CC_REF_ROUND(sqrt_rd)(a); }
+static inline double __dsqrt_ru(double a) { CC_SHIM_TICK(); return CC_REF_ROUND(sqrt_ru)(a); }
+static inline double __drcp_rd(double a) { CC_SHIM_TICK(); return CC_REF_ROUND(rcp_rd)(a); }
+static inline double __drcp_ru(double a) { CC_SHIM_TICK(); return CC_REF_ROUND(rcp_ru)(a); }
 
 #define CC_REF_F32(name, mode, expr)                                          \
     static inline float name(float a, float b) {                             \
