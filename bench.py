@@ -459,7 +459,7 @@ PROOFS = {
 }
 
 
-def proof_comparison(prover, which="full"):
+def proof_comparison(prover, which="full", n_microbench_records=10_000_000):
     """Wall time of a whole tight proof in three forms, all with identical
     criticals, generation sizes and leaf counts:
       plain    -- every criterion re-evaluated in every cell, the reference's
@@ -483,18 +483,38 @@ def proof_comparison(prover, which="full"):
     rec, ncells = learn.proof_records(prover, root, cg.make_grid(la0, r0), per_cell=16)
     hist = learn.train(prover, rec, epochs=4, batch=8192)
     train_s = time.perf_counter() - t0
-    rep = learn.prediction_report(learn.predict(prover, rec), rec.labels_np)
+    logits_proof = learn.predict(prover, rec)
+    rep = learn.prediction_report(logits_proof, rec.labels_np)
     res = {}
     for name, kw in (("batched", {}), ("learned", {"learned": True}), ("plain", {"plain": True})):
         t0 = time.perf_counter()
         crit, st = prover.tight_find_critical_intervals(root, grid, **kw)
         res[name] = (time.perf_counter() - t0, crit, st)
+    # the same network trained instead on ~1e7 records of the criteria
+    # microbench (boxes labelled by their verdict masks), driving the same proof
+    t0 = time.perf_counter()
+    prover.mlp_init(4)
+    rec_mb = learn.Records(prover, W.tight_microbench(n_microbench_records, seed=44))
+    hist_mb = learn.train(prover, rec_mb, epochs=4, batch=8192)
+    train_mb_s = time.perf_counter() - t0
+    rep_mb = learn.prediction_report(learn.predict(prover, rec), rec.labels_np)  # on the proof's own records
+    del rec_mb
+    t0 = time.perf_counter()
+    crit, st = prover.tight_find_critical_intervals(root, grid, learned=True)
+    res["learned_microbench"] = (time.perf_counter() - t0, crit, st)
     bt, bc, bs = res["batched"]
     keys = ("gen_sizes", "leaf_evals", "trapped_leaves")
     same = all(np.array_equal(r[1].view(np.uint64), bc.view(np.uint64)) and all(r[2][k] == bs[k] for k in keys)
                for r in res.values())
+    split_pred = logits_proof[:, 6] > 0
     out.update({"plain_s": res["plain"][0], "batched_s": bt, "learned_s": res["learned"][0],
                 "speedup_batched": res["plain"][0] / bt, "speedup_learned": res["plain"][0] / res["learned"][0],
+                "learned_microbench_s": res["learned_microbench"][0],
+                "speedup_learned_microbench": res["plain"][0] / res["learned_microbench"][0],
+                "training_microbench": {"records": n_microbench_records, "seconds": train_mb_s, "loss": hist_mb,
+                                        "error_rate_per_output_on_proof_records": rep_mb["error_rate_per_output"]},
+                "split_output": {"error_rate": rep["split_error_rate"],
+                                 "predicted_split_share": float(split_pred.mean()), "acted_on": False},
                 "leaves": bs["leaf_evals"], "criticals": len(bc), "gen_sizes": bs["gen_sizes"],
                 "identical_criticals": bool(same),
                 "identical_trace_plain_batched": bool(res["plain"][2]["digest"] == bs["digest"]),
@@ -576,6 +596,42 @@ def sb_proof_run(prover, warm=True):
                               "failures": st["cert_failures"]}}
 
 
+SB_FULL = {
+    # the reference's own size-bound proof (rectangle_size_bound.cu:36-62,
+    # 312-382): lambda in [1, 2.5], 256 x 128 x 128 tasks, r3..r6 in 64, one
+    # refinement generation (lambda x 64, r 32,32,16,16,16,32)
+    "sb_reference": ("size-bound proof, the reference's own: lambda [1, 2.5] x 256, r1 x 128, r2 x 128, r3..r6 x 64, "
+                     "1 refinement generation (lambda x 64, r 32,32,16,16,16,32)", (1.0, 2.5),
+                     (256, (128, 128, 64, 64, 64, 64), 64, (32, 32, 16, 16, 16, 32), 1)),
+    # the size-bound run over lambda in [1, 8]: 1024 lambda pieces x 256 r1
+    # pieces (r2 and r3..r6 as the reference), refinement generations with
+    # the reference's refinement splits while criticals remain, at most 24
+    "config3": ("size-bound proof, lambda [1, 8] x 1024, r1 x 256, r2 x 128, r3..r6 x 64, up to 24 refinement "
+                "generations (lambda x 64, r 32,32,16,16,16,32)", (1.0, 8.0),
+                (1024, (256, 128, 64, 64, 64, 64), 64, (32, 32, 16, 16, 16, 32), 24)),
+}
+
+
+def sb_full_run(prover, which):
+    """A whole size-bound proof (SB_FULL) in the batched, certified form."""
+    import circlecover_gb300 as cg
+    from circlecover_gb300 import workloads as W
+    desc, (la_lo, la_hi), (la0, r0, lag, rg, gens) = SB_FULL[which]
+    prover.sb_find_critical_intervals(W.sb_root(1.0, 1.01), cg.make_sb_grid(1, (2, 2, 2, 2, 2, 2)))  # buffers
+    t0 = time.perf_counter()
+    crit, flags, st = prover.sb_find_critical_intervals(W.sb_root(la_lo, la_hi), cg.make_sb_grid(la0, r0, lag, rg, gens))
+    dt = time.perf_counter() - t0
+    return {"workload": desc, "seconds": dt, "leaves": st["leaf_evals"], "leaves_per_s": st["leaf_evals"] / dt,
+            "criticals": int(len(crit)), "trapped": int(flags.sum()), "gen_sizes": st["gen_sizes"],
+            "task_counts": st["task_counts"], "leaf_outcomes": st["leaf_counts"], "digest": st["digest"],
+            "kernel_launches": st["kernel_launches"],
+            "fp32_prefilter": {"decided_empty": st["fp32_decided"],
+                               "decided_share": st["fp32_decided"] / max(1, st["leaf_evals"]),
+                               "widening_R_mean": st["widening_mean"], "widening_R_max": st["widening_max"]},
+            "certification": {"fp32_true_certified": st["fp32_certified"],
+                              "empty_anchors_certified": st["empty_anchors"], "failures": st["cert_failures"]}}
+
+
 def sb_forms(prover):
     """The size-bound proof in its three forms on a smaller workload (lambda
     [1, 1.1] x 8, r1 x 32, r2 x 32, r3..r6 x 16): plain (one thread runs a
@@ -613,9 +669,19 @@ def main():
     ap.add_argument("--no-proof", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="tight_eval",
-                    choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof", "config1", "cpu_variants"])
+                    choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof", "config1", "cpu_variants",
+                             "sb_reference", "config3"])
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload in SB_FULL:  # a whole size-bound proof (minutes)
+        import __graft_entry__
+        __graft_entry__.build()
+        import circlecover_gb300 as cg
+        with cg.Prover(local) as prover:
+            r = sb_full_run(prover, args.workload)
+            if rank == 0:
+                print(json.dumps(r), flush=True)
+        return
     if args.workload == "cpu_variants":  # the CPU implementations side by side (no GPU)
         print(json.dumps(cpu_variants(args.cpu_sample)), flush=True)
         return

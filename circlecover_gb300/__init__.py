@@ -215,6 +215,7 @@ EXPORTS = [
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
     "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume", "cc_last_eval_counts", "cc_set_eval_graph",
     "cc_eval_graph_stats", "cc_set_eval_certify", "cc_last_eval_cert", "cc_tight_refine",
+    "cc_sb_generation",
 ]
 
 MLP_PARAMS = 5319
@@ -513,6 +514,33 @@ class Prover:
         d["empty_anchors"] = int(st.empty_anchors)
         d["cert_failures"] = int(st.cert_failures)
         return arr, fl, d
+
+    def sb_generation(self, parents, gen, la_splits, r_splits, lo=0, hi=(1 << 64) - 1, fp32=True):
+        """One size-bound generation over the tasks [lo, hi)
+        (cc_sb_generation): (criticals, flags, stats)."""
+        parents = np.ascontiguousarray(np.asarray(parents, dtype=SB_BOX).reshape(-1))
+        rs = (ctypes.c_int * 6)(*r_splits)
+        out = ctypes.c_void_p()
+        fl = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcSbProveStats()
+        f = self.lib.cc_sb_generation
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                      ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                      ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(CcSbProveStats)]
+        self._check(f(self.h, parents.ctypes.data if len(parents) else None, len(parents), gen, la_splits, rs, lo, hi,
+                      0 if fp32 else 2, ctypes.byref(out), ctypes.byref(n), ctypes.byref(fl), ctypes.byref(st)),
+                    "cc_sb_generation")
+        arr = np.zeros(n.value, dtype=SB_BOX)
+        flags = np.zeros(n.value, dtype=np.uint32)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * SB_BOX.itemsize)
+            ctypes.memmove(flags.ctypes.data, fl.value, n.value * 4)
+        self.lib.cc_free(out)
+        self.lib.cc_free(fl)
+        d = sb_stats_to_dict(st)
+        d["cert_failures"] = int(st.cert_failures)
+        return arr, flags, d
 
     # ---- learned strategy ordering (device pointers are raw ints, e.g.
     # torch.Tensor.data_ptr())

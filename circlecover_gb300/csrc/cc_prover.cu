@@ -228,53 +228,105 @@ __global__ void __launch_bounds__(128) k_eval_collect(size_t n, uint32_t* __rest
 // A record group's state byte names the call that settled the criterion
 // (bits 2-4, 1-based; 0: none); without record buffers every call is
 // evaluated.  Failures go to the repair queue.
-// Each block takes 128 consecutive jobs at a time and sorts them by the
-// call that settled the FP32 run (the three-strip group: by its bits) in
-// shared memory, so that a warp's lanes mostly certify the same call and
-// take the same path through the FP64 criterion.
+// Each block takes a window of 1024 consecutive jobs at a time and sorts it
+// in shared memory by a path key: the call that settled the FP32 run (the
+// three-strip group: its bits) and the box features that select the
+// criterion's blocks on the way to that call (the r1 placements exist for r1
+// above 1/4 -- the strip -- and below 1/2 -- the corner; r1_r2's side by side
+// needs r2 above 1/4, its stacked placement r1 up to 1/2; the leaf criterion's
+// strips need r3 above 1/4), so that the lanes of a warp mostly run the same
+// path through the FP64 criterion.
+constexpr int kCertWindow = 1024;
+constexpr int kCertKeys = 64;
+
+template <Layout L, int K>
+__device__ __forceinline__ int cert_path_key(const double* __restrict__ in, size_t n, uint32_t i, int call) {
+    auto lo = [&](int k) -> double {  // lower bound of interval k (0 la, 1..4 r1..r4)
+        return L == Layout::SoA ? __ldg(in + (size_t)(2 * k) * n + i) : __ldg(in + (size_t)i * 10 + 2 * k);
+    };
+    int f = 0;
+    if (K == 0) {
+        const double r1 = lo(1);
+        f = (r1 > 0.25 ? 2 : 0) | (r1 < 0.5 ? 1 : 0);
+    } else if (K == 1) {
+        f = (lo(2) > 0.25 ? 2 : 0) | (lo(1) <= 0.5 ? 1 : 0);
+    } else if (K == 3) {
+        f = lo(3) > 0.25 ? 1 : 0;
+    }
+    return ((call & 7) << 3) | f;
+}
+
 template <Layout L, int K>
 __global__ void __launch_bounds__(128) k_eval_cert(const double* __restrict__ in, size_t n, EvalQueues q) {
-    __shared__ uint32_t s_box[128];
-    __shared__ uint8_t s_key[128];
-    __shared__ int s_cnt[8];
+    __shared__ uint32_t s_box[kCertWindow];
+    __shared__ uint8_t s_key[kCertWindow];
+    __shared__ int s_cnt[kCertKeys + 1];
+    constexpr int kPer = kCertWindow / 128;
     const unsigned long long c = q.counts[kCntCert + K];
     const unsigned long long nq = c < q.cap ? c : q.cap;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long stride = (unsigned long long)gridDim.x * kCertWindow;
     // block-uniform loop: every thread of the block runs every iteration
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < nq; base += stride) {
-        if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * kCertWindow; base < nq; base += stride) {
+        for (int k = threadIdx.x; k <= kCertKeys; k += 128) s_cnt[k] = 0;
         __syncthreads();
-        const unsigned long long j = base + threadIdx.x;
-        uint32_t i = 0;
-        int key = 7;  // past the end: sorted last
-        if (j < nq) {
-            i = q.cert[K][j];
-            if (K < kRecGroups) key = q.states ? (int)((q.states[(size_t)K * n + i] >> 2) & 7) : 6;
-            else key = q.cflags[i] & 3;
+        uint32_t box[kPer];
+        int key[kPer], rank[kPer];
+#pragma unroll
+        for (int t = 0; t < kPer; ++t) {
+            const unsigned long long j = base + (unsigned long long)t * 128 + threadIdx.x;
+            box[t] = 0;
+            key[t] = kCertKeys;  // past the end: sorted last
+            if (j < nq) {
+                box[t] = q.cert[K][j];
+                if (K < kRecGroups) {
+                    const int call = q.states ? (int)((q.states[(size_t)K * n + box[t]] >> 2) & 7) : 6;
+                    key[t] = cert_path_key<L, K>(in, n, box[t], call);
+                } else {
+                    key[t] = q.cflags[box[t]] & 3;
+                }
+            }
+            rank[t] = atomicAdd(&s_cnt[key[t]], 1);
         }
-        const int rank = atomicAdd(&s_cnt[key], 1);
         __syncthreads();
-        int off = rank;
-        for (int k = 0; k < key; ++k) off += s_cnt[k];
-        s_box[off] = i;
-        s_key[off] = (uint8_t)key;
-        __syncthreads();
-        const uint32_t b_i = s_box[threadIdx.x];
-        const int b_key = s_key[threadIdx.x];
-        const bool valid = b_key != 7;
-        bool fail = false;
-        if (valid) {
-            const ct::Box b = load_box<L>(in, n, b_i);
-            if (K < kRecGroups) {
-                fail = !ct::certify_group<rec_group(K)>(b, q.states ? b_key : -1);
-            } else {
-                fail = !ct::certify_r123(b, ((b_key & 1) ? (1u << 2) : 0u) | ((b_key & 2) ? (1u << 6) : 0u));
+        if (threadIdx.x == 0) {  // exclusive prefix over the keys
+            int acc = 0;
+            for (int k = 0; k <= kCertKeys; ++k) {
+                const int v = s_cnt[k];
+                s_cnt[k] = acc;
+                acc += v;
             }
         }
-        __syncwarp();
-        const unsigned long long s = cc::prove::warp_append(&q.counts[kCntRepair], valid && fail, q.cap,
-                                                            &q.counts[kCntOverflow]);
-        if (s != ~0ULL) q.repair[s] = b_i;
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < kPer; ++t) {
+            const int off = s_cnt[key[t]] + rank[t];
+            s_box[off] = box[t];
+            s_key[off] = (uint8_t)(key[t] >> 3);  // the call (record groups)
+        }
+        __syncthreads();
+        const unsigned long long left = nq - base;
+        const int valid_n = left < (unsigned long long)kCertWindow ? (int)left : kCertWindow;
+#pragma unroll 1
+        for (int t = 0; t < kPer; ++t) {
+            const int slot = t * 128 + threadIdx.x;
+            const bool valid = slot < valid_n;
+            bool fail = false;
+            uint32_t b_i = 0;
+            if (valid) {
+                b_i = s_box[slot];
+                const ct::Box b = load_box<L>(in, n, b_i);
+                if (K < kRecGroups) {
+                    fail = !ct::certify_group<rec_group(K)>(b, q.states ? (int)s_key[slot] : -1);
+                } else {
+                    const uint8_t f = q.cflags[b_i];
+                    fail = !ct::certify_r123(b, ((f & 1) ? (1u << 2) : 0u) | ((f & 2) ? (1u << 6) : 0u));
+                }
+            }
+            __syncwarp();
+            const unsigned long long s = cc::prove::warp_append(&q.counts[kCntRepair], valid && fail, q.cap,
+                                                                &q.counts[kCntOverflow]);
+            if (s != ~0ULL) q.repair[s] = b_i;
+        }
         __syncthreads();  // s_cnt and the sorted arrays are rewritten next iteration
     }
 }

@@ -1237,7 +1237,8 @@ int drain_criticals(Engine& e) {
 // A generation after the first stops at a chunk boundary when cc_interrupt
 // was called (the initial pass is not interruptible, as in the reference:
 // rectangle_size_bound.cu:325, 341).
-int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla, const int* rn) {
+int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla, const int* rn,
+                   unsigned long long task_lo = 0, unsigned long long task_hi = ~0ULL) {
     int st;
     void* p;
     if ((st = ccrt::ensure(e.h, kSlotBase + S_PARENTS, parents.size() * sizeof(Box6), &p))) return st;
@@ -1252,9 +1253,10 @@ int run_generation(Engine& e, const std::vector<Box6>& parents, int gen, int nla
     if (chunk < 1) chunk = 1;
     TaskGrid tg{gen, nla, rn[0], rn[1], rn[3], rn[4], rn[5], per_parent};
     LeafGrid lg{gen, rn[3], rn[4], rn[5], 0u, 0ULL};
-    for (unsigned long long t0 = 0; t0 < ntasks; t0 += chunk) {
+    const unsigned long long t_end = task_hi < ntasks ? task_hi : ntasks;
+    for (unsigned long long t0 = task_lo; t0 < t_end; t0 += chunk) {
         if (gen > 0 && e.h->interrupt.load()) return CC_ERR_INTERRUPTED;
-        const unsigned long long t1 = t0 + chunk < ntasks ? t0 + chunk : ntasks;
+        const unsigned long long t1 = t0 + chunk < t_end ? t0 + chunk : t_end;
         CC_CUDA(e.h, cudaMemsetAsync(e.dc, 0, 2 * sizeof(unsigned long long), e.s));  // n_task, n_cell
         int tgrid = (int)std::min<unsigned long long>((t1 - t0 + kThreads - 1) / kThreads, (unsigned long long)e.grid);
         k_sbp_tasks<<<tgrid, kThreads, 0, e.s>>>(e.parents, t0, t1, tg, e.tasks, chunk, e.dc);
@@ -1407,20 +1409,8 @@ static unsigned long long sb_cert_failures_so_far() {
     return v + cc::cert_failures_host.load();
 }
 
-extern "C" int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, int options,
-                              cc_sb_box** criticals, size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats) {
-    if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
-    if (!grid_ok(grid)) return ccrt::fail(h, CC_ERR_PARAM, "cc_sb_prove: split counts must be in [1, 2047]");
-    const auto t_start = std::chrono::steady_clock::now();
-    const unsigned long long fails0 = sb_cert_failures_so_far();
-    h->launches = 0;
-    h->interrupt.store(0);
-    CC_CUDA(h, cudaSetDevice(h->device));
-    *criticals = nullptr;
-    *n_crit = 0;
-    if (flags) *flags = nullptr;
-
-    Engine e;
+// the engine's device buffers and work-unit sizes (shared by the entry points)
+static int engine_setup(cc_handle* h, int options, Engine& e) {
     e.h = h;
     e.plain = (options & CC_PROVE_PLAIN) != 0;
     e.fp32 = !e.plain && !(options & CC_SB_NO_FP32_PREFILTER);
@@ -1460,6 +1450,47 @@ extern "C" int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_g
     e.hc = (SbCounters*)h->pinned;
     CC_CUDA(h, cudaMemsetAsync(e.dc, 0, sizeof(SbCounters), e.s));
 
+    return CC_OK;
+}
+
+static int fill_stats(Engine& e, cc_sb_prove_stats* stats, uint64_t trapped_leaves, const std::vector<uint64_t>& gen_sizes,
+                      int generations_run, std::chrono::steady_clock::time_point t_start, unsigned long long fails0);
+
+// criticals of a generation, merged as the reference merges that generation
+// (rectangle_size_bound.cu:351-362), to caller-owned arrays
+static int emit_criticals(cc_handle* h, std::vector<Crit>& cur, cc_sb_box** criticals, size_t* n_crit,
+                          uint32_t** flags) {
+    *n_crit = cur.size();
+    *criticals = (cc_sb_box*)std::malloc(sizeof(cc_sb_box) * (cur.size() + 1));
+    if (flags) *flags = (uint32_t*)std::malloc(sizeof(uint32_t) * (cur.size() + 1));
+    if (!*criticals || (flags && !*flags)) return ccrt::fail(h, CC_ERR_OOM, "cc_sb_prove: host allocation");
+    for (size_t i = 0; i < cur.size(); ++i) {
+        (*criticals)[i].la = cc_iv{cur[i].box.la.lo, cur[i].box.la.hi};
+        for (int k = 0; k < 6; ++k) (*criticals)[i].r[k] = cc_iv{cur[i].box.r[k].lo, cur[i].box.r[k].hi};
+        if (flags) (*flags)[i] = cur[i].trapped;
+    }
+    return CC_OK;
+}
+
+static int merge_width(int gen) { return gen == 0 ? 0 : (gen % 3 == 0 ? 3 : (gen % 3 == 1 ? 2 : 1)); }
+
+extern "C" int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, int options,
+                              cc_sb_box** criticals, size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats) {
+    if (!h || !root || !grid || !criticals || !n_crit) return CC_ERR_PARAM;
+    if (!grid_ok(grid)) return ccrt::fail(h, CC_ERR_PARAM, "cc_sb_prove: split counts must be in [1, 2047]");
+    const auto t_start = std::chrono::steady_clock::now();
+    const unsigned long long fails0 = sb_cert_failures_so_far();
+    h->launches = 0;
+    h->interrupt.store(0);
+    CC_CUDA(h, cudaSetDevice(h->device));
+    *criticals = nullptr;
+    *n_crit = 0;
+    if (flags) *flags = nullptr;
+
+    Engine e;
+    int st = engine_setup(h, options, e);
+    if (st) return st;
+
     std::vector<uint64_t> gen_sizes;
     int generations_run = 0;
     uint64_t trapped_leaves = 0;
@@ -1488,22 +1519,21 @@ extern "C" int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_g
             found[i].trapped = (uint32_t)(e.found[i].idx >> 63);
             trapped_leaves += found[i].trapped;
         }
-        const int n_merged = gen == 0 ? 0 : (gen % 3 == 0 ? 3 : (gen % 3 == 1 ? 2 : 1));
-        cur = merge(found, n_merged);
+        cur = merge(found, merge_width(gen));
         gen_sizes.push_back(cur.size());
         if (gen > 0) generations_run = gen;
     }
 
-    *n_crit = cur.size();
-    *criticals = (cc_sb_box*)std::malloc(sizeof(cc_sb_box) * (cur.size() + 1));
-    if (flags) *flags = (uint32_t*)std::malloc(sizeof(uint32_t) * (cur.size() + 1));
-    if (!*criticals || (flags && !*flags)) return ccrt::fail(h, CC_ERR_OOM, "cc_sb_prove: host allocation");
-    for (size_t i = 0; i < cur.size(); ++i) {
-        (*criticals)[i].la = cc_iv{cur[i].box.la.lo, cur[i].box.la.hi};
-        for (int k = 0; k < 6; ++k) (*criticals)[i].r[k] = cc_iv{cur[i].box.r[k].lo, cur[i].box.r[k].hi};
-        if (flags) (*flags)[i] = cur[i].trapped;
-    }
-    if (stats) {
+    if ((st = emit_criticals(h, cur, criticals, n_crit, flags))) return st;
+    if (stats && (st = fill_stats(e, stats, trapped_leaves, gen_sizes, generations_run, t_start, fails0))) return st;
+    return status;
+}
+
+static int fill_stats(Engine& e, cc_sb_prove_stats* stats, uint64_t trapped_leaves, const std::vector<uint64_t>& gen_sizes,
+                      int generations_run, std::chrono::steady_clock::time_point t_start, unsigned long long fails0) {
+    cc_handle* h = e.h;
+    int st;
+    {
         std::memset(stats, 0, sizeof(*stats));
         if ((st = sync_counters(e))) return st;
         std::memcpy(stats->task_counts, e.hc->task_counts, sizeof(stats->task_counts));
@@ -1527,5 +1557,54 @@ extern "C" int cc_sb_prove_ex(cc_handle* h, const cc_sb_box* root, const cc_sb_g
         stats->empty_anchors = e.empty_anchors;
         stats->cert_failures = sb_cert_failures_so_far() - fails0;
     }
-    return status;
+    return CC_OK;
+}
+
+// One generation of the size-bound proof over the tasks [task_lo, task_hi)
+// (task = parent * (la x r1 x r2 splits) + lambda piece * (r1 x r2) + r1
+// piece * r2 splits + r2 piece; rectangle_size_bound.cu:276-310), criticals
+// merged as the reference merges generation `gen`.
+extern "C" int cc_sb_generation(cc_handle* h, const cc_sb_box* parents, size_t n_parents, int gen, int la_splits,
+                                const int r_splits[6], uint64_t task_lo, uint64_t task_hi, int options,
+                                cc_sb_box** criticals, size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats) {
+    if (!h || (n_parents && !parents) || !r_splits || !criticals || !n_crit || task_lo > task_hi || gen < 0 ||
+        gen > CC_MAX_GENERATIONS)
+        return CC_ERR_PARAM;
+    cc_sb_grid g{};
+    g.la_splits_init = la_splits;
+    g.la_splits_gen = la_splits;
+    for (int k = 0; k < 6; ++k) g.r_splits_init[k] = g.r_splits_gen[k] = r_splits[k];
+    if (!grid_ok(&g)) return ccrt::fail(h, CC_ERR_PARAM, "cc_sb_generation: split counts must be in [1, 2047]");
+    const auto t_start = std::chrono::steady_clock::now();
+    const unsigned long long fails0 = sb_cert_failures_so_far();
+    h->launches = 0;
+    h->interrupt.store(0);
+    CC_CUDA(h, cudaSetDevice(h->device));
+    *criticals = nullptr;
+    *n_crit = 0;
+    if (flags) *flags = nullptr;
+    Engine e;
+    int st = engine_setup(h, options, e);
+    if (st) return st;
+    std::vector<Box6> ps(n_parents);
+    for (size_t i = 0; i < n_parents; ++i) {
+        ps[i].la = Iv{parents[i].la.lb, parents[i].la.ub};
+        for (int k = 0; k < 6; ++k) ps[i].r[k] = Iv{parents[i].r[k].lb, parents[i].r[k].ub};
+    }
+    e.found.clear();
+    if (n_parents && (st = run_generation(e, ps, gen, la_splits, r_splits, task_lo, task_hi))) return st;
+    std::vector<Crit> found(e.found.size());
+    uint64_t trapped_leaves = 0;
+    for (size_t i = 0; i < e.found.size(); ++i) {
+        found[i].box = e.found[i].box;
+        found[i].trapped = (uint32_t)(e.found[i].idx >> 63);
+        trapped_leaves += found[i].trapped;
+    }
+    std::vector<Crit> cur = merge(found, merge_width(gen));
+    if ((st = emit_criticals(h, cur, criticals, n_crit, flags))) return st;
+    if (stats) {
+        const std::vector<uint64_t> sizes{cur.size()};
+        if ((st = fill_stats(e, stats, trapped_leaves, sizes, 0, t_start, fails0))) return st;
+    }
+    return CC_OK;
 }

@@ -638,52 +638,81 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
 }
 
 // FP64 certification of the leaf verdicts the FP32 enclosures decided "true"
-// in stages 4a, 4a2 and 4b of the current slice: each block sorts its 128
-// jobs by (criterion, settling call) in shared memory, so that a warp's
-// lanes mostly run the same path, and runs the FP64 criterion with only that
-// call evaluated (tight::certify_leaf).  A failure is counted in fp32[3];
-// the host then redoes the chunk in the plain FP64 form.
+// in stages 4a, 4a2 and 4b of the current slice.  Each block takes windows
+// of 1024 jobs and sorts them in shared memory by a path key -- criterion,
+// the call that settled the FP32 run, and the box features that select the
+// criterion's placements on the way (2x2: r1 at least 1/2 takes the
+// one-strip form; leaf r1_r2_r3: r2 and r3 above 1/4, where their strips
+// exist) -- so that a warp's lanes mostly run the same path, then runs the
+// FP64 criterion with only that call evaluated (tight::certify_leaf).  A
+// failure is counted in fp32[3]; the host then redoes the chunk in the plain
+// FP64 form.
+constexpr int kLeafCertWindow = 1024;
+constexpr int kLeafCertKeys = 128;
 __global__ void __launch_bounds__(128) k_stage_cert(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
                                                     const CertLeaf* __restrict__ cq, int s4, Caps caps, Counters* c) {
-    __shared__ CertLeaf s_job[128];
-    __shared__ int s_cnt[32];
+    __shared__ CertLeaf s_job[kLeafCertWindow];
+    __shared__ int s_cnt[kLeafCertKeys + 1];
+    constexpr int kPer = kLeafCertWindow / 128;
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cert;
     const unsigned long long total = n_in < caps.leaf ? n_in : caps.leaf;
     unsigned ok_n = 0, fail_n = 0;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < total;
-         base += (unsigned long long)gridDim.x * blockDim.x) {
-        if (threadIdx.x < 32) s_cnt[threadIdx.x] = 0;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * kLeafCertWindow; base < total;
+         base += (unsigned long long)gridDim.x * kLeafCertWindow) {
+        for (int k = threadIdx.x; k <= kLeafCertKeys; k += 128) s_cnt[k] = 0;
         __syncthreads();
-        const unsigned long long j = base + threadIdx.x;
-        CertLeaf job{0, 0, 0, 0};
-        int key = 31;  // past the end: sorted last
-        if (j < total) {
-            job = cq[j];
-            key = (job.crit << 4) | (job.call < 15 ? job.call : 15);
-        }
-        const int rank = atomicAdd(&s_cnt[key], 1);
-        __syncthreads();
-        int off = rank;
-        for (int k = 0; k < key; ++k) off += s_cnt[k];
-        s_job[off] = job;
-        __syncthreads();
-        const bool valid = (int)threadIdx.x < (int)(total - base < 128 ? total - base : 128);
-        if (valid) {
-            const CertLeaf m = s_job[threadIdx.x];
-            const Cell4& p = cells[m.cell4];
-            const Task tk = tasks[p.task];
-            trap_clear();
-            const Box v = leaf_box(p, tk.la, subinterval(p.r4r, m.i4, s4));
-            bool ok;
-            if (m.crit == 0) {
-                Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
-                tighten_lb(R, 0.0);
-                ok = tight::certify_leaf(tight::TwoByTwo{}, v, R, m.call);
-            } else {
-                ok = tight::certify_leaf(tight::LeafR123{}, v, p.R4, m.call);
+        CertLeaf job[kPer];
+        int key[kPer], rank[kPer];
+#pragma unroll
+        for (int t = 0; t < kPer; ++t) {
+            const unsigned long long j = base + (unsigned long long)t * 128 + threadIdx.x;
+            job[t] = CertLeaf{0, 0, 0, 0};
+            key[t] = kLeafCertKeys;  // past the end: sorted last
+            if (j < total) {
+                job[t] = cq[j];
+                const Cell4& p = cells[job[t].cell4];
+                int f;
+                if (job[t].crit == 0) f = p.r1.lo >= 0.5 ? 1 : 0;
+                else f = (p.r2.lo > 0.25 ? 2 : 0) | (p.r3.lo > 0.25 ? 1 : 0);
+                key[t] = (job[t].crit << 6) | ((job[t].call < 15 ? job[t].call : 15) << 2) | f;
             }
-            if (ok) ++ok_n;
-            else ++fail_n;
+            rank[t] = atomicAdd(&s_cnt[key[t]], 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {  // exclusive prefix over the keys
+            int acc = 0;
+            for (int k = 0; k <= kLeafCertKeys; ++k) {
+                const int v = s_cnt[k];
+                s_cnt[k] = acc;
+                acc += v;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < kPer; ++t) s_job[s_cnt[key[t]] + rank[t]] = job[t];
+        __syncthreads();
+        const unsigned long long left = total - base;
+        const int valid_n = left < (unsigned long long)kLeafCertWindow ? (int)left : kLeafCertWindow;
+#pragma unroll 1
+        for (int t = 0; t < kPer; ++t) {
+            const int slot = t * 128 + threadIdx.x;
+            if (slot < valid_n) {
+                const CertLeaf m = s_job[slot];
+                const Cell4& p = cells[m.cell4];
+                const Task tk = tasks[p.task];
+                trap_clear();
+                const Box v = leaf_box(p, tk.la, subinterval(p.r4r, m.i4, s4));
+                bool ok;
+                if (m.crit == 0) {
+                    Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
+                    tighten_lb(R, 0.0);
+                    ok = tight::certify_leaf(tight::TwoByTwo{}, v, R, m.call);
+                } else {
+                    ok = tight::certify_leaf(tight::LeafR123{}, v, p.R4, m.call);
+                }
+                if (ok) ++ok_n;
+                else ++fail_n;
+            }
         }
         __syncthreads();  // s_cnt and s_job are rewritten next iteration
     }

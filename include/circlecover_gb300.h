@@ -468,6 +468,20 @@ int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, size_t n, cc_t
 int cc_sb_prove(cc_handle* h, const cc_sb_box* root, const cc_sb_grid* grid, cc_sb_box** criticals, size_t* n_crit,
                 uint32_t** flags, cc_sb_prove_stats* stats);
 
+/* One generation of the size-bound proof restricted to the tasks [task_lo,
+ * task_hi) of that generation (task = parent * (la_splits * r1 splits * r2
+ * splits) + lambda piece * (r1 * r2 splits) + r1 piece * r2 splits + r2
+ * piece, the order of the reference's host loops,
+ * rectangle_size_bound/rectangle_size_bound.cu:276-310); generation `gen`
+ * (0 = the initial pass) selects the trace keys and the merge of the found
+ * leaves (merge_critical_intervals<N> with N = 0 for gen 0, else 2, 1, 3 by
+ * gen mod 3; :351-362).  The unit the sampled parity tests of the full runs
+ * check against the reference's criteria; stats as cc_sb_prove (gen_sizes[0]
+ * = the criticals returned).  options as cc_sb_prove_ex. */
+int cc_sb_generation(cc_handle* h, const cc_sb_box* parents, size_t n_parents, int gen, int la_splits,
+                     const int r_splits[6], uint64_t task_lo, uint64_t task_hi, int options, cc_sb_box** criticals,
+                     size_t* n_crit, uint32_t** flags, cc_sb_prove_stats* stats);
+
 /* cc_sb_prove with options: CC_PROVE_PLAIN runs the plain form (one thread
  * per leaf runs the whole cascade, as the reference's kernel does; no
  * pre-filter); CC_SB_NO_FP32_PREFILTER keeps the batched passes but decides

@@ -142,6 +142,31 @@ class _Lib:
         return arr, stats_to_dict(st)
 
 
+    def sb_generation(self, parents, gen, la_splits, r_splits, lo=0, hi=(1 << 64) - 1, threads=1):
+        """One size-bound generation over the tasks [lo, hi) on the host,
+        merged as generation `gen`: (criticals, flags, stats dict)."""
+        from circlecover_gb300 import CcSbProveStats, sb_stats_to_dict
+        parents = np.ascontiguousarray(np.asarray(parents, dtype=SB_BOX).reshape(-1))
+        rs = (ctypes.c_int * 6)(*r_splits)
+        out = ctypes.c_void_p()
+        flags = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        st = CcSbProveStats()
+        f = getattr(self.lib, self.prefix + "_sb_generation")
+        f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                      ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                      ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p]
+        f(parents.ctypes.data if len(parents) else None, len(parents), gen, la_splits, rs, lo, hi, threads,
+          ctypes.byref(out), ctypes.byref(flags), ctypes.byref(n), ctypes.addressof(st))
+        arr = np.zeros(n.value, dtype=SB_BOX)
+        fl = np.zeros(n.value, dtype=np.uint32)
+        if n.value:
+            ctypes.memmove(arr.ctypes.data, out.value, n.value * SB_BOX.itemsize)
+            ctypes.memmove(fl.ctypes.data, flags.value, n.value * 4)
+        getattr(self.lib, self.prefix + "_free")(out)
+        getattr(self.lib, self.prefix + "_free")(flags)
+        return arr, fl, sb_stats_to_dict(st)
+
     def sb_prove(self, root, grid, threads=1):
         """The size-bound proof on the host: (criticals SB_BOX array, flags, stats dict)."""
         from circlecover_gb300 import CcSbProveStats, sb_stats_to_dict

@@ -287,12 +287,32 @@ int ccport_sb_eval(const cc_sb_box* boxes, size_t n, uint32_t* masks, uint64_t* 
     return 0;
 }
 
+static void port_sb_out(const SbDriver::Result& res, cc_sb_box** out, uint32_t** flags, size_t* n_out,
+                        cc_sb_prove_stats* stats);
+
+int ccport_sb_generation(const cc_sb_box* parents, size_t n, int gen, int la_splits, const int* r_splits, uint64_t lo,
+                         uint64_t hi, int threads, cc_sb_box** out, uint32_t** flags, size_t* n_out,
+                         cc_sb_prove_stats* stats) {
+    std::vector<csb::Box6> ps(n);
+    for (size_t i = 0; i < n; ++i) {
+        ps[i].la = to_iv(parents[i].la);
+        for (int k = 0; k < 6; ++k) ps[i].r[k] = to_iv(parents[i].r[k]);
+    }
+    port_sb_out(SbDriver::generation_range(ps, gen, la_splits, r_splits, threads, lo, hi), out, flags, n_out, stats);
+    return 0;
+}
+
 int ccport_sb_prove(const cc_sb_box* root, const cc_sb_grid* grid, int threads, cc_sb_box** out, uint32_t** flags,
                     size_t* n_out, cc_sb_prove_stats* stats) {
     csb::Box6 r;
     r.la = to_iv(root->la);
     for (int i = 0; i < 6; ++i) r.r[i] = to_iv(root->r[i]);
-    SbDriver::Result res = SbDriver::prove(r, *grid, threads);
+    port_sb_out(SbDriver::prove(r, *grid, threads), out, flags, n_out, stats);
+    return 0;
+}
+
+static void port_sb_out(const SbDriver::Result& res, cc_sb_box** out, uint32_t** flags, size_t* n_out,
+                        cc_sb_prove_stats* stats) {
     size_t n = res.criticals.size();
     *n_out = n;
     *out = (cc_sb_box*)std::malloc(sizeof(cc_sb_box) * (n + 1));
@@ -315,7 +335,6 @@ int ccport_sb_prove(const cc_sb_box* root, const cc_sb_grid* grid, int threads, 
         for (size_t g = 0; g < res.gen_sizes.size() && g <= CC_MAX_GENERATIONS; ++g) stats->gen_sizes[g] = res.gen_sizes[g];
         stats->generations_run = res.generations_run;
     }
-    return 0;
 }
 
 /* interval times scalar, for the rounding test */

@@ -239,13 +239,36 @@ extern "C" int ccref_sb_eval(const cc_sb_box* boxes, size_t n, uint32_t* masks, 
     return 0;
 }
 
+static void sb_result_out(const cc_oracle::SbDriver<RefSbC>::Result& res, cc_sb_box** out, uint32_t** flags,
+                          size_t* n_out, cc_sb_prove_stats* stats);
+
+/* one generation over the tasks [lo, hi) of the parents, merged as
+ * generation gen (the sampled-range oracle of the full size-bound runs) */
+extern "C" int ccref_sb_generation(const cc_sb_box* parents, size_t n, int gen, int la_splits, const int* r_splits,
+                                   uint64_t lo, uint64_t hi, int threads, cc_sb_box** out, uint32_t** flags,
+                                   size_t* n_out, cc_sb_prove_stats* stats) {
+    using Driver = cc_oracle::SbDriver<RefSbC>;
+    std::vector<rsb::Variables> ps(n);
+    for (size_t i = 0; i < n; ++i) {
+        ps[i].la = IV(parents[i].la.lb, parents[i].la.ub);
+        for (int k = 0; k < 6; ++k) ps[i].radii[k] = IV(parents[i].r[k].lb, parents[i].r[k].ub);
+    }
+    sb_result_out(Driver::generation_range(ps, gen, la_splits, r_splits, threads, lo, hi), out, flags, n_out, stats);
+    return 0;
+}
+
 extern "C" int ccref_sb_prove(const cc_sb_box* root, const cc_sb_grid* grid, int threads, cc_sb_box** out,
                               uint32_t** flags, size_t* n_out, cc_sb_prove_stats* stats) {
     using Driver = cc_oracle::SbDriver<RefSbC>;
     rsb::Variables r;
     r.la = IV(root->la.lb, root->la.ub);
     for (int i = 0; i < 6; ++i) r.radii[i] = IV(root->r[i].lb, root->r[i].ub);
-    Driver::Result res = Driver::prove(r, *grid, threads);
+    sb_result_out(Driver::prove(r, *grid, threads), out, flags, n_out, stats);
+    return 0;
+}
+
+static void sb_result_out(const cc_oracle::SbDriver<RefSbC>::Result& res, cc_sb_box** out, uint32_t** flags,
+                          size_t* n_out, cc_sb_prove_stats* stats) {
     size_t n = res.criticals.size();
     *n_out = n;
     *out = (cc_sb_box*)std::malloc(sizeof(cc_sb_box) * (n + 1));
@@ -268,7 +291,6 @@ extern "C" int ccref_sb_prove(const cc_sb_box* root, const cc_sb_grid* grid, int
         for (size_t g = 0; g < res.gen_sizes.size() && g <= CC_MAX_GENERATIONS; ++g) stats->gen_sizes[g] = res.gen_sizes[g];
         stats->generations_run = res.generations_run;
     }
-    return 0;
 }
 
 /* the box of one task of find_critical_intervals_in (r1 tightened across the

@@ -150,14 +150,17 @@ struct SbDriver {
     };
 
     /* find_critical_intervals_in over every parent (rectangle_size_bound.cu:276-310, 344-350) */
+    /* (restricted to the tasks [lo, hi), in the order of the reference's
+     * host loops: parent, lambda piece, r1 piece, r2 piece) */
     static void generation(const std::vector<Box>& parents, int gen, int nla, const int* rn, int threads,
-                           std::vector<Leaf>& out, SbTrace& trace) {
+                           std::vector<Leaf>& out, SbTrace& trace, uint64_t lo = 0, uint64_t hi = ~0ULL) {
         const uint64_t per_parent = (uint64_t)nla * rn[0] * rn[1];
-        const uint64_t ntasks = parents.size() * per_parent;
+        const uint64_t ntasks_all = parents.size() * per_parent;
+        const uint64_t ntasks = hi < ntasks_all ? hi : ntasks_all;
         int nt = threads > 0 ? threads : 1;
         std::vector<SbTrace> traces(nt);
         std::vector<std::vector<Leaf>> found(nt);
-        std::atomic<uint64_t> next{0};
+        std::atomic<uint64_t> next{lo};
         auto work = [&](int tid) {
             traces[tid].clear();
             for (;;) {
@@ -181,6 +184,22 @@ struct SbDriver {
             trace.add(traces[i]);
             out.insert(out.end(), found[i].begin(), found[i].end());
         }
+    }
+
+    /* merge width of generation gen (rectangle_size_bound.cu:351-362) */
+    static int merge_width(int gen) { return gen == 0 ? 0 : (gen % 3 == 0 ? 3 : (gen % 3 == 1 ? 2 : 1)); }
+
+    /* one generation over the tasks [lo, hi), merged as generation gen */
+    static Result generation_range(const std::vector<Box>& parents, int gen, int nla, const int* rn, int threads,
+                                   uint64_t lo, uint64_t hi) {
+        Result res;
+        res.trace.clear();
+        std::vector<Leaf> found;
+        generation(parents, gen, nla, rn, threads, found, res.trace, lo, hi);
+        for (const Leaf& l : found) res.trapped_leaves += l.trapped;
+        res.criticals = merge(found, merge_width(gen));
+        res.gen_sizes.push_back(res.criticals.size());
+        return res;
     }
 
     /* find_critical_intervals (rectangle_size_bound.cu:312-370) */

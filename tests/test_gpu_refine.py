@@ -1,0 +1,68 @@
+"""GPU tier: adaptive refinement of near-critical tight boxes
+(cc_tight_refine) against the same refinement driven by the CPU oracle's
+verdict masks: per level, the boxes no criterion certifies and that are not
+empty are bisected along lambda, r1, r2, r3, r4 in turn (mid = 0.5 lo + 0.5
+hi, rounded to nearest); trapped boxes and the undecided boxes of the last
+level are the criticals.  The GPU's criticals (as a set: a level's order is
+not fixed), flags and per-level counts equal the oracle-driven ones."""
+import numpy as np
+import pytest
+
+from circlecover_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_refine(port, boxes, max_depth):
+    crit, flags, live, decided = [], [], [], []
+    cur = boxes.copy()
+    for d in range(max_depth + 1):
+        if not len(cur):
+            break
+        m = port.tight_eval(cur, threads=16)
+        trapped = (m >> 31) != 0
+        done = ~trapped & ((m & 0x7F) != 0)
+        live.append(len(cur))
+        decided.append(int(done.sum()))
+        last = d == max_depth
+        keep = trapped | (~done & last)
+        crit.append(cur[keep])
+        flags.append(np.where(trapped[keep], 1, 2).astype(np.uint32))
+        split = cur[~trapped & ~done] if not last else cur[:0]
+        dim = d % 5
+        lo_half, hi_half = split.copy(), split.copy()
+        if dim == 0:
+            v = split["la"]
+            mid = 0.5 * v[:, 0] + 0.5 * v[:, 1]
+            lo_half["la"][:, 1] = mid
+            hi_half["la"][:, 0] = mid
+        else:
+            v = split["r"][:, dim - 1]
+            mid = 0.5 * v[:, 0] + 0.5 * v[:, 1]
+            lo_half["r"][:, dim - 1, 1] = mid
+            hi_half["r"][:, dim - 1, 0] = mid
+        nxt = np.empty(2 * len(split), dtype=W.TIGHT_BOX)
+        nxt[0::2], nxt[1::2] = lo_half, hi_half
+        cur = nxt
+    return np.concatenate(crit), np.concatenate(flags), live, decided
+
+
+def as_set(boxes, flags):
+    rows = boxes.view(np.uint64).reshape(len(boxes), -1)
+    return sorted(tuple(r) + (int(f),) for r, f in zip(rows, flags))
+
+
+def test_refine_equals_oracle_driven_refinement(prover, port):
+    boxes = W.tight_near_critical(2000, seed=505)
+    got, gflags, st = prover.tight_refine(boxes, max_depth=7)
+    want, wflags, live, decided = oracle_refine(port, boxes, 7)
+    assert st["live"] == live and st["decided"] == decided
+    assert as_set(got, gflags) == as_set(want, wflags)
+    assert st["depths_run"] == len(live) and not st["stopped_at_cap"]
+
+
+def test_refine_stops_at_the_population_cap(prover):
+    boxes = W.tight_near_critical(4000, seed=506)
+    _, flags, st = prover.tight_refine(boxes, max_depth=30, max_live=6000)
+    assert st["stopped_at_cap"] and max(st["live"]) <= 6000
+    assert (flags == 2).sum() + (flags == 1).sum() == len(flags)
