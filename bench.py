@@ -438,6 +438,7 @@ def run_ours(args, ws, rank, local):
         line["sb_proof"] = sb_proof_run(prover)
         line["sb_forms"] = sb_forms(prover)
         line["near_critical"] = near_critical_run(prover)
+        line["near_critical"]["refinement"] = near_critical_refinement()
     if ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
     prover.close()
@@ -566,6 +567,76 @@ def near_critical_run(prover, n=1 << 22):
             "critical_share": float(((m & 0x7F) == 0).mean()), "first_success": cmp}
 
 
+def _refine_summary(crit, flags, st):
+    live = np.array(st["live"], dtype=np.float64)
+    occ = {k: [round(v / max(1.0, l), 5) for v, l in zip(st[k], live)]
+           for k in ("fp64_boxes", "cover_jobs", "gaps_jobs", "cert_jobs")}
+    out = {"seconds": st["seconds"], "depths_run": st["depths_run"], "stopped_at_cap": st["stopped_at_cap"],
+           "boxes_evaluated": int(live.sum()), "boxes_per_s": float(live.sum() / st["seconds"]),
+           "criticals": int(len(crit)), "trapped": int((flags == 1).sum()), "live": st["live"],
+           "decided": st["decided"], "ms": [round(x, 3) for x in st["ms"]],
+           "kernel_launches": st["kernel_launches"]}
+    if st["order"] == 0:
+        out["queue_share_of_live"] = occ
+    else:
+        steps, wmax = np.array(st["steps"], dtype=np.float64), np.array(st["warp_max_steps"], dtype=np.float64)
+        out["mean_steps"] = float(steps.sum() / max(1.0, live.sum()))
+        out["lane_share_per_depth"] = [round(a / max(1.0, 32 * b), 4) for a, b in zip(steps, wmax)]
+        out["lane_share"] = float(steps.sum() / max(1.0, 32 * wmax.sum()))
+    return out
+
+
+def near_critical_refinement(n=1 << 22, max_depth=32, max_live=1 << 25, n_orders=1 << 18):
+    """Config 5: the near-critical boxes refined by bisection to depth 32
+    (cc_tight_refine).  On a fresh handle: the certified evaluation of all
+    criteria per level with the default pass settings, then with the passes
+    tuned on the near-critical boxes themselves (same criticals); per depth
+    the live and decided boxes, the device time and the queue occupancy.
+    On the first n_orders boxes: the same refinement by first-success
+    evaluation in the plain order and with the trained network's choice
+    first, with the share of lanes working per warp (load balance)."""
+    import torch
+    import circlecover_gb300 as cg
+    from circlecover_gb300 import learn
+    from circlecover_gb300 import workloads as W
+    boxes = W.tight_near_critical(n, seed=5)
+    res = {"workload": "near-critical stress refinement: 2^22 boxes, 90%% within 1e-4 of the critical weight, "
+                       "bisection (lambda, r1..r4 in turn) to depth %d, at most %d live boxes per level"
+                       % (max_depth, max_live)}
+
+    def rows(crit):  # criticals as a sorted set of bit patterns (a level's order is not fixed)
+        r = crit.view(np.uint64).reshape(len(crit), -1)
+        return r[np.lexsort(r.T[::-1])] if len(r) else r
+
+    def same(a, b):
+        return bool(np.array_equal(rows(a[0]), rows(b[0])) and a[2]["live"] == b[2]["live"])
+
+    with cg.Prover(0) as p:
+        p.tight_refine(boxes[:4096], max_depth=4)  # buffers, kernels
+        r_def = p.tight_refine(boxes, max_depth, max_live)
+        m = 1 << 22
+        soa = torch.from_numpy(W.to_soa(boxes[:m])).cuda()
+        msk = torch.empty(m, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        tune = p.autotune_eval(soa.data_ptr(), m, msk.data_ptr())
+        del soa, msk
+        r_tuned = p.tight_refine(boxes, max_depth, max_live)
+        res["default"] = _refine_summary(*r_def)
+        res["autotuned"] = _refine_summary(*r_tuned)
+        res["autotune"] = tune
+        res["identical_default_autotuned"] = same(r_def, r_tuned)
+        sub = boxes[:n_orders]
+        p.mlp_init(5)
+        learn.train(p, learn.Records(p, W.tight_near_critical(1 << 20, seed=77)), epochs=4, batch=8192)
+        orders = {}
+        for order in ("masks", "first_plain", "first_learned"):
+            p.tight_refine(sub[:2048], 2, order=order)
+            orders[order] = p.tight_refine(sub, max_depth, max_live, order=order)
+        res["orders"] = {"boxes": n_orders, **{k: _refine_summary(*v) for k, v in orders.items()},
+                         "identical_criticals": all(same(v, orders["masks"]) for v in orders.values())}
+    return res
+
+
 SB_SLICE = dict(la=(1.0, 1.0 + 1.5 * 2 / 256), grid=(2, (32, 32, 64, 64, 64, 64)))
 
 
@@ -670,7 +741,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="tight_eval",
                     choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof", "config1", "cpu_variants",
-                             "sb_reference", "config3"])
+                             "sb_reference", "config3", "near_critical"])
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.workload in SB_FULL:  # a whole size-bound proof (minutes)
@@ -681,6 +752,13 @@ def main():
             r = sb_full_run(prover, args.workload)
             if rank == 0:
                 print(json.dumps(r), flush=True)
+        return
+    if args.workload == "near_critical":  # config 5's refinement alone
+        import __graft_entry__
+        __graft_entry__.build()
+        r = near_critical_refinement()
+        if rank == 0:
+            print(json.dumps(r), flush=True)
         return
     if args.workload == "cpu_variants":  # the CPU implementations side by side (no GPU)
         print(json.dumps(cpu_variants(args.cpu_sample)), flush=True)

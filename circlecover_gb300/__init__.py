@@ -102,7 +102,17 @@ class CcRefineStats(ctypes.Structure):
                 ("decided", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
                 ("ms", ctypes.c_float * (REFINE_MAX_DEPTH + 1)),
                 ("depths_run", ctypes.c_int32), ("stopped_at_cap", ctypes.c_int32),
-                ("seconds", ctypes.c_double), ("kernel_launches", ctypes.c_uint64)]
+                ("seconds", ctypes.c_double), ("kernel_launches", ctypes.c_uint64),
+                ("fp64_boxes", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("cover_jobs", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("gaps_jobs", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("cert_jobs", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("steps", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("warp_max_steps", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("order", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+REFINE_ORDERS = {"masks": 0, "first_plain": 1, "first_learned": 2}
 
 
 class CcTuneResult(ctypes.Structure):
@@ -214,7 +224,7 @@ EXPORTS = [
     "cc_mlp_init", "cc_mlp_set_weights", "cc_mlp_get_weights", "cc_mlp_features", "cc_mlp_gradients",
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
     "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume", "cc_last_eval_counts", "cc_set_eval_graph",
-    "cc_eval_graph_stats", "cc_set_eval_certify", "cc_last_eval_cert", "cc_tight_refine",
+    "cc_eval_graph_stats", "cc_set_eval_certify", "cc_last_eval_cert", "cc_tight_refine", "cc_set_refine_order",
     "cc_sb_generation",
 ]
 
@@ -275,6 +285,7 @@ def load_library(path=LIB_PATH):
     lib.cc_set_stage_timing.argtypes = [vp, ctypes.c_int]
     lib.cc_set_eval_graph.argtypes = [vp, ctypes.c_int]
     lib.cc_set_eval_certify.argtypes = [vp, ctypes.c_int]
+    lib.cc_set_refine_order.argtypes = [vp, ctypes.c_int]
     lib.cc_last_eval_cert.argtypes = [vp, vp]
     lib.cc_eval_graph_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]
     lib.cc_last_stage_times.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
@@ -584,9 +595,13 @@ class Prover:
                                             ctypes.c_void_p(outcome_ptr),
                                             ctypes.c_void_p(evals_ptr) if evals_ptr else None), "cc_tight_first")
 
-    def tight_refine(self, boxes, max_depth, max_live=0):
+    def tight_refine(self, boxes, max_depth, max_live=0, order="masks"):
         """Adaptive refinement of host boxes (cc_tight_refine): (criticals,
-        flags, stats dict with per-depth live / decided counts and ms)."""
+        flags, stats dict with per-depth live / decided counts, ms, queue
+        occupancy and criterion steps).  order: "masks" (the certified
+        evaluation of all criteria), "first_plain" or "first_learned"
+        (cc_set_refine_order)."""
+        self._check(self.lib.cc_set_refine_order(self.h, REFINE_ORDERS[order]), "cc_set_refine_order")
         boxes = np.ascontiguousarray(boxes, dtype=TIGHT_BOX)
         out = ctypes.c_void_p()
         fl = ctypes.c_void_p()
@@ -606,10 +621,17 @@ class Prover:
         self.lib.cc_free(out)
         self.lib.cc_free(fl)
         d = int(st.depths_run)
-        return arr, flags, {"live": [int(x) for x in st.live[:d]], "decided": [int(x) for x in st.decided[:d]],
+
+        def per_depth(a):
+            return [int(x) for x in a[:d]]
+        return arr, flags, {"live": per_depth(st.live), "decided": per_depth(st.decided),
                             "ms": [float(x) for x in st.ms[:d]], "depths_run": d,
                             "stopped_at_cap": bool(st.stopped_at_cap), "seconds": float(st.seconds),
-                            "kernel_launches": int(st.kernel_launches)}
+                            "kernel_launches": int(st.kernel_launches), "fp64_boxes": per_depth(st.fp64_boxes),
+                            "cover_jobs": per_depth(st.cover_jobs), "gaps_jobs": per_depth(st.gaps_jobs),
+                            "cert_jobs": per_depth(st.cert_jobs), "steps": per_depth(st.steps),
+                            "warp_max_steps": per_depth(st.warp_max_steps),
+                            "order": int(st.order)}
 
     def tight_summary(self, criticals):
         """Max_distances of a critical set (cc_tight_summary), as the raw

@@ -575,30 +575,44 @@ int cc_mlp_infer_async(cc_handle* h, const float* feat, const unsigned long long
     return CC_OK;
 }
 
+int cc_first_success_async(cc_handle* h, const double* soa, size_t n, float depth, float* scratch, uint8_t* outcome,
+                           uint8_t* evals, cudaStream_t st) {
+    static_assert(kFirstScratchFloats == kF + 8, "scratch layout: features, then 8 logits per box");
+    if (!n) return CC_OK;
+    float* logits = nullptr;
+    if (scratch) {
+        if (!h->mlp) return ccrt::fail(h, CC_ERR_PARAM, "learned order: no trained network (cc_mlp_init)");
+        MlpState* s = static_cast<MlpState*>(h->mlp);
+        int rc = mlp_pack(h, s);
+        if (rc) return rc;
+        float* feat = scratch;
+        logits = feat + n * kF;
+        k_mlp_features<<<grid_for(h, n, 128), 128, 0, st>>>(soa, n, depth, feat);
+        CC_LAUNCHED(h);
+        k_mlp_infer<<<grid_for(h, (n + 15) / 16 * 32, 128), 128, 0, st>>>(s->frag, s->bias, feat, n, nullptr, logits);
+        CC_LAUNCHED(h);
+    }
+    k_tight_first<<<grid_for(h, n, 128), 128, 0, st>>>(soa, n, logits, outcome, evals);
+    CC_LAUNCHED(h);
+    return CC_OK;
+}
+
 extern "C" int cc_tight_first(cc_handle* h, const double* soa, size_t n, int learned, uint8_t* outcome,
                               uint8_t* evals) {
     if (!h || (n && (!soa || !outcome))) return CC_ERR_PARAM;
     h->launches = 0;
     if (!n) return CC_OK;
     CC_CUDA(h, cudaSetDevice(h->device));
-    float* logits = nullptr;
+    float* scratch = nullptr;
     if (learned) {
         if (!h->mlp) return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_first: no trained network (cc_mlp_init)");
-        MlpState* s = static_cast<MlpState*>(h->mlp);
         void* p;
-        int st = ccrt::ensure(h, 23, n * (kF + 8) * sizeof(float), &p);
+        int st = ccrt::ensure(h, 23, n * kFirstScratchFloats * sizeof(float), &p);
         if (st) return st;
-        float* feat = (float*)p;
-        logits = feat + n * kF;
-        if ((st = mlp_pack(h, s))) return st;
-        k_mlp_features<<<grid_for(h, n, 128), 128, 0, h->stream>>>(soa, n, 0.0f, feat);
-        CC_LAUNCHED(h);
-        k_mlp_infer<<<grid_for(h, (n + 15) / 16 * 32, 128), 128, 0, h->stream>>>(s->frag, s->bias, feat, n, nullptr,
-                                                                                logits);
-        CC_LAUNCHED(h);
+        scratch = (float*)p;
     }
-    k_tight_first<<<grid_for(h, n, 128), 128, 0, h->stream>>>(soa, n, logits, outcome, evals);
-    CC_LAUNCHED(h);
+    int rc = cc_first_success_async(h, soa, n, 0.0f, scratch, outcome, evals, h->stream);
+    if (rc) return rc;
     CC_CUDA(h, cudaStreamSynchronize(h->stream));
     return CC_OK;
 }

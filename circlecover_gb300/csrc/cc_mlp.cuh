@@ -42,3 +42,11 @@ __device__ inline void features(const double v[10], Iv W, float depth, float* f)
 // (no synchronisation); the network must have been initialised
 int cc_mlp_infer_async(cc_handle* h, const float* feat, const unsigned long long* n_dev, unsigned long long cap,
                        float* logits, cudaStream_t s);
+
+// First-success outcomes (as cc_tight_first) of n boxes in SoA device memory
+// on stream s, no synchronisation.  With scratch != nullptr the network's
+// most likely criterion runs first: scratch holds n * kFirstScratchFloats
+// floats (features at `depth`, then logits).  evals may be nullptr.
+constexpr int kFirstScratchFloats = CC_MLP_FEATURES + 8;
+int cc_first_success_async(cc_handle* h, const double* soa, size_t n, float depth, float* scratch, uint8_t* outcome,
+                           uint8_t* evals, cudaStream_t s);

@@ -2036,7 +2036,8 @@ extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, siz
 // Adaptive refinement of a set of tight boxes to a depth cap (no reference
 // counterpart; the near-critical stress workload).  Every level runs the
 // certified evaluation (the six criteria and the emptiness bits, passes 0-5)
-// on its boxes; k_refine_split then sorts them: certified or empty boxes are
+// on its boxes -- or the first-success evaluation in the plain or the learned
+// order; k_refine_split then sorts them: certified or empty boxes are
 // done, trapped ones are kept as criticals, the others are bisected into the
 // next level -- or kept as criticals at the last level.  The boxes of a level
 // are independent and of uneven cost (the criteria's branches and
@@ -2044,10 +2045,44 @@ extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, siz
 // compacted queues.
 namespace {
 
-enum { S_REF_A = 28, S_REF_B = 29, S_REF_MASKS = 30, S_REF_CRIT = 31 };
+enum { S_REF_A = 28, S_REF_B = 29, S_REF_MASKS = 30, S_REF_CRIT = 31, S_REF_SOA = 40, S_REF_FIRST = 41,
+       S_REF_MLP = 42 };
 
 struct RefineCounters {
     unsigned long long n_next, n_crit, n_decided, overflow;
+    unsigned long long fp64, cover, gaps, cert, steps, warp_max_steps;
+};
+
+// one evaluation batch's queue sizes added to the level's occupancy
+__global__ void k_refine_tally(const unsigned long long* __restrict__ counts, RefineCounters* c) {
+    if (threadIdx.x != 0) return;
+    c->fp64 += counts[kCntFull];
+    c->cover += counts[kCntCover];
+    c->gaps += counts[kCntGaps];
+    unsigned long long cert = 0;
+    for (int k = 0; k < kCertQueues; ++k) cert += counts[kCntCert + k];
+    c->cert += cert;
+}
+
+// a level's verdicts: the evaluation's masks, or first-success outcomes
+struct MaskVerdicts {
+    const uint32_t* m;
+    __device__ __forceinline__ void get(size_t i, bool& trapped, bool& decided, unsigned& steps) const {
+        const uint32_t x = m[i];
+        trapped = (x >> 31) != 0;
+        decided = !trapped && (x & 0x7Fu) != 0;
+        steps = 0;
+    }
+};
+struct FirstVerdicts {
+    const uint8_t* o;
+    const uint8_t* ev;
+    __device__ __forceinline__ void get(size_t i, bool& trapped, bool& decided, unsigned& steps) const {
+        const uint8_t x = o[i];
+        trapped = (x & 0x80u) != 0;
+        decided = !trapped && (x & 0x7Fu) != 7u;
+        steps = ev[i];
+    }
 };
 
 __device__ __forceinline__ void bisect_dim(const cc_tight_box& b, int dim, cc_tight_box& lo_half, cc_tight_box& hi_half) {
@@ -2062,29 +2097,35 @@ __device__ __forceinline__ void bisect_dim(const cc_tight_box& b, int dim, cc_ti
     u.lb = mid;
 }
 
-__global__ void __launch_bounds__(128) k_refine_split(const cc_tight_box* __restrict__ in, size_t n,
-                                                      const uint32_t* __restrict__ masks, int depth, int last,
-                                                      cc_tight_box* __restrict__ out, unsigned long long out_pairs,
-                                                      cc_tight_box* __restrict__ crit, uint32_t* __restrict__ crit_flags,
-                                                      unsigned long long crit_cap, RefineCounters* c) {
+template <class V>
+__global__ void __launch_bounds__(128) k_refine_split(const cc_tight_box* __restrict__ in, size_t n, V verdicts,
+                                                      int depth, int last, cc_tight_box* __restrict__ out,
+                                                      unsigned long long out_pairs, cc_tight_box* __restrict__ crit,
+                                                      uint32_t* __restrict__ crit_flags, unsigned long long crit_cap,
+                                                      RefineCounters* c) {
     unsigned decided_n = 0;
+    unsigned long long steps_n = 0, warp_max_n = 0;
     const int dim = depth % 5;
     CC_WARP_LOOP(n) {
         const unsigned long long i = base_ + (threadIdx.x & 31);
         const bool valid = i < n;
         bool split = false, keep = false;
         uint32_t flag = 0;
+        unsigned lane_steps = 0;
         cc_tight_box b{};
         if (valid) {
-            const uint32_t m = masks[i];
-            const bool trapped = (m >> 31) != 0;
-            const bool decided = !trapped && (m & 0x7Fu) != 0;
+            bool trapped, decided;
+            unsigned st;
+            verdicts.get(i, trapped, decided, st);
+            steps_n += st;
+            lane_steps = st;
             decided_n += decided ? 1u : 0u;
             b = in[i];
             split = !trapped && !decided && !last;
             keep = trapped || (!decided && last);
             flag = trapped ? 1u : 2u;
         }
+        warp_max_n += __reduce_max_sync(0xffffffffu, lane_steps);
         unsigned long long s = cc::prove::warp_append(&c->n_next, split, out_pairs, &c->overflow);
         if (s != ~0ULL) bisect_dim(b, dim, out[2 * s], out[2 * s + 1]);
         s = cc::prove::warp_append(&c->n_crit, keep, crit_cap, &c->overflow);
@@ -2094,11 +2135,22 @@ __global__ void __launch_bounds__(128) k_refine_split(const cc_tight_box* __rest
         }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) decided_n += __shfl_xor_sync(0xffffffffu, decided_n, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        decided_n += __shfl_xor_sync(0xffffffffu, decided_n, o);
+        steps_n += __shfl_xor_sync(0xffffffffu, steps_n, o);
+    }
     if ((threadIdx.x & 31) == 0 && decided_n) atomicAdd(&c->n_decided, (unsigned long long)decided_n);
+    if ((threadIdx.x & 31) == 0 && steps_n) atomicAdd(&c->steps, steps_n);
+    if ((threadIdx.x & 31) == 0 && warp_max_n) atomicAdd(&c->warp_max_steps, warp_max_n);
 }
 
 }  // namespace
+
+extern "C" int cc_set_refine_order(cc_handle* h, int order) {
+    if (!h || order < CC_REFINE_MASKS || order > CC_REFINE_FIRST_LEARNED) return CC_ERR_PARAM;
+    h->refine_order = order;
+    return CC_OK;
+}
 
 extern "C" int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n, int max_depth, size_t max_live,
                                cc_tight_box** criticals, uint32_t** flags, size_t* n_crit, cc_refine_stats* stats) {
@@ -2112,7 +2164,11 @@ extern "C" int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n
     h->interrupt.store(0);
     const auto t0 = std::chrono::steady_clock::now();
     if (max_live < 2) max_live = (size_t)1 << 26;
+    const int order = h->refine_order;
+    if (order == CC_REFINE_FIRST_LEARNED && !h->mlp)
+        return ccrt::fail(h, CC_ERR_PARAM, "cc_tight_refine: learned order without a trained network (cc_mlp_init)");
     cc_refine_stats st{};
+    st.order = order;
     cudaStream_t s = h->stream;
     void *a, *cnt_p;
     int rc;
@@ -2136,17 +2192,43 @@ extern "C" int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n
         if ((rc = ccrt::ensure(h, next_slot, (last ? 1 : 2 * cur_n) * sizeof(cc_tight_box), &next))) return rc;
         if ((rc = ccrt::ensure(h, S_REF_MASKS, cur_n * sizeof(uint32_t), &masks))) return rc;
         if ((rc = ccrt::ensure(h, S_REF_CRIT, cur_n * (sizeof(cc_tight_box) + sizeof(uint32_t)), &crit))) return rc;
+        void *soa = nullptr, *first = nullptr, *mlp = nullptr;
+        if (order != CC_REFINE_MASKS) {
+            const size_t m = std::min(chunk, cur_n);
+            if ((rc = ccrt::ensure(h, S_REF_SOA, m * sizeof(cc_tight_box), &soa))) return rc;
+            if ((rc = ccrt::ensure(h, S_REF_FIRST, 2 * cur_n, &first))) return rc;
+            if (order == CC_REFINE_FIRST_LEARNED &&
+                (rc = ccrt::ensure(h, S_REF_MLP, m * kFirstScratchFloats * sizeof(float), &mlp)))
+                return rc;
+        }
         CC_CUDA(h, cudaMemsetAsync(dc, 0, sizeof(RefineCounters), s));
         CC_CUDA(h, cudaEventRecord(ev.e0, s));
         for (size_t off = 0; off < cur_n; off += chunk) {
             const size_t m = std::min(chunk, cur_n - off);
-            rc = eval_batch<Layout::AoS>(h, (const double*)((cc_tight_box*)cur + off), m, (uint32_t*)masks + off, s,
-                                         false);
-            if (rc) return rc;
+            const double* part = (const double*)((cc_tight_box*)cur + off);
+            if (order == CC_REFINE_MASKS) {
+                rc = eval_batch<Layout::AoS>(h, part, m, (uint32_t*)masks + off, s, false);
+                if (rc) return rc;
+                k_refine_tally<<<1, 32, 0, s>>>(h->eval_counts, dc);
+                CC_LAUNCHED(h);
+            } else {
+                k_aos_to_soa<<<h->sm_count * 8, 256, 0, s>>>(part, m, (double*)soa);
+                CC_LAUNCHED(h);
+                rc = cc_first_success_async(h, (const double*)soa, m, (float)d, (float*)mlp, (uint8_t*)first + off,
+                                            (uint8_t*)first + cur_n + off, s);
+                if (rc) return rc;
+            }
         }
-        k_refine_split<<<eval_grid(h, cur_n), 128, 0, s>>>(
-            (const cc_tight_box*)cur, cur_n, (const uint32_t*)masks, d, last ? 1 : 0, (cc_tight_box*)next,
-            last ? 0 : cur_n, (cc_tight_box*)crit, (uint32_t*)((cc_tight_box*)crit + cur_n), cur_n, dc);
+        cc_tight_box* crit_boxes = (cc_tight_box*)crit;
+        uint32_t* crit_fl = (uint32_t*)(crit_boxes + cur_n);
+        if (order == CC_REFINE_MASKS)
+            k_refine_split<<<eval_grid(h, cur_n), 128, 0, s>>>(
+                (const cc_tight_box*)cur, cur_n, MaskVerdicts{(const uint32_t*)masks}, d, last ? 1 : 0,
+                (cc_tight_box*)next, last ? 0 : cur_n, crit_boxes, crit_fl, cur_n, dc);
+        else
+            k_refine_split<<<eval_grid(h, cur_n), 128, 0, s>>>(
+                (const cc_tight_box*)cur, cur_n, FirstVerdicts{(const uint8_t*)first, (const uint8_t*)first + cur_n}, d,
+                last ? 1 : 0, (cc_tight_box*)next, last ? 0 : cur_n, crit_boxes, crit_fl, cur_n, dc);
         CC_LAUNCHED(h);
         CC_CUDA(h, cudaEventRecord(ev.e1, s));
         RefineCounters hc;
@@ -2158,6 +2240,12 @@ extern "C" int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n
         st.live[d] = cur_n;
         st.decided[d] = hc.n_decided;
         st.ms[d] = ms;
+        st.fp64_boxes[d] = hc.fp64;
+        st.cover_jobs[d] = hc.cover;
+        st.gaps_jobs[d] = hc.gaps;
+        st.cert_jobs[d] = hc.cert;
+        st.steps[d] = hc.steps;
+        st.warp_max_steps[d] = hc.warp_max_steps;
         st.depths_run = d + 1;
         if (hc.n_crit) {
             const size_t old = out.size();

@@ -29,7 +29,7 @@ struct cc_handle {
         void* ptr = nullptr;
         size_t bytes = 0;
     };
-    Buf bufs[40];
+    Buf bufs[44];
     // pinned host staging for the host-memory entry points
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -39,6 +39,8 @@ struct cc_handle {
     int tune_grid[CC_EVAL_STAGES] = {8, 8, 8, 8, 8, 8};
     // FP64 certification of the evaluation's FP32 decisions (cc_set_eval_certify)
     bool eval_certify = true;
+    // how cc_tight_refine decides a level's boxes (cc_set_refine_order)
+    int refine_order = CC_REFINE_MASKS;
     // where the tight proof writes its state after each generation (empty: off)
     std::string checkpoint_path;
     // sample of r3 cells logged by the last tight proof (CC_PROVE_LOG_CELLS)

@@ -535,8 +535,25 @@ int cc_tight_first(cc_handle* h, const double* soa, size_t n, int learned, uint8
  * undecided at the last level are kept as criticals (flag 2); the last level
  * comes early when the next one would hold more than max_live boxes (0: 2^26),
  * which stats->stopped_at_cap reports.  *criticals / *flags (cc_free) in
- * level order.  cc_interrupt stops after the current level. */
+ * level order.  cc_interrupt stops after the current level.
+ *
+ * cc_set_refine_order chooses how a level decides its boxes:
+ *   CC_REFINE_MASKS        the certified evaluation of all six criteria and
+ *                          the emptiness bits (the default);
+ *   CC_REFINE_FIRST_PLAIN  first-success evaluation in FP64 (cc_tight_first):
+ *                          the criteria in the reference's order until one
+ *                          certifies the box;
+ *   CC_REFINE_FIRST_LEARNED  the same with the network's most likely criterion
+ *                          first (features at the level's depth; needs a
+ *                          trained network, cc_mlp_init).
+ * A box is decided in every order exactly when some criterion certifies it or
+ * R / R4 is empty; only the trap flag can differ (a first-success run stops
+ * before a later criterion's trap site). */
 #define CC_REFINE_MAX_DEPTH 48
+#define CC_REFINE_MASKS 0
+#define CC_REFINE_FIRST_PLAIN 1
+#define CC_REFINE_FIRST_LEARNED 2
+int cc_set_refine_order(cc_handle* h, int order);
 typedef struct cc_refine_stats {
     uint64_t live[CC_REFINE_MAX_DEPTH + 1];    /* boxes evaluated at each depth */
     uint64_t decided[CC_REFINE_MAX_DEPTH + 1]; /* of which certified or empty */
@@ -545,6 +562,21 @@ typedef struct cc_refine_stats {
     int32_t stopped_at_cap;
     double seconds;                            /* wall time of the call */
     uint64_t kernel_launches;
+    /* queue occupancy per depth (CC_REFINE_MASKS): boxes the FP32 pass left
+     * to the FP64 pass, strip-width and gap-width bisection jobs, and FP32
+     * "true" verdicts sent to FP64 certification */
+    uint64_t fp64_boxes[CC_REFINE_MAX_DEPTH + 1];
+    uint64_t cover_jobs[CC_REFINE_MAX_DEPTH + 1];
+    uint64_t gaps_jobs[CC_REFINE_MAX_DEPTH + 1];
+    uint64_t cert_jobs[CC_REFINE_MAX_DEPTH + 1];
+    /* criterion steps run per depth (first-success orders), and the sum over
+     * groups of 32 consecutive boxes (one warp of the first-success kernel)
+     * of their largest step count: steps / (32 * warp_max_steps) is the
+     * share of lanes that work while the warp runs criteria */
+    uint64_t steps[CC_REFINE_MAX_DEPTH + 1];
+    uint64_t warp_max_steps[CC_REFINE_MAX_DEPTH + 1];
+    int32_t order;
+    int32_t pad;
 } cc_refine_stats;
 int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n, int max_depth, size_t max_live,
                     cc_tight_box** criticals, uint32_t** flags, size_t* n_crit, cc_refine_stats* stats);

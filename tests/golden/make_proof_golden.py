@@ -14,17 +14,18 @@ Per generation the fixture holds its parents and, for task ranges of that
 generation, the oracle's criticals (hex floats), trace digest, per-outcome
 counts and leaf count, computed by the restated driver (oracle/
 tight_driver.hpp) on the REFERENCE's own criteria (oracle/_ref/libccref.so,
-built from the reference sources).  Generation 0 is covered whole (all 256
-tasks), so its criticals -- the parents of generation 1 -- are
-reference-made.  The refinement generations cover 1.3e8 leaves per task, too
-many to run whole on the CPU (about an hour per task on 8 cores): one
-single-task range per generation is run (a task that produced criticals on
-the GPU, else a seeded one); the parents of generations 2 and later are the
-GPU's output of the previous generation, stored as they are
-("parents_source").
+built from the reference sources).  The CPU evaluates about 4e4 leaves per
+second on 8 cores, so no generation is run whole: generation 0 (2.7e6 to
+3.9e6 leaves per task) is sampled by every task that produced criticals on
+the GPU (at most GEN0_HOT) and GEN0_RANDOM seeded others; a refinement
+generation (1.3e8 leaves per task, about an hour each) by one task that
+produced criticals on the GPU, else a seeded one.  The parents of
+generation 1 and later are the GPU's output of the previous generation,
+stored as they are ("parents_source"); the ranges that produced them are
+among the sampled ones.
 
 Steps (the second one takes hours on 8 cores; it resumes from the partial
-file it writes after every range):
+file it writes after every range, generation 0 of both roots first):
 
   python tests/golden/make_proof_golden.py import DIR   # GPU lists <root>_genNN.npy
   python tests/golden/make_proof_golden.py run [THREADS]
@@ -48,6 +49,8 @@ ROOTS = {"full": ((1.0, W.TIGHT_LAMBDA_MAX), 256, (128, 128, 128, 128)),
          "config1": ((1.0, 1.1), 256, (64, 128, 128, 128))}
 SAMPLE_SEED = 20261204
 SAMPLES_PER_GEN = 1
+GEN0_HOT = 8
+GEN0_RANDOM = 2
 
 
 def box_hex(b):
@@ -107,17 +110,15 @@ def import_gpu(src):
                      "parents_source": "reference root" if g == 0 else "GPU output of generation %d" % (g - 1)}
             if out is not None:
                 entry["gpu_criticals"] = [box_hex(b) for b in out]
-            if g == 0:
-                entry["ranges"] = [[0, n_tasks]]
-            else:
-                hot = sorted({t for t in task_of(parents, la, out) if t >= 0}) if out is not None else []
-                pick = list(hot[:SAMPLES_PER_GEN])
-                others = [t for t in range(n_tasks) if t not in pick]
-                while len(pick) < SAMPLES_PER_GEN and others:
-                    t = int(rng.choice(others))
-                    others.remove(t)
-                    pick.append(t)
-                entry["ranges"] = [[t, t + 1] for t in sorted(pick)]
+            hot = sorted({t for t in task_of(parents, la, out) if t >= 0}) if out is not None else []
+            want = GEN0_HOT + GEN0_RANDOM if g == 0 else SAMPLES_PER_GEN
+            pick = list(hot[:GEN0_HOT if g == 0 else SAMPLES_PER_GEN])
+            others = [t for t in range(n_tasks) if t not in pick]
+            while len(pick) < want and others:
+                t = int(rng.choice(others))
+                others.remove(t)
+                pick.append(t)
+            entry["ranges"] = [[t, t + 1] for t in sorted(pick)]
             entry["oracle"] = []
             gens.append(entry)
             if out is None or not len(out):
@@ -135,21 +136,22 @@ def run(threads):
     O.ensure_built()
     ref = O.Ref()
     fx = json.load(open(OUT))
-    for name in ROOTS:
-        for entry in fx[name]["generations"]:
-            done = {(o["lo"], o["hi"]) for o in entry["oracle"]}
-            parents = boxes_from_hex(entry["parents"])
-            for lo, hi in entry["ranges"]:
-                if (lo, hi) in done:
-                    continue
-                crit, st = ref.tight_generation(parents, entry["la_splits"], entry["r_splits"], lo, hi,
-                                                threads=threads)
-                entry["oracle"].append({"lo": lo, "hi": hi, "criticals": [box_hex(b) for b in crit],
-                                        "digest": st["digest"], "counts": st["counts"],
-                                        "leaf_evals": st["leaf_evals"], "trapped": st["trapped_leaves"]})
-                with open(OUT, "w") as f:
-                    json.dump(fx, f, indent=1)
-                print(name, entry["gen"], lo, hi, len(crit), st["leaf_evals"], flush=True)
+    # generation 0 of every root first, then the refinement generations
+    order = sorted(((e["gen"], name, e) for name in ROOTS for e in fx[name]["generations"]), key=lambda x: x[:2])
+    for _, name, entry in order:
+        done = {(o["lo"], o["hi"]) for o in entry["oracle"]}
+        parents = boxes_from_hex(entry["parents"])
+        for lo, hi in entry["ranges"]:
+            if (lo, hi) in done:
+                continue
+            crit, st = ref.tight_generation(parents, entry["la_splits"], entry["r_splits"], lo, hi,
+                                            threads=threads)
+            entry["oracle"].append({"lo": lo, "hi": hi, "criticals": [box_hex(b) for b in crit],
+                                    "digest": st["digest"], "counts": st["counts"],
+                                    "leaf_evals": st["leaf_evals"], "trapped": st["trapped_leaves"]})
+            with open(OUT, "w") as f:
+                json.dump(fx, f, indent=1)
+            print(name, entry["gen"], lo, hi, len(crit), st["leaf_evals"], flush=True)
 
 
 if __name__ == "__main__":

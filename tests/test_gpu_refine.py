@@ -66,3 +66,29 @@ def test_refine_stops_at_the_population_cap(prover):
     _, flags, st = prover.tight_refine(boxes, max_depth=30, max_live=6000)
     assert st["stopped_at_cap"] and max(st["live"]) <= 6000
     assert (flags == 2).sum() + (flags == 1).sum() == len(flags)
+
+
+def test_refine_orders_decide_the_same_boxes(prover):
+    """First-success refinement (plain order, and the network's choice first)
+    decides exactly the boxes the certified masks decide at every level, so
+    live and decided counts and the criticals agree; it reports its steps."""
+    from circlecover_gb300 import learn
+    boxes = W.tight_near_critical(3000, seed=507)
+    got, gflags, st = prover.tight_refine(boxes, max_depth=9)
+    assert st["order"] == 0 and sum(st["fp64_boxes"]) + sum(st["cover_jobs"]) > 0
+    assert all(f <= l for f, l in zip(st["fp64_boxes"], st["live"]))
+    prover.mlp_init(9)
+    learn.train(prover, learn.Records(prover, W.tight_near_critical(1 << 14, seed=508)), epochs=1, batch=4096)
+    for order in ("first_plain", "first_learned"):
+        c, f, s = prover.tight_refine(boxes, max_depth=9, order=order)
+        assert s["order"] == (1 if order == "first_plain" else 2)
+        assert all(k >= l - d for k, l, d in zip(s["steps"], s["live"], s["decided"])), order
+        assert all(k <= 32 * w and w <= k for k, w in zip(s["steps"], s["warp_max_steps"])), order
+        # a trap site reached after the certifying criterion keeps a box in
+        # the masks order only; without traps both refinements are the same
+        if not (gflags == 1).any() and not (f == 1).any():
+            assert s["live"] == st["live"] and s["decided"] == st["decided"], order
+            assert as_set(c, f) == as_set(got, gflags), order
+        else:
+            assert s["decided"][0] >= st["decided"][0], order
+    prover.tight_refine(boxes[:1], max_depth=0)  # back to the default order
