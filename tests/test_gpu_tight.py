@@ -10,6 +10,7 @@ Bit-exact everywhere (integer verdict masks, FP64 interval endpoints):
   golden proofs and the CPU port.
 """
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -58,6 +59,24 @@ def test_eval_matches_port_large(prover, port):
     for seed, gen, n in [(21, W.tight_microbench, 1 << 18), (22, W.tight_near_critical, 1 << 17)]:
         boxes = gen(n, seed=seed)
         assert np.array_equal(prover.tight_eval(boxes), port.tight_eval(boxes, threads=16))
+
+
+def test_eval_whole_microbench_matches_port(prover, port):
+    """Config 2 at its full size: all 2^24 boxes of the bench workload (seed
+    1), certified masks from the device entry point equal the port's (all
+    host threads, about half a minute)."""
+    import torch
+    n = 1 << 24
+    boxes = W.tight_microbench(n, seed=1)
+    soa = torch.from_numpy(W.to_soa(boxes)).cuda()
+    masks = torch.empty(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    prover.tight_eval_device(soa.data_ptr(), n, masks.data_ptr())
+    torch.cuda.synchronize()
+    got = masks.cpu().numpy().view(np.uint32)
+    del soa, masks
+    want = port.tight_eval(boxes, threads=os.cpu_count() or 16)
+    assert np.array_equal(got, want), int((got != want).sum())
 
 
 def test_eval_device_soa(prover, port):
