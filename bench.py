@@ -439,6 +439,7 @@ def run_ours(args, ws, rank, local):
         line["sb_forms"] = sb_forms(prover)
         line["near_critical"] = near_critical_run(prover)
         line["near_critical"]["refinement"] = near_critical_refinement()
+        line["small_batch"] = small_batch_run(prover)
     if ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
     prover.close()
@@ -529,6 +530,36 @@ def proof_comparison(prover, which="full", n_microbench_records=10_000_000):
     return out
 
 
+def small_batch_run(prover, n=1 << 16, reps=20):
+    """Batches of 65,536 boxes (the largest the allocation-free entry takes):
+    cc_tight_eval_device (handle-owned queues, recorded calls, graph replay)
+    next to cc_tight_eval_device_static (a fixed array, no recorded calls:
+    the one-kernel FP32 pass), CUDA events on one stream; same masks."""
+    import torch
+    from circlecover_gb300 import workloads as W
+    boxes = W.tight_microbench(n, seed=1)
+    soa = torch.from_numpy(W.to_soa(boxes)).cuda()
+    m_dev = torch.empty(n, dtype=torch.int32, device="cuda")
+    m_st = torch.empty(n, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    out = {"boxes": n}
+    for name, call, m in (("device", prover.tight_eval_device, m_dev),
+                          ("static", prover.tight_eval_device_static, m_st)):
+        for _ in range(3):
+            call(soa.data_ptr(), n, m.data_ptr(), stream.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            call(soa.data_ptr(), n, m.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = {"ms": ms, "boxes_per_s": n / (ms * 1e-3)}
+    out["same_masks"] = bool(torch.equal(m_dev, m_st))
+    return out
+
+
 def near_critical_run(prover, n=1 << 22):
     """Near-critical stress: 2^22 boxes, 90 % with total weight within 1e-4
     (relative) of the critical weight, 10 % drawn as the microbench.  Verdict
@@ -567,13 +598,30 @@ def near_critical_run(prover, n=1 << 22):
             "critical_share": float(((m & 0x7F) == 0).mean()), "first_success": cmp}
 
 
+def proof_batched_only(prover, which="full"):
+    """The batched, certified form of a tight proof alone (for launch lists
+    and profiles of the proof's kernels)."""
+    import circlecover_gb300 as cg
+    from circlecover_gb300 import workloads as W
+    desc, (la_lo, la_hi), (la0, r0) = PROOFS[which]
+    root = W.tight_root(la_lo, la_hi if la_hi is not None else W.TIGHT_LAMBDA_MAX)
+    prover.tight_find_critical_intervals(W.tight_root(1.0, 1.0001), cg.make_grid(2, (8, 8, 8, 8)))  # buffers
+    t0 = time.perf_counter()
+    crit, st = prover.tight_find_critical_intervals(root, cg.make_grid(la0, r0, TIGHT_GENS, TIGHT_R_GEN))
+    return {"workload": desc, "form": "batched", "seconds": time.perf_counter() - t0, "leaves": st["leaf_evals"],
+            "criticals": len(crit), "gen_sizes": st["gen_sizes"], "digest": st["digest"],
+            "fp32_first": st["fp32_first"], "cert_failures": st["cert_failures"],
+            "kernel_launches": st["kernel_launches"]}
+
+
 def _refine_summary(crit, flags, st):
     live = np.array(st["live"], dtype=np.float64)
     occ = {k: [round(v / max(1.0, l), 5) for v, l in zip(st[k], live)]
            for k in ("fp64_boxes", "cover_jobs", "gaps_jobs", "cert_jobs")}
     out = {"seconds": st["seconds"], "depths_run": st["depths_run"], "stopped_at_cap": st["stopped_at_cap"],
            "boxes_evaluated": int(live.sum()), "boxes_per_s": float(live.sum() / st["seconds"]),
-           "criticals": int(len(crit)), "trapped": int((flags == 1).sum()), "live": st["live"],
+           "criticals": int(len(crit)), "trapped": int((flags == 1).sum()), "cut": int((flags == 3).sum()),
+           "live": st["live"],
            "decided": st["decided"], "ms": [round(x, 3) for x in st["ms"]],
            "kernel_launches": st["kernel_launches"]}
     if st["order"] == 0:
@@ -586,30 +634,31 @@ def _refine_summary(crit, flags, st):
     return out
 
 
-def near_critical_refinement(n=1 << 22, max_depth=32, max_live=1 << 25, n_orders=1 << 18):
+def near_critical_refinement(n=1 << 22, max_depth=32, max_live=1 << 25, n_orders=1 << 18, orders_live=1 << 23):
     """Config 5: the near-critical boxes refined by bisection to depth 32
-    (cc_tight_refine).  On a fresh handle: the certified evaluation of all
-    criteria per level with the default pass settings, then with the passes
-    tuned on the near-critical boxes themselves (same criticals); per depth
-    the live and decided boxes, the device time and the queue occupancy.
-    On the first n_orders boxes: the same refinement by first-success
-    evaluation in the plain order and with the trained network's choice
-    first, with the share of lanes working per warp (load balance)."""
+    (cc_tight_refine).  The undecided population about doubles per level
+    (the boxes around the critical configurations are never certified), so
+    a level carries at most max_live boxes on: the first ones in level order,
+    the others are kept as criticals (flag 3, `cut`).  On a fresh handle: the
+    certified evaluation of all criteria per level with the default pass
+    settings, then with the passes tuned on the near-critical boxes
+    themselves (same criticals); per depth the live and decided boxes, the
+    device time and the queue occupancy.  On the first n_orders boxes (cap
+    orders_live): the same refinement by first-success evaluation in the
+    plain order and with the trained network's choice first, with the share
+    of lanes working per warp (load balance)."""
     import torch
     import circlecover_gb300 as cg
     from circlecover_gb300 import learn
     from circlecover_gb300 import workloads as W
     boxes = W.tight_near_critical(n, seed=5)
     res = {"workload": "near-critical stress refinement: 2^22 boxes, 90%% within 1e-4 of the critical weight, "
-                       "bisection (lambda, r1..r4 in turn) to depth %d, at most %d live boxes per level"
-                       % (max_depth, max_live)}
+                       "bisection (lambda, r1..r4 in turn) to depth %d, at most %d live boxes per level (the "
+                       "first in level order; the rest kept as cut criticals)" % (max_depth, max_live)}
 
-    def rows(crit):  # criticals as a sorted set of bit patterns (a level's order is not fixed)
-        r = crit.view(np.uint64).reshape(len(crit), -1)
-        return r[np.lexsort(r.T[::-1])] if len(r) else r
-
-    def same(a, b):
-        return bool(np.array_equal(rows(a[0]), rows(b[0])) and a[2]["live"] == b[2]["live"])
+    def same(a, b):  # criticals, flags and level sizes (the output order is deterministic)
+        return bool(len(a[0]) == len(b[0]) and np.array_equal(a[0].view(np.uint64), b[0].view(np.uint64))
+                    and np.array_equal(a[1], b[1]) and a[2]["live"] == b[2]["live"])
 
     with cg.Prover(0) as p:
         p.tight_refine(boxes[:4096], max_depth=4)  # buffers, kernels
@@ -631,7 +680,7 @@ def near_critical_refinement(n=1 << 22, max_depth=32, max_live=1 << 25, n_orders
         orders = {}
         for order in ("masks", "first_plain", "first_learned"):
             p.tight_refine(sub[:2048], 2, order=order)
-            orders[order] = p.tight_refine(sub, max_depth, max_live, order=order)
+            orders[order] = p.tight_refine(sub, max_depth, orders_live, order=order)
         res["orders"] = {"boxes": n_orders, **{k: _refine_summary(*v) for k, v in orders.items()},
                          "identical_criticals": all(same(v, orders["masks"]) for v in orders.values())}
     return res
@@ -741,7 +790,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--workload", default="tight_eval",
                     choices=["tight_eval", "sb_proof", "sb_forms", "tight_proof", "config1", "cpu_variants",
-                             "sb_reference", "config3", "near_critical"])
+                             "sb_reference", "config3", "near_critical", "tight_proof_batched"])
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.workload in SB_FULL:  # a whole size-bound proof (minutes)
@@ -762,6 +811,15 @@ def main():
         return
     if args.workload == "cpu_variants":  # the CPU implementations side by side (no GPU)
         print(json.dumps(cpu_variants(args.cpu_sample)), flush=True)
+        return
+    if args.workload == "tight_proof_batched":  # the batched form of the full tight proof alone
+        import __graft_entry__
+        __graft_entry__.build()
+        import circlecover_gb300 as cg
+        with cg.Prover(local) as prover:
+            r = proof_batched_only(prover)
+            if rank == 0:
+                print(json.dumps(r), flush=True)
         return
     if args.workload in ("tight_proof", "config1"):  # the tight proof forms alone
         import __graft_entry__

@@ -109,6 +109,7 @@ class CcRefineStats(ctypes.Structure):
                 ("cert_jobs", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
                 ("steps", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
                 ("warp_max_steps", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
+                ("cut", ctypes.c_uint64 * (REFINE_MAX_DEPTH + 1)),
                 ("order", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
@@ -225,7 +226,7 @@ EXPORTS = [
     "cc_mlp_train_step", "cc_mlp_infer", "cc_tight_first", "cc_tight_cell_log", "cc_autotune_eval",
     "cc_tight_generation", "cc_set_checkpoint", "cc_tight_resume", "cc_last_eval_counts", "cc_set_eval_graph",
     "cc_eval_graph_stats", "cc_set_eval_certify", "cc_last_eval_cert", "cc_tight_refine", "cc_set_refine_order",
-    "cc_sb_generation",
+    "cc_sb_generation", "cc_tight_eval_device_static",
 ]
 
 MLP_PARAMS = 5319
@@ -249,6 +250,7 @@ def load_library(path=LIB_PATH):
     lib.cc_last_error.restype = ctypes.c_char_p
     lib.cc_tight_eval.argtypes = [vp, vp, sz, vp]
     lib.cc_tight_eval_device.argtypes = [vp, vp, sz, vp, vp]
+    lib.cc_tight_eval_device_static.argtypes = [vp, sz, vp, vp]
     lib.cc_last_launch_count.argtypes = [vp]
     lib.cc_last_launch_count.restype = ctypes.c_uint64
     missing = [name for name in EXPORTS if not hasattr(lib, name)]
@@ -355,6 +357,14 @@ class Prover:
         self._check(self.lib.cc_tight_eval_device(self.h, ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
                                                   ctypes.c_void_p(stream_ptr) if stream_ptr else None),
                     "cc_tight_eval_device")
+
+    def tight_eval_device_static(self, soa_ptr, n, masks_ptr, stream_ptr=None):
+        """The allocation-free entry point (cc_tight_eval_device_static, no
+        handle; at most 65,536 boxes per call, calls on one device must not
+        overlap): same arguments as tight_eval_device."""
+        self._check(self.lib.cc_tight_eval_device_static(ctypes.c_void_p(soa_ptr), n, ctypes.c_void_p(masks_ptr),
+                                                         ctypes.c_void_p(stream_ptr) if stream_ptr else None),
+                    "cc_tight_eval_device_static")
 
     def autotune_eval(self, soa_ptr, n, masks_ptr):
         """Tune the evaluation passes on a device sample (cc_autotune_eval);
@@ -630,7 +640,7 @@ class Prover:
                             "kernel_launches": int(st.kernel_launches), "fp64_boxes": per_depth(st.fp64_boxes),
                             "cover_jobs": per_depth(st.cover_jobs), "gaps_jobs": per_depth(st.gaps_jobs),
                             "cert_jobs": per_depth(st.cert_jobs), "steps": per_depth(st.steps),
-                            "warp_max_steps": per_depth(st.warp_max_steps),
+                            "warp_max_steps": per_depth(st.warp_max_steps), "cut": per_depth(st.cut),
                             "order": int(st.order)}
 
     def tight_summary(self, criticals):
@@ -655,10 +665,11 @@ class Prover:
                     "cc_selftest_round")
         return out
 
-    def selftest_certify(self, group, boxes, call):
+    def selftest_certify(self, group, boxes, call, record=False):
         """FP64 certification runs of criterion group `group` (0 r1, 1 r1_r2,
         2 2x2, 3 leaf r1_r2_r3) with call number call[i] per box (1-based;
-        0 none; -1 all): bool array, the criterion held."""
+        0 none; -1 all): bool array, the criterion held (record: in the
+        record form the evaluation uses)."""
         boxes = np.ascontiguousarray(boxes, dtype=TIGHT_BOX)
         call = np.ascontiguousarray(call, dtype=np.int32)
         out = np.zeros(len(boxes), dtype=np.uint8)
@@ -667,7 +678,7 @@ class Prover:
                       ctypes.c_void_p]
         self._check(f(self.h, group, boxes.ctypes.data, call.ctypes.data, len(boxes), out.ctypes.data),
                     "cc_selftest_certify")
-        return out.astype(bool)
+        return ((out >> (1 if record else 0)) & 1).astype(bool)
 
     def selftest_round_to_floats(self, x):
         """(n, 4) floats per double: the FP32 enclosures' rounding down and up,

@@ -89,15 +89,17 @@ enum TrapSite : uint32_t {
 // one status byte per thread, kept in shared memory so that any device
 // function can set it without threading a context argument through every
 // criterion; 1024 threads per block at most.
-// Bits 6 and 7 of the byte are mode bits (cc_tight.cuh): bit 7 makes the
+// Bits 5, 6 and 7 of the byte are mode bits (cc_tight.cuh): bit 7 makes the
 // FP32 can_recurse record its arguments instead of evaluating, bit 6 makes
 // the FP64 can_recurse evaluate only one chosen call of a certification run
-// (cc_cert_state) and answer "false" to the others.  trap_clear() clears
-// both, trap() keeps them.
+// (cc_cert_state) and answer "false" to the others, and bit 5 (with bit 6)
+// makes that chosen call store its arguments (cc_cert_out) and answer "true"
+// instead of evaluating.  trap_clear() clears them, trap() keeps them.
 static __shared__ uint8_t cc_trap_words[1024];
 static constexpr uint8_t kTrapModeBit = 0x80;
 static constexpr uint8_t kCertModeBit = 0x40;
-static constexpr uint8_t kTrapModeBits = kTrapModeBit | kCertModeBit;
+static constexpr uint8_t kCertRecordBit = 0x20;
+static constexpr uint8_t kTrapModeBits = kTrapModeBit | kCertModeBit | kCertRecordBit;
 CC_FN void trap(uint32_t site) {
     cc_trap_words[threadIdx.x] = (uint8_t)((cc_trap_words[threadIdx.x] & kTrapModeBits) | site);
 }
@@ -107,6 +109,13 @@ CC_FN void trap_clear() { cc_trap_words[threadIdx.x] = TRAP_NONE; }
 // can_recurse calls, the high byte is the number (1-based) of the one call a
 // certification run evaluates (0: none).
 static __shared__ uint16_t cc_cert_state[1024];
+// The arguments of a certification run's chosen call (record form, bit 5):
+// ub_w, ub_h, ub_largest, lb_weight.  cc_cert_out points to one per thread
+// of the block, in the shared memory of the kernel that sets bit 5.
+struct CertCall {
+    double w, h, largest, lb;
+};
+static __shared__ CertCall* cc_cert_out;
 // FP64 certifications that failed in this translation unit's kernels since
 // the library was loaded: an FP32 decision the FP64 check did not confirm
 // (the FP64 result is used instead).  Expected to stay 0; the host reads it

@@ -256,12 +256,23 @@ __device__ __forceinline__ int cert_path_key(const double* __restrict__ in, size
     return ((call & 7) << 3) | f;
 }
 
+// With record buffers, a record group's run stops at its chosen call (the
+// record form of certify_group): the call's FP64 arguments go to the box's
+// record slot K, the state byte is marked pending (kCertPending), and
+// k_eval_cert_calls evaluates all those calls afterwards on full warps --
+// can_recurse is most of a run's work, and the lanes of a warp reach it at
+// different call sites.
+constexpr uint8_t kCertPending = 0x80;  // state byte: the chosen call awaits k_eval_cert_calls
+static_assert(sizeof(cc::CertCall) == sizeof(ct::CrArgs), "a record slot holds one chosen call");
+
 template <Layout L, int K>
 __global__ void __launch_bounds__(128) k_eval_cert(const double* __restrict__ in, size_t n, EvalQueues q) {
     __shared__ uint32_t s_box[kCertWindow];
     __shared__ uint8_t s_key[kCertWindow];
     __shared__ int s_cnt[kCertKeys + 1];
+    __shared__ cc::CertCall s_call[128];
     constexpr int kPer = kCertWindow / 128;
+    if (K < kRecGroups && threadIdx.x == 0) cc::cc_cert_out = s_call;
     const unsigned long long c = q.counts[kCntCert + K];
     const unsigned long long nq = c < q.cap ? c : q.cap;
     const unsigned long long stride = (unsigned long long)gridDim.x * kCertWindow;
@@ -316,7 +327,17 @@ __global__ void __launch_bounds__(128) k_eval_cert(const double* __restrict__ in
                 b_i = s_box[slot];
                 const ct::Box b = load_box<L>(in, n, b_i);
                 if (K < kRecGroups) {
-                    fail = !ct::certify_group<rec_group(K)>(b, q.states ? (int)s_key[slot] : -1);
+                    bool reached = false;
+                    fail = !ct::certify_group<rec_group(K)>(b, q.states ? (int)s_key[slot] : -1, q.args != nullptr,
+                                                            &reached);
+                    if (q.states) {
+                        uint8_t& st = q.states[(size_t)K * n + b_i];
+                        const bool pending = !fail && reached;
+                        if (pending)
+                            reinterpret_cast<cc::CertCall*>(q.args)[(size_t)b_i * ct::kCrRecordSlots + K] =
+                                s_call[threadIdx.x];
+                        st = (uint8_t)((st & (uint8_t)~kCertPending) | (pending ? kCertPending : 0));
+                    }
                 } else {
                     const uint8_t f = q.cflags[b_i];
                     fail = !ct::certify_r123(b, ((f & 1) ? (1u << 2) : 0u) | ((f & 2) ? (1u << 6) : 0u));
@@ -326,6 +347,90 @@ __global__ void __launch_bounds__(128) k_eval_cert(const double* __restrict__ in
             const unsigned long long s = cc::prove::warp_append(&q.counts[kCntRepair], valid && fail, q.cap,
                                                                 &q.counts[kCntOverflow]);
             if (s != ~0ULL) q.repair[s] = b_i;
+        }
+        __syncthreads();  // s_cnt and the sorted arrays are rewritten next iteration
+    }
+}
+
+// pass 4, last kernel: the chosen can_recurse call of every record-form
+// certification run that reached it, on the FP64 arguments k_eval_cert
+// stored; a false result or a trap fails the certification (the box goes to
+// the repair queue).  The calls take different branches of can_recurse_t
+// (size-bound ratio or not, orientation, the critical ratio's formula), so
+// each block sorts a window of 1,024 jobs by that path (ct::call_path_key)
+// before it evaluates them.
+__global__ void __launch_bounds__(128) k_eval_cert_calls(size_t n, EvalQueues q) {
+    __shared__ uint32_t s_slot[kCertWindow];
+    __shared__ uint8_t s_key[kCertWindow];
+    __shared__ int s_cnt[ct::kCallPathKeys + 2];
+    constexpr int kPer = kCertWindow / 128;
+    constexpr int kNone = ct::kCallPathKeys;  // nothing to evaluate (not pending, or past the end)
+    if (!q.states || !q.args) return;
+    unsigned long long cnt[kRecGroups], total = 0;
+#pragma unroll
+    for (int k = 0; k < kRecGroups; ++k) {
+        const unsigned long long c = q.counts[kCntCert + k];
+        cnt[k] = c < q.cap ? c : q.cap;
+        total += cnt[k];
+    }
+    const cc::CertCall* calls = reinterpret_cast<const cc::CertCall*>(q.args);
+    const unsigned long long stride = (unsigned long long)gridDim.x * kCertWindow;
+    // block-uniform loop: every thread of the block runs every iteration
+    for (unsigned long long base = (unsigned long long)blockIdx.x * kCertWindow; base < total; base += stride) {
+        for (int k = threadIdx.x; k < ct::kCallPathKeys + 2; k += 128) s_cnt[k] = 0;
+        __syncthreads();
+        uint32_t slot[kPer];
+        int key[kPer], rank[kPer];
+#pragma unroll
+        for (int t = 0; t < kPer; ++t) {
+            const unsigned long long j = base + (unsigned long long)t * 128 + threadIdx.x;
+            slot[t] = 0;
+            key[t] = kNone;
+            if (j < total) {
+                unsigned long long jj = j;
+                int k = 0;
+                while (k < kRecGroups - 1 && jj >= cnt[k]) jj -= cnt[k++];
+                const uint32_t b_i = q.cert[k][jj];
+                if (q.states[(size_t)k * n + b_i] & kCertPending) {
+                    slot[t] = b_i * (uint32_t)ct::kCrRecordSlots + (uint32_t)k;
+                    key[t] = ct::call_path_key(calls[slot[t]]);
+                }
+            }
+            rank[t] = atomicAdd(&s_cnt[key[t]], 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {  // exclusive prefix over the keys
+            int acc = 0;
+            for (int k = 0; k <= kNone; ++k) {
+                const int v = s_cnt[k];
+                s_cnt[k] = acc;
+                acc += v;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < kPer; ++t) {
+            const int off = s_cnt[key[t]] + rank[t];
+            s_slot[off] = slot[t];
+            s_key[off] = (uint8_t)key[t];
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int t = 0; t < kPer; ++t) {
+            const int pos = t * 128 + threadIdx.x;
+            bool fail = false;
+            const uint32_t sl = s_slot[pos];
+            if (s_key[pos] != kNone) {
+                const cc::CertCall a = calls[sl];
+                cc::trap_clear();
+                const bool ok = ct::can_recurse_t<double>(a.w, a.h, a.largest, a.lb);
+                fail = !ok || cc::trap_status() != cc::TRAP_NONE;
+                cc::trap_clear();
+            }
+            __syncwarp();
+            const unsigned long long s = cc::prove::warp_append(&q.counts[kCntRepair], fail, q.cap,
+                                                                &q.counts[kCntOverflow]);
+            if (s != ~0ULL) q.repair[s] = sl / (uint32_t)ct::kCrRecordSlots;
         }
         __syncthreads();  // s_cnt and the sorted arrays are rewritten next iteration
     }
@@ -529,7 +634,7 @@ CC_EVAL_LAUNCH(k_eval_gaps, in, n, q, masks)
 // pass launches at all
 static int pass_kernels(int pass, const EvalQueues& q) {
     if (pass == 0) return q.args ? 1 + kRecGroups * (1 + ct::kCrRecordSlots) + 1 : ct::F32_GROUPS + 1;
-    if (pass == 4) return q.cert[0] ? kCertQueues : 0;
+    if (pass == 4) return q.cert[0] ? kCertQueues + (q.args ? 1 : 0) : 0;
     if (pass == 5) return q.cert[0] ? 1 : 0;
     return 1;
 }
@@ -549,6 +654,7 @@ static void launch_pass(int pass, int minb, int g, cudaStream_t s, const double*
             k_eval_cert<L, 2><<<g, 128, 0, s>>>(in, n, q);
             k_eval_cert<L, 3><<<g, 128, 0, s>>>(in, n, q);
             k_eval_cert<L, 4><<<g, 128, 0, s>>>(in, n, q);
+            if (q.args) k_eval_cert_calls<<<g, 128, 0, s>>>(n, q);
             break;
         default:
             if (q.cert[0]) k_eval_repair<L><<<g, 128, 0, s>>>(in, n, q, masks);
@@ -766,13 +872,27 @@ __global__ void k_selftest_bisection_f32(int which, const double* __restrict__ a
 }
 
 // the FP64 certification run of record group K on each box, with the call
-// number given per box (1-based; 0 none; -1 every call evaluated)
+// number given per box (1-based; 0 none; -1 every call evaluated): bit 0 the
+// direct form, bit 1 the record form (the chosen call evaluated afterwards)
 template <int K>
-__global__ void k_selftest_certify(const double* __restrict__ aos, size_t n, const int* __restrict__ call,
-                                   uint8_t* __restrict__ out) {
+__global__ void __launch_bounds__(128) k_selftest_certify(const double* __restrict__ aos, size_t n,
+                                                          const int* __restrict__ call, uint8_t* __restrict__ out) {
+    __shared__ cc::CertCall s_call[128];
+    if (threadIdx.x == 0) cc::cc_cert_out = s_call;
+    __syncthreads();
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    out[i] = ct::certify_group<rec_group(K)>(load_box<Layout::AoS>(aos, n, i), call[i]) ? 1 : 0;
+    const ct::Box b = load_box<Layout::AoS>(aos, n, i);
+    const bool direct = ct::certify_group<rec_group(K)>(b, call[i]);
+    bool reached = false;
+    bool record = ct::certify_group<rec_group(K)>(b, call[i], true, &reached);
+    if (record && reached) {
+        const cc::CertCall a = s_call[threadIdx.x];
+        cc::trap_clear();
+        record = ct::can_recurse_t<double>(a.w, a.h, a.largest, a.lb) && cc::trap_status() == cc::TRAP_NONE;
+        cc::trap_clear();
+    }
+    out[i] = (uint8_t)((direct ? 1 : 0) | (record ? 2 : 0));
 }
 
 // the whole bisection (with the FP32 shortcuts) of each row
@@ -1547,6 +1667,7 @@ __global__ void k_cell_log(const Task* __restrict__ tasks, const Cell4* __restri
 
 enum { S_CELL_FEAT = 32, S_CELL_LOGITS, S_CELL_LOG };
 constexpr int S_CERT = 27;  // FP32 "true" leaf verdicts awaiting their FP64 certification
+constexpr int S_CERT_CALLS = 44;  // their chosen can_recurse calls (k_stage_cert)
 // run_chunk's answer when an FP64 certification failed: redo the chunk in the
 // plain form (FP64 criteria only)
 constexpr int kRedoPlain = 1000;
@@ -1564,6 +1685,11 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
     int st;
     if (hoist && (st = ccrt::ensure(h, S_LEAF2, caps.leaf2 * sizeof(Leaf2), &d_leaf2))) return st;
     if (hoist && (st = ccrt::ensure(h, S_CERT, caps.leaf * sizeof(CertLeaf), &d_cert))) return st;
+    // the chosen calls of the certification runs, one entry per queued leaf
+    // (windows of 1,024 may reach past the count by less than a window)
+    void* d_cert_calls = nullptr;
+    if (hoist && (st = ccrt::ensure(h, S_CERT_CALLS, (caps.leaf + 1024) * sizeof(cc::CertCall), &d_cert_calls)))
+        return st;
     if ((st = ccrt::ensure(h, S_GAPS, caps.gaps * sizeof(GapsLeaf), &d_gaps))) return st;
     if ((st = ccrt::ensure(h, S_PARENTS, np * sizeof(cc_tight_box), &d_par))) return st;
     if ((st = ccrt::ensure(h, S_TASKS, ntasks * sizeof(Task), &d_tasks))) return st;
@@ -1677,8 +1803,8 @@ int run_chunk(cc_handle* h, const std::vector<cc_tight_box>& parents, size_t a, 
                                      (Critical*)d_crit, caps, cnt, task_base);
         CC_LAUNCHED(h);
         if (hoist) {  // FP64 certification of the slice's FP32 "true" leaf verdicts
-            k_stage_cert<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const CertLeaf*)d_cert, s[3],
-                                            caps, cnt);
+            k_stage_cert<<<g, 128, 0, sm>>>((const Task*)d_tasks, (const Cell4*)d_c4, (const CertLeaf*)d_cert,
+                                            (cc::CertCall*)d_cert_calls, s[3], caps, cnt);
             CC_LAUNCHED(h);
         }
     }
@@ -2037,7 +2163,7 @@ extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, siz
 // counterpart; the near-critical stress workload).  Every level runs the
 // certified evaluation (the six criteria and the emptiness bits, passes 0-5)
 // on its boxes -- or the first-success evaluation in the plain or the learned
-// order; k_refine_split then sorts them: certified or empty boxes are
+// order; the split kernels then sort them: certified or empty boxes are
 // done, trapped ones are kept as criticals, the others are bisected into the
 // next level -- or kept as criticals at the last level.  The boxes of a level
 // are independent and of uneven cost (the criteria's branches and
@@ -2046,11 +2172,11 @@ extern "C" int cc_tight_summary(cc_handle* h, const cc_tight_box* criticals, siz
 namespace {
 
 enum { S_REF_A = 28, S_REF_B = 29, S_REF_MASKS = 30, S_REF_CRIT = 31, S_REF_SOA = 40, S_REF_FIRST = 41,
-       S_REF_MLP = 42 };
+       S_REF_MLP = 42, S_REF_BLOCKS = 43 };
 
 struct RefineCounters {
     unsigned long long n_next, n_crit, n_decided, overflow;
-    unsigned long long fp64, cover, gaps, cert, steps, warp_max_steps;
+    unsigned long long fp64, cover, gaps, cert, steps, warp_max_steps, n_cut;
 };
 
 // one evaluation batch's queue sizes added to the level's occupancy
@@ -2097,51 +2223,141 @@ __device__ __forceinline__ void bisect_dim(const cc_tight_box& b, int dim, cc_ti
     u.lb = mid;
 }
 
+// The split of a level, in three kernels that keep the level's order (so a
+// refinement is deterministic and its levels are those of the oracle's
+// sequential model): each block owns a contiguous range of the level;
+// k_refine_count counts its split candidates (undecided, not trapped, not
+// the last level) and its kept boxes (trapped, or undecided at the last
+// level); k_refine_scan turns the counts into each block's output offsets,
+// carrying at most pair_cap candidates (the first ones in level order) into
+// the next level and keeping the others as criticals (flag 3: cut by the
+// population cap); k_refine_emit writes the children (lo half, hi half) and
+// the criticals at those offsets, in level order within each block.
+struct RefineBlocks {
+    unsigned long long* cand;  // per block: split candidates, then their offset (exclusive scan)
+    unsigned long long* keep;  // per block: kept boxes, then their offset (cut candidates included)
+    unsigned long long per_block;
+    int n_blocks;
+};
+
 template <class V>
-__global__ void __launch_bounds__(128) k_refine_split(const cc_tight_box* __restrict__ in, size_t n, V verdicts,
-                                                      int depth, int last, cc_tight_box* __restrict__ out,
-                                                      unsigned long long out_pairs, cc_tight_box* __restrict__ crit,
-                                                      uint32_t* __restrict__ crit_flags, unsigned long long crit_cap,
+__global__ void __launch_bounds__(128) k_refine_count(size_t n, V verdicts, int last, RefineBlocks rb,
                                                       RefineCounters* c) {
-    unsigned decided_n = 0;
-    unsigned long long steps_n = 0, warp_max_n = 0;
-    const int dim = depth % 5;
-    CC_WARP_LOOP(n) {
-        const unsigned long long i = base_ + (threadIdx.x & 31);
-        const bool valid = i < n;
-        bool split = false, keep = false;
-        uint32_t flag = 0;
+    __shared__ unsigned long long s_sum[2][4];
+    const unsigned long long lo = (unsigned long long)blockIdx.x * rb.per_block;
+    const unsigned long long hi = lo + rb.per_block < n ? lo + rb.per_block : n;
+    unsigned long long cand = 0, keep = 0, decided_n = 0, steps_n = 0, warp_max_n = 0;
+    for (unsigned long long base = lo + (threadIdx.x & ~31u); base < hi; base += blockDim.x) {
+        const unsigned long long i = base + (threadIdx.x & 31);
         unsigned lane_steps = 0;
-        cc_tight_box b{};
-        if (valid) {
+        if (i < hi) {
             bool trapped, decided;
-            unsigned st;
-            verdicts.get(i, trapped, decided, st);
-            steps_n += st;
-            lane_steps = st;
-            decided_n += decided ? 1u : 0u;
-            b = in[i];
-            split = !trapped && !decided && !last;
-            keep = trapped || (!decided && last);
-            flag = trapped ? 1u : 2u;
+            verdicts.get(i, trapped, decided, lane_steps);
+            steps_n += lane_steps;
+            decided_n += decided ? 1 : 0;
+            cand += (!trapped && !decided && !last) ? 1 : 0;
+            keep += (trapped || (!decided && last)) ? 1 : 0;
         }
         warp_max_n += __reduce_max_sync(0xffffffffu, lane_steps);
-        unsigned long long s = cc::prove::warp_append(&c->n_next, split, out_pairs, &c->overflow);
-        if (s != ~0ULL) bisect_dim(b, dim, out[2 * s], out[2 * s + 1]);
-        s = cc::prove::warp_append(&c->n_crit, keep, crit_cap, &c->overflow);
-        if (s != ~0ULL) {
-            crit[s] = b;
-            crit_flags[s] = flag;
-        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
+        cand += __shfl_xor_sync(0xffffffffu, cand, o);
+        keep += __shfl_xor_sync(0xffffffffu, keep, o);
         decided_n += __shfl_xor_sync(0xffffffffu, decided_n, o);
         steps_n += __shfl_xor_sync(0xffffffffu, steps_n, o);
     }
-    if ((threadIdx.x & 31) == 0 && decided_n) atomicAdd(&c->n_decided, (unsigned long long)decided_n);
-    if ((threadIdx.x & 31) == 0 && steps_n) atomicAdd(&c->steps, steps_n);
-    if ((threadIdx.x & 31) == 0 && warp_max_n) atomicAdd(&c->warp_max_steps, warp_max_n);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_sum[0][w] = cand;
+        s_sum[1][w] = keep;
+        if (decided_n) atomicAdd(&c->n_decided, decided_n);
+        if (steps_n) atomicAdd(&c->steps, steps_n);
+        if (warp_max_n) atomicAdd(&c->warp_max_steps, warp_max_n);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        rb.cand[blockIdx.x] = s_sum[0][0] + s_sum[0][1] + s_sum[0][2] + s_sum[0][3];
+        rb.keep[blockIdx.x] = s_sum[1][0] + s_sum[1][1] + s_sum[1][2] + s_sum[1][3];
+    }
+}
+
+__global__ void k_refine_scan(RefineBlocks rb, unsigned long long pair_cap, RefineCounters* c) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned long long cand_acc = 0, keep_acc = 0, cut_total = 0;
+    for (int b = 0; b < rb.n_blocks; ++b) {
+        const unsigned long long nc = rb.cand[b], nk = rb.keep[b];
+        // candidates of this block past the cap are kept instead
+        const unsigned long long room = pair_cap > cand_acc ? pair_cap - cand_acc : 0;
+        const unsigned long long cut = nc > room ? nc - room : 0;
+        rb.cand[b] = cand_acc;
+        rb.keep[b] = keep_acc;
+        cand_acc += nc;
+        keep_acc += nk + cut;
+        cut_total += cut;
+    }
+    c->n_next = cand_acc < pair_cap ? cand_acc : pair_cap;
+    c->n_crit = keep_acc;
+    c->n_cut = cut_total;
+}
+
+// exclusive rank of `flag` among the block's 128 threads (in thread order),
+// and the block's total; every thread calls it
+__device__ __forceinline__ unsigned block_rank(bool flag, unsigned* s_warp, unsigned& total) {
+    const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned ballot = __ballot_sync(0xffffffffu, flag);
+    if (lane == 0) s_warp[w] = __popc(ballot);
+    __syncthreads();
+    unsigned before = 0;
+    total = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        before += (unsigned)k < w ? s_warp[k] : 0u;
+        total += s_warp[k];
+    }
+    __syncthreads();  // s_warp is rewritten by the next call
+    return before + __popc(ballot & ((1u << lane) - 1u));
+}
+
+template <class V>
+__global__ void __launch_bounds__(128) k_refine_emit(const cc_tight_box* __restrict__ in, size_t n, V verdicts,
+                                                     int depth, int last, RefineBlocks rb,
+                                                     unsigned long long pair_cap, cc_tight_box* __restrict__ out,
+                                                     cc_tight_box* __restrict__ crit,
+                                                     uint32_t* __restrict__ crit_flags) {
+    __shared__ unsigned s_warp[4];
+    const unsigned long long lo = (unsigned long long)blockIdx.x * rb.per_block;
+    const unsigned long long hi = lo + rb.per_block < n ? lo + rb.per_block : n;
+    unsigned long long cand_at = rb.cand[blockIdx.x], keep_at = rb.keep[blockIdx.x];
+    const int dim = depth % 5;
+    for (unsigned long long base = lo; base < hi; base += blockDim.x) {  // block-uniform loop
+        const unsigned long long i = base + threadIdx.x;
+        bool cand = false, keep = false, trapped = false;
+        if (i < hi) {
+            bool decided;
+            unsigned st;
+            verdicts.get(i, trapped, decided, st);
+            cand = !trapped && !decided && !last;
+            keep = trapped || (!decided && last);
+        }
+        unsigned n_cand;
+        const unsigned long long r = cand_at + block_rank(cand, s_warp, n_cand);
+        const bool split = cand && r < pair_cap;
+        const bool kept = keep || (cand && !split);
+        unsigned n_kept;
+        const unsigned long long k = keep_at + block_rank(kept, s_warp, n_kept);
+        if (split || kept) {
+            const cc_tight_box b = in[i];
+            if (split) {
+                bisect_dim(b, dim, out[2 * r], out[2 * r + 1]);
+            } else {
+                crit[k] = b;
+                crit_flags[k] = trapped ? 1u : (keep ? 2u : 3u);
+            }
+        }
+        cand_at += n_cand;
+        keep_at += n_kept;
+    }
 }
 
 }  // namespace
@@ -2184,12 +2400,20 @@ extern "C" int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n
     int cur_slot = S_REF_A, next_slot = S_REF_B;
     size_t cur_n = n;
     const size_t chunk = (size_t)1 << 24;  // evaluation batches: bounded scratch
+    const unsigned long long pair_cap = max_live / 2;  // children pairs a level may carry on
     for (int d = 0; d <= max_depth && cur_n; ++d) {
-        const bool last = d == max_depth || 2 * cur_n > max_live;
-        if (last && d < max_depth) st.stopped_at_cap = 1;
-        void *cur, *next, *masks, *crit;
+        const bool last = d == max_depth;
+        const size_t next_n = last ? 1 : 2 * std::min<size_t>(cur_n, pair_cap);
+        void *cur, *next, *masks, *crit, *blocks;
         if ((rc = ccrt::ensure(h, cur_slot, cur_n * sizeof(cc_tight_box), &cur))) return rc;
-        if ((rc = ccrt::ensure(h, next_slot, (last ? 1 : 2 * cur_n) * sizeof(cc_tight_box), &next))) return rc;
+        if ((rc = ccrt::ensure(h, next_slot, next_n * sizeof(cc_tight_box), &next))) return rc;
+        RefineBlocks rb;
+        rb.n_blocks = eval_grid(h, cur_n);
+        rb.per_block = (cur_n + rb.n_blocks - 1) / rb.n_blocks;
+        if ((rc = ccrt::ensure(h, S_REF_BLOCKS, 2 * (size_t)rb.n_blocks * sizeof(unsigned long long), &blocks)))
+            return rc;
+        rb.cand = (unsigned long long*)blocks;
+        rb.keep = rb.cand + rb.n_blocks;
         if ((rc = ccrt::ensure(h, S_REF_MASKS, cur_n * sizeof(uint32_t), &masks))) return rc;
         if ((rc = ccrt::ensure(h, S_REF_CRIT, cur_n * (sizeof(cc_tight_box) + sizeof(uint32_t)), &crit))) return rc;
         void *soa = nullptr, *first = nullptr, *mlp = nullptr;
@@ -2221,14 +2445,22 @@ extern "C" int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n
         }
         cc_tight_box* crit_boxes = (cc_tight_box*)crit;
         uint32_t* crit_fl = (uint32_t*)(crit_boxes + cur_n);
+        const int lastf = last ? 1 : 0;
+        const MaskVerdicts mv{(const uint32_t*)masks};
+        const FirstVerdicts fv{(const uint8_t*)first, (const uint8_t*)first + cur_n};
         if (order == CC_REFINE_MASKS)
-            k_refine_split<<<eval_grid(h, cur_n), 128, 0, s>>>(
-                (const cc_tight_box*)cur, cur_n, MaskVerdicts{(const uint32_t*)masks}, d, last ? 1 : 0,
-                (cc_tight_box*)next, last ? 0 : cur_n, crit_boxes, crit_fl, cur_n, dc);
+            k_refine_count<<<rb.n_blocks, 128, 0, s>>>(cur_n, mv, lastf, rb, dc);
         else
-            k_refine_split<<<eval_grid(h, cur_n), 128, 0, s>>>(
-                (const cc_tight_box*)cur, cur_n, FirstVerdicts{(const uint8_t*)first, (const uint8_t*)first + cur_n}, d,
-                last ? 1 : 0, (cc_tight_box*)next, last ? 0 : cur_n, crit_boxes, crit_fl, cur_n, dc);
+            k_refine_count<<<rb.n_blocks, 128, 0, s>>>(cur_n, fv, lastf, rb, dc);
+        CC_LAUNCHED(h);
+        k_refine_scan<<<1, 32, 0, s>>>(rb, pair_cap, dc);
+        CC_LAUNCHED(h);
+        const cc_tight_box* cb = (const cc_tight_box*)cur;
+        cc_tight_box* nb = (cc_tight_box*)next;
+        if (order == CC_REFINE_MASKS)
+            k_refine_emit<<<rb.n_blocks, 128, 0, s>>>(cb, cur_n, mv, d, lastf, rb, pair_cap, nb, crit_boxes, crit_fl);
+        else
+            k_refine_emit<<<rb.n_blocks, 128, 0, s>>>(cb, cur_n, fv, d, lastf, rb, pair_cap, nb, crit_boxes, crit_fl);
         CC_LAUNCHED(h);
         CC_CUDA(h, cudaEventRecord(ev.e1, s));
         RefineCounters hc;
@@ -2246,6 +2478,8 @@ extern "C" int cc_tight_refine(cc_handle* h, const cc_tight_box* boxes, size_t n
         st.cert_jobs[d] = hc.cert;
         st.steps[d] = hc.steps;
         st.warp_max_steps[d] = hc.warp_max_steps;
+        st.cut[d] = hc.n_cut;
+        if (hc.n_cut) st.stopped_at_cap = 1;
         st.depths_run = d + 1;
         if (hc.n_crit) {
             const size_t old = out.size();

@@ -29,7 +29,7 @@ struct cc_handle {
         void* ptr = nullptr;
         size_t bytes = 0;
     };
-    Buf bufs[44];
+    Buf bufs[48];
     // pinned host staging for the host-memory entry points
     void* pinned = nullptr;
     size_t pinned_bytes = 0;

@@ -143,10 +143,15 @@ CC_FN bool can_recurse_t(S ub_w, S ub_h, S ub_largest, S lb_weight) {
 // the criterion holds, whatever the FP32 evaluation did.
 CC_FN bool can_recurse(double ub_w, double ub_h, double ub_largest, double lb_weight) {
 #if CC_DEVICE_BUILD
-    if (cc_trap_words[threadIdx.x] & kCertModeBit) {
+    const uint8_t mode = cc_trap_words[threadIdx.x];
+    if (mode & kCertModeBit) {
         const uint16_t s = cc_cert_state[threadIdx.x];
         cc_cert_state[threadIdx.x] = (uint16_t)(s + 1);
         if ((s & 0xff) + 1 != (s >> 8)) return false;
+        if (mode & kCertRecordBit) {  // the chosen call, evaluated later (cert_record_begin)
+            cc_cert_out[threadIdx.x] = CertCall{ub_w, ub_h, ub_largest, lb_weight};
+            return true;
+        }
     }
 #endif
     return can_recurse_t<double>(ub_w, ub_h, ub_largest, lb_weight);
@@ -158,10 +163,42 @@ CC_FN void cert_begin(int call) {
     cc_cert_state[threadIdx.x] = (uint16_t)(call << 8);
     cc_trap_words[threadIdx.x] = kCertModeBit;
 }
-CC_FN void cert_end() { cc_trap_words[threadIdx.x] &= (uint8_t)~kCertModeBit; }
+CC_FN void cert_end() { cc_trap_words[threadIdx.x] &= (uint8_t)~(kCertModeBit | kCertRecordBit); }
+// The branches can_recurse_t takes on a recorded call, as a sort key for
+// running recorded calls on warps that follow one path: 0 the size-bound
+// ratio (the largest disk at most 9/64 of the shorter side squared), else 1
+// + 3 * (wide rectangle) + the critical ratio's formula (three-disk,
+// two-disk, both) for the aspect ratio.  Computed in FP32 near the
+// thresholds; it only groups the calls, the evaluation is can_recurse_t's.
+static constexpr int kCallPathKeys = 7;
+CC_FN int call_path_key(const CertCall& a) {
+    const float w = (float)a.w, h = (float)a.h;
+    const float side = fminf(w, h);
+    const float norm = (float)a.largest / (side * side);
+    if (!(norm > 0.140625f)) return 0;
+    const bool tall = w <= h;
+    const float aspect = tall ? h / w : w / h;
+    const int f = aspect <= 1.0357f ? 0 : (aspect >= 1.0359f ? 1 : 2);
+    return 1 + (tall ? 0 : 3) + f;
+}
+// A certification run in record form: the chosen call stores its arguments
+// in cc_cert_out[threadIdx.x] and answers "true", so the criterion returns
+// true right there (the call sites' form); the call itself is evaluated
+// afterwards on the stored arguments, by can_recurse_t.  After the run,
+// cert_reached() tells whether the run got to the chosen call.
+CC_FN void cert_record_begin(int call) {
+    cc_cert_state[threadIdx.x] = (uint16_t)(call << 8);
+    cc_trap_words[threadIdx.x] = kCertModeBit | kCertRecordBit;
+}
+CC_FN bool cert_reached() {
+    const uint16_t s = cc_cert_state[threadIdx.x];
+    return (s & 0xff) >= (s >> 8);
+}
 // the FP32 can_recurse counts its calls (low byte of cc_cert_state)
 CC_FN void cert_count_reset() { cc_cert_state[threadIdx.x] = 0; }
 CC_FN int cert_count() { return cc_cert_state[threadIdx.x] & 0xff; }
+// the FP32 run's last can_recurse call answered "true"
+CC_FN bool cert_last_true() { return (cc_cert_state[threadIdx.x] & 0x8000) != 0; }
 
 // One out-of-line copy for the FP32 evaluation (it is called from many
 // sites), with a shortcut before its costly part.  Where largest_norm is
@@ -208,10 +245,8 @@ __device__ __noinline__ inline bool can_recurse_record(f32::Fv ub_w, f32::Fv ub_
     return false;
 }
 
-__device__ __noinline__ inline bool can_recurse(f32::Fv ub_w, f32::Fv ub_h, f32::Fv ub_largest, f32::Fv lb_weight) {
+__device__ __forceinline__ bool can_recurse_f32(f32::Fv ub_w, f32::Fv ub_h, f32::Fv ub_largest, f32::Fv lb_weight) {
     using f32::Fv;
-    if (cc_trap_words[threadIdx.x] & kTrapModeBit) return can_recurse_record(ub_w, ub_h, ub_largest, lb_weight);
-    cc_cert_state[threadIdx.x]++;  // call count for a later certification run (cert_count)
     const Fv ub_area = f32::mul(ub_w, ub_h);
     const Fv s = f32::rcp_up(f32::lesser(ub_w, ub_h));
     const Fv largest_norm = f32::mul(f32::mul(s, s), ub_largest);
@@ -229,6 +264,15 @@ __device__ __noinline__ inline bool can_recurse(f32::Fv ub_w, f32::Fv ub_h, f32:
         if (lb_weight.hi < need_lo) return false;
     }
     return can_recurse_t<f32::Fv>(ub_w, ub_h, ub_largest, lb_weight);
+}
+// The call count for a later certification run (cert_count) and, in bit 15,
+// whether this call answered "true" (cert_last_true).
+__device__ __noinline__ inline bool can_recurse(f32::Fv ub_w, f32::Fv ub_h, f32::Fv ub_largest, f32::Fv lb_weight) {
+    if (cc_trap_words[threadIdx.x] & kTrapModeBit) return can_recurse_record(ub_w, ub_h, ub_largest, lb_weight);
+    const bool r = can_recurse_f32(ub_w, ub_h, ub_largest, lb_weight);
+    const uint16_t s = cc_cert_state[threadIdx.x];
+    cc_cert_state[threadIdx.x] = (uint16_t)((((s & 0xff) + 1) & 0xff) | (r ? 0x8000 : 0));
+    return r;
 }
 #endif
 
@@ -1320,11 +1364,18 @@ CC_FN_INL uint32_t eval_group_f32(const Box& in64, EncBox* keep = nullptr) {
 // whose FP32 answer settled the criterion; 0: none, the criterion held
 // without one), or with all its calls for call < 0.  True if it holds
 // without reaching a trap site.
+// Record form (record, call > 0): the chosen call only stores its arguments
+// (cc_cert_out) and answers "true"; *reached tells whether the run got to it.
+// Then true with *reached means "certified if can_recurse_t holds on the
+// stored arguments"; true without it, certified outright (the criterion held
+// before that call, every earlier call answering "false").
 template <int G>
-CC_FN_INL bool certify_group(const Box& in, int call) {
+CC_FN_INL bool certify_group(const Box& in, int call, bool record = false, bool* reached = nullptr) {
     const Iv la = in.la, r1 = in.r[0], r2 = in.r[1], r3 = in.r[2];
     const Iv weight = required_weight_for(la);
-    if (call >= 0) cert_begin(call);
+    record = record && call > 0;
+    if (record) cert_record_begin(call);
+    else if (call >= 0) cert_begin(call);
     else trap_clear();
     bool ok;
     if (G == F32_R1) {
@@ -1343,6 +1394,7 @@ CC_FN_INL bool certify_group(const Box& in, int call) {
         ok = G == F32_2X2 ? two_by_two_strategies(v, R) : r1_r2_r3_strategies(v, R4);
     }
     const bool clean = trap_status() == TRAP_NONE;
+    if (reached) *reached = record && cert_reached();
     cert_end();
     trap_clear();
     return ok && clean;
@@ -1418,7 +1470,9 @@ CC_FN_INL bool first_f32(Crit crit, const Box& v, Iv rest, int* how = nullptr) {
 // first_f32 with the certification of a decided "true" left to the caller
 // (the proof queues it for a certification pass): *how as first_f32 (2:
 // FP32 "true", not yet certified), *calls = the number of the call that
-// settled the FP32 run (its last call; 0 if none), for certify_leaf.
+// settled the FP32 run (its last call, if that call answered "true"; 0 if
+// none did: the criterion then held with every call "false"), for
+// certify_leaf.
 template <class Crit>
 CC_FN_INL bool first_f32_deferred(Crit crit, const Box& v, Iv rest, int* how, int* calls) {
     const uint32_t saved = trap_status();
@@ -1426,7 +1480,7 @@ CC_FN_INL bool first_f32_deferred(Crit crit, const Box& v, Iv rest, int* how, in
     cert_count_reset();
     const bool ok32 = crit(enclose(v), f32::of(rest));
     const bool decided = trap_status() == TRAP_NONE;
-    *calls = cert_count();
+    *calls = cert_last_true() ? cert_count() : 0;
     trap_clear();
     if (saved != TRAP_NONE) trap(saved);
     if (decided) {
@@ -1438,11 +1492,18 @@ CC_FN_INL bool first_f32_deferred(Crit crit, const Box& v, Iv rest, int* how, in
 }
 // The FP64 certification of a deferred "true": the criterion with only call
 // number `call` evaluated; true if it holds without reaching a trap site.
+// Record form (record, call > 0) as in certify_group: the chosen call only
+// stores its arguments (cc_cert_out), *reached tells whether the run got to
+// it, and the caller evaluates it afterwards (can_recurse_t).
 template <class Crit>
-CC_FN_INL bool certify_leaf(Crit crit, const Box& v, Iv rest, int call) {
-    cert_begin(call);
+CC_FN_INL bool certify_leaf(Crit crit, const Box& v, Iv rest, int call, bool record = false,
+                            bool* reached = nullptr) {
+    record = record && call > 0;
+    if (record) cert_record_begin(call);
+    else cert_begin(call);
     const bool ok = crit(v, rest);
     const bool clean = trap_status() == TRAP_NONE;
+    if (reached) *reached = record && cert_reached();
     cert_end();
     trap_clear();
     return ok && clean;

@@ -649,11 +649,24 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
 // FP64 form.
 constexpr int kLeafCertWindow = 1024;
 constexpr int kLeafCertKeys = 128;
+// A recorded call written earlier in this kernel (by any thread of the
+// block, before a barrier): loaded from L2 (ld.global.cg), never through the
+// non-coherent read-only path.
+__device__ __forceinline__ cc::CertCall load_call(const cc::CertCall* p) {
+    const double* d = reinterpret_cast<const double*>(p);
+    return cc::CertCall{__ldcg(d), __ldcg(d + 1), __ldcg(d + 2), __ldcg(d + 3)};
+}
+
 __global__ void __launch_bounds__(128) k_stage_cert(const Task* __restrict__ tasks, const Cell4* __restrict__ cells,
-                                                    const CertLeaf* __restrict__ cq, int s4, Caps caps, Counters* c) {
+                                                    const CertLeaf* __restrict__ cq, cc::CertCall* calls, int s4,
+                                                    Caps caps, Counters* c) {
     __shared__ CertLeaf s_job[kLeafCertWindow];
     __shared__ int s_cnt[kLeafCertKeys + 1];
+    __shared__ uint8_t s_pend[kLeafCertWindow];
+    __shared__ uint16_t s_order[kLeafCertWindow];
     constexpr int kPer = kLeafCertWindow / 128;
+    constexpr int kNone = tight::kCallPathKeys;  // no recorded call to evaluate
+    static_assert(kNone + 1 <= kLeafCertKeys + 1, "s_cnt holds the call keys");
     const unsigned long long n_in = *(volatile unsigned long long*)&c->n_cert;
     const unsigned long long total = n_in < caps.leaf ? n_in : caps.leaf;
     unsigned ok_n = 0, fail_n = 0;
@@ -693,28 +706,79 @@ __global__ void __launch_bounds__(128) k_stage_cert(const Task* __restrict__ tas
         __syncthreads();
         const unsigned long long left = total - base;
         const int valid_n = left < (unsigned long long)kLeafCertWindow ? (int)left : kLeafCertWindow;
+        // the criteria in record form: a run stops at its chosen call, whose
+        // arguments go to calls[base + slot] (cc_cert_out points at the
+        // block's 128 entries of this round) ...
 #pragma unroll 1
         for (int t = 0; t < kPer; ++t) {
             const int slot = t * 128 + threadIdx.x;
+            if (threadIdx.x == 0) cc::cc_cert_out = calls + base + (unsigned long long)t * 128;
+            __syncthreads();
+            uint8_t pend = 0;
             if (slot < valid_n) {
                 const CertLeaf m = s_job[slot];
                 const Cell4& p = cells[m.cell4];
                 const Task tk = tasks[p.task];
                 trap_clear();
                 const Box v = leaf_box(p, tk.la, subinterval(p.r4r, m.i4, s4));
-                bool ok;
+                bool ok, reached = false;
                 if (m.crit == 0) {
                     Iv R = tk.weight - v.r[0] - v.r[1] - v.r[2] - v.r[3];
                     tighten_lb(R, 0.0);
-                    ok = tight::certify_leaf(tight::TwoByTwo{}, v, R, m.call);
+                    ok = tight::certify_leaf(tight::TwoByTwo{}, v, R, m.call, true, &reached);
                 } else {
-                    ok = tight::certify_leaf(tight::LeafR123{}, v, p.R4, m.call);
+                    ok = tight::certify_leaf(tight::LeafR123{}, v, p.R4, m.call, true, &reached);
                 }
+                if (ok && reached) pend = 1;
+                else if (ok) ++ok_n;
+                else ++fail_n;
+            }
+            s_pend[slot] = pend;
+            __syncthreads();  // cc_cert_out is moved next round
+        }
+        // ... and the chosen calls of the window run afterwards, sorted by the
+        // branches can_recurse_t takes on them (tight::call_path_key), so the
+        // lanes of a warp follow one path (the block's global writes above are
+        // visible to all its threads after the barrier, read with load_call)
+        for (int k = threadIdx.x; k <= kNone; k += 128) s_cnt[k] = 0;
+        __syncthreads();
+        int ckey[kPer], crank[kPer];
+#pragma unroll
+        for (int t = 0; t < kPer; ++t) {
+            const int slot = t * 128 + threadIdx.x;
+            ckey[t] = (slot < valid_n && s_pend[slot]) ? tight::call_path_key(load_call(calls + base + slot)) : kNone;
+            crank[t] = atomicAdd(&s_cnt[ckey[t]], 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int k = 0; k <= kNone; ++k) {
+                const int v = s_cnt[k];
+                s_cnt[k] = acc;
+                acc += v;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < kPer; ++t) {
+            const int off = s_cnt[ckey[t]] + crank[t];
+            s_order[off] = (uint16_t)(t * 128 + threadIdx.x);
+            s_pend[off] = (uint8_t)ckey[t];  // the key, now in sorted order
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int t = 0; t < kPer; ++t) {
+            const int pos = t * 128 + threadIdx.x;
+            if (s_pend[pos] != kNone) {
+                const cc::CertCall a = load_call(calls + base + s_order[pos]);
+                trap_clear();
+                const bool ok = tight::can_recurse_t<double>(a.w, a.h, a.largest, a.lb) && trap_status() == TRAP_NONE;
+                trap_clear();
                 if (ok) ++ok_n;
                 else ++fail_n;
             }
         }
-        __syncthreads();  // s_cnt and s_job are rewritten next iteration
+        __syncthreads();  // s_cnt, s_job, s_pend and s_order are rewritten next iteration
     }
     unsigned v0 = ok_n, v1 = fail_n;
 #pragma unroll

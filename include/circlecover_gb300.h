@@ -532,10 +532,14 @@ int cc_tight_first(cc_handle* h, const double* soa, size_t n, int learned, uint8
  * other box is bisected at mid = 0.5 lo + 0.5 hi (rounded to nearest; the
  * halves' union is the box) along lambda, r1, r2, r3, r4 in turn by depth
  * (depth mod 5), and both halves go to the next level.  Boxes still
- * undecided at the last level are kept as criticals (flag 2); the last level
- * comes early when the next one would hold more than max_live boxes (0: 2^26),
- * which stats->stopped_at_cap reports.  *criticals / *flags (cc_free) in
- * level order.  cc_interrupt stops after the current level.
+ * undecided at the last level are kept as criticals (flag 2).  A level holds
+ * at most max_live boxes (0: 2^26): of the boxes to bisect, the first
+ * max_live / 2 in level order go on, the others are kept as criticals
+ * (flag 3), which stats->cut and stats->stopped_at_cap report.  The next
+ * level lists the halves (lower, upper) in the order of their boxes, and
+ * *criticals / *flags (cc_free) come in level order and, within a level, in
+ * box order, so a refinement is deterministic.  cc_interrupt stops after the
+ * current level.
  *
  * cc_set_refine_order chooses how a level decides its boxes:
  *   CC_REFINE_MASKS        the certified evaluation of all six criteria and
@@ -559,7 +563,7 @@ typedef struct cc_refine_stats {
     uint64_t decided[CC_REFINE_MAX_DEPTH + 1]; /* of which certified or empty */
     float ms[CC_REFINE_MAX_DEPTH + 1];         /* device time of each depth (CUDA events) */
     int32_t depths_run;
-    int32_t stopped_at_cap;
+    int32_t stopped_at_cap;                    /* some level cut boxes (flag 3) */
     double seconds;                            /* wall time of the call */
     uint64_t kernel_launches;
     /* queue occupancy per depth (CC_REFINE_MASKS): boxes the FP32 pass left
@@ -575,6 +579,7 @@ typedef struct cc_refine_stats {
      * share of lanes that work while the warp runs criteria */
     uint64_t steps[CC_REFINE_MAX_DEPTH + 1];
     uint64_t warp_max_steps[CC_REFINE_MAX_DEPTH + 1];
+    uint64_t cut[CC_REFINE_MAX_DEPTH + 1];     /* boxes kept as criticals by the population cap */
     int32_t order;
     int32_t pad;
 } cc_refine_stats;
@@ -631,8 +636,10 @@ int cc_selftest_bisection_width(cc_handle* h, int which, const double* args, siz
  * r1_r2_r3_strategies) on n boxes in host memory, at the arguments of
  * cc_tight_eval, each with its own call number call[i]: 1-based number of
  * the one can_recurse call evaluated (every other call answers "false"), 0
- * for none, -1 for all (the plain FP64 criterion).  out[i] = 1 if the
- * criterion holds without reaching a trap site. */
+ * for none, -1 for all (the plain FP64 criterion).  out[i] bit 0 = the
+ * criterion holds without reaching a trap site; bit 1 = the same run in the
+ * record form the evaluation uses (the chosen call stores its arguments and
+ * answers "true", then can_recurse is evaluated on them) certifies it. */
 int cc_selftest_certify(cc_handle* h, int group, const cc_tight_box* boxes, const int* call, size_t n,
                         uint8_t* out);
 /* Measured FP64 instruction throughput of the device (ops/s; one FP64

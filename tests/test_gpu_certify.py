@@ -43,13 +43,20 @@ def test_certifier_never_accepts_a_false_criterion(prover, port, group):
     full = prover.selftest_certify(group, boxes, np.full(n, -1))
     assert np.array_equal(full, truth)
     accepted_any = np.zeros(n, dtype=bool)
+    record_any = np.zeros(n, dtype=bool)
     for call in range(0, 6):
         got = prover.selftest_certify(group, boxes, np.full(n, call))
         # one call evaluated, the others forced to "false": never a false accept
         assert not (got & ~truth).any(), (group, call, np.nonzero(got & ~truth)[0][:8])
         accepted_any |= got
-    # and every true criterion is accepted with some call number
+        # the record form (the call evaluated afterwards on its stored
+        # arguments) accepts no more than the direct form
+        rec = prover.selftest_certify(group, boxes, np.full(n, call), record=True)
+        assert not (rec & ~got).any(), (group, call, np.nonzero(rec & ~got)[0][:8])
+        record_any |= rec
+    # and every true criterion is accepted with some call number, in both forms
     assert np.array_equal(accepted_any, truth)
+    assert np.array_equal(record_any, truth)
 
 
 def test_certified_masks_equal_uncertified_and_oracle(port):

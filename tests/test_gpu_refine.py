@@ -2,9 +2,11 @@
 (cc_tight_refine) against the same refinement driven by the CPU oracle's
 verdict masks: per level, the boxes no criterion certifies and that are not
 empty are bisected along lambda, r1, r2, r3, r4 in turn (mid = 0.5 lo + 0.5
-hi, rounded to nearest); trapped boxes and the undecided boxes of the last
-level are the criticals.  The GPU's criticals (as a set: a level's order is
-not fixed), flags and per-level counts equal the oracle-driven ones."""
+hi, rounded to nearest), the first max_live / 2 of them in level order, the
+halves listed in the order of their boxes; trapped boxes, the undecided
+boxes of the last level and the boxes past the cap are the criticals.  The
+GPU's criticals (in order), flags and per-level counts equal the
+oracle-driven ones."""
 import numpy as np
 import pytest
 
@@ -13,7 +15,7 @@ from circlecover_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 
-def oracle_refine(port, boxes, max_depth):
+def oracle_refine(port, boxes, max_depth, max_live=1 << 26):
     crit, flags, live, decided = [], [], [], []
     cur = boxes.copy()
     for d in range(max_depth + 1):
@@ -25,10 +27,12 @@ def oracle_refine(port, boxes, max_depth):
         live.append(len(cur))
         decided.append(int(done.sum()))
         last = d == max_depth
-        keep = trapped | (~done & last)
+        cand = ~trapped & ~done & (not last)
+        cut = cand & (np.cumsum(cand) > max_live // 2)
+        keep = trapped | (~done & last) | cut
         crit.append(cur[keep])
-        flags.append(np.where(trapped[keep], 1, 2).astype(np.uint32))
-        split = cur[~trapped & ~done] if not last else cur[:0]
+        flags.append(np.where(trapped[keep], 1, np.where(cut[keep], 3, 2)).astype(np.uint32))
+        split = cur[cand & ~cut]
         dim = d % 5
         lo_half, hi_half = split.copy(), split.copy()
         if dim == 0:
@@ -47,9 +51,8 @@ def oracle_refine(port, boxes, max_depth):
     return np.concatenate(crit), np.concatenate(flags), live, decided
 
 
-def as_set(boxes, flags):
-    rows = boxes.view(np.uint64).reshape(len(boxes), -1)
-    return sorted(tuple(r) + (int(f),) for r, f in zip(rows, flags))
+def same_bits(a, b):
+    return len(a) == len(b) and np.array_equal(a.view(np.uint64), b.view(np.uint64))
 
 
 def test_refine_equals_oracle_driven_refinement(prover, port):
@@ -57,15 +60,22 @@ def test_refine_equals_oracle_driven_refinement(prover, port):
     got, gflags, st = prover.tight_refine(boxes, max_depth=7)
     want, wflags, live, decided = oracle_refine(port, boxes, 7)
     assert st["live"] == live and st["decided"] == decided
-    assert as_set(got, gflags) == as_set(want, wflags)
+    assert same_bits(got, want) and np.array_equal(gflags, wflags)
     assert st["depths_run"] == len(live) and not st["stopped_at_cap"]
 
 
-def test_refine_stops_at_the_population_cap(prover):
+def test_refine_population_cap_cuts_in_level_order(prover, port):
+    """A cap of 6,000 live boxes: the refinement still runs to its depth, the
+    boxes past the cap are kept (flag 3) exactly as the sequential model
+    keeps them, and a second run gives the same output."""
     boxes = W.tight_near_critical(4000, seed=506)
-    _, flags, st = prover.tight_refine(boxes, max_depth=30, max_live=6000)
-    assert st["stopped_at_cap"] and max(st["live"]) <= 6000
-    assert (flags == 2).sum() + (flags == 1).sum() == len(flags)
+    got, flags, st = prover.tight_refine(boxes, max_depth=12, max_live=6000)
+    assert st["stopped_at_cap"] and max(st["live"]) <= 6000 and sum(st["cut"]) == int((flags == 3).sum()) > 0
+    want, wflags, live, decided = oracle_refine(port, boxes, 12, max_live=6000)
+    assert st["live"] == live and st["decided"] == decided
+    assert same_bits(got, want) and np.array_equal(flags, wflags)
+    again, aflags, _ = prover.tight_refine(boxes, max_depth=12, max_live=6000)
+    assert same_bits(again, got) and np.array_equal(aflags, flags)
 
 
 def test_refine_orders_decide_the_same_boxes(prover):
@@ -88,7 +98,7 @@ def test_refine_orders_decide_the_same_boxes(prover):
         # the masks order only; without traps both refinements are the same
         if not (gflags == 1).any() and not (f == 1).any():
             assert s["live"] == st["live"] and s["decided"] == st["decided"], order
-            assert as_set(c, f) == as_set(got, gflags), order
+            assert same_bits(c, got) and np.array_equal(f, gflags), order
         else:
             assert s["decided"][0] >= st["decided"][0], order
     prover.tight_refine(boxes[:1], max_depth=0)  # back to the default order
