@@ -664,34 +664,44 @@ CC_FN_INL bool r1_r2_r3_strategies(Iv la, Iv weight, Iv r1, Iv r2, Iv r3, double
 }
 
 // Disks 2 and 3 form a strip, disk 1 covers the rest of a column
-// (r1_r2_r3_strategies.cu:101-121).
+// (r1_r2_r3_strategies.cu:101-121).  Each of the three-disk placements below
+// is split into the part before its recursion check, returning 0 (fails), 1
+// (holds) or 2 (holds iff can_recurse(w, h, ub_r4, lb_R4)), and the check:
+// the proof prepares the first part once per r3 cell (leaf123_prepare).
 template <class S>
-CC_FN bool three_disk_big_strip(S ub_la, S r1, S r2, S r3, S ub_r4, S lb_R4) {
+CC_FN int three_disk_big_strip_wh(S ub_la, S r1, S r2, S r3, S& w, S& h) {
     S S_sq = add_dn(add_dn(mul_dn(2.0, r2), add_dn(mul_dn(2.0, r3), -0.25)),
                     add_dn(add_dn(-mul_up(4.0, mul_up(r2, r2)), mul_dn(8.0, mul_dn(r2, r3))),
                            -mul_up(4.0, mul_up(r3, r3))));
     if (S_sq <= 0.0) {
-        return false;
+        return 0;
     }
     S side = sqrt_dn(S_sq);
     S la_rem = add_up(ub_la, -side);
     S h1_sq = add_dn(mul_dn(4.0, r1), -mul_up(la_rem, la_rem));
     if (h1_sq <= 0.0) {
-        return false;
+        return 0;
     }
     if (h1_sq >= 1.0) {
-        return true;
+        return 1;
     }
-    S h_rem = add_up(1.0, -sqrt_dn(h1_sq));
-    return can_recurse(la_rem, h_rem, ub_r4, lb_R4);
+    w = la_rem;
+    h = add_up(1.0, -sqrt_dn(h1_sq));
+    return 2;
+}
+template <class S>
+CC_FN bool three_disk_big_strip(S ub_la, S r1, S r2, S r3, S ub_r4, S lb_R4) {
+    S w, h;
+    const int st = three_disk_big_strip_wh<S>(ub_la, r1, r2, r3, w, h);
+    return st == 2 ? can_recurse(w, h, ub_r4, lb_R4) : st == 1;
 }
 
 // disk 3 in a corner, disks 1 and 2 along its sides (r1_r2_r3_strategies.cu:123-165)
 template <class S>
-CC_FN bool three_disk_small_corner(S ub_la, S r1, S r2, S r3, S ub_r4, S lb_R4) {
+CC_FN int three_disk_small_corner_wh(S ub_la, S r1, S r2, S r3, S& w, S& h) {
     S c3 = sqrt_dn(mul_dn(2.0, r3));
     if (c3 >= 1.0) {
-        return false;
+        return 0;
     }
     S la_left = add_up(ub_la, -c3);
     S la_half = mul_up(la_left, 0.5);
@@ -702,56 +712,73 @@ CC_FN bool three_disk_small_corner(S ub_la, S r1, S r2, S r3, S ub_r4, S lb_R4) 
         S la_after_1 = add_up(ub_la, -c1);
         S c2 = sqrt_dn(add_dn(mul_dn(4.0, r2), -mul_up(la_left, la_left)));
         S one_after_2 = add_up(1.0, -c2);
-        return can_recurse(la_after_1, one_after_2, ub_r4, lb_R4);
+        w = la_after_1;
+        h = one_after_2;
+        return 2;
     }
     if (la_half >= sqrt_dn(r1)) {
-        return false;
+        return 0;
     }
     if (one_left >= mul_dn(2.0, sqrt_dn(r2))) {
-        return false;
+        return 0;
     }
     S c2 = sqrt_dn(add_dn(mul_dn(4.0, r2), -mul_up(one_left, one_left)));
     S la_after_2 = add_up(ub_la, -c2);
     S c1 = sqrt_dn(add_dn(mul_dn(4.0, r1), -mul_up(la_left, la_left)));
     S one_after_1 = add_up(1.0, -c1);
-    return can_recurse(la_after_2, one_after_1, ub_r4, lb_R4);
+    w = la_after_2;
+    h = one_after_1;
+    return 2;
+}
+template <class S>
+CC_FN bool three_disk_small_corner(S ub_la, S r1, S r2, S r3, S ub_r4, S lb_R4) {
+    S w, h;
+    const int st = three_disk_small_corner_wh<S>(ub_la, r1, r2, r3, w, h);
+    return st == 2 ? can_recurse(w, h, ub_r4, lb_R4) : st == 1;
 }
 
 // disks 1 and 3 at the sides, 2 in between, a pocket remains
 // (r1_r2_r3_strategies.cu:167-204)
 template <class I>
-CC_FN bool three_disk_r1_r3_pocket(I la, I r1, I r2, I r3, typename I::S ub_r4, typename I::S lb_R4) {
-    using S = typename I::S;
+CC_FN int three_disk_r1_r3_pocket_wh(I la, I r1, I r2, I r3, typename I::S& w, typename I::S& h) {
     if (r1.lo <= 0.25) {
-        return false;
+        return 0;
     }
     I S1 = 2.0 * sqrt(r1 - 0.25);
     I la_m_S1 = la - S1;
     I h2_rest = 0.25 * la_m_S1 * la_m_S1;
     if (r2.lo <= h2_rest.hi) {
-        return false;
+        return 0;
     }
     I h2 = 2.0 * sqrt(r2 - h2_rest);
     I one_m_h2 = 1.0 - h2;
     I S3_rest = 0.25 * one_m_h2 * one_m_h2;
     if (r3.lo <= S3_rest.hi) {
-        return false;
+        return 0;
     }
     I S3 = 2.0 * sqrt(r3 - S3_rest);
     I X = la - S1 - S3;
     if (X.hi <= 0.0) {
-        return true;
+        return 1;
     }
     I t = la - 0.5 * S1 - S3;
     I Y_rest = t * t;
     if (r1.lo <= Y_rest.hi) {
-        return false;
+        return 0;
     }
     I Y = 0.5 - sqrt(r1 - Y_rest);
     if (Y.hi <= 0.0) {
-        return true;
+        return 1;
     }
-    return can_recurse(X.hi, Y.hi, ub_r4, lb_R4);
+    w = X.hi;
+    h = Y.hi;
+    return 2;
+}
+template <class I>
+CC_FN bool three_disk_r1_r3_pocket(I la, I r1, I r2, I r3, typename I::S ub_r4, typename I::S lb_R4) {
+    typename I::S w, h;
+    const int st = three_disk_r1_r3_pocket_wh(la, r1, r2, r3, w, h);
+    return st == 2 ? can_recurse(w, h, ub_r4, lb_R4) : st == 1;
 }
 
 // Region around the three-disk worst case settled by hand in the paper
@@ -1887,6 +1914,54 @@ CC_FN bool r123_check(const R123Prep& p, double ub_r4) {
     if (p.strips_state == 1) return true;
     if (p.strips_state == 2 && cr_check(p.strips, ub_r4, p.lb_R4)) return true;
     return p.has_cover && cr_check(p.cover, ub_r4, p.lb_R4);
+}
+
+// The leaf form r1_r2_r3_strategies(box, R4) for a fixed la, r1..r3 and R4
+// as a function of the upper bound of r4 (r1_r2_r3_strategies.cu:101-247):
+// the three placements up to their recursion checks, the checks' rectangles
+// (cr_prepare) and the pocket settled by hand, computed once.  The trap
+// status each placement leaves is replayed when the check gets there, so
+// leaf123_check(p, ub_r4) performs the criterion's operations on the same
+// values: the same result and trap status as r1_r2_r3_strategies(b, R4)
+// with b.r[3].hi = ub_r4.  The proof prepares it per r3 cell, for the
+// leaves whose r4 lower bound does not tighten r3 (their tightened r1..r3
+// are the cell's own).
+struct LeafPrep {
+    CrPrep cr[3];
+    double lb_R4;
+    uint8_t st[3];    // big strip, small corner, r1-r3 pocket: 0 fails, 1 holds, 2 recursion check
+    uint8_t trap[4];  // trap status after each placement and after the pocket by hand (0: none)
+    uint8_t hand;     // three_disk_pocket_by_hand
+};
+CC_FN LeafPrep leaf123_prepare(const Box& b, Iv R4) {
+    LeafPrep p;
+    const uint32_t saved = trap_status();
+    trap_clear();
+    p.lb_R4 = R4.lo;
+    const double ub_la = b.la.hi, r1 = b.r[0].lo, r2 = b.r[1].lo, r3 = b.r[2].lo;
+    double w = 0.0, h = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        const int st = k == 0   ? three_disk_big_strip_wh<double>(ub_la, r1, r2, r3, w, h)
+                       : k == 1 ? three_disk_small_corner_wh<double>(ub_la, r1, r2, r3, w, h)
+                                : three_disk_r1_r3_pocket_wh(b.la, b.r[0], b.r[1], b.r[2], w, h);
+        p.st[k] = (uint8_t)st;
+        if (st == 2) p.cr[k] = cr_prepare(w, h);
+        p.trap[k] = (uint8_t)trap_status();
+        trap_clear();
+    }
+    p.hand = three_disk_pocket_by_hand(b.la, b.r[0], b.r[1], b.r[2]) ? 1 : 0;
+    p.trap[3] = (uint8_t)trap_status();
+    trap_clear();
+    if (saved != TRAP_NONE) trap(saved);
+    return p;
+}
+CC_FN bool leaf123_check(const LeafPrep& p, double ub_r4) {
+    for (int k = 0; k < 3; ++k) {
+        if (p.trap[k]) trap(p.trap[k]);
+        if (p.st[k] == 1 || (p.st[k] == 2 && cr_check(p.cr[k], ub_r4, p.lb_R4))) return true;
+    }
+    if (p.trap[3]) trap(p.trap[3]);
+    return p.hand != 0;
 }
 
 // criteria with the reference's signatures (weight computed inside)

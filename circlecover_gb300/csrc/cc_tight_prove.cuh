@@ -71,6 +71,7 @@ struct Cell4 {  // a surviving r3 cell
     int16_t i1, i2, i3;
     int16_t order;  // learned order: 1 = try the r1_r2_r3 leaf criterion before 2x2
     tight::R123Prep p3;
+    tight::LeafPrep lp;  // the leaf form of r1_r2_r3 for the leaves whose r4 does not tighten r3
 };
 
 struct Leaf {  // a leaf that survived stage 4a
@@ -400,6 +401,13 @@ __global__ void __launch_bounds__(128) k_stage3(const Box* __restrict__ parents,
                         cell.R4 = tk.weight - cell.r1 - cell.r2 - cell.r3;
                         tighten_lb(cell.R4, 0.0);
                         outcome = empty(cell.R4) ? CC_T_L3_R4EMPTY : CC_T_L3_SPLIT;
+                        if (Hoist && outcome == CC_T_L3_SPLIT) {
+                            // the leaf box of a leaf whose r4 lower bound is at most r3's
+                            Box vb{tk.la, {cell.r1, cell.r2, cell.r3, cell.r3}};
+                            tighten_lb(vb.r[1], vb.r[2].lo);
+                            tighten_lb(vb.r[0], vb.r[1].lo);
+                            cell.lp = tight::leaf123_prepare(vb, cell.R4);
+                        }
                     }
                 }
             }
@@ -471,7 +479,10 @@ __global__ void __launch_bounds__(128) k_stage4a(const Task* __restrict__ tasks,
                     outcome = -3;  // on to stage 4a2
                     if (p.order) {  // learned order: the cheap leaf criterion first
                         int how = -1;
-                        const bool ok4 = tight::first_f32_deferred(tight::LeafR123{}, v, p.R4, &how, &calls);
+                        // prepared per cell in FP64 where r4 leaves r1..r3 as the cell's, else FP32 first
+                        const bool ok4 = r4.lo <= p.r3.lo
+                                             ? tight::leaf123_check(p.lp, r4.hi)
+                                             : tight::first_f32_deferred(tight::LeafR123{}, v, p.R4, &how, &calls);
                         tally.note_stage(how);
                         if (ok4 && trap_status() == TRAP_NONE) {
                             outcome = CC_T_L4_R123LEAF;
@@ -602,8 +613,11 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
             tighten_lb(R, 0.0);
             tight::GapsStart g;
             int how = -1;
+            // batched form: the leaf criterion prepared per cell in FP64 where r4
+            // leaves r1..r3 as the cell's, else FP32 first
             if (!(lf.trapped & 2) &&
-                (F32 ? tight::first_f32_deferred(tight::LeafR123{}, v, p.R4, &how, &calls)
+                (F32 ? (r4.lo <= p.r3.lo ? tight::leaf123_check(p.lp, r4.hi)
+                                         : tight::first_f32_deferred(tight::LeafR123{}, v, p.R4, &how, &calls))
                      : tight::r1_r2_r3_strategies(v, p.R4))) {
                 outcome = CC_T_L4_R123LEAF;
             } else if (tight::gaps_enters(v.r[0].lo, v.r[1].lo, g)) {

@@ -403,6 +403,44 @@ size_t ccport_prepared_mismatches(const cc_tight_box* boxes, size_t n, int n_ub)
     return bad;
 }
 
+/* The proof's prepared leaf form vs the leaf form itself: for every box (as
+ * an r3 cell: r1..r3 tightened against each other, R4 = weight - r1 - r2 -
+ * r3 tightened at 0) and n_ub upper bounds of r4 spread over [0, r3.lo] and
+ * just outside, compare leaf123_check(leaf123_prepare(...), ub) with
+ * r1_r2_r3_strategies(box with r4.hi = ub, R4), result and trap status.
+ * Returns the number of disagreements. */
+size_t ccport_leafprep_mismatches(const cc_tight_box* boxes, size_t n, int n_ub) {
+    size_t bad = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const cc_tight_box& b = boxes[i];
+        Iv la = to_iv(b.la), r1 = to_iv(b.r[0]), r2 = to_iv(b.r[1]), r3 = to_iv(b.r[2]);
+        Iv w = ct::required_weight_for(la);
+        Iv R4 = w - r1 - r2 - r3;
+        cc::tighten_lb(R4, 0.0);
+        ct::Box vb{la, {r1, r2, r3, r3}};
+        cc::tighten_lb(vb.r[1], vb.r[2].lo);
+        cc::tighten_lb(vb.r[0], vb.r[1].lo);
+        cc::trap_clear();
+        const ct::LeafPrep p = ct::leaf123_prepare(vb, R4);
+        for (int j = 0; j < n_ub; ++j) {
+            double t = n_ub > 1 ? (double)j / (n_ub - 1) : 1.0;
+            double ub = r3.lo * (1.25 * t - 0.125);
+            if (!(ub >= 0)) ub = r3.lo;
+            cc::trap_clear();
+            const bool a = ct::leaf123_check(p, ub);
+            const uint32_t ta = cc::trap_status();
+            ct::Box v = vb;
+            v.r[3] = Iv{0.0, ub};
+            cc::trap_clear();
+            const bool c = ct::r1_r2_r3_strategies(v, R4);
+            const uint32_t tc = cc::trap_status();
+            cc::trap_clear();
+            bad += (a != c) || (ta != tc);
+        }
+    }
+    return bad;
+}
+
 /* the rounding layer itself, for the primitive tests (op: 0 add, 1 mul, 2 div, 3 sqrt, 4 rcp) */
 void ccport_round(int op, int up, int exact_fenv, const double* a, const double* b, double* out, size_t n) {
     for (size_t i = 0; i < n; ++i) {

@@ -162,6 +162,24 @@ def test_theory_constants(ref):
     assert abs(three - two) < 1e-12
 
 
+def test_prepared_leaf_form_equals_plain(port):
+    """The proof's leaf form of r1_r2_r3_strategies prepared once per r3 cell
+    (leaf123_prepare / leaf123_check) gives the criterion's result and trap
+    status for every upper bound of r4 below r3."""
+    import ctypes
+    lib = port.lib
+    lib.ccport_leafprep_mismatches.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    lib.ccport_leafprep_mismatches.restype = ctypes.c_size_t
+    for gen, seed in [(W.tight_microbench, 64), (W.tight_near_critical, 65)]:
+        boxes = np.ascontiguousarray(gen(20000, seed=seed))
+        assert lib.ccport_leafprep_mismatches(boxes.ctypes.data, len(boxes), 9) == 0
+    root = W.tight_root(1.0, 1.02)
+    g = O.make_grid(2, (8, 8, 8, 8), (), (8, 8, 8, 8))
+    crit, st = port.tight_prove(root, g, threads=4)
+    edge = np.ascontiguousarray(np.concatenate([crit, W.tight_near_critical(5000, seed=66)]))
+    assert lib.ccport_leafprep_mismatches(edge.ctypes.data, len(edge), 17) == 0
+
+
 def test_prepared_criteria_equal_plain(port):
     """The proof engine's hoisted criteria (prepare once per parent cell, check
     per child bound) agree with the plain criteria for every bound."""
