@@ -93,8 +93,9 @@ enum : int {
     kCntRepair = 9,        // boxes to evaluate again in FP64 alone
     kCntCoverCert = 10,    // true strip-width results certified
     kCntGapsCert = 11,     // true gap-width results certified
+    kCntCoverLoop = 12,    // strip-width jobs whose bisection resumes with FP64 steps (pass 2, second kernel)
 };
-static constexpr int kEvalCounters = 12;
+static constexpr int kEvalCounters = 13;
 static constexpr int kCertQueues = 5;
 // the groups whose can_recurse calls are recorded, and their verdict bits
 static constexpr int kRecGroups = 4;
@@ -490,20 +491,55 @@ __global__ void __launch_bounds__(128, MinB) k_eval_main(const double* __restric
     }
 }
 
-template <Layout L, int MinB = 1>
+// pass 2 in two kernels.  The strip-width bisections decide their leading
+// steps in FP32 (while the whole warp agrees) and most jobs are settled
+// there; the rest need FP64 steps to the fixpoint, which a warp would run
+// for its few remaining lanes.  So the first kernel stops a job at its first
+// FP64 step and queues its bracket (in the record buffer, unused between the
+// call rounds and the certification pass), and the second runs those FP64
+// steps on full warps.  Without record buffers (the allocation-free entry)
+// the first kernel finishes every job itself.
+static_assert(sizeof(ct::CoverResume) <= ct::kCrRecordSlots * sizeof(ct::CrArgs), "a resume state per box slot");
+template <Layout L, int MinB = 1, bool Resume = false>
 __global__ void __launch_bounds__(128, MinB) k_eval_cover(const double* __restrict__ in, size_t n, EvalQueues q,
                                                           uint32_t* __restrict__ masks) {
-    const unsigned long long nq = q.counts[0] < q.cap ? q.counts[0] : q.cap;
+    const unsigned long long c = Resume ? q.counts[kCntCoverLoop] : q.counts[0];
+    const unsigned long long nq = c < q.cap ? c : q.cap;
+    ct::CoverResume* states = reinterpret_cast<ct::CoverResume*>(q.args);
+    if (Resume && !states) return;
     const bool certify = q.cert[0] != nullptr;
     unsigned long long certified = 0;
-    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < nq;
-         j += (unsigned long long)gridDim.x * blockDim.x) {
-        const uint32_t i = q.cover_box[j];
-        bool repair = false;
-        uint32_t m = ct::cover_pass_box(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr, certify, &repair);
-        if (m) masks[i] |= m;
-        if (repair) eval_repair_push(q, i);
-        else if (certify && (m & (1u << 2)) && !(m >> 31)) ++certified;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nq;
+         base += stride) {
+        const unsigned long long j = base + (threadIdx.x & 31);
+        ct::CoverResume st;
+        st.it = -1;
+        if (j < nq) {
+            uint32_t i;
+            bool repair = false;
+            uint32_t m;
+            if (Resume) {
+                st = states[j];
+                i = st.box;
+                m = ct::cover_pass_resume(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr, certify, &repair, st);
+                st.it = -1;
+            } else {
+                i = q.cover_box[j];
+                m = ct::cover_pass_box(load_box<L>(in, n, i), q.enc ? q.enc + i : nullptr, certify, &repair,
+                                       states ? &st : nullptr);
+                st.box = i;
+            }
+            if (m) masks[i] |= m;
+            if (repair) eval_repair_push(q, i);
+            else if (certify && (m & (1u << 2)) && !(m >> 31)) ++certified;
+        }
+        if (!Resume) {
+            __syncwarp();
+            const unsigned long long s = cc::prove::warp_append(&q.counts[kCntCoverLoop], st.it >= 0, q.cap,
+                                                                &q.counts[kCntOverflow]);
+            if (s != ~0ULL) states[s] = st;
+        }
     }
     if (certify) warp_tally(&q.counts[kCntCoverCert], certified);
 }
@@ -625,27 +661,50 @@ static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in,
     k_eval_collect<<<g, 128, 0, s>>>(n, masks, q);
 }
 CC_EVAL_LAUNCH(k_eval_main, in, n, masks, q)
-CC_EVAL_LAUNCH(k_eval_cover, in, n, q, masks)
 CC_EVAL_LAUNCH(k_eval_gaps, in, n, q, masks)
 #undef CC_EVAL_LAUNCH
+// pass 2: the counter of the second kernel's queue starts at zero (the
+// autotuner reruns the pass on its own); no second kernel without record
+// buffers
+template <Layout L>
+static cudaError_t launch_k_eval_cover(int minb, int g, cudaStream_t s, const double* in, size_t n,
+                                       uint32_t* masks, EvalQueues q) {
+    const cudaError_t e = cudaMemsetAsync(&q.counts[kCntCoverLoop], 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    const bool resume = q.args != nullptr;
+    if (L == Layout::SoA && minb == 4) {
+        k_eval_cover<L, 4, false><<<g, 128, 0, s>>>(in, n, q, masks);
+        if (resume) k_eval_cover<L, 4, true><<<g, 128, 0, s>>>(in, n, q, masks);
+    } else if (L == Layout::SoA && minb == 8) {
+        k_eval_cover<L, 8, false><<<g, 128, 0, s>>>(in, n, q, masks);
+        if (resume) k_eval_cover<L, 8, true><<<g, 128, 0, s>>>(in, n, q, masks);
+    } else {
+        k_eval_cover<L, 1, false><<<g, 128, 0, s>>>(in, n, q, masks);
+        if (resume) k_eval_cover<L, 1, true><<<g, 128, 0, s>>>(in, n, q, masks);
+    }
+    return cudaSuccess;
+}
 
 // kernels launched by pass k beyond one (the FP32 pass's groups, rounds and
 // collection; the certification pass's five group kernels) and whether a
 // pass launches at all
 static int pass_kernels(int pass, const EvalQueues& q) {
     if (pass == 0) return q.args ? 1 + kRecGroups * (1 + ct::kCrRecordSlots) + 1 : ct::F32_GROUPS + 1;
+    if (pass == 2) return q.args ? 2 : 1;
     if (pass == 4) return q.cert[0] ? kCertQueues + (q.args ? 1 : 0) : 0;
     if (pass == 5) return q.cert[0] ? 1 : 0;
     return 1;
 }
 
+// the launches of one pass; the status of a memory operation among them (a
+// launch's own error is left to cudaGetLastError)
 template <Layout L>
-static void launch_pass(int pass, int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks,
-                        EvalQueues q) {
+static cudaError_t launch_pass(int pass, int minb, int g, cudaStream_t s, const double* in, size_t n,
+                               uint32_t* masks, EvalQueues q) {
     switch (pass) {
         case 0: launch_k_eval_f32<L>(minb, g, s, in, n, masks, q); break;
         case 1: launch_k_eval_main<L>(minb, g, s, in, n, masks, q); break;
-        case 2: launch_k_eval_cover<L>(minb, g, s, in, n, masks, q); break;
+        case 2: return launch_k_eval_cover<L>(minb, g, s, in, n, masks, q);
         case 3: launch_k_eval_gaps<L>(minb, g, s, in, n, masks, q); break;
         case 4:
             if (!q.cert[0]) break;
@@ -660,6 +719,7 @@ static void launch_pass(int pass, int minb, int g, cudaStream_t s, const double*
             if (q.cert[0]) k_eval_repair<L><<<g, 128, 0, s>>>(in, n, q, masks);
             break;
     }
+    return cudaSuccess;
 }
 
 // the launch sequence of the four passes
@@ -673,7 +733,7 @@ static int eval_launches(cc_handle* h, const double* in, size_t n, uint32_t* mas
         if (h->timing) CC_CUDA(h, cudaEventRecord(h->stage_ev[pass], s));
         int g = h->sm_count * h->tune_grid[pass];
         if ((size_t)g > need) g = (int)need;
-        launch_pass<L>(pass, h->tune_minb[pass], g, s, in, n, masks, q);
+        CC_CUDA(h, launch_pass<L>(pass, h->tune_minb[pass], g, s, in, n, masks, q));
         CC_LAUNCHED(h);
         h->launches += pass_kernels(pass, q) - 1;
     }
@@ -1097,7 +1157,7 @@ extern "C" int cc_autotune_eval(cc_handle* h, const double* soa, size_t n, uint3
             if (pass == 0) CC_CUDA(h, cudaMemsetAsync(q.counts, 0, kEvalCounters * sizeof(unsigned long long), s));
             if (pass == 1) CC_CUDA(h, cudaMemcpyAsync(q.counts, snap, sizeof(snap), cudaMemcpyHostToDevice, s));
             CC_CUDA(h, cudaEventRecord(e0, s));
-            launch_pass<Layout::SoA>(pass, minb, g, s, soa, n, masks, q);
+            CC_CUDA(h, launch_pass<Layout::SoA>(pass, minb, g, s, soa, n, masks, q));
             CC_LAUNCHED(h);
             CC_CUDA(h, cudaEventRecord(e1, s));
             CC_CUDA(h, cudaEventSynchronize(e1));
@@ -1231,7 +1291,12 @@ extern "C" int cc_tight_eval_device_static(const double* soa, size_t n, uint32_t
     const size_t need = (n + 127) / 128;
     int g = g_static_sms[dev] * 8;
     if ((size_t)g > need) g = (int)need;
-    for (int pass = 0; pass < CC_EVAL_STAGES; ++pass) launch_pass<Layout::SoA>(pass, 1, g, s, soa, n, masks, q);
+    for (int pass = 0; pass < CC_EVAL_STAGES; ++pass) {
+        if (launch_pass<Layout::SoA>(pass, 1, g, s, soa, n, masks, q) != cudaSuccess) {
+            cudaGetLastError();  // the memory operation's own error
+            return CC_ERR_CUDA;
+        }
+    }
     if (cudaPeekAtLastError() != cudaSuccess) {
         cudaGetLastError();  // a launch of this call failed
         return CC_ERR_CUDA;

@@ -558,8 +558,20 @@ struct NoEarly {
     CC_METHOD int operator()(double, double) const { return -1; }
 };
 
+// A strip-width bisection stopped at its first FP64 step (where the FP32
+// steps end and the final check is not decided for the whole bracket), to be
+// resumed in a later pass on full warps: its bracket and step count, and the
+// box.  *decided is kBisectionDeferred then.
+struct CoverResume {
+    double lo, hi;
+    int32_t it;
+    uint32_t box;
+};
+static constexpr int kBisectionDeferred = 2;
+
 template <class Early>
-CC_FN double cover_strip_width_early(double la_hi, double r1, double r2, double r3, Early early, int* decided) {
+CC_FN double cover_strip_width_early(double la_hi, double r1, double r2, double r3, Early early, int* decided,
+                                     CoverResume* stop = nullptr) {
     double lo = 0.3;
     double hi = la_hi;
     *decided = -1;
@@ -573,6 +585,8 @@ CC_FN double cover_strip_width_early(double la_hi, double r1, double r2, double 
         if (whole == f32::YES) return bisect_all_true(lo, hi);
     }
     bool f32_steps = true;
+#else
+    (void)stop;
 #endif
     for (int it = 0;; ++it) {
         double mid = 0.5 * (lo + hi);
@@ -592,6 +606,13 @@ CC_FN double cover_strip_width_early(double la_hi, double r1, double r2, double 
             if (f32_steps) {
                 f32_steps = false;
                 if (finite && (*decided = early(lo, hi)) != f32::UNKNOWN) return lo;
+                if (stop) {
+                    stop->lo = lo;
+                    stop->hi = hi;
+                    stop->it = it;
+                    *decided = kBisectionDeferred;
+                    return lo;
+                }
             }
             ok = strip_width_realizable(r1, r2, r3, mid);
         }
@@ -608,6 +629,22 @@ CC_FN double cover_strip_width_early(double la_hi, double r1, double r2, double 
 }
 
 CC_FN double cover_strip_width_fp64(double la_hi, double r1, double r2, double r3);
+
+// The FP64 steps of a bisection stopped by cover_strip_width_early: the same
+// loop from the same bracket and step count.
+CC_FN double cover_strip_width_resume(double r1, double r2, double r3, double lo, double hi, int it) {
+    for (;; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (it >= CC_BISECTION_CAP) {
+            trap(TRAP_BISECTION_CAP);
+            break;
+        }
+        if (strip_width_realizable(r1, r2, r3, mid)) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
 
 // The widest realizable strip.  On the device the bisection's FP32 steps are
 // followed by an FP64 certificate: the width it returns must pass the FP64
@@ -1592,17 +1629,44 @@ CC_FN_INL bool gaps_certificate(const Box& b, double gap) {
     return ok;
 }
 
-CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr, bool certify = false,
-                                  bool* repair = nullptr) {
-    using f32::Fv;
-    const Iv la = b.la, r1 = b.r[0], r2 = b.r[1], r3 = b.r[2];
+// FP32 bound of R4 for the strip's final check (from the kept enclosure if
+// there is one); *lb_ok: no comparison on the way was undecided
+CC_FN_INL f32::Fv cover_lb_R4(const Box& b, const EncBox* enc, bool* lb_ok) {
     trap_clear();
-    const Fv lb_R4 = enc ? (enc->weight - enc->b.r[0] - enc->b.r[1] - enc->b.r[2]).lo : [&] {
+    const f32::Fv lb_R4 = enc ? (enc->weight - enc->b.r[0] - enc->b.r[1] - enc->b.r[2]).lo : [&] {
         const BoxT<f32::IvF> e = enclose(b);
         return (required_weight_for(e.la) - e.r[0] - e.r[1] - e.r[2]).lo;
     }();
-    const bool lb_ok = trap_status() == TRAP_NONE;
+    *lb_ok = trap_status() == TRAP_NONE;
     trap_clear();
+    return lb_R4;
+}
+// the strip's final check on the bisection's width, with its certificate
+CC_FN_INL uint32_t cover_pass_tail(const Box& b, bool lb_ok, f32::Fv lb_R4, double width, bool certify, bool* repair) {
+    uint32_t trapped = trap_status();
+    trap_clear();
+    bool ok = lb_ok ? cover_strip_finish<f32::Fv>(b.la.hi, width, b.r[3].hi, lb_R4) : false;
+    if (!lb_ok || trap_status() != TRAP_NONE) {
+        trap_clear();
+        ok = cover_strip_finish<double>(b.la.hi, width, b.r[3].hi,
+                                        (required_weight_for(b.la) - b.r[0] - b.r[1] - b.r[2]).lo);
+        trapped |= trap_status();
+    }
+    uint32_t m = ok ? (1u << 2) : 0u;
+    if (trapped != TRAP_NONE) m |= 1u << 31;
+    else if (ok && certify && !cover_certificate(b, width)) *repair = true;
+    return m;
+}
+// resume (optional): a box whose bisection reaches its FP64 steps stops
+// there: resume->it >= 0 holds the state (the caller sets resume->box) and
+// 0 is returned; cover_pass_resume computes it later (the same result)
+CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr, bool certify = false,
+                                  bool* repair = nullptr, CoverResume* resume = nullptr) {
+    using f32::Fv;
+    const Iv la = b.la, r1 = b.r[0], r2 = b.r[1], r3 = b.r[2];
+    bool lb_ok;
+    const Fv lb_R4 = cover_lb_R4(b, enc, &lb_ok);
+    if (resume) resume->it = -1;
     // cover_strip_finish for every width in [lo, hi]
     auto finish = [&](double lo, double hi) -> int {
         if (!lb_ok) return f32::UNKNOWN;
@@ -1612,24 +1676,21 @@ CC_FN_INL uint32_t cover_pass_box(const Box& b, const EncBox* enc = nullptr, boo
         return d;
     };
     int decided;
-    const double width = cover_strip_width_early(la.hi, r1.lo, r2.lo, r3.lo, finish, &decided);
+    const double width = cover_strip_width_early(la.hi, r1.lo, r2.lo, r3.lo, finish, &decided, resume);
+    if (decided == kBisectionDeferred) return 0u;
     if (decided != f32::UNKNOWN) {
         if (decided != f32::YES) return 0u;
         if (certify && !cover_certificate(b, width)) *repair = true;
         return 1u << 2;
     }
-    uint32_t trapped = trap_status();
-    trap_clear();
-    bool ok = lb_ok ? cover_strip_finish<Fv>(la.hi, width, b.r[3].hi, lb_R4) : false;
-    if (!lb_ok || trap_status() != TRAP_NONE) {
-        trap_clear();
-        ok = cover_strip_finish<double>(la.hi, width, b.r[3].hi, (required_weight_for(la) - r1 - r2 - r3).lo);
-        trapped |= trap_status();
-    }
-    uint32_t m = ok ? (1u << 2) : 0u;
-    if (trapped != TRAP_NONE) m |= 1u << 31;
-    else if (ok && certify && !cover_certificate(b, width)) *repair = true;
-    return m;
+    return cover_pass_tail(b, lb_ok, lb_R4, width, certify, repair);
+}
+CC_FN_INL uint32_t cover_pass_resume(const Box& b, const EncBox* enc, bool certify, bool* repair,
+                                     const CoverResume& r) {
+    bool lb_ok;
+    const f32::Fv lb_R4 = cover_lb_R4(b, enc, &lb_ok);
+    const double width = cover_strip_width_resume(b.r[0].lo, b.r[1].lo, b.r[2].lo, r.lo, r.hi, r.it);
+    return cover_pass_tail(b, lb_ok, lb_R4, width, certify, repair);
 }
 
 CC_FN_INL uint32_t gaps_pass_box(const Box& b, const EncBox* enc = nullptr, bool certify = false,
