@@ -475,6 +475,27 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaf_filter(const SbTask* __re
     // the trace of the empty leaves, summed per thread and flushed once
     unsigned long long digest = 0;
     unsigned int n_empty = 0, n_valid = 0;
+    // nearly every warp step has an anchor: they are staged per warp in
+    // shared memory and appended 32 at a time (one global atomic per 32)
+    __shared__ uint32_t s_anchor[kThreads / 32][64];
+    uint32_t* stage = s_anchor[threadIdx.x >> 5];
+    const unsigned lane = threadIdx.x & 31;
+    int staged = 0;  // warp-uniform
+    auto flush = [&](int k) {  // append the first k staged anchors (k <= 32), every lane calls it
+        unsigned long long at = 0;
+        if (lane == 0) at = atomicAdd(&c->n_anchor, (unsigned long long)k);
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if ((int)lane < k) {
+            if (at + lane < anchor_cap) anchors[at + lane] = stage[lane];
+            else atomicExch(&c->overflow, 1ULL);
+        }
+        uint32_t rest = 0;  // the anchors left, moved to the front
+        if ((int)lane < staged - k) rest = stage[k + lane];
+        __syncwarp();
+        if ((int)lane < staged - k) stage[lane] = rest;
+        __syncwarp();
+        staged -= k;
+    };
     SB_WARP_LOOP(l1 - l0) {
         const unsigned long long idx = l0 + base_ + (threadIdx.x & 31);
         const bool valid = idx < l1;
@@ -501,9 +522,13 @@ __global__ void __launch_bounds__(kThreads) k_sbp_leaf_filter(const SbTask* __re
         const bool anchor = valid && empty && ((threadIdx.x & 31) == 0 || prev_row != row || !prev_empty);
         unsigned long long slot = warp_append(n_cand, valid && !empty, cand_cap, &c->overflow);
         if (slot != ~0ULL) cand[slot] = (uint32_t)(idx - l0);
-        slot = warp_append(&c->n_anchor, anchor, anchor_cap, &c->overflow);
-        if (slot != ~0ULL) anchors[slot] = (uint32_t)(idx - l0);
+        const unsigned ballot = __ballot_sync(0xffffffffu, anchor);
+        if (anchor) stage[staged + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)(idx - l0);
+        staged += __popc(ballot);
+        __syncwarp();
+        if (staged >= 32) flush(32);
     }
+    if (staged > 0) flush(staged);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         digest += __shfl_xor_sync(0xffffffffu, digest, o);
