@@ -182,12 +182,20 @@ __global__ void __launch_bounds__(128) k_eval_calls(const ct::CrArgs* __restrict
     }
 }
 
+// The appends of a tile of 128 boxes are aggregated per block: one atomic per
+// queue and tile, issued by different threads at once (appended warp by warp,
+// a warp waited for eight atomics in a row per 32 boxes).
+constexpr int kCollectQueues = 3 + kCertQueues;  // full, cover, gaps, the certification queues
 __global__ void __launch_bounds__(128) k_eval_collect(size_t n, uint32_t* __restrict__ masks, EvalQueues q) {
+    __shared__ unsigned s_warp[kCollectQueues][4];
+    __shared__ unsigned long long s_base[kCollectQueues];
+    const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n_queues = q.cert[0] ? kCollectQueues : 3;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n;
-         base += stride) {
-        unsigned long long i = base + (threadIdx.x & 31);
-        bool valid = i < n;
+    // block-uniform loop: every thread of the block runs every iteration
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const unsigned long long i = base + threadIdx.x;
+        const bool valid = i < n;
         uint32_t m = valid ? masks[i] : 0u;
         if (valid && q.states) {
             for (int k = 0; k < kRecGroups; ++k) {
@@ -201,26 +209,47 @@ __global__ void __launch_bounds__(128) k_eval_collect(size_t n, uint32_t* __rest
         const bool need_gaps = !undecided && (m & ct::kF32Gaps);
         if (valid && (q.states || (m & (ct::kF32Undecided | ct::kF32Cover | ct::kF32Gaps))))
             masks[i] = m & ~(ct::kF32Undecided | ct::kF32Cover | ct::kF32Gaps);
-        unsigned long long s = cc::prove::warp_append(&q.counts[3], valid && undecided, q.cap, &q.counts[2]);
-        if (s != ~0ULL) q.full[s] = (uint32_t)i;
-        s = cc::prove::warp_append(&q.counts[0], valid && need_cover, q.cap, &q.counts[2]);
-        if (s != ~0ULL) q.cover_box[s] = (uint32_t)i;
-        s = cc::prove::warp_append(&q.counts[1], valid && need_gaps, q.cap, &q.counts[2]);
-        if (s != ~0ULL) q.gaps_box[s] = (uint32_t)i;
-        if (q.cert[0]) {  // the FP32 pass's "true" bits, to certify in FP64
-            const bool fp32 = valid && !undecided;
-            for (int k = 0; k < kRecGroups; ++k) {
-                s = cc::prove::warp_append(&q.counts[kCntCert + k], fp32 && ((m >> rec_group(k)) & 1u), q.cap,
-                                           &q.counts[kCntOverflow]);
-                if (s != ~0ULL) q.cert[k][s] = (uint32_t)i;
-            }
-            const uint8_t cf = (uint8_t)(((m >> 2) & 1u) | (((m >> 6) & 1u) << 1));
-            s = cc::prove::warp_append(&q.counts[kCntCert + 4], fp32 && cf, q.cap, &q.counts[kCntOverflow]);
-            if (s != ~0ULL) {
-                q.cert[4][s] = (uint32_t)i;
-                q.cflags[i] = cf;
-            }
+        // the FP32 pass's "true" bits, to certify in FP64
+        const bool fp32 = valid && !undecided && q.cert[0] != nullptr;
+        const uint8_t cf = (uint8_t)(((m >> 2) & 1u) | (((m >> 6) & 1u) << 1));
+        bool want[kCollectQueues];
+        want[0] = valid && undecided;
+        want[1] = valid && need_cover;
+        want[2] = valid && need_gaps;
+        for (int k = 0; k < kRecGroups; ++k) want[3 + k] = fp32 && ((m >> rec_group(k)) & 1u);
+        want[3 + kRecGroups] = fp32 && cf;
+        unsigned ballot[kCollectQueues];
+#pragma unroll
+        for (int k = 0; k < kCollectQueues; ++k) {
+            ballot[k] = __ballot_sync(0xffffffffu, want[k]);
+            if (lane == 0) s_warp[k][w] = __popc(ballot[k]);
         }
+        __syncthreads();
+        if ((int)threadIdx.x < n_queues) {
+            const int k = threadIdx.x;
+            const unsigned tot = s_warp[k][0] + s_warp[k][1] + s_warp[k][2] + s_warp[k][3];
+            unsigned long long* ctr = k == 0 ? &q.counts[kCntFull]
+                                    : k == 1 ? &q.counts[kCntCover]
+                                    : k == 2 ? &q.counts[kCntGaps]
+                                             : &q.counts[kCntCert + (k - 3)];
+            s_base[k] = tot ? atomicAdd(ctr, (unsigned long long)tot) : 0ULL;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kCollectQueues; ++k) {
+            if (!want[k]) continue;
+            unsigned before = __popc(ballot[k] & ((1u << lane) - 1u));
+            for (unsigned v = 0; v < w; ++v) before += s_warp[k][v];
+            const unsigned long long slot = s_base[k] + before;
+            if (slot >= q.cap) {
+                atomicExch(&q.counts[kCntOverflow], 1ULL);
+                continue;
+            }
+            uint32_t* dst = k == 0 ? q.full : k == 1 ? q.cover_box : k == 2 ? q.gaps_box : q.cert[k - 3];
+            dst[slot] = (uint32_t)i;
+            if (k == 3 + kRecGroups) q.cflags[i] = cf;
+        }
+        __syncthreads();  // s_warp and s_base are rewritten next iteration
     }
 }
 
