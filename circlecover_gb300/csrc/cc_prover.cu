@@ -642,14 +642,15 @@ static int eval_queues(cc_handle* h, size_t cap, EvalQueues* q) {
 // record buffers, the heavy groups (r1, r1_r2, 2x2, leaf) run as a record
 // pass plus call rounds; the three-strip group runs in one kernel either way.
 template <Layout L>
-static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks,
-                              EvalQueues q) {
+static cudaError_t launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in, size_t n, uint32_t* masks,
+                                     EvalQueues q) {
+    cudaError_t e;
     if (q.args) {
 #define CC_F32_RECORD(K)                                                                                      \
     {                                                                                                         \
         constexpr int G = rec_group(K);                                                                       \
         uint8_t* st = q.states + (size_t)(K) * n;                                                             \
-        cudaMemsetAsync(q.rc, 0, 2 * sizeof(unsigned long long), s);                                          \
+        if ((e = cudaMemsetAsync(q.rc, 0, 2 * sizeof(unsigned long long), s)) != cudaSuccess) return e;       \
         if (minb == 4)                                                                                        \
             k_eval_record<G, 4><<<g, 128, 0, s>>>(q.enc, n, masks, q.args, st, q.q[0], &q.rc[0], &q.counts[2]); \
         else if (minb == 8)                                                                                   \
@@ -657,7 +658,8 @@ static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in,
         else                                                                                                  \
             k_eval_record<G, 1><<<g, 128, 0, s>>>(q.enc, n, masks, q.args, st, q.q[0], &q.rc[0], &q.counts[2]); \
         for (int r = 0; r < ct::kCrRecordSlots; ++r) {                                                        \
-            cudaMemsetAsync(&q.rc[(r + 1) & 1], 0, sizeof(unsigned long long), s);                            \
+            e = cudaMemsetAsync(&q.rc[(r + 1) & 1], 0, sizeof(unsigned long long), s);                        \
+            if (e != cudaSuccess) return e;                                                                   \
             k_eval_calls<<<g, 128, 0, s>>>(q.args, st, r, q.q[r & 1], &q.rc[r & 1], q.q[(r + 1) & 1],          \
                                           &q.rc[(r + 1) & 1], n, &q.counts[2]);                               \
         }                                                                                                     \
@@ -671,7 +673,7 @@ static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in,
         CC_F32_RECORD(3)
 #undef CC_F32_RECORD
         k_eval_collect<<<g, 128, 0, s>>>(n, masks, q);
-        return;
+        return cudaSuccess;
     }
 #define CC_F32_GROUP(G)                                                                         \
     if constexpr (L == Layout::SoA) {                                                           \
@@ -688,6 +690,8 @@ static void launch_k_eval_f32(int minb, int g, cudaStream_t s, const double* in,
     CC_F32_GROUP(4)
 #undef CC_F32_GROUP
     k_eval_collect<<<g, 128, 0, s>>>(n, masks, q);
+    (void)e;
+    return cudaSuccess;
 }
 CC_EVAL_LAUNCH(k_eval_main, in, n, masks, q)
 CC_EVAL_LAUNCH(k_eval_gaps, in, n, q, masks)
@@ -731,7 +735,7 @@ template <Layout L>
 static cudaError_t launch_pass(int pass, int minb, int g, cudaStream_t s, const double* in, size_t n,
                                uint32_t* masks, EvalQueues q) {
     switch (pass) {
-        case 0: launch_k_eval_f32<L>(minb, g, s, in, n, masks, q); break;
+        case 0: return launch_k_eval_f32<L>(minb, g, s, in, n, masks, q);
         case 1: launch_k_eval_main<L>(minb, g, s, in, n, masks, q); break;
         case 2: return launch_k_eval_cover<L>(minb, g, s, in, n, masks, q);
         case 3: launch_k_eval_gaps<L>(minb, g, s, in, n, masks, q); break;
