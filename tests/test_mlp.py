@@ -117,3 +117,38 @@ def test_gpu_learned_proof_finds_the_same_criticals(prover, golden_prove):
         assert st["gen_sizes"] == c["stats"]["gen_sizes"] and st["leaf_evals"] == c["stats"]["leaf_evals"]
         reordered += st["counts"][3][3] - c["stats"]["counts"][3][3]
     assert reordered > 0  # the leaf criterion certified leaves the 2x2 criterion used to
+
+
+@pytest.mark.gpu
+def test_gpu_learned_order_saves_leaf_work(prover):
+    """What the network gains: on the initial pass of the small plain-method
+    workload (lambda in [1, 1.1], 64 lambda pieces, r splits 32 x 64^3) the
+    learned leaf order puts the prepared leaf criterion before the 2x2 one in
+    the cells where it certifies, so the FP32-first 2x2 evaluations the
+    batched form makes (nearly all of them "false") mostly disappear; the
+    criticals and the leaf count are the same, and it is not slower."""
+    import time
+    import circlecover_gb300 as cg
+    from circlecover_gb300 import learn
+    from circlecover_gb300 import workloads as W
+    root = W.tight_root(1.0, 1.1)
+    grid = cg.make_grid(64, (32, 64, 64, 64))
+    prover.mlp_init(13)
+    rec, ncells = learn.proof_records(prover, root, grid, per_cell=8)
+    learn.train(prover, rec, epochs=3, batch=4096)
+    res = {}
+    for name, kw in (("batched", {}), ("learned", {"learned": True})):
+        prover.tight_find_critical_intervals(root, grid, **kw)  # warm
+        best = float("inf")
+        for _ in range(2):
+            t0 = time.perf_counter()
+            crit, st = prover.tight_find_critical_intervals(root, grid, **kw)
+            best = min(best, time.perf_counter() - t0)
+        res[name] = (best, crit, st)
+    (tb, cb, sb), (tl, cl, sl) = res["batched"], res["learned"]
+    assert np.array_equal(cb.view(np.uint64), cl.view(np.uint64)) and sb["leaf_evals"] == sl["leaf_evals"]
+    fp32_b, fp32_l = sum(sb["fp32_first"][:3]), sum(sl["fp32_first"][:3])
+    print("FP32-first leaf evaluations: batched %d, learned %d; seconds: batched %.3f, learned %.3f"
+          % (fp32_b, fp32_l, tb, tl))
+    assert fp32_l < 0.2 * fp32_b
+    assert tl < 1.1 * tb
