@@ -51,22 +51,27 @@ __device__ __forceinline__ ct::Box load_box(const double* __restrict__ in, size_
     return b;
 }
 
-// ---- four-pass evaluation -------------------------------------------------
+// ---- six-pass evaluation --------------------------------------------------
 // GB300 issues FP32 instructions at many times the FP64 rate, and a warp pays
 // for every path any of its lanes takes.  So:
 //   pass 0  every box: the criteria on FP32 enclosures of the FP64 values
 //           (ct::eval_group_f32), one kernel per criterion group (the whole
 //           FP32 evaluation does not fit the instruction cache), each ORing
-//           its bits into the box's mask; then k_eval_collect appends the
-//           boxes some group could not decide to the `full` queue and the
-//           boxes that need a bisection to its queue (one atomic per warp);
+//           its bits into the box's mask -- the heavy groups record their
+//           can_recurse calls and evaluate them in rounds over compacted
+//           queues; then k_eval_collect appends the boxes some group could
+//           not decide to the `full` queue, the boxes that need a bisection
+//           and every "true" bit to certify to their queues (one atomic per
+//           queue and block);
 //   pass 1  k_eval_main on the `full` queue: the FP64 criteria (ct::eval_main);
-//   pass 2  k_eval_cover: boxes that need the strip-width bisection (~19% of
-//           the microbench: ~700 operations each), on full warps;
-//   pass 3  k_eval_gaps: boxes that need the gap-width bisection (~30%);
+//   pass 2  k_eval_cover: boxes that need the strip-width bisection (~14% of
+//           the microbench), with the FP64 steps resumed in a second kernel
+//           on full warps;
+//   pass 3  k_eval_gaps: boxes that need the gap-width bisection (~31%);
 //   pass 4  k_eval_cert: FP64 certification of every verdict bit pass 0
-//           decided "true", one kernel per criterion group on its queue
-//           (passes 2 and 3 certify their own true results);
+//           decided "true", one kernel per criterion group on its queue, and
+//           k_eval_cert_calls for the recorded calls (passes 2 and 3 certify
+//           their own true results);
 //   pass 5  k_eval_repair: the boxes whose certification failed, evaluated
 //           again in FP64 alone.
 // The queues hold box indices; each pass reads the box itself.

@@ -658,9 +658,10 @@ __global__ void __launch_bounds__(128) k_stage4b(const Task* __restrict__ tasks,
 // criterion's placements on the way (2x2: r1 at least 1/2 takes the
 // one-strip form; leaf r1_r2_r3: r2 and r3 above 1/4, where their strips
 // exist) -- so that a warp's lanes mostly run the same path, then runs the
-// FP64 criterion with only that call evaluated (tight::certify_leaf).  A
-// failure is counted in fp32[3]; the host then redoes the chunk in the plain
-// FP64 form.
+// FP64 criterion in record form up to that call (tight::certify_leaf), and
+// finally evaluates the recorded calls of the window, sorted again by the
+// branches can_recurse_t takes on them.  A failure is counted in fp32[3];
+// the host then redoes the chunk in the plain FP64 form.
 constexpr int kLeafCertWindow = 1024;
 constexpr int kLeafCertKeys = 128;
 // A recorded call written earlier in this kernel (by any thread of the
