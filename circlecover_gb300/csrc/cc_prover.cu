@@ -760,7 +760,7 @@ static cudaError_t launch_pass(int pass, int minb, int g, cudaStream_t s, const 
     return cudaSuccess;
 }
 
-// the launch sequence of the four passes
+// the launch sequence of the six passes
 template <Layout L>
 static int eval_launches(cc_handle* h, const double* in, size_t n, uint32_t* masks, cudaStream_t s,
                          const EvalQueues& q) {
@@ -779,7 +779,7 @@ static int eval_launches(cc_handle* h, const double* in, size_t n, uint32_t* mas
     return CC_OK;
 }
 
-// The four passes on one batch already on the device.  With the handle's
+// The six passes on one batch already on the device.  With the handle's
 // evaluation graph on (the default) and graph_ok, the launch sequence is captured once
 // into a CUDA graph and replayed by one cudaGraphLaunch while the same
 // arguments repeat (a batch loop over fixed buffers); a call with other
