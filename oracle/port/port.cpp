@@ -403,6 +403,40 @@ size_t ccport_prepared_mismatches(const cc_tight_box* boxes, size_t n, int n_ub)
     return bad;
 }
 
+/* The strip-width bisection stopped after k steps and resumed from its
+ * bracket and step count (cover_strip_width_resume, as the evaluation's
+ * second strip-width kernel does) vs the bisection run in one go, for every
+ * box whose strip enters and k = 0, 1, 2, 5, 20, 40.  Returns the number of
+ * disagreements (result bits or trap status). */
+size_t ccport_resume_mismatches(const cc_tight_box* boxes, size_t n) {
+    size_t bad = 0;
+    static const int ks[] = {0, 1, 2, 5, 20, 40};
+    for (size_t i = 0; i < n; ++i) {
+        const cc_tight_box& b = boxes[i];
+        const double la_hi = b.la.ub, r1 = b.r[0].lb, r2 = b.r[1].lb, r3 = b.r[2].lb;
+        if (!ct::cover_strip_enters(r1, r2, r3)) continue;
+        cc::trap_clear();
+        const double whole = ct::cover_strip_width_fp64(la_hi, r1, r2, r3);
+        const uint32_t tw = cc::trap_status();
+        for (int k : ks) {
+            double lo = 0.3, hi = la_hi;
+            int it = 0;
+            for (; it < k; ++it) {  // the first k steps of the same loop
+                const double mid = 0.5 * (lo + hi);
+                if (mid <= lo || mid >= hi) break;
+                if (ct::strip_width_realizable(r1, r2, r3, mid)) lo = mid;
+                else hi = mid;
+            }
+            cc::trap_clear();
+            const double res = ct::cover_strip_width_resume(r1, r2, r3, lo, hi, it);
+            const uint32_t tr = cc::trap_status();
+            cc::trap_clear();
+            bad += (std::memcmp(&res, &whole, sizeof(double)) != 0) || tr != tw;
+        }
+    }
+    return bad;
+}
+
 /* The proof's prepared leaf form vs the leaf form itself: for every box (as
  * an r3 cell: r1..r3 tightened against each other, R4 = weight - r1 - r2 -
  * r3 tightened at 0) and n_ub upper bounds of r4 spread over [0, r3.lo] and

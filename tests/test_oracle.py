@@ -180,6 +180,20 @@ def test_prepared_leaf_form_equals_plain(port):
     assert lib.ccport_leafprep_mismatches(edge.ctypes.data, len(edge), 17) == 0
 
 
+def test_strip_bisection_resumes_exactly(port):
+    """The strip-width bisection resumed from its bracket and step count after
+    any number of steps (how the evaluation's second strip-width kernel
+    continues the jobs the first stopped) ends with the same width and trap
+    status as the bisection run in one go."""
+    import ctypes
+    lib = port.lib
+    lib.ccport_resume_mismatches.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+    lib.ccport_resume_mismatches.restype = ctypes.c_size_t
+    for gen, seed in [(W.tight_microbench, 67), (W.tight_near_critical, 68)]:
+        boxes = np.ascontiguousarray(gen(20000, seed=seed))
+        assert lib.ccport_resume_mismatches(boxes.ctypes.data, len(boxes)) == 0
+
+
 def test_prepared_criteria_equal_plain(port):
     """The proof engine's hoisted criteria (prepare once per parent cell, check
     per child bound) agree with the plain criteria for every bound."""
