@@ -121,6 +121,24 @@ def profile_per_box():
     return out
 
 
+def hbm_view(traffic_bytes, ms):
+    """The dominant pass against the HBM roofline: its DRAM traffic (ncu bytes
+    per box x boxes) per second of its live time, as a fraction of the copy
+    bandwidth measured on this machine (MEASURED_PEAKS.json, when present)."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = None
+    if os.path.exists(path):
+        try:
+            peak = float(json.load(open(path))["hbm_gbs"])
+        except (ValueError, KeyError, OSError):
+            peak = None
+    if not traffic_bytes or not ms or ms <= 0:
+        return None
+    achieved = traffic_bytes / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if peak else None, "source": "MEASURED_PEAKS.json hbm_gbs (measured copy)"}
+
+
 def peaks(prover):
     """Instruction-throughput ceilings measured on this GPU by the library's
     probe (cc_selftest_peak): FP64 directed add/mul, FP32 directed add/mul and
@@ -404,6 +422,7 @@ def run_ours(args, ws, rank, local):
     step_ref_ops = ops_per_box * n / (ms * 1e-3)
     roof.update({
         "kernel": dom, "traffic": dp.get("traffic_bytes"), "algorithmic_bytes": 84 * n,
+        "hbm": hbm_view(dp.get("traffic_bytes"), dp.get("ms")),
         "lanes_per_inst": dp.get("lanes_per_inst"), "passes": passes,
         "peaks": {k: v / 1e12 for k, v in pk.items()}, "peaks_unit": "T thread-instructions/s (issue: T warp-inst/s)",
         "fp64_equivalent": {"ref_fp64_ops_per_box": ops_per_box, "rate": step_ref_ops / 1e12,
