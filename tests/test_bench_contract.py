@@ -46,3 +46,23 @@ def test_reference_arm_under_two_ranks():
     assert len(lines) == 1, r.stdout[-2000:]
     _check_line(lines[0])
     assert lines[0]["n_gpus"] == 2
+
+
+def test_roofline_inputs_are_committed():
+    """The bench's roofline reads per-box ncu counts of every evaluation pass
+    from the committed profile summary; each pass has all five counts, and
+    the pass rooflines and the HBM view come out finite from them."""
+    sys.path.insert(0, ROOT)
+    import bench
+    import circlecover_gb300 as cg
+    per_box = bench.profile_per_box()
+    metrics = ("warp_inst", "thread_inst", "fp64_inst", "fp32_inst", "dram_bytes")
+    for name in cg.EVAL_PASSES:
+        assert all(m in per_box.get(name, {}) for m in metrics), name
+    pk = {"fp64": 0.53e12, "issue": 1.2e12}
+    stage_ms = [10.0, 0.5, 5.0, 2.5, 13.0, 0.01]
+    passes = bench.pass_rooflines(stage_ms, 1 << 24, pk, per_box)
+    assert passes["k_eval_cert"]["bound"] == "fp64" and 0 < passes["k_eval_cert"]["fp64_useful_frac"] < 2
+    assert passes["k_eval_f32"]["bound"] == "issue" and 0 < passes["k_eval_f32"]["issue_frac"] < 2
+    hv = bench.hbm_view(passes["k_eval_cert"]["traffic_bytes"], 13.0)
+    assert hv["unit"] == "GB/s" and hv["achieved"] > 0
