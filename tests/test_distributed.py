@@ -1,9 +1,10 @@
-"""Sharding a tight proof over processes: every generation's tasks split into
+"""Sharding the proofs over processes: every generation's tasks split into
 contiguous ranges over the ranks of a gloo process group, criticals
-all-gathered in rank order.  Checked on the CPU (the oracle port computes each
-rank's range) against the single-process proof: same criticals, same
-generation sizes, same summed trace.  On a GPU the same driver takes
-Prover.tight_generation."""
+all-gathered in rank order (and, for the size-bound proof, merged again over
+the whole generation).  Checked on the CPU (the oracle port computes each
+rank's range) against the single-process proofs of the golden fixtures: same
+criticals, same generation sizes, same summed trace.  On a GPU the same
+drivers take Prover.tight_generation and Prover.sb_generation."""
 import json
 import os
 import socket
@@ -70,6 +71,57 @@ def test_sharded_proof_equals_single_process(tmp_path, world):
         assert st["digest"] == case["stats"]["digest"]
         assert st["counts"] == case["stats"]["counts"]
         assert st["leaf_evals"] == case["stats"]["leaf_evals"]
+
+
+def _sb_rank_main(rank, world, port, case, out_dir):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from oracle import oracle as O
+    from test_sb_prove import box6_from_hex
+    p = O.Port()
+
+    def gather(obj):
+        out = [None] * world
+        dist.all_gather_object(out, obj)
+        return out
+
+    def generation(parents, gen, k, splits, lo, hi):
+        return p.sb_generation(parents, gen, k, splits, lo, hi, threads=2)
+
+    crit, flags, st = D.prove_sb_sharded(generation, box6_from_hex(case["root"]), case["la_init"], case["r_init"],
+                                         case["la_gen"], case["r_gen"], case["gens"], rank, world, gather)
+    np.save(os.path.join(out_dir, "crit%d.npy" % rank), crit)
+    np.save(os.path.join(out_dir, "flags%d.npy" % rank), flags)
+    with open(os.path.join(out_dir, "stats%d.json" % rank), "w") as f:
+        json.dump({k: v for k, v in st.items()}, f)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("name,world", [("three_generations", 2), ("three_generations", 3), ("mixed_disks", 2)])
+def test_sharded_size_bound_proof_equals_single_process(tmp_path, name, world):
+    """The size-bound proof sharded over gloo ranks, generation by generation
+    (the three-generation case uses all three merge widths), equals the
+    reference's single-process proof in the golden fixture."""
+    import torch.multiprocessing as mp
+    from test_sb_prove import boxes6_from_hex
+    with open(os.path.join(GOLDEN, "sb_prove_golden.json")) as f:
+        case = next(c for c in json.load(f)["cases"] if c["name"] == name)
+    mp.spawn(_sb_rank_main, args=(world, free_port(), case, str(tmp_path)), nprocs=world, join=True)
+    want = boxes6_from_hex(case["criticals"])
+    for r in range(world):
+        crit = np.load(tmp_path / ("crit%d.npy" % r))
+        flags = np.load(tmp_path / ("flags%d.npy" % r))
+        st = json.load(open(tmp_path / ("stats%d.json" % r)))
+        assert len(crit) == len(want) and np.array_equal(crit.view(np.uint64), want.view(np.uint64))
+        assert [int(x) for x in flags] == case["flags"]
+        assert st["gen_sizes"] == case["stats"]["gen_sizes"]
+        assert st["digest"] == case["stats"]["digest"]
+        assert st["leaf_evals"] == case["stats"]["leaf_evals"]
+        for k in ("task_counts", "cell_counts", "leaf_counts", "trapped_leaves"):
+            assert st[k] == case["stats"][k], k
 
 
 @pytest.mark.gpu
