@@ -150,3 +150,34 @@ def _two_ranges(prover, parents, k, splits, lo, hi):
     st["leaf_evals"] = sa["leaf_evals"] + sb["leaf_evals"]
     st["trapped_leaves"] = sa["trapped_leaves"] + sb["trapped_leaves"]
     return np.concatenate([a, b]), st
+
+
+@pytest.mark.gpu
+def test_gpu_sharded_size_bound_proof(prover):
+    """On one GPU: the size-bound driver with three ranks emulated in one
+    process (each rank's range by cc_sb_generation, gathered in rank order)
+    gives the reference's proof of the three-generation golden case."""
+    from test_sb_prove import box6_from_hex, boxes6_from_hex
+    with open(os.path.join(GOLDEN, "sb_prove_golden.json")) as f:
+        case = next(c for c in json.load(f)["cases"] if c["name"] == "three_generations")
+    world = 3
+
+    def gen_all_ranks(parents, gen, k, splits, lo, hi):  # lo, hi of rank 0; the others computed here
+        n = len(parents) * k * splits[0] * splits[1]
+        return [prover.sb_generation(parents, gen, k, splits, *D.task_range(n, r, world)) for r in range(world)]
+
+    state = {}
+
+    def generation(parents, gen, k, splits, lo, hi):
+        state["parts"] = gen_all_ranks(parents, gen, k, splits, lo, hi)
+        return state["parts"][0]
+
+    def gather(obj):
+        return [obj] + [(p[0], p[1], p[2]) for p in state["parts"][1:]]
+
+    crit, flags, st = D.prove_sb_sharded(generation, box6_from_hex(case["root"]), case["la_init"], case["r_init"],
+                                         case["la_gen"], case["r_gen"], case["gens"], 0, world, gather)
+    want = boxes6_from_hex(case["criticals"])
+    assert len(crit) == len(want) and np.array_equal(crit.view(np.uint64), want.view(np.uint64))
+    assert [int(x) for x in flags] == case["flags"]
+    assert st["gen_sizes"] == case["stats"]["gen_sizes"] and st["digest"] == case["stats"]["digest"]
