@@ -8,12 +8,13 @@
 * the known theory constants of the reference.
 """
 import math
+import os
 from fractions import Fraction
 
 import numpy as np
 import pytest
 
-from conftest import boxes_from_hex, box_from_hex
+from conftest import GOLDEN, boxes_from_hex, box_from_hex
 from circlecover_gb300 import workloads as W
 from oracle import oracle as O
 
@@ -178,6 +179,14 @@ def test_prepared_leaf_form_equals_plain(port):
     crit, st = port.tight_prove(root, g, threads=4)
     edge = np.ascontiguousarray(np.concatenate([crit, W.tight_near_critical(5000, seed=66)]))
     assert lib.ccport_leafprep_mismatches(edge.ctypes.data, len(edge), 17) == 0
+    # the golden boxes: microbench, near-critical and the hand-made edge cases
+    # (point intervals, lambda = 1 and the break-even, empty and subnormal radii)
+    z = np.load(os.path.join(GOLDEN, "tight_eval_golden.npz"))
+    gold = np.ascontiguousarray(z["boxes"]).view(W.TIGHT_BOX).reshape(-1)
+    assert lib.ccport_leafprep_mismatches(gold.ctypes.data, len(gold), 9) == 0
+    lib.ccport_resume_mismatches.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+    lib.ccport_resume_mismatches.restype = ctypes.c_size_t
+    assert lib.ccport_resume_mismatches(gold.ctypes.data, len(gold)) == 0
 
 
 def test_strip_bisection_resumes_exactly(port):
